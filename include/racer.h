@@ -1,0 +1,148 @@
+/* warporacer3d GB300 rollout library: C ABI.
+ *
+ * Drop-in replacement for the compute beneath the reference's Mojo structs
+ * (AlistairKeiller/warporacer3d): Sim (racer/sim.mojo:269-348), Policy and
+ * Activations (racer/ppo.mojo:47-138), Trainer (racer/ppo.mojo:141-337),
+ * checkpoints (racer/ppo.mojo:341-355) and the benchmark loop's policy step
+ * (main.mojo:40-48,82-92). A Mojo host binds these with `external_call`
+ * through an `OwnedDLHandle` on libracer.so (INTEGRATION.md shows the shim).
+ *
+ * Conventions
+ *  - Every function returns 0 on success and a nonzero code on failure;
+ *    racer_last_error() then describes the failure (per calling thread).
+ *    Codes: 1 invalid argument, 2 CUDA error, 3 unsupported.
+ *  - Pointers named *_dev are device pointers; buffers are float32 and
+ *    feature-major as in the reference: a [rows, n] matrix stores row r at
+ *    offset r * n (racer/device.mojo:20-32).
+ *  - Each object enqueues its work on the CUDA stream given at creation
+ *    (NULL = the legacy default stream) in call order, like the reference's
+ *    single DeviceContext queue. Calls on one object are not re-entrant;
+ *    distinct objects may be used from distinct threads.
+ *  - Functions that return host values (racer_trainer_rollout's mean reward,
+ *    racer_trainer_update's KL, racer_download) synchronise the stream, as
+ *    the reference's device.read does.
+ */
+#ifndef RACER_H
+#define RACER_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define RACER_STATE 11 /* state rows: x y z heading speed steer steps progress episode friction return */
+
+/* ---- errors and memory helpers (racer/device.mojo:48-54,121-134) ---- */
+const char* racer_last_error(void);
+int racer_version(void);
+int racer_alloc(size_t bytes, void** dev);                                   /* device.alloc, zero-filled */
+int racer_free(void* dev);
+int racer_upload(void* dev, const void* host, size_t bytes, void* stream);   /* device.write */
+int racer_download(void* host, const void* dev, size_t bytes, void* stream); /* device.read */
+int racer_synchronize(void* stream);
+
+/* ---- Sim: racer/sim.mojo:269-348 ---- */
+typedef struct racer_sim racer_sim;
+typedef struct {
+  float* state;       /* [11, n] */
+  float* obs;         /* [beams + 5, n]; row beams + 4 is the constant 1 */
+  float* actions;     /* [2, n] steer, throttle in [-1, 1] */
+  float* reward;      /* [n] */
+  float* done;        /* [n] 0 running, 1 crash, 2 timeout */
+  const float* track; /* the track array, uploaded unchanged */
+} racer_sim_buffers;
+
+/* Sim.__init__ (racer/sim.mojo:280-289): uploads the track array
+ * (racer/track.py:15-18 layout) and allocates n cars. beams >= 2. */
+int racer_sim_create(const float* track, size_t len, int n, uint64_t seed, int beams, void* stream,
+                     racer_sim** out);
+int racer_sim_destroy(racer_sim* sim);
+int racer_sim_get_buffers(racer_sim* sim, racer_sim_buffers* out);
+/* Sim.reset (racer/sim.mojo:291-305): spawn every car, then a step at rest. */
+int racer_sim_reset(racer_sim* sim);
+/* Sim.step (racer/sim.mojo:307-321): physics for every car, then the lidar.
+ * actions [2, n], reward [n], done [n], obs [beams + 5, n] are device views
+ * (for example slices of rollout storage). */
+int racer_sim_step(racer_sim* sim, const float* actions_dev, float* reward_dev, float* done_dev, float* obs_dev);
+/* Sim.step that also records the probe iterations of every beam into
+ * iters_dev [beams, n] (int32): the measured per-beam work. */
+int racer_sim_step_counted(racer_sim* sim, const float* actions_dev, float* reward_dev, float* done_dev,
+                           float* obs_dev, int32_t* iters_dev);
+/* Sim.sample (racer/sim.mojo:323-348): output [3, n], log_std [2] ->
+ * actions [2, n], logp [n], value [n]. */
+int racer_sim_sample(racer_sim* sim, const float* output_dev, const float* log_std_dev, float* actions_dev,
+                     float* logp_dev, float* value_dev, int deterministic, int64_t step);
+
+/* ---- Policy and Activations: racer/ppo.mojo:47-138 ---- */
+typedef struct racer_policy racer_policy;
+typedef struct racer_acts racer_acts;
+/* Policy.__init__ (racer/ppo.mojo:68-90) for IN = beams + 5 inputs. */
+int racer_policy_create(int beams, uint64_t seed, void* stream, racer_policy** out);
+int racer_policy_destroy(racer_policy* policy);
+/* theta [P] = W0 [64, IN] | W1 [64, 65] | W2 [3, 65] | log std [2]. */
+int racer_policy_theta(racer_policy* policy, float** theta_dev, int* p);
+/* Call after writing theta directly (a checkpoint load): refreshes the
+ * policy's derived weight copies. */
+int racer_policy_sync(racer_policy* policy);
+/* Activations.__init__ (racer/ppo.mojo:56-60): h1, h2 [65, cols] with row 64 = 1, o [3, cols]. */
+int racer_acts_create(racer_policy* policy, int cols, racer_acts** out);
+int racer_acts_destroy(racer_acts* acts);
+int racer_acts_buffers(racer_acts* acts, float** h1_dev, float** h2_dev, float** o_dev);
+/* Policy.forward (racer/ppo.mojo:108-111): x [IN, cols]. */
+int racer_policy_forward(racer_policy* policy, const float* x_dev, racer_acts* acts);
+/* Policy.backward (racer/ppo.mojo:113-138): d3 [3, cols] -> d2, d1 [65, cols],
+ * W0/W1/W2 entries of grad [P]. */
+int racer_policy_backward(racer_policy* policy, const float* x_dev, racer_acts* acts, const float* d3_dev,
+                          float* d2_dev, float* d1_dev, float* grad_dev);
+/* save/load (racer/ppo.mojo:341-355): one float32 .npy holding [iteration, theta]. */
+int racer_policy_save(racer_policy* policy, const char* path, int iteration);
+int racer_policy_load(racer_policy* policy, const char* path, int* iteration);
+
+/* ---- Trainer: racer/ppo.mojo:141-337 (rollout length is a parameter) ---- */
+typedef struct racer_trainer racer_trainer;
+typedef struct {
+  float *obs, *actions, *logp, *value, *reward, *done, *advantage; /* rollout storage */
+  float *x, *d3, *d2, *d1, *grad, *first, *second, *stats;         /* minibatch scratch, Adam, stats[5] */
+  racer_acts* acts;                                                  /* the minibatch activations */
+  int batch;
+} racer_trainer_buffers;
+int racer_trainer_create(int n, int beams, int rollout, void* stream, racer_trainer** out);
+int racer_trainer_destroy(racer_trainer* trainer);
+int racer_trainer_get_buffers(racer_trainer* trainer, racer_trainer_buffers* out);
+/* Trainer.rollout (racer/ppo.mojo:187-232): returns the mean reward per step. */
+int racer_trainer_rollout(racer_trainer* trainer, racer_sim* sim, racer_policy* policy, racer_acts* acts,
+                          int iteration, float* mean_reward);
+/* Trainer.update (racer/ppo.mojo:234-257): returns the last minibatch's KL estimate. */
+int racer_trainer_update(racer_trainer* trainer, racer_policy* policy, float* kl);
+/* Trainer.minibatch (racer/ppo.mojo:259-315) with explicit advantage moments. */
+int racer_trainer_minibatch(racer_trainer* trainer, racer_policy* policy, int m, float adv_mean, float adv_scale);
+
+/* ---- Runner policy step (main.mojo:40-48) and graph-captured rollouts ---- */
+/* One step of every car acting with the policy: forward on sim obs, sample
+ * into sim actions (logp and value into scratch_dev [2, n]), Sim.step. */
+int racer_runner_step(racer_sim* sim, racer_policy* policy, racer_acts* acts, float* scratch_dev,
+                      int deterministic, int64_t t);
+/* `steps` consecutive Runner steps replayed from one CUDA graph (captured on
+ * first use for each (policy, acts, steps, deterministic)); the sampling
+ * offsets are step0, step0 + 1, ... */
+int racer_rollout(racer_sim* sim, racer_policy* policy, racer_acts* acts, float* scratch_dev, int steps,
+                  int deterministic, int64_t step0);
+
+/* ---- measurement ---- */
+/* Kernel launches in the CUDA graph racer_rollout replays for these arguments
+ * (captured here if needed), plus the one launch that sets its step offset. */
+int racer_rollout_kernel_count(racer_sim* sim, racer_policy* policy, racer_acts* acts, float* scratch_dev, int steps,
+                               int deterministic, int64_t* count);
+/* Times `reps` launches of the physics kernel and of the lidar kernel on the
+ * sim's stream with CUDA events (actions as given; the sim state advances),
+ * returning their mean durations in ms and the probe iterations of the last
+ * lidar pass summed over all beams. */
+int racer_sim_profile(racer_sim* sim, const float* actions_dev, int reps, float* physics_ms, float* lidar_ms,
+                      int64_t* probe_iterations);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* RACER_H */

@@ -1,0 +1,134 @@
+"""GPU policy, trainer and runner against the CPU oracle.
+
+Policy initialisation, GAE and sampling are element-wise and bit-exact;
+the GEMMs differ from the oracle only in summation order and precision, so
+they are compared within tolerances stated per test; the PPO gradient is
+checked against float64 central differences with the reference's GPU
+tolerance (tests/test_mojo.mojo:208).
+"""
+import numpy as np
+import pytest
+
+import oracle as O
+import warporacer3d_gb300 as W
+from test_oracle import N, host_loss
+
+pytestmark = pytest.mark.gpu
+
+# Forward tolerance: |gpu - oracle| <= FWD_ATOL + FWD_RTOL * |oracle| per output.
+FWD_ATOL, FWD_RTOL = 2e-2, 2e-2
+
+
+def test_policy_init_bit_exact():
+    for beams in (108, 1081):
+        g = W.Policy(42, beams=beams)
+        c = O.Policy(42, beams=beams)
+        assert np.array_equal(g.theta.numpy(), c.theta)
+
+
+@pytest.mark.parametrize("beams,cols", [(108, 1000), (1081, 384)])
+def test_policy_forward(beams, cols):
+    g = W.Policy(3, beams=beams)
+    c = O.Policy(3, beams=beams)
+    rng = np.random.default_rng(0)
+    x = rng.uniform(-1, 1, (beams + 5, cols)).astype(np.float32)
+    x[-1] = 1
+    xd = W.DevArray.empty(x.shape)
+    xd.write(x)
+    ga, ca = W.Activations(g, cols), O.Activations(cols)
+    g.forward(xd, ga)
+    c.forward(x, ca)
+    for name in ("h1", "h2", "o"):
+        a, b = getattr(ga, name).numpy(), getattr(ca, name)
+        assert np.all(np.abs(a - b) <= FWD_ATOL + FWD_RTOL * np.abs(b)), (name, np.abs(a - b).max())
+    assert np.all(ga.h1.numpy()[64] == 1) and np.all(ga.h2.numpy()[64] == 1)
+
+
+def test_gae_bit_exact_and_gradient_and_update():
+    """tests/test_mojo.mojo:162-215 on the GPU: GAE, FD gradient (GPU tolerance), KL after one update."""
+    flat = W.track("flat")
+    sim = W.Sim(flat, N, 42)
+    sim.reset()
+    s = sim.state.numpy()
+    for i in range(N):
+        s[O.STEPS, i] = np.float32(O.HORIZON - 5 - 7 * i)
+    sim.state.write(s)
+    policy = W.Policy(42)
+    acts = W.Activations(policy, N)
+    trainer = W.Trainer(N)
+    assert np.isfinite(trainer.rollout(sim, policy, acts, 0))
+    reward, done = trainer.reward.numpy(), trainer.done.numpy()
+    value, adv = trainer.value.numpy(), trainer.advantage.numpy()
+    last = acts.o.numpy()
+    ref_adv = np.zeros_like(adv)
+    O.lib().orc_gae(N, O.ROLLOUT, reward, done, value, np.ascontiguousarray(last[2]), ref_adv)
+    assert np.array_equal(adv, ref_adv), "GAE is bit-exact given the same inputs"
+    assert int((done != 0).sum()) == N, "every car's episode ended once during the rollout"
+    trainer.minibatch(policy, 0, 0.0, 1.0)
+    analytic = trainer.grad.numpy()
+
+    class View:  # the host loss reads rollout storage as numpy
+        pass
+    v = View()
+    v.obs, v.actions, v.logp = trainer.obs.numpy(), trainer.actions.numpy(), trainer.logp.numpy()
+    v.value, v.advantage, v.batch = value, adv, trainer.batch
+    pol = O.Policy(42)  # layout only
+    w = policy.theta.numpy().astype(np.float64)
+    largest = 0.0
+    i = 0
+    while i < pol.P:
+        w[i] += 1e-4
+        plus = host_loss(w, v, pol)
+        w[i] -= 2e-4
+        numeric = (plus - host_loss(w, v, pol)) / 2e-4
+        w[i] += 1e-4
+        assert abs(numeric - analytic[i]) <= 3e-2 * abs(numeric) + 1e-3, (i, analytic[i], numeric)
+        largest = max(largest, abs(numeric))
+        i += 293 if i < pol.LOGSTD - 293 else 1
+    assert largest > 1e-3
+    kl = trainer.update(policy)
+    assert np.isfinite(kl) and 0 <= kl < 0.1
+
+
+def test_runner_graph_matches_steps():
+    track = W.track("bridge")
+    n = 256
+    a = W.Runner(track, n, beams=108, seed=9)
+    b = W.Runner(track, n, beams=108, seed=9)
+    for t in range(12):
+        a.step(False, 100 + t)
+    b.rollout(12, False, 100)
+    b.synchronize()
+    for name in ("state", "obs", "reward", "done", "actions"):
+        assert np.array_equal(getattr(a.sim, name).numpy(), getattr(b.sim, name).numpy()), name
+
+
+def test_runner_step_matches_oracle_given_actions():
+    """A policy-driven step: the sim part is bit-exact when the oracle replays the GPU's actions."""
+    track = W.track("ramp")
+    n = 128
+    r = W.Runner(track, n, beams=108, seed=4)
+    cpu = O.Sim(track, n, 4, beams=108)
+    cpu.state[:] = r.sim.state.numpy()
+    cpu.obs[:] = r.sim.obs.numpy()
+    for t in range(8):
+        r.step(False, t)
+        cpu.actions[:] = r.sim.actions.numpy()
+        cpu.step(cpu.actions, cpu.reward, cpu.done, cpu.obs)
+        for name in ("state", "obs", "reward", "done"):
+            assert np.array_equal(getattr(r.sim, name).numpy(), getattr(cpu, name), equal_nan=True), (t, name)
+
+
+def test_checkpoint_roundtrip(tmp_path):
+    p = W.Policy(1)
+    path = tmp_path / "agent.npy"
+    W.save(p, path, 17)
+    arr = np.load(path)
+    assert arr.dtype == np.float32 and arr.shape == (1 + p.P,) and arr[0] == 17
+    assert np.array_equal(arr[1:], p.theta.numpy())
+    q = W.Policy(2)
+    assert W.load(q, path) == 17
+    assert np.array_equal(q.theta.numpy(), p.theta.numpy())
+    np.save(tmp_path / "short.npy", np.zeros(5, np.float32))
+    with pytest.raises(W.RacerError, match="does not match the network size"):
+        W.load(q, tmp_path / "short.npy")

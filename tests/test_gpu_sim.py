@@ -1,0 +1,164 @@
+"""GPU parity of the simulator kernels against the CPU oracle.
+
+The CUDA simulator kernels and the oracle perform the same binary32
+operations, so state, observations (lidar ranges included), rewards, done
+flags and per-beam probe counts must be identical bit for bit, step after
+step, on every built-in track and on the reference's corridor fixture.
+"""
+import math
+
+import numpy as np
+import pytest
+
+import oracle as O
+import warporacer3d_gb300 as W
+
+pytestmark = pytest.mark.gpu
+
+
+def same(a, b):
+    return np.array_equal(np.asarray(a), np.asarray(b), equal_nan=True)
+
+
+def diff_report(name, a, b):
+    a, b = np.asarray(a), np.asarray(b)
+    bad = np.argwhere(~((a == b) | (np.isnan(a) & np.isnan(b))))
+    return f"{name}: {len(bad)} of {a.size} differ; first {bad[:5].tolist()} gpu {a[tuple(bad[0])]} cpu {b[tuple(bad[0])]}"
+
+
+def check_sim(gpu, cpu, what=""):
+    for name in ("state", "obs", "reward", "done"):
+        g = getattr(gpu, name).numpy()
+        c = getattr(cpu, name)
+        assert same(g, c), what + diff_report(name, g, c)
+
+
+@pytest.mark.parametrize("name,beams,n", [("flat", 108, 96), ("ramp", 108, 96), ("bank", 108, 96),
+                                          ("bridge", 108, 96), ("bridge", 1081, 40)])
+def test_reset_and_steps_bit_exact(name, beams, n):
+    track = W.track(name)
+    gpu = W.Sim(track, n, 42, beams=beams)
+    cpu = O.Sim(track, n, 42, beams=beams)
+    gpu.reset()
+    cpu.reset()
+    check_sim(gpu, cpu, "reset ")
+    rng = np.random.default_rng(7)
+    for step in range(25):
+        act = rng.uniform(-1.2, 1.2, (2, n)).astype(np.float32)
+        act[1] = np.abs(act[1]) * (1 if step % 5 else -1)  # mostly throttle, sometimes brake
+        gpu.actions.write(act)
+        cpu.actions[:] = act
+        gpu.step(gpu.actions, gpu.reward, gpu.done, gpu.obs)
+        cpu.step(cpu.actions, cpu.reward, cpu.done, cpu.obs)
+        check_sim(gpu, cpu, f"step {step} ")
+
+
+def test_timeouts_and_crashes_respawn_bit_exact():
+    track = W.track("ramp")
+    n = 64
+    gpu, cpu = W.Sim(track, n, 3, beams=108), O.Sim(track, n, 3, beams=108)
+    gpu.reset()
+    cpu.reset()
+    s = cpu.state.copy()
+    s[O.STEPS] = np.float32(2995)  # every episode times out within a few steps
+    gpu.state.write(s)
+    cpu.state[:] = s
+    act = np.stack([np.linspace(-1, 1, n), np.ones(n)]).astype(np.float32)  # hard steering into walls
+    gpu.actions.write(act)
+    cpu.actions[:] = act
+    seen = set()
+    for step in range(40):
+        gpu.step(gpu.actions, gpu.reward, gpu.done, gpu.obs)
+        cpu.step(cpu.actions, cpu.reward, cpu.done, cpu.obs)
+        check_sim(gpu, cpu, f"step {step} ")
+        seen |= set(np.unique(cpu.done).tolist())
+    assert {1.0, 2.0} <= seen, "both crashes and timeouts occurred"
+
+
+def test_lidar_iterations_match_oracle():
+    track = W.track("bridge")
+    n, beams = 32, 1081
+    gpu, cpu = W.Sim(track, n, 11, beams=beams), O.Sim(track, n, 11, beams=beams)
+    gpu.reset()
+    cpu.reset()
+    it_gpu = W.DevArray.empty((beams, n), np.int32)
+    it_cpu = np.zeros((beams, n), np.int32)
+    gpu.step(gpu.actions, gpu.reward, gpu.done, gpu.obs, iters=it_gpu)
+    cpu.step(cpu.actions, cpu.reward, cpu.done, cpu.obs, iters=it_cpu)
+    check_sim(gpu, cpu)
+    assert same(it_gpu.numpy(), it_cpu)
+    assert 3 < it_cpu.mean() < 20
+
+
+def test_corridor_on_gpu():
+    """tests/test_mojo.mojo:58-92 run through the CUDA kernels."""
+    track = O.corridor()
+    n, beams = 4, 108
+    sim = W.Sim(track, n, 1, beams=beams)
+    ref = O.Sim(track, n, 1, beams=beams)
+    s = np.zeros((O.STATE, n), np.float32)
+    s[O.X], s[O.FRICTION], s[O.PROGRESS] = 1, 1, np.float32(0.5 / 0.15)
+    s[O.HEADING, 1] = np.float32(math.pi)
+    sim.state.write(s)
+    ref.state[:] = s
+    act = np.array([[0, 0, 0, 1], [0, 1, 1, 1]], np.float32)
+    sim.actions.write(act)
+    ref.actions[:] = act
+    sim.step(sim.actions, sim.reward, sim.done, sim.obs)
+    ref.step(ref.actions, ref.reward, ref.done, ref.obs)
+    o = sim.obs.numpy()
+    assert abs(o[4 + beams // 2, 0] * 10 - 7.1) <= 0.1
+    assert abs(o[4 + beams // 2, 1] * 10 - 0.73) <= 0.1
+    crashed = False
+    for _ in range(60):
+        sim.step(sim.actions, sim.reward, sim.done, sim.obs)
+        ref.step(ref.actions, ref.reward, ref.done, ref.obs)
+        check_sim(sim, ref)
+        done = sim.done.numpy()
+        assert done[0] == 0 and done[2] == 0 and done[3] == 0
+        if done[1] == O.CRASH and not crashed:
+            st = sim.state.numpy()
+            assert st[O.STEPS, 1] == 0 and st[O.EPISODE, 1] == 1
+            crashed = True
+    assert crashed
+    st = sim.state.numpy()
+    assert st[O.SPEED, 2] == O.SPEED_MAX and st[O.X, 2] > 3.5 and abs(st[O.Y, 2]) < 1e-4
+    assert abs(st[O.RETURN, 2] - 10 * (st[O.X, 2] - 1)) <= 0.01
+    assert st[O.Y, 3] > 0.1 and st[O.X, 3] < st[O.X, 2]
+
+
+def test_drive_parity_flat():
+    """tests/test_mojo.mojo:111-123,229-233 (CPU/GPU drive parity, there within 3e-3; here exact)."""
+    track = W.track("flat")
+    n = 8
+    gpu, cpu = W.Sim(track, n, 42), O.Sim(track, n, 42)
+    gpu.reset()
+    cpu.reset()
+    act = np.array([[0.2] * 8, [1] * 8], np.float32)
+    gpu.actions.write(act)
+    cpu.actions[:] = act
+    for _ in range(10):
+        gpu.step(gpu.actions, gpu.reward, gpu.done, gpu.obs)
+        cpu.step(cpu.actions, cpu.reward, cpu.done, cpu.obs)
+    a = np.concatenate([cpu.state[:O.STEER + 1].ravel(), cpu.obs.ravel()])
+    b = np.concatenate([gpu.state.numpy()[:O.STEER + 1].ravel(), gpu.obs.numpy().ravel()])
+    assert np.allclose(a, b, atol=3e-3, rtol=0)
+    assert same(a, b)
+
+
+def test_sample_bit_exact():
+    n = 300
+    gpu = W.Sim(W.track("flat"), n, 5)
+    cpu = O.Sim(W.track("flat"), n, 5)
+    rng = np.random.default_rng(1)
+    out = rng.normal(0, 0.3, (3, n)).astype(np.float32)
+    ls = np.array([-0.5, -1.25], np.float32)
+    o_dev, ls_dev = W.DevArray.empty((3, n)), W.DevArray.empty((2,))
+    o_dev.write(out)
+    ls_dev.write(ls)
+    a_dev, lp_dev, v_dev = W.DevArray.empty((2, n)), W.DevArray.empty((n,)), W.DevArray.empty((n,))
+    for det, step in ((0, 0), (0, 12345), (1, 7)):
+        gpu.sample(o_dev, ls_dev, a_dev, lp_dev, v_dev, det, step)
+        a, lp, v = np.zeros((2, n), np.float32), np.zeros(n, np.float32), np.zeros(n, np.float32)
+        cpu.sample(out, ls, a, lp, v, det, step)
+        assert same(a_dev.numpy(), a) and same(lp_dev.numpy(), lp) and same(v_dev.numpy(), v)

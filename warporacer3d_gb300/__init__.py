@@ -1,0 +1,21 @@
+"""warporacer3d rollout hot path on GB300 (sm_103a).
+
+Simulator (RK4 slope bicycle, layered map probes, sphere-traced lidar), the
+tanh-MLP policy and PPO's GAE/update kernels in libracer.so, behind a C ABI
+(include/racer.h) that mirrors the reference's Sim / Policy / Trainer
+structs. The Python classes here are a thin host over that ABI.
+"""
+from pathlib import Path
+
+import numpy as np
+
+from ._lib import RacerError, load_library  # noqa: F401
+from .racer import (CRASH, STATE, TIMEOUT, Activations, DevArray, Policy, Runner, Sim, Trainer, load,  # noqa: F401
+                    save)
+
+TRACKS = Path(__file__).resolve().parent / "tracks"
+
+
+def track(name):
+    """A built-in track array (flat, ramp, bank, bridge) as compiled by the reference's racer/track.py."""
+    return np.load(TRACKS / f"{name}.npz")["track"]

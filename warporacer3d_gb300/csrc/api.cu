@@ -1,0 +1,731 @@
+// C ABI of the warporacer3d GB300 library (declared in include/racer.h).
+//
+// Host-side objects mirror the reference's Mojo structs: racer_sim owns the
+// buffers of Sim (racer/sim.mojo:269-289), racer_policy the parameters of
+// Policy (racer/ppo.mojo:63-90), racer_acts an Activations
+// (racer/ppo.mojo:47-60), racer_trainer the rollout storage, minibatch
+// scratch and Adam state of Trainer (racer/ppo.mojo:141-185). Every method
+// enqueues CUDA kernels on the object's stream; nothing runs on the CPU.
+#include <cuda_runtime.h>
+#include <math.h>
+#include <stdio.h>
+#include <string.h>
+
+#include <map>
+#include <string>
+#include <tuple>
+#include <vector>
+
+#include "../../include/racer.h"
+#include "common.cuh"
+#include "kernels.h"
+#include "policy_fwd.h"
+
+namespace racer_host {
+static thread_local std::string g_error;
+void set_error(const std::string& msg) { g_error = msg; }
+const char* get_error() { return g_error.c_str(); }
+}  // namespace racer_host
+
+using namespace racer;
+using racer_host::set_error;
+
+#define RACER_ARG(cond, msg)   \
+  do {                         \
+    if (!(cond)) {             \
+      set_error(msg);          \
+      return 1;                \
+    }                          \
+  } while (0)
+
+#define RACER_LAUNCHED()                                                                            \
+  do {                                                                                              \
+    cudaError_t err_ = cudaGetLastError();                                                          \
+    if (err_ != cudaSuccess) {                                                                      \
+      set_error(std::string("kernel launch: ") + cudaGetErrorString(err_));                         \
+      return 2;                                                                                     \
+    }                                                                                               \
+  } while (0)
+
+namespace {
+
+template <typename T>
+int dalloc(T** p, size_t count, int fill_byte = 0) {
+  RACER_TRY(cudaMalloc((void**)p, count * sizeof(T) + 16));
+  RACER_TRY(cudaMemset(*p, fill_byte, count * sizeof(T) + 16));
+  return 0;
+}
+
+// A stream the library may capture: NULL (the legacy default stream) becomes
+// an owned blocking stream, which stays ordered with default-stream work.
+int own_stream(void* given, cudaStream_t* out, bool* owned) {
+  if (given) {
+    *out = (cudaStream_t)given;
+    *owned = false;
+    return 0;
+  }
+  RACER_TRY(cudaStreamCreate(out));
+  *owned = true;
+  return 0;
+}
+
+__global__ void k_fill(float* p, long count, float v) {
+  long i = (long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < count) p[i] = v;
+}
+__global__ void k_set_i64(int64_t* p, int64_t v) {
+  if (threadIdx.x == 0 && blockIdx.x == 0) *p = v;
+}
+
+}  // namespace
+
+struct racer_sim {
+  int n = 0, beams = 0, in_rows = 0;
+  uint64_t seed = 0;
+  size_t track_len = 0;
+  TrackDev t{};
+  float* d_track = nullptr;
+  float2* d_cl = nullptr;
+  float2* beam_dir = nullptr;
+  float *state = nullptr, *obs = nullptr, *actions = nullptr, *reward = nullptr, *done = nullptr;
+  int64_t* step_base = nullptr;
+  cudaStream_t st = nullptr;
+  bool owned = false;
+  std::map<std::tuple<const void*, const void*, const void*, int, int>, cudaGraphExec_t> graphs;
+  std::map<std::tuple<const void*, const void*, const void*, int, int>, size_t> graph_kernels;
+};
+
+struct racer_acts {
+  int cols = 0;
+  float *h1 = nullptr, *h2 = nullptr, *o = nullptr;
+};
+
+struct racer_trainer {
+  int n = 0, beams = 0, in_rows = 0, rollout = 0, batch = 0, step = 0;
+  float *obs = nullptr, *actions = nullptr, *logp = nullptr, *value = nullptr, *reward = nullptr, *done = nullptr,
+        *advantage = nullptr;
+  float *x = nullptr, *d3 = nullptr, *d2 = nullptr, *d1 = nullptr, *grad = nullptr, *first = nullptr,
+        *second = nullptr, *stats = nullptr, *red = nullptr;
+  racer_acts* acts = nullptr;
+  cudaStream_t st = nullptr;
+  bool owned = false;
+};
+
+extern "C" {
+
+const char* racer_last_error(void) { return racer_host::get_error(); }
+int racer_version(void) { return 1; }
+
+int racer_alloc(size_t bytes, void** dev) {
+  RACER_ARG(dev, "racer_alloc: null output");
+  RACER_TRY(cudaMalloc(dev, bytes ? bytes : 1));
+  RACER_TRY(cudaMemset(*dev, 0, bytes ? bytes : 1));
+  return 0;
+}
+int racer_free(void* dev) {
+  if (dev) RACER_TRY(cudaFree(dev));
+  return 0;
+}
+int racer_upload(void* dev, const void* host, size_t bytes, void* stream) {
+  RACER_TRY(cudaMemcpyAsync(dev, host, bytes, cudaMemcpyHostToDevice, (cudaStream_t)stream));
+  RACER_TRY(cudaStreamSynchronize((cudaStream_t)stream));
+  return 0;
+}
+int racer_download(void* host, const void* dev, size_t bytes, void* stream) {
+  RACER_TRY(cudaMemcpyAsync(host, dev, bytes, cudaMemcpyDeviceToHost, (cudaStream_t)stream));
+  RACER_TRY(cudaStreamSynchronize((cudaStream_t)stream));
+  return 0;
+}
+int racer_synchronize(void* stream) {
+  RACER_TRY(cudaStreamSynchronize((cudaStream_t)stream));
+  return 0;
+}
+
+// ---------------- Sim ----------------
+
+// Checks the track array against its header (racer/track.py:15-18,123-125;
+// racer/sim.mojo:96-102 only requires 12 floats, the GPU needs every grid in
+// bounds): positive finite cell, grid sizes, and every nearest-waypoint entry
+// an integer in [0, waypoints).
+static int check_track(const float* d, size_t len) {
+  RACER_ARG(d, "track: null pointer");
+  RACER_ARG(len >= 12, "not a track array (fewer than 12 header floats)");
+  for (int k = 0; k < 9; ++k) RACER_ARG(isfinite(d[k]), "track header holds a non-finite value");
+  RACER_ARG(d[0] >= 2 && d[1] >= 2 && d[0] == floorf(d[0]) && d[1] == floorf(d[1]), "track: bad grid size");
+  RACER_ARG(d[4] > 0, "track: cell size must be positive");
+  RACER_ARG(d[5] >= 1 && d[5] == floorf(d[5]), "track: bad waypoint count");
+  RACER_ARG(d[7] >= 1 && d[7] <= 16 && d[7] == floorf(d[7]), "track: bad layer count");
+  RACER_ARG(d[6] > 0, "track: waypoint spacing must be positive");
+  size_t nx = (size_t)d[0], ny = (size_t)d[1], w = (size_t)d[5], L = (size_t)d[7];
+  RACER_ARG(len == 12 + 3 * L * nx * ny + 4 * w, "track array length does not match its header");
+  for (size_t l = 0; l < L; ++l) {
+    const float* near = d + 12 + (3 * l + 2) * nx * ny;
+    for (size_t k = 0; k < nx * ny; ++k) {
+      float v = near[k];
+      RACER_ARG(v >= 0 && v < (float)w && v == floorf(v), "track: nearest-waypoint grid out of range");
+    }
+  }
+  return 0;
+}
+
+int racer_sim_create(const float* track, size_t len, int n, uint64_t seed, int beams, void* stream,
+                     racer_sim** out) {
+  RACER_ARG(out, "racer_sim_create: null output");
+  RACER_ARG(n >= 1, "racer_sim_create: n must be positive");
+  RACER_ARG(beams >= 2, "racer_sim_create: beams must be at least 2");
+  if (int rc = check_track(track, len)) return rc;
+  racer_sim* s = new racer_sim();
+  s->n = n;
+  s->beams = beams;
+  s->in_rows = beams + 5;
+  s->seed = seed;
+  s->track_len = len;
+  int rc = 0;
+  if ((rc = own_stream(stream, &s->st, &s->owned))) { delete s; return rc; }
+  int nx = (int)track[0], ny = (int)track[1], L = (int)track[7];
+  std::vector<float2> cl((size_t)nx * ny * L);
+  for (int l = 0; l < L; ++l) {
+    const float* c = track + 12 + (size_t)(3 * l) * nx * ny;
+    const float* h = c + (size_t)nx * ny;
+    for (size_t k = 0; k < (size_t)nx * ny; ++k) cl[k * L + l] = make_float2(c[k], h[k]);
+  }
+  std::vector<float2> dirs(beams);
+  beam_table(beams, dirs.data());
+  if ((rc = dalloc(&s->d_track, len)) || (rc = dalloc(&s->d_cl, cl.size())) || (rc = dalloc(&s->beam_dir, beams)) ||
+      (rc = dalloc(&s->state, (size_t)STATE * n)) || (rc = dalloc(&s->obs, (size_t)s->in_rows * n)) ||
+      (rc = dalloc(&s->actions, 2 * (size_t)n)) || (rc = dalloc(&s->reward, n)) || (rc = dalloc(&s->done, n)) ||
+      (rc = dalloc(&s->step_base, 1))) {
+    racer_sim_destroy(s);
+    return rc;
+  }
+  cudaMemcpy(s->d_track, track, len * sizeof(float), cudaMemcpyHostToDevice);
+  cudaMemcpy(s->d_cl, cl.data(), cl.size() * sizeof(float2), cudaMemcpyHostToDevice);
+  cudaMemcpy(s->beam_dir, dirs.data(), beams * sizeof(float2), cudaMemcpyHostToDevice);
+  cudaError_t err = cudaGetLastError();
+  if (err != cudaSuccess) {
+    set_error(std::string("racer_sim_create upload: ") + cudaGetErrorString(err));
+    racer_sim_destroy(s);
+    return 2;
+  }
+  TrackDev& t = s->t;
+  t.d = s->d_track;
+  t.cl = s->d_cl;
+  t.nx = nx;
+  t.ny = ny;
+  t.waypoints = (int)track[5];
+  t.layers = L;
+  t.x0 = track[2];
+  t.y0 = track[3];
+  t.cell = track[4];
+  t.spacing = track[6];
+  t.slope = track[8];
+  t.nxf = (float)nx;
+  t.nyf = (float)ny;
+  t.route = 12 + 3L * L * nx * ny;
+  *out = s;
+  return 0;
+}
+
+int racer_sim_destroy(racer_sim* s) {
+  if (!s) return 0;
+  for (auto& kv : s->graphs) cudaGraphExecDestroy(kv.second);
+  cudaFree(s->d_track);
+  cudaFree(s->d_cl);
+  cudaFree(s->beam_dir);
+  cudaFree(s->state);
+  cudaFree(s->obs);
+  cudaFree(s->actions);
+  cudaFree(s->reward);
+  cudaFree(s->done);
+  cudaFree(s->step_base);
+  if (s->owned && s->st) cudaStreamDestroy(s->st);
+  delete s;
+  return 0;
+}
+
+int racer_sim_get_buffers(racer_sim* s, racer_sim_buffers* out) {
+  RACER_ARG(s && out, "racer_sim_get_buffers: null argument");
+  out->state = s->state;
+  out->obs = s->obs;
+  out->actions = s->actions;
+  out->reward = s->reward;
+  out->done = s->done;
+  out->track = s->d_track;
+  return 0;
+}
+
+static int sim_step_on(racer_sim* s, const float* actions, float* reward, float* done, float* obs, int32_t* iters,
+                       cudaStream_t st) {
+  launch_advance(s->t, s->state, actions, reward, done, obs, s->n, s->beams, s->seed, st);
+  launch_lidar(s->t, s->state, obs, s->n, s->beams, s->beam_dir, iters, st);
+  RACER_LAUNCHED();
+  return 0;
+}
+
+int racer_sim_reset(racer_sim* s) {
+  RACER_ARG(s, "racer_sim_reset: null sim");
+  launch_spawn(s->t, s->state, s->actions, s->n, s->seed, s->st);
+  return sim_step_on(s, s->actions, s->reward, s->done, s->obs, nullptr, s->st);
+}
+
+int racer_sim_step(racer_sim* s, const float* actions, float* reward, float* done, float* obs) {
+  RACER_ARG(s && actions && reward && done && obs, "racer_sim_step: null argument");
+  return sim_step_on(s, actions, reward, done, obs, nullptr, s->st);
+}
+
+int racer_sim_step_counted(racer_sim* s, const float* actions, float* reward, float* done, float* obs,
+                           int32_t* iters) {
+  RACER_ARG(s && actions && reward && done && obs && iters, "racer_sim_step_counted: null argument");
+  return sim_step_on(s, actions, reward, done, obs, iters, s->st);
+}
+
+int racer_sim_sample(racer_sim* s, const float* output, const float* log_std, float* actions, float* logp,
+                     float* value, int deterministic, int64_t step) {
+  RACER_ARG(s && output && log_std && actions && logp && value, "racer_sim_sample: null argument");
+  launch_sample(s->n, s->seed, output, log_std, actions, logp, value, deterministic, nullptr, step, s->st);
+  RACER_LAUNCHED();
+  return 0;
+}
+
+// ---------------- Policy ----------------
+
+int racer_policy_create(int beams, uint64_t seed, void* stream, racer_policy** out) {
+  RACER_ARG(out, "racer_policy_create: null output");
+  RACER_ARG(beams >= 2, "racer_policy_create: beams must be at least 2");
+  racer_policy* p = nullptr;
+  int rc = policy_new(beams + 5, stream, &p);
+  if (rc) return rc;
+  launch_policy_init(beams + 5, seed, policy_theta(p), policy_stream(p));
+  RACER_LAUNCHED();
+  if ((rc = policy_refresh(p))) {
+    policy_delete(p);
+    return rc;
+  }
+  *out = p;
+  return 0;
+}
+
+int racer_policy_destroy(racer_policy* p) {
+  policy_delete(p);
+  return 0;
+}
+
+int racer_policy_theta(racer_policy* p, float** theta, int* count) {
+  RACER_ARG(p, "racer_policy_theta: null policy");
+  if (theta) *theta = policy_theta(p);
+  if (count) *count = policy_params(p);
+  return 0;
+}
+
+int racer_policy_sync(racer_policy* p) {
+  RACER_ARG(p, "racer_policy_sync: null policy");
+  return policy_refresh(p);
+}
+
+int racer_acts_create(racer_policy* p, int cols, racer_acts** out) {
+  RACER_ARG(p && out, "racer_acts_create: null argument");
+  RACER_ARG(cols >= 1, "racer_acts_create: cols must be positive");
+  racer_acts* a = new racer_acts();
+  a->cols = cols;
+  int rc;
+  if ((rc = dalloc(&a->h1, (size_t)HA * cols)) || (rc = dalloc(&a->h2, (size_t)HA * cols)) ||
+      (rc = dalloc(&a->o, (size_t)OUT * cols))) {
+    racer_acts_destroy(a);
+    return rc;
+  }
+  long count = (long)HA * cols;
+  k_fill<<<(unsigned)((count + 255) / 256), 256>>>(a->h1, count, 1.0f);
+  k_fill<<<(unsigned)((count + 255) / 256), 256>>>(a->h2, count, 1.0f);
+  RACER_TRY(cudaDeviceSynchronize());
+  *out = a;
+  return 0;
+}
+
+int racer_acts_destroy(racer_acts* a) {
+  if (!a) return 0;
+  cudaFree(a->h1);
+  cudaFree(a->h2);
+  cudaFree(a->o);
+  delete a;
+  return 0;
+}
+
+int racer_acts_buffers(racer_acts* a, float** h1, float** h2, float** o) {
+  RACER_ARG(a, "racer_acts_buffers: null acts");
+  if (h1) *h1 = a->h1;
+  if (h2) *h2 = a->h2;
+  if (o) *o = a->o;
+  return 0;
+}
+
+static int forward_on(racer_policy* p, const float* x, racer_acts* a, cudaStream_t st) {
+  return policy_forward(p, x, a->cols, a->h1, a->h2, a->o, st);
+}
+
+int racer_policy_forward(racer_policy* p, const float* x, racer_acts* a) {
+  RACER_ARG(p && x && a, "racer_policy_forward: null argument");
+  return forward_on(p, x, a, policy_stream(p));
+}
+
+int racer_policy_backward(racer_policy* p, const float* x, racer_acts* a, const float* d3, float* d2, float* d1,
+                          float* grad) {
+  RACER_ARG(p && x && a && d3 && d2 && d1 && grad, "racer_policy_backward: null argument");
+  return policy_backward(p, x, a->cols, a->h1, a->h2, d3, d2, d1, grad, policy_stream(p));
+}
+
+// .npy v1.0 float32 vector (racer/ppo.mojo:341-355, racer/device.mojo:137-143).
+int racer_policy_save(racer_policy* p, const char* path, int iteration) {
+  RACER_ARG(p && path, "racer_policy_save: null argument");
+  int count = policy_params(p);
+  std::vector<float> values((size_t)count + 1);
+  values[0] = (float)iteration;
+  RACER_TRY(cudaMemcpyAsync(values.data() + 1, policy_theta(p), count * sizeof(float), cudaMemcpyDeviceToHost,
+                            policy_stream(p)));
+  RACER_TRY(cudaStreamSynchronize(policy_stream(p)));
+  char dict[128];
+  snprintf(dict, sizeof dict, "{'descr': '<f4', 'fortran_order': False, 'shape': (%d,), }", count + 1);
+  std::string header(dict);
+  size_t total = 10 + header.size() + 1;
+  header.append((64 - total % 64) % 64, ' ');
+  header.push_back('\n');
+  FILE* f = fopen(path, "wb");
+  RACER_ARG(f, std::string("racer_policy_save: cannot open ") + path);
+  unsigned short hl = (unsigned short)header.size();
+  unsigned char pre[10] = {0x93, 'N', 'U', 'M', 'P', 'Y', 1, 0, (unsigned char)(hl & 0xff), (unsigned char)(hl >> 8)};
+  bool ok = fwrite(pre, 1, 10, f) == 10 && fwrite(header.data(), 1, header.size(), f) == header.size() &&
+            fwrite(values.data(), sizeof(float), values.size(), f) == values.size();
+  ok = (fclose(f) == 0) && ok;
+  RACER_ARG(ok, std::string("racer_policy_save: write failed for ") + path);
+  return 0;
+}
+
+int racer_policy_load(racer_policy* p, const char* path, int* iteration) {
+  RACER_ARG(p && path, "racer_policy_load: null argument");
+  FILE* f = fopen(path, "rb");
+  RACER_ARG(f, std::string("racer_policy_load: cannot open ") + path);
+  unsigned char pre[10];
+  std::vector<char> header;
+  bool ok = fread(pre, 1, 8, f) == 8 && pre[0] == 0x93 && memcmp(pre + 1, "NUMPY", 5) == 0;
+  size_t hl = 0;
+  if (ok && pre[6] == 1) {
+    ok = fread(pre + 8, 1, 2, f) == 2;
+    hl = pre[8] | (pre[9] << 8);
+  } else if (ok && (pre[6] == 2 || pre[6] == 3)) {
+    unsigned char b[4];
+    ok = fread(b, 1, 4, f) == 4;
+    hl = b[0] | (b[1] << 8) | (b[2] << 16) | ((size_t)b[3] << 24);
+  } else {
+    ok = false;
+  }
+  if (ok) {
+    header.resize(hl + 1, 0);
+    ok = fread(header.data(), 1, hl, f) == hl;
+  }
+  std::string h(header.begin(), header.end());
+  bool f4 = h.find("'<f4'") != std::string::npos, f8 = h.find("'<f8'") != std::string::npos;
+  ok = ok && (f4 || f8) && h.find("'fortran_order': False") != std::string::npos;
+  size_t lp = h.find("'shape': ("), count = 0;
+  if (ok && lp != std::string::npos) count = strtoul(h.c_str() + lp + 10, nullptr, 10);
+  int want = policy_params(p) + 1;
+  std::vector<float> values(want);
+  if (ok && count == (size_t)want) {
+    if (f4) {
+      ok = fread(values.data(), sizeof(float), want, f) == (size_t)want;
+    } else {
+      std::vector<double> dv(want);
+      ok = fread(dv.data(), sizeof(double), want, f) == (size_t)want;
+      for (int k = 0; k < want; ++k) values[k] = (float)dv[k];
+    }
+  } else if (ok) {
+    fclose(f);
+    set_error("checkpoint does not match the network size");
+    return 1;
+  }
+  fclose(f);
+  RACER_ARG(ok, std::string("racer_policy_load: not a float .npy vector: ") + path);
+  RACER_TRY(cudaMemcpyAsync(policy_theta(p), values.data() + 1, (want - 1) * sizeof(float), cudaMemcpyHostToDevice,
+                            policy_stream(p)));
+  RACER_TRY(cudaStreamSynchronize(policy_stream(p)));
+  if (iteration) *iteration = (int)values[0];
+  return policy_refresh(p);
+}
+
+// ---------------- Trainer ----------------
+
+int racer_trainer_create(int n, int beams, int rollout, void* stream, racer_trainer** out) {
+  RACER_ARG(out, "racer_trainer_create: null output");
+  RACER_ARG(n >= 1 && beams >= 2 && rollout >= 1, "racer_trainer_create: bad sizes");
+  RACER_ARG(((long)n * rollout) % MINIBATCHES == 0, "racer_trainer_create: n * rollout must divide into 4 minibatches");
+  racer_trainer* tr = new racer_trainer();
+  tr->n = n;
+  tr->beams = beams;
+  tr->in_rows = beams + 5;
+  tr->rollout = rollout;
+  tr->batch = (int)((long)n * rollout / MINIBATCHES);
+  int rc;
+  if ((rc = own_stream(stream, &tr->st, &tr->owned))) { delete tr; return rc; }
+  size_t R = rollout, IN = tr->in_rows, B = tr->batch, P = (size_t)H * IN + H * HA + OUT * HA + 2;
+  if ((rc = dalloc(&tr->obs, (R + 1) * IN * n)) || (rc = dalloc(&tr->actions, R * 2 * n)) ||
+      (rc = dalloc(&tr->logp, R * n)) || (rc = dalloc(&tr->value, R * n)) || (rc = dalloc(&tr->reward, R * n)) ||
+      (rc = dalloc(&tr->done, R * n)) || (rc = dalloc(&tr->advantage, R * n)) || (rc = dalloc(&tr->x, IN * B)) ||
+      (rc = dalloc(&tr->d3, (OUT + 3) * B)) || (rc = dalloc(&tr->d2, (size_t)HA * B)) ||
+      (rc = dalloc(&tr->d1, (size_t)HA * B)) || (rc = dalloc(&tr->grad, P)) || (rc = dalloc(&tr->first, P)) ||
+      (rc = dalloc(&tr->second, P)) || (rc = dalloc(&tr->stats, STATS)) || (rc = dalloc(&tr->red, 4096))) {
+    racer_trainer_destroy(tr);
+    return rc;
+  }
+  racer_acts* a = new racer_acts();
+  a->cols = tr->batch;
+  if ((rc = dalloc(&a->h1, (size_t)HA * B)) || (rc = dalloc(&a->h2, (size_t)HA * B)) ||
+      (rc = dalloc(&a->o, (size_t)OUT * B))) {
+    racer_acts_destroy(a);
+    racer_trainer_destroy(tr);
+    return rc;
+  }
+  long count = (long)HA * B;
+  k_fill<<<(unsigned)((count + 255) / 256), 256>>>(a->h1, count, 1.0f);
+  k_fill<<<(unsigned)((count + 255) / 256), 256>>>(a->h2, count, 1.0f);
+  tr->acts = a;
+  RACER_TRY(cudaDeviceSynchronize());
+  *out = tr;
+  return 0;
+}
+
+int racer_trainer_destroy(racer_trainer* tr) {
+  if (!tr) return 0;
+  for (float* p : {tr->obs, tr->actions, tr->logp, tr->value, tr->reward, tr->done, tr->advantage, tr->x, tr->d3,
+                   tr->d2, tr->d1, tr->grad, tr->first, tr->second, tr->stats, tr->red})
+    cudaFree(p);
+  racer_acts_destroy(tr->acts);
+  if (tr->owned && tr->st) cudaStreamDestroy(tr->st);
+  delete tr;
+  return 0;
+}
+
+int racer_trainer_get_buffers(racer_trainer* tr, racer_trainer_buffers* out) {
+  RACER_ARG(tr && out, "racer_trainer_get_buffers: null argument");
+  out->obs = tr->obs;
+  out->actions = tr->actions;
+  out->logp = tr->logp;
+  out->value = tr->value;
+  out->reward = tr->reward;
+  out->done = tr->done;
+  out->advantage = tr->advantage;
+  out->x = tr->x;
+  out->d3 = tr->d3;
+  out->d2 = tr->d2;
+  out->d1 = tr->d1;
+  out->grad = tr->grad;
+  out->first = tr->first;
+  out->second = tr->second;
+  out->stats = tr->stats;
+  out->acts = tr->acts;
+  out->batch = tr->batch;
+  return 0;
+}
+
+int racer_trainer_rollout(racer_trainer* tr, racer_sim* s, racer_policy* p, racer_acts* a, int iteration,
+                          float* mean_reward) {
+  RACER_ARG(tr && s && p && a, "racer_trainer_rollout: null argument");
+  RACER_ARG(s->n == tr->n && s->beams == tr->beams && a->cols == tr->n && policy_inputs(p) == tr->in_rows,
+            "racer_trainer_rollout: sizes of sim, policy, activations and trainer differ");
+  cudaStream_t st = tr->st;
+  const size_t n = tr->n, IN = tr->in_rows, R = tr->rollout;
+  const float* logstd = policy_theta(p) + policy_params(p) - 2;
+  RACER_TRY(cudaMemcpyAsync(tr->obs, s->obs, IN * n * sizeof(float), cudaMemcpyDeviceToDevice, st));
+  for (size_t t = 0; t < R; ++t) {
+    int rc = forward_on(p, tr->obs + t * IN * n, a, st);
+    if (rc) return rc;
+    launch_sample((int)n, s->seed, a->o, logstd, tr->actions + t * 2 * n, tr->logp + t * n, tr->value + t * n, 0,
+                  nullptr, (int64_t)iteration * (int64_t)R + (int64_t)t, st);
+    if ((rc = sim_step_on(s, tr->actions + t * 2 * n, tr->reward + t * n, tr->done + t * n, tr->obs + (t + 1) * IN * n,
+                          nullptr, st)))
+      return rc;
+  }
+  RACER_TRY(cudaMemcpyAsync(s->obs, tr->obs + R * IN * n, IN * n * sizeof(float), cudaMemcpyDeviceToDevice, st));
+  int rc = forward_on(p, tr->obs + R * IN * n, a, st);
+  if (rc) return rc;
+  launch_gae((int)n, (int)R, tr->reward, tr->done, tr->value, a->o + 2 * n, tr->advantage, st);
+  launch_rowsum(tr->reward, 1, (int)(R * n), (long)(R * n), tr->stats + ST_REWARD, tr->red, 0, st);
+  RACER_LAUNCHED();
+  float stats[STATS];
+  RACER_TRY(cudaMemcpyAsync(stats, tr->stats, sizeof stats, cudaMemcpyDeviceToHost, st));
+  RACER_TRY(cudaStreamSynchronize(st));
+  if (mean_reward) *mean_reward = stats[ST_REWARD] / (float)(R * n);
+  return 0;
+}
+
+static int minibatch_on(racer_trainer* tr, racer_policy* p, int m, int use_moments, float adv_mean,
+                        float adv_scale) {
+  cudaStream_t st = tr->st;
+  const int B = tr->batch, IN = tr->in_rows, P = policy_params(p);
+  const float* logstd = policy_theta(p) + P - 2;
+  launch_gather(IN, tr->n, B, m, tr->obs, tr->x, st);
+  int rc = forward_on(p, tr->x, tr->acts, st);
+  if (rc) return rc;
+  launch_loss(tr->n, B, m, tr->actions, tr->logp, tr->value, tr->advantage, tr->acts->o, logstd,
+              tr->stats + ST_ADV, use_moments, adv_mean, adv_scale, tr->d3, st);
+  if ((rc = policy_backward(p, tr->x, B, tr->acts->h1, tr->acts->h2, tr->d3, tr->d2, tr->d1, tr->grad, st)))
+    return rc;
+  launch_rowsum(tr->d3 + (size_t)OUT * B, 2, B, B, tr->grad + P - 2, tr->red, 0, st);
+  launch_rowsum(tr->grad, 1, P, P, tr->stats + ST_NORM, tr->red + 2048, 1, st);
+  RACER_LAUNCHED();
+  return 0;
+}
+
+int racer_trainer_minibatch(racer_trainer* tr, racer_policy* p, int m, float adv_mean, float adv_scale) {
+  RACER_ARG(tr && p && m >= 0 && m < MINIBATCHES, "racer_trainer_minibatch: bad argument");
+  RACER_ARG(policy_inputs(p) == tr->in_rows, "racer_trainer_minibatch: policy and trainer sizes differ");
+  return minibatch_on(tr, p, m, 0, adv_mean, adv_scale);
+}
+
+int racer_trainer_update(racer_trainer* tr, racer_policy* p, float* kl) {
+  RACER_ARG(tr && p, "racer_trainer_update: null argument");
+  RACER_ARG(policy_inputs(p) == tr->in_rows, "racer_trainer_update: policy and trainer sizes differ");
+  cudaStream_t st = tr->st;
+  const int P = policy_params(p);
+  launch_moments(tr->advantage, (long)tr->rollout * tr->n, tr->stats, tr->red, st);
+  for (int epoch = 0; epoch < EPOCHS; ++epoch) {
+    for (int m = 0; m < MINIBATCHES; ++m) {
+      int rc = minibatch_on(tr, p, (m + epoch) % MINIBATCHES, 1, 0.0f, 1.0f);
+      if (rc) return rc;
+      tr->step += 1;
+      float c1 = 1.0f - powf(0.9f, (float)tr->step), c2 = 1.0f - powf(0.999f, (float)tr->step);
+      launch_adam(P, P - 2, c1, c2, tr->stats, policy_theta(p), tr->grad, tr->first, tr->second, st);
+      RACER_LAUNCHED();
+      if ((rc = policy_refresh_on(p, st))) return rc;
+    }
+  }
+  launch_rowsum(tr->d3 + (size_t)(OUT + 2) * tr->batch, 1, tr->batch, tr->batch, tr->stats + ST_KL, tr->red, 0, st);
+  RACER_LAUNCHED();
+  float stats[STATS];
+  RACER_TRY(cudaMemcpyAsync(stats, tr->stats, sizeof stats, cudaMemcpyDeviceToHost, st));
+  RACER_TRY(cudaStreamSynchronize(st));
+  if (kl) *kl = stats[ST_KL] / (float)tr->batch;
+  return 0;
+}
+
+// ---------------- Runner ----------------
+
+static int runner_step_on(racer_sim* s, racer_policy* p, racer_acts* a, float* scratch, int det,
+                          const int64_t* base, int64_t add, cudaStream_t st) {
+  const float* logstd = policy_theta(p) + policy_params(p) - 2;
+  int rc = forward_on(p, s->obs, a, st);
+  if (rc) return rc;
+  launch_sample(s->n, s->seed, a->o, logstd, s->actions, scratch, scratch + s->n, det, base, add, st);
+  return sim_step_on(s, s->actions, s->reward, s->done, s->obs, nullptr, st);
+}
+
+int racer_runner_step(racer_sim* s, racer_policy* p, racer_acts* a, float* scratch, int det, int64_t t) {
+  RACER_ARG(s && p && a && scratch, "racer_runner_step: null argument");
+  RACER_ARG(a->cols == s->n && policy_inputs(p) == s->in_rows, "racer_runner_step: sizes differ");
+  return runner_step_on(s, p, a, scratch, det, nullptr, t, s->st);
+}
+
+// Captures (once) the graph of `steps` Runner steps for these arguments.
+static int rollout_graph(racer_sim* s, racer_policy* p, racer_acts* a, float* scratch, int steps, int det,
+                         cudaGraphExec_t* exec_out, size_t* kernels) {
+  auto key = std::make_tuple((const void*)p, (const void*)a, (const void*)scratch, steps, det);
+  auto it = s->graphs.find(key);
+  if (it == s->graphs.end()) {
+    cudaGraph_t g;
+    RACER_TRY(cudaStreamBeginCapture(s->st, cudaStreamCaptureModeThreadLocal));
+    int rc = 0;
+    for (int k = 0; k < steps && !rc; ++k) rc = runner_step_on(s, p, a, scratch, det, s->step_base, k, s->st);
+    cudaError_t end = cudaStreamEndCapture(s->st, &g);
+    if (rc) return rc;
+    RACER_TRY(end);
+    size_t count = 0;
+    RACER_TRY(cudaGraphGetNodes(g, nullptr, &count));
+    std::vector<cudaGraphNode_t> nodes(count);
+    size_t kcount = 0;
+    if (count) RACER_TRY(cudaGraphGetNodes(g, nodes.data(), &count));
+    for (auto nd : nodes) {
+      cudaGraphNodeType type;
+      RACER_TRY(cudaGraphNodeGetType(nd, &type));
+      kcount += type == cudaGraphNodeTypeKernel;
+    }
+    cudaGraphExec_t exec;
+    cudaError_t inst = cudaGraphInstantiate(&exec, g, 0);
+    cudaGraphDestroy(g);
+    RACER_TRY(inst);
+    it = s->graphs.emplace(key, exec).first;
+    s->graph_kernels[key] = kcount;
+  }
+  *exec_out = it->second;
+  if (kernels) *kernels = s->graph_kernels[key];
+  return 0;
+}
+
+int racer_rollout(racer_sim* s, racer_policy* p, racer_acts* a, float* scratch, int steps, int det, int64_t step0) {
+  RACER_ARG(s && p && a && scratch && steps >= 1, "racer_rollout: bad argument");
+  RACER_ARG(a->cols == s->n && policy_inputs(p) == s->in_rows, "racer_rollout: sizes differ");
+  cudaGraphExec_t exec;
+  if (int rc = rollout_graph(s, p, a, scratch, steps, det, &exec, nullptr)) return rc;
+  k_set_i64<<<1, 32, 0, s->st>>>(s->step_base, step0);
+  RACER_LAUNCHED();
+  RACER_TRY(cudaGraphLaunch(exec, s->st));
+  return 0;
+}
+
+int racer_rollout_kernel_count(racer_sim* s, racer_policy* p, racer_acts* a, float* scratch, int steps, int det,
+                               int64_t* count) {
+  RACER_ARG(s && p && a && scratch && steps >= 1 && count, "racer_rollout_kernel_count: bad argument");
+  RACER_ARG(a->cols == s->n && policy_inputs(p) == s->in_rows, "racer_rollout_kernel_count: sizes differ");
+  cudaGraphExec_t exec;
+  size_t k = 0;
+  if (int rc = rollout_graph(s, p, a, scratch, steps, det, &exec, &k)) return rc;
+  *count = (int64_t)k + 1;
+  return 0;
+}
+
+__global__ void k_sum_i32(const int32_t* v, long count, unsigned long long* out) {
+  unsigned long long acc = 0;
+  for (long i = (long)blockIdx.x * blockDim.x + threadIdx.x; i < count; i += (long)gridDim.x * blockDim.x)
+    acc += (unsigned long long)v[i];
+  atomicAdd(out, acc);
+}
+
+int racer_sim_profile(racer_sim* s, const float* actions, int reps, float* physics_ms, float* lidar_ms,
+                      int64_t* probe_iterations) {
+  RACER_ARG(s && actions && reps >= 1, "racer_sim_profile: bad argument");
+  cudaStream_t st = s->st;
+  std::vector<cudaEvent_t> ev(3 * reps);
+  for (auto& e : ev) RACER_TRY(cudaEventCreate(&e));
+  for (int r = 0; r < reps; ++r) {
+    RACER_TRY(cudaEventRecord(ev[3 * r], st));
+    launch_advance(s->t, s->state, actions, s->reward, s->done, s->obs, s->n, s->beams, s->seed, st);
+    RACER_TRY(cudaEventRecord(ev[3 * r + 1], st));
+    launch_lidar(s->t, s->state, s->obs, s->n, s->beams, s->beam_dir, nullptr, st);
+    RACER_TRY(cudaEventRecord(ev[3 * r + 2], st));
+  }
+  RACER_LAUNCHED();
+  int32_t* iters = nullptr;
+  unsigned long long* total = nullptr;
+  RACER_TRY(cudaMalloc((void**)&iters, (size_t)s->beams * s->n * sizeof(int32_t)));
+  RACER_TRY(cudaMalloc((void**)&total, sizeof(unsigned long long)));
+  RACER_TRY(cudaMemsetAsync(total, 0, sizeof(unsigned long long), st));
+  launch_lidar(s->t, s->state, s->obs, s->n, s->beams, s->beam_dir, iters, st);
+  k_sum_i32<<<152, 256, 0, st>>>(iters, (long)s->beams * s->n, total);
+  RACER_LAUNCHED();
+  unsigned long long host_total = 0;
+  RACER_TRY(cudaMemcpyAsync(&host_total, total, sizeof host_total, cudaMemcpyDeviceToHost, st));
+  RACER_TRY(cudaStreamSynchronize(st));
+  cudaFree(iters);
+  cudaFree(total);
+  double phys = 0, lid = 0;
+  for (int r = 0; r < reps; ++r) {
+    float a = 0, b = 0;
+    RACER_TRY(cudaEventElapsedTime(&a, ev[3 * r], ev[3 * r + 1]));
+    RACER_TRY(cudaEventElapsedTime(&b, ev[3 * r + 1], ev[3 * r + 2]));
+    phys += a;
+    lid += b;
+  }
+  for (auto& e : ev) cudaEventDestroy(e);
+  if (physics_ms) *physics_ms = (float)(phys / reps);
+  if (lidar_ms) *lidar_ms = (float)(lid / reps);
+  if (probe_iterations) *probe_iterations = (int64_t)host_total;
+  return 0;
+}
+
+}  // extern "C"

@@ -1,0 +1,63 @@
+// Shared definitions for the warporacer3d GB300 kernels: simulator and
+// policy constants (racer/sim.mojo:15-56, racer/ppo.mojo:17-37), the device
+// view of a track, and host-side error plumbing for the C ABI.
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+#include <stdio.h>
+#include <string>
+
+namespace racer {
+
+// racer/sim.mojo:15-56
+constexpr float WHEELBASE = 0.3302f, HALF_DIAG = 0.3f, GRIP = 1.05f, GRAV = 9.81f;
+constexpr float STEER_MAX = 0.4189f, STEER_RATE = 3.2f, ACCEL_MAX = 9.51f, SPEED_MAX = 5.0f;
+constexpr int SUBSTEPS = 4;
+constexpr float DT = (float)(1.0 / 240);
+constexpr int HORIZON = 3000;
+constexpr float RANGE = 10.0f, FOV = 4.71238898f;
+constexpr float MOUNT_X = 0.27f, MOUNT_Z = 0.23f;
+enum { X = 0, Y, Z, HEADING, SPEED, STEER, STEPS, PROGRESS, EPISODE, FRICTION, RETURN, STATE };
+constexpr int OUT = 3;
+constexpr int CRASH = 1, TIMEOUT = 2;
+constexpr int HEADER = 12;
+constexpr float PI_F = 3.14159274f;      // Float32(pi)
+constexpr float TWO_PI_F = 6.28318548f;  // Float32(2 pi)
+constexpr float HALF_LOG_2PI = 0.918938533f;  // Float32(0.5 log(2 pi))
+
+// racer/ppo.mojo:17-31
+constexpr int H = 64, HA = H + 1;
+constexpr int MINIBATCHES = 4, EPOCHS = 4, ROLLOUT = 32;
+constexpr float GAMMA = 0.99f, LAMBDA = 0.95f, CLIP = 0.2f, LR = 3e-4f, MAX_NORM = 0.5f;
+enum { ST_REWARD = 0, ST_ADV = 1, ST_ADV2 = 2, ST_NORM = 3, ST_KL = 4, STATS = 5 };
+
+// Device view of one track. `d` is the reference's float32 track array,
+// uploaded unchanged (header, per layer clearance/height/nearest, route).
+// `cl` is the same clearance and height repacked per cell as
+// [ny * nx][layers] float2 (clearance, height), so one probe of every layer is
+// a single contiguous 8 * layers byte read (one float4 for two layers).
+struct TrackDev {
+  const float* d;
+  const float2* cl;
+  int nx, ny, waypoints, layers;
+  float x0, y0, cell, spacing, slope;
+  float nxf, nyf;
+  long route;
+};
+
+}  // namespace racer
+
+// Host-side error state of the C ABI (one message per thread).
+namespace racer_host {
+void set_error(const std::string& msg);
+const char* get_error();
+}  // namespace racer_host
+
+#define RACER_TRY(expr)                                                                      \
+  do {                                                                                       \
+    cudaError_t err_ = (expr);                                                               \
+    if (err_ != cudaSuccess) {                                                               \
+      racer_host::set_error(std::string(#expr) + ": " + cudaGetErrorString(err_));           \
+      return 2;                                                                              \
+    }                                                                                        \
+  } while (0)

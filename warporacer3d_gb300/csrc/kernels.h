@@ -1,0 +1,44 @@
+// Host-side launchers of the CUDA kernels, shared by the C-ABI layer.
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "common.cuh"
+
+namespace racer {
+
+// sim.cu (bit-exact simulator kernels)
+void launch_spawn(const TrackDev& t, float* state, float* actions, int n, uint64_t seed, cudaStream_t st);
+void launch_advance(const TrackDev& t, float* state, const float* actions, float* reward, float* done, float* obs,
+                    int n, int beams, uint64_t seed, cudaStream_t st);
+void launch_lidar(const TrackDev& t, const float* state, float* obs, int n, int beams, const float2* beam_dir,
+                  int* iters, cudaStream_t st);
+int lidar_max_iters(const TrackDev& t);
+void launch_sample(int n, uint64_t seed, const float* output, const float* log_std, float* actions, float* logp,
+                   float* value, int deterministic, const int64_t* step_base, int64_t step_add, cudaStream_t st);
+void launch_add_i64(int64_t* p, int64_t v, cudaStream_t st);
+void beam_table(int beams, float2* out);
+
+// ppo.cu (element-wise PPO kernels, bit-exact with the CPU restatement)
+void launch_policy_init(int in, uint64_t seed, float* theta, cudaStream_t st);
+void launch_gae(int n, int rollout, const float* reward, const float* done, const float* value,
+                const float* last_value, float* advantage, cudaStream_t st);
+void launch_gather(int in, int n, int batch, int m, const float* obs, float* x, cudaStream_t st);
+void launch_loss(int n, int batch, int m, const float* actions, const float* logp, const float* value,
+                 const float* advantage, const float* o, const float* log_std, const float* adv_moments,
+                 int use_moments, float adv_mean, float adv_scale, float* d3, cudaStream_t st);
+void launch_adam(int p, int logstd, float c1, float c2, const float* stats, float* theta, const float* grad,
+                 float* first, float* second, cudaStream_t st);
+// row sums: out[r] = sum_j x[r * ld + j] for r < rows, j < cols (deterministic two-pass)
+void launch_rowsum(const float* x, int rows, int cols, long ld, float* out, float* scratch, int squares,
+                   cudaStream_t st);
+void launch_moments(const float* adv, long count, float* stats, float* scratch, cudaStream_t st);
+
+// mlp.cu (policy GEMMs)
+void launch_sgemm(const float* A, int lda, const float* B, int ldb, float* C, int ldc, int M, int N, int K,
+                  int squash, cudaStream_t st);
+void launch_backward(int in, const float* theta, const float* x, int cols, const float* h1, const float* h2,
+                     const float* d3, float* d2, float* d1, float* grad, float* scratch, cudaStream_t st);
+size_t backward_scratch_floats(int in, int cols);
+
+}  // namespace racer

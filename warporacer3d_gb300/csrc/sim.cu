@@ -1,0 +1,369 @@
+// Simulator kernels: spawn, physics (RK4 bicycle, crash, reward, respawn),
+// sphere-traced lidar and Gaussian action sampling.
+//
+// Reference behaviour: racer/sim.mojo:59-348 (Map lookups :108-152,
+// derivative :155-167, spawn :170-181, advance :184-235, scan :238-266,
+// Sim.reset/step/sample :291-348).
+//
+// This translation unit is compiled with --fmad=false and IEEE division and
+// square root, and every transcendental comes from rmath.h, so each kernel is
+// the same sequence of binary32 operations as the CPU restatement: layer,
+// waypoint and crash outputs, the state and the ranges match it bit for bit.
+//
+// Layout in HBM (feature-major, as the reference): state [11, n],
+// actions [2, n], reward [n], done [n], obs [beams + 5, n]. The track array is
+// kept unchanged and, for the probes, repacked per cell as
+// [ny * nx][layers] float2 (clearance, height): one 16-byte load answers a
+// two-layer probe.
+#include "common.cuh"
+#include "kernels.h"
+#include "philox.h"
+#include "rmath.h"
+
+namespace racer {
+namespace {
+
+struct Spot {
+  int layer;
+  float clearance, height;
+};
+struct Surface {
+  float height, sx, sy;
+};
+
+__device__ __forceinline__ float clampf_(float x, float lo, float hi) { return fminf(fmaxf(x, lo), hi); }
+
+__device__ __forceinline__ void slopes(const Surface& g, float heading, float* along, float* across) {
+  float s, c;
+  rmath::sincosf_(heading, &s, &c);
+  *along = g.sx * c + g.sy * s;
+  *across = -g.sx * s + g.sy * c;
+}
+
+// Nearest-cell index (racer/sim.mojo:108-114); false off the map or for
+// non-finite coordinates.
+__device__ __forceinline__ bool cell_of(const TrackDev& t, float x, float y, long* idx) {
+  float fx = floorf((x - t.x0) / t.cell + 0.5f);
+  float fy = floorf((y - t.y0) / t.cell + 0.5f);
+  if (!(fx >= 0.0f && fx < t.nxf && fy >= 0.0f && fy < t.nyf)) return false;
+  *idx = (long)fy * t.nx + (long)fx;
+  return true;
+}
+
+// racer/sim.mojo:116-124. LAYERS = 0 reads the layer count from the track.
+template <int LAYERS>
+__device__ __forceinline__ Spot probe(const TrackDev& t, float x, float y, float z) {
+  long idx;
+  if (!cell_of(t, x, y, &idx)) return Spot{0, -1.0f, -1.0f};  // off the map every grid reads -1
+  Spot best;
+  float gap = 1e30f;
+  if (LAYERS == 2) {
+    float4 v = __ldg(reinterpret_cast<const float4*>(t.cl) + idx);
+    best = Spot{0, -1.0f, v.y};
+    if (v.x > 0.0f && fabsf(v.y - z) < gap) {
+      best = Spot{0, v.x, v.y};
+      gap = fabsf(v.y - z);
+    }
+    if (v.z > 0.0f && fabsf(v.w - z) < gap) best = Spot{1, v.z, v.w};
+  } else if (LAYERS == 1) {
+    float2 v = __ldg(t.cl + idx);
+    best = Spot{0, -1.0f, v.y};
+    if (v.x > 0.0f && fabsf(v.y - z) < gap) best = Spot{0, v.x, v.y};
+  } else {
+    const int L = t.layers;
+    const float2* p = t.cl + idx * L;
+    float2 v0 = __ldg(p);
+    best = Spot{0, -1.0f, v0.y};
+    for (int l = 0; l < L; ++l) {
+      float2 v = __ldg(p + l);
+      if (v.x > 0.0f && fabsf(v.y - z) < gap) {
+        best = Spot{l, v.x, v.y};
+        gap = fabsf(v.y - z);
+      }
+    }
+  }
+  return best;
+}
+
+// racer/sim.mojo:126-140: bilinear height and its gradient.
+__device__ __forceinline__ Surface surface(const TrackDev& t, int layer, float x, float y) {
+  float fx = (x - t.x0) / t.cell;
+  float fy = (y - t.y0) / t.cell;
+  float flx = floorf(fx), fly = floorf(fy);
+  int ix = flx >= 0.0f ? (flx <= (float)(t.nx - 2) ? (int)flx : t.nx - 2) : 0;
+  int iy = fly >= 0.0f ? (fly <= (float)(t.ny - 2) ? (int)fly : t.ny - 2) : 0;
+  float tx = clampf_(fx - (float)ix, 0.0f, 1.0f);
+  float ty = clampf_(fy - (float)iy, 0.0f, 1.0f);
+  const float* hp = t.d + HEADER + (long)(3 * layer + 1) * t.nx * t.ny + (long)iy * t.nx + ix;
+  float h0 = __ldg(hp), h1 = __ldg(hp + 1), h2 = __ldg(hp + t.nx), h3 = __ldg(hp + t.nx + 1);
+  float w0 = (1.0f - tx) * (1.0f - ty), w1 = tx * (1.0f - ty), w2 = (1.0f - tx) * ty, w3 = tx * ty;
+  Surface s;
+  s.height = (h0 * w0 + h2 * w2) + (h1 * w1 + h3 * w3);
+  s.sx = ((h1 - h0) * (1.0f - ty) + (h3 - h2) * ty) / t.cell;
+  s.sy = ((h2 - h0) * (1.0f - tx) + (h3 - h1) * tx) / t.cell;
+  return s;
+}
+
+__device__ __forceinline__ float waypoint(const TrackDev& t, long w, int field) {
+  return __ldg(t.d + t.route + 4 * w + field);
+}
+
+// racer/sim.mojo:146-152. Off the map the nearest grid reads -1 and the
+// route lookup lands on d[route - 4 + field], as in the reference.
+__device__ __forceinline__ float progress(const TrackDev& t, int layer, float x, float y) {
+  long idx;
+  long w = -1;
+  if (cell_of(t, x, y, &idx)) w = (long)__ldg(t.d + HEADER + (long)(3 * layer + 2) * t.nx * t.ny + idx);
+  float heading = waypoint(t, w, 3);
+  float s, c;
+  rmath::sincosf_(heading, &s, &c);
+  float along = (x - waypoint(t, w, 0)) * c + (y - waypoint(t, w, 1)) * s;
+  return (float)w + along / t.spacing;
+}
+
+struct V4 {
+  float x, y, h, s;  // position, heading, speed
+};
+
+// racer/sim.mojo:155-167
+__device__ __forceinline__ V4 derivative(const V4& p, float steer, float accel, float grip, float along,
+                                         float across) {
+  float nz = 1.0f / sqrtf((1.0f + along * along) + across * across);
+  float load = (grip * GRAV) * nz;
+  float v = fmaxf(fabsf(p.s), 0.5f) * (p.s >= 0.0f ? 1.0f : -1.0f);
+  float slide = (GRAV * across) * nz;
+  float ss, cs;
+  rmath::sincosf_(steer, &ss, &cs);
+  float lateral = clampf_((((v * p.s) * ss) / cs) / WHEELBASE + slide, -load, load);
+  float yaw = (lateral - slide) / v;
+  float longitudinal = sqrtf(fmaxf(load * load - lateral * lateral, 0.0f));
+  float dv = clampf_(accel, -longitudinal, longitudinal) - (GRAV * along) * nz;
+  float sh, ch;
+  rmath::sincosf_(p.h, &sh, &ch);
+  return V4{p.s * ch, p.s * sh, yaw, dv};
+}
+
+__device__ __forceinline__ V4 axpy(const V4& p, const V4& k, float h) {
+  return V4{p.x + k.x * h, p.y + k.y * h, p.h + k.h * h, p.s + k.s * h};
+}
+
+// racer/sim.mojo:170-181
+__device__ void spawn(const TrackDev& t, float* s, int n, int i, uint64_t seed) {
+  float episode = s[(long)EPISODE * n + i] + 1.0f;
+  float r[4];
+  philox::uniform4(seed, (uint64_t)i, (uint64_t)episode, r);
+  int w = min((int)(r[0] * (float)t.waypoints), t.waypoints - 1);
+  for (int row = 0; row < STATE; ++row) s[(long)row * n + i] = 0.0f;
+  s[(long)X * n + i] = waypoint(t, w, 0);
+  s[(long)Y * n + i] = waypoint(t, w, 1);
+  s[(long)Z * n + i] = waypoint(t, w, 2);
+  s[(long)HEADING * n + i] = waypoint(t, w, 3);
+  s[(long)PROGRESS * n + i] = (float)w;
+  s[(long)EPISODE * n + i] = episode;
+  s[(long)FRICTION * n + i] = 0.85f + 0.3f * r[1];
+}
+
+__global__ void k_spawn(TrackDev t, float* state, float* actions, int n, uint64_t seed) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  spawn(t, state, n, i, seed);
+  actions[i] = 0.0f;
+  actions[(long)n + i] = 0.0f;
+}
+
+// racer/sim.mojo:184-235: one 60 Hz step of car i.
+template <int LAYERS>
+__global__ void k_advance(TrackDev t, float* s, const float* act, float* reward, float* done, float* obs, int n,
+                          int beams, uint64_t seed) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  V4 p{s[(long)X * n + i], s[(long)Y * n + i], s[(long)HEADING * n + i], s[(long)SPEED * n + i]};
+  Spot spot = probe<LAYERS>(t, p.x, p.y, s[(long)Z * n + i]);
+  Surface ground = surface(t, spot.layer, p.x, p.y);
+  float steer = s[(long)STEER * n + i];
+  float rate = clampf_(act[i], -1.0f, 1.0f) * STEER_RATE;
+  float accel = clampf_(act[(long)n + i], -1.0f, 1.0f) * ACCEL_MAX;
+  float grip = GRIP * s[(long)FRICTION * n + i];
+  bool crashed = false;
+  const float half_dt = DT / 2.0f, sixth_dt = DT / 6.0f;
+#pragma unroll 1
+  for (int sub = 0; sub < SUBSTEPS; ++sub) {
+    float along, across;
+    slopes(ground, p.h, &along, &across);
+    float mid = steer + (rate * DT) / 2.0f;
+    V4 k1 = derivative(p, steer, accel, grip, along, across);
+    V4 k2 = derivative(axpy(p, k1, half_dt), mid, accel, grip, along, across);
+    V4 k3 = derivative(axpy(p, k2, half_dt), mid, accel, grip, along, across);
+    V4 k4 = derivative(axpy(p, k3, DT), steer + rate * DT, accel, grip, along, across);
+    p.x = p.x + ((k1.x + 2.0f * (k2.x + k3.x)) + k4.x) * sixth_dt;
+    p.y = p.y + ((k1.y + 2.0f * (k2.y + k3.y)) + k4.y) * sixth_dt;
+    p.h = p.h + ((k1.h + 2.0f * (k2.h + k3.h)) + k4.h) * sixth_dt;
+    p.s = p.s + ((k1.s + 2.0f * (k2.s + k3.s)) + k4.s) * sixth_dt;
+    p.s = clampf_(p.s, -SPEED_MAX, SPEED_MAX);
+    steer = clampf_(steer + rate * DT, -STEER_MAX, STEER_MAX);
+    spot = probe<LAYERS>(t, p.x, p.y, spot.height);
+    ground = surface(t, spot.layer, p.x, p.y);
+    crashed = crashed || spot.clearance < HALF_DIAG || ground.sx * ground.sx + ground.sy * ground.sy > 1.0f;
+  }
+  if (p.h > PI_F) p.h -= TWO_PI_F;
+  if (p.h < -PI_F) p.h += TWO_PI_F;
+  float prog = progress(t, spot.layer, p.x, p.y);
+  float dp = prog - s[(long)PROGRESS * n + i];
+  float half = (float)t.waypoints / 2.0f;
+  dp = dp > half ? dp - 2.0f * half : (dp < -half ? dp + 2.0f * half : dp);
+  float score = crashed ? -2.0f : ((10.0f * dp) * t.spacing - (0.001f * steer) * steer);
+  float steps = s[(long)STEPS * n + i] + 1.0f;
+  float reason = (float)(crashed ? CRASH : (steps >= (float)HORIZON ? TIMEOUT : 0));
+  s[(long)X * n + i] = p.x;
+  s[(long)Y * n + i] = p.y;
+  s[(long)Z * n + i] = spot.height;
+  s[(long)HEADING * n + i] = p.h;
+  s[(long)SPEED * n + i] = p.s;
+  s[(long)STEER * n + i] = steer;
+  s[(long)STEPS * n + i] = steps;
+  s[(long)PROGRESS * n + i] = prog;
+  s[(long)RETURN * n + i] = s[(long)RETURN * n + i] + score;
+  reward[i] = score;
+  done[i] = reason;
+  float heading = p.h, speed = p.s;
+  if (reason > 0.0f) {
+    spawn(t, s, n, i, seed);
+    float sx = s[(long)X * n + i], sy = s[(long)Y * n + i];
+    ground = surface(t, probe<LAYERS>(t, sx, sy, s[(long)Z * n + i]).layer, sx, sy);
+    heading = s[(long)HEADING * n + i];
+    speed = 0.0f;
+    steer = 0.0f;
+  }
+  float along, across;
+  slopes(ground, heading, &along, &across);
+  obs[i] = steer / STEER_MAX;
+  obs[(long)n + i] = speed / SPEED_MAX;
+  obs[2L * n + i] = along;
+  obs[3L * n + i] = across;
+  obs[(long)(beams + 4) * n + i] = 1.0f;
+}
+
+// racer/sim.mojo:238-266, one thread per (car, beam). Block = 8 warps; warp w
+// marches 32 consecutive beams of car blockIdx.x * 8 + w, so the lanes of a
+// warp start at one origin and probe neighbouring cells.
+template <int LAYERS>
+__global__ void __launch_bounds__(256) k_lidar(TrackDev t, const float* s, float* obs, int n, int beams,
+                                               const float2* beam_dir, int max_iters, int* iters) {
+  int i = blockIdx.x * 8 + (threadIdx.x >> 5);
+  int b = blockIdx.y * 32 + (threadIdx.x & 31);
+  if (i >= n || b >= beams) return;
+  float heading = s[(long)HEADING * n + i];
+  float sh, ch;
+  rmath::sincosf_(heading, &sh, &ch);
+  float fz = obs[2L * n + i], lz = obs[3L * n + i];
+  float2 az = __ldg(beam_dir + b);  // (cos azimuth, sin azimuth)
+  float dx = az.x * ch + az.y * -sh;
+  float dy = az.x * sh + az.y * ch;
+  float dz = az.x * fz + az.y * lz;
+  float norm = sqrtf((dx * dx + dz * dz) + (dy * dy + 0.0f));
+  dx = dx / norm;
+  dy = dy / norm;
+  dz = dz / norm;
+  float ox = (s[(long)X * n + i] + MOUNT_X * ch) + 0.0f;
+  float oy = (s[(long)Y * n + i] + MOUNT_X * sh) + 0.0f;
+  float oz = (s[(long)Z * n + i] + MOUNT_X * fz) + MOUNT_Z;
+  float horizontal = sqrtf(dx * dx + dy * dy);
+  float descent = (1.5f * t.slope) * horizontal + fmaxf(-dz, 0.0f);
+  const float cell = t.cell, min_step = 0.5f * t.cell;
+  float tt = 0.0f, last = 0.0f, last_floor = 0.0f, range = -1.0f;
+  int count = 0;
+  while (tt < RANGE && count < max_iters) {
+    ++count;
+    float px = ox + tt * dx, py = oy + tt * dy, pz = oz + tt * dz;
+    Spot spot = probe<LAYERS>(t, px, py, pz);
+    float floor_ = (pz - spot.height) - 0.03f;
+    if (floor_ < 0.0f) {
+      range = fminf(last + ((tt - last) * last_floor) / (last_floor - floor_), RANGE);
+      break;
+    }
+    float step = fminf(spot.clearance - cell, floor_ / descent);
+    if (step < min_step) break;
+    last = tt;
+    last_floor = floor_;
+    tt += step;
+  }
+  if (range < 0.0f) range = fminf(tt, RANGE);
+  obs[(long)(4 + b) * n + i] = range / RANGE;
+  if (iters) iters[(long)b * n + i] = count;
+}
+
+// racer/sim.mojo:323-348. step = *step_base (if given) + step_add.
+__global__ void k_sample(int n, uint64_t seed, const float* output, const float* log_std, float* actions, float* logp,
+                         float* value, int deterministic, const int64_t* step_base, int64_t step_add) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  int64_t step = (step_base ? *step_base : 0) + step_add;
+  float noise[4];
+  philox::normal4(seed + 1, (uint64_t)i, (uint64_t)step, noise);
+  float probability = 0.0f;
+  for (int a = 0; a < 2; ++a) {
+    float z = deterministic ? 0.0f : noise[a];
+    float ls = log_std[a];
+    actions[(long)a * n + i] = output[(long)a * n + i] + rmath::expf_(ls) * z;
+    probability -= ((0.5f * z) * z + ls) + HALF_LOG_2PI;
+  }
+  logp[i] = probability;
+  value[i] = output[2L * n + i];
+}
+
+__global__ void k_add_i64(int64_t* p, int64_t v) {
+  if (threadIdx.x == 0 && blockIdx.x == 0) *p += v;
+}
+
+}  // namespace
+
+// ---- host launchers ----
+void launch_spawn(const TrackDev& t, float* state, float* actions, int n, uint64_t seed, cudaStream_t st) {
+  k_spawn<<<(n + 127) / 128, 128, 0, st>>>(t, state, actions, n, seed);
+}
+
+void launch_advance(const TrackDev& t, float* state, const float* actions, float* reward, float* done, float* obs,
+                    int n, int beams, uint64_t seed, cudaStream_t st) {
+  dim3 grid((n + 127) / 128);
+  if (t.layers == 1)
+    k_advance<1><<<grid, 128, 0, st>>>(t, state, actions, reward, done, obs, n, beams, seed);
+  else if (t.layers == 2)
+    k_advance<2><<<grid, 128, 0, st>>>(t, state, actions, reward, done, obs, n, beams, seed);
+  else
+    k_advance<0><<<grid, 128, 0, st>>>(t, state, actions, reward, done, obs, n, beams, seed);
+}
+
+int lidar_max_iters(const TrackDev& t) { return (int)ceilf(RANGE / (0.5f * t.cell)) + 2; }
+
+void launch_lidar(const TrackDev& t, const float* state, float* obs, int n, int beams, const float2* beam_dir,
+                  int* iters, cudaStream_t st) {
+  dim3 grid((n + 7) / 8, (beams + 31) / 32);
+  int cap = lidar_max_iters(t);
+  if (t.layers == 1)
+    k_lidar<1><<<grid, 256, 0, st>>>(t, state, obs, n, beams, beam_dir, cap, iters);
+  else if (t.layers == 2)
+    k_lidar<2><<<grid, 256, 0, st>>>(t, state, obs, n, beams, beam_dir, cap, iters);
+  else
+    k_lidar<0><<<grid, 256, 0, st>>>(t, state, obs, n, beams, beam_dir, cap, iters);
+}
+
+void launch_sample(int n, uint64_t seed, const float* output, const float* log_std, float* actions, float* logp,
+                   float* value, int deterministic, const int64_t* step_base, int64_t step_add, cudaStream_t st) {
+  k_sample<<<(n + 127) / 128, 128, 0, st>>>(n, seed, output, log_std, actions, logp, value, deterministic,
+                                            step_base, step_add);
+}
+
+void launch_add_i64(int64_t* p, int64_t v, cudaStream_t st) { k_add_i64<<<1, 32, 0, st>>>(p, v); }
+
+// Per-beam (cos, sin) of the azimuth -FOV/2 + b * FOV/(beams-1), computed with
+// the same binary32 operations as racer/sim.mojo:246-247.
+void beam_table(int beams, float2* out) {
+  for (int b = 0; b < beams; ++b) {
+    float az = -FOV / 2.0f + (float)b * (FOV / (float)(beams - 1));
+    float s, c;
+    rmath::sincosf_(az, &s, &c);
+    out[b] = make_float2(c, s);
+  }
+}
+
+}  // namespace racer

@@ -1,0 +1,328 @@
+"""Host-side mirror of the reference's Mojo structs over the C ABI.
+
+    Sim          racer/sim.mojo:269-348
+    Activations  racer/ppo.mojo:47-60
+    Policy       racer/ppo.mojo:63-138
+    Trainer      racer/ppo.mojo:141-337 (rollout length is a parameter)
+    save / load  racer/ppo.mojo:341-355
+    Runner       main.mojo:22-124 (step, benchmark, evaluate, train)
+
+Buffers live on the GPU and are exposed as DevArray views (a device pointer
+with a shape, like the reference's `mat[rows](buffer, cols, offset)`);
+`.numpy()` reads one back and `.write()` uploads into it. All compute is in
+libracer.so; nothing here computes on the CPU.
+"""
+import ctypes
+import time
+
+import numpy as np
+
+from ._lib import RacerError, SimBuffers, TrainerBuffers, call, load_library
+
+STATE = 11
+X, Y, Z, HEADING, SPEED, STEER, STEPS, PROGRESS, EPISODE, FRICTION, RETURN = range(11)
+OUT, H, HA = 3, 64, 65
+CRASH, TIMEOUT = 1, 2
+ROLLOUT, EPOCHS, MINIBATCHES = 32, 4, 4
+RANGE = 10.0
+
+
+class DevArray:
+    """A float32 (or int32) device array view: pointer, shape, owner."""
+
+    def __init__(self, ptr, shape, dtype=np.float32, owner=None, stream=None):
+        self.ptr = int(ptr)
+        self.shape = tuple(int(s) for s in shape)
+        self.dtype = np.dtype(dtype)
+        self.owner = owner
+        self.stream = stream
+
+    @classmethod
+    def empty(cls, shape, dtype=np.float32):
+        nbytes = int(np.prod(shape)) * np.dtype(dtype).itemsize
+        p = ctypes.c_void_p()
+        call("racer_alloc", nbytes, ctypes.byref(p))
+        arr = cls(p.value, shape, dtype)
+        arr._owned = True
+        return arr
+
+    def __del__(self):
+        if getattr(self, "_owned", False) and self.ptr:
+            try:
+                load_library().racer_free(ctypes.c_void_p(self.ptr))
+            except Exception:
+                pass
+            self.ptr = 0
+
+    @property
+    def nbytes(self):
+        return int(np.prod(self.shape)) * self.dtype.itemsize
+
+    def __getitem__(self, i):
+        """Leading-index view (rollout storage step t, a row of a matrix)."""
+        if i < 0:
+            i += self.shape[0]
+        inner = self.shape[1:]
+        step = int(np.prod(inner)) * self.dtype.itemsize if inner else self.dtype.itemsize
+        return DevArray(self.ptr + i * step, inner if inner else (1,), self.dtype, self, self.stream)
+
+    def rows(self, start, stop):
+        inner = self.shape[1:]
+        step = int(np.prod(inner)) * self.dtype.itemsize
+        return DevArray(self.ptr + start * step, (stop - start,) + inner, self.dtype, self, self.stream)
+
+    @property
+    def c(self):
+        return ctypes.c_void_p(self.ptr)
+
+    def numpy(self):
+        out = np.empty(self.shape, self.dtype)
+        call("racer_download", out.ctypes.data_as(ctypes.c_void_p), self.c, self.nbytes, self.stream)
+        return out
+
+    def write(self, values):
+        v = np.ascontiguousarray(np.asarray(values, self.dtype).reshape(self.shape))
+        call("racer_upload", self.c, v.ctypes.data_as(ctypes.c_void_p), self.nbytes, self.stream)
+
+
+def _stream(stream):
+    """Accept None, an int handle, or an object with .cuda_stream (torch.cuda.Stream)."""
+    if stream is None:
+        return None
+    if isinstance(stream, ctypes.c_void_p):
+        return stream
+    return ctypes.c_void_p(int(getattr(stream, "cuda_stream", stream)))
+
+
+class Sim:
+    """n cars on a track (racer/sim.mojo:269-348)."""
+
+    def __init__(self, track, n, seed, beams=108, stream=None):
+        d = np.ascontiguousarray(track, np.float32)
+        self.n, self.seed, self.beams, self.IN = n, seed, beams, beams + 5
+        self.stream = _stream(stream)
+        h = ctypes.c_void_p()
+        call("racer_sim_create", d.ctypes.data_as(ctypes.POINTER(ctypes.c_float)), d.size, n, seed, beams,
+             self.stream, ctypes.byref(h))
+        self.handle = h
+        b = SimBuffers()
+        call("racer_sim_get_buffers", h, ctypes.byref(b))
+        s = self.stream
+        self.state = DevArray(b.state, (STATE, n), owner=self, stream=s)
+        self.obs = DevArray(b.obs, (self.IN, n), owner=self, stream=s)
+        self.actions = DevArray(b.actions, (2, n), owner=self, stream=s)
+        self.reward = DevArray(b.reward, (n,), owner=self, stream=s)
+        self.done = DevArray(b.done, (n,), owner=self, stream=s)
+
+    def __del__(self):
+        if getattr(self, "handle", None):
+            load_library().racer_sim_destroy(self.handle)
+            self.handle = None
+
+    def reset(self):
+        call("racer_sim_reset", self.handle)
+
+    def step(self, actions, reward, done, obs, iters=None):
+        if iters is None:
+            call("racer_sim_step", self.handle, actions.c, reward.c, done.c, obs.c)
+        else:
+            call("racer_sim_step_counted", self.handle, actions.c, reward.c, done.c, obs.c, iters.c)
+
+    def sample(self, output, log_std, actions, logp, value, deterministic, step):
+        call("racer_sim_sample", self.handle, output.c, log_std.c, actions.c, logp.c, value.c, int(deterministic),
+             step)
+
+
+class Policy:
+    """Tanh MLP IN -> 64 -> 64 -> 3 with log std (racer/ppo.mojo:63-138)."""
+
+    def __init__(self, seed, beams=108, stream=None):
+        self.IN = beams + 5
+        self.W0, self.W1 = 0, H * self.IN
+        self.W2 = self.W1 + H * HA
+        self.LOGSTD = self.W2 + OUT * HA
+        self.P = self.LOGSTD + 2
+        self.stream = _stream(stream)
+        h = ctypes.c_void_p()
+        call("racer_policy_create", beams, seed, self.stream, ctypes.byref(h))
+        self.handle = h
+        ptr, count = ctypes.c_void_p(), ctypes.c_int()
+        call("racer_policy_theta", h, ctypes.byref(ptr), ctypes.byref(count))
+        assert count.value == self.P
+        self.theta = DevArray(ptr.value, (self.P,), owner=self, stream=self.stream)
+
+    def __del__(self):
+        if getattr(self, "handle", None):
+            load_library().racer_policy_destroy(self.handle)
+            self.handle = None
+
+    def log_std(self):
+        return DevArray(self.theta.ptr + 4 * self.LOGSTD, (2,), owner=self, stream=self.stream)
+
+    def sync(self):
+        call("racer_policy_sync", self.handle)
+
+    def forward(self, x, acts):
+        call("racer_policy_forward", self.handle, x.c, acts.handle)
+
+    def backward(self, x, acts, d3, d2, d1, grad):
+        call("racer_policy_backward", self.handle, x.c, acts.handle, d3.c, d2.c, d1.c, grad.c)
+
+
+class Activations:
+    """h1, h2 [65, cols] (row 64 = 1) and o [3, cols] (racer/ppo.mojo:47-60)."""
+
+    def __init__(self, policy, cols, handle=None):
+        self.cols = cols
+        if handle is None:
+            h = ctypes.c_void_p()
+            call("racer_acts_create", policy.handle, cols, ctypes.byref(h))
+            self._owned = True
+        else:
+            h = ctypes.c_void_p(handle)
+            self._owned = False
+        self.handle = h
+        a, b, c = ctypes.c_void_p(), ctypes.c_void_p(), ctypes.c_void_p()
+        call("racer_acts_buffers", h, ctypes.byref(a), ctypes.byref(b), ctypes.byref(c))
+        self.h1 = DevArray(a.value, (HA, cols), owner=self)
+        self.h2 = DevArray(b.value, (HA, cols), owner=self)
+        self.o = DevArray(c.value, (OUT, cols), owner=self)
+
+    def __del__(self):
+        if getattr(self, "_owned", False) and getattr(self, "handle", None):
+            load_library().racer_acts_destroy(self.handle)
+            self.handle = None
+
+
+class Trainer:
+    """Rollout storage, minibatch scratch and Adam state (racer/ppo.mojo:141-337)."""
+
+    def __init__(self, n, beams=108, rollout=ROLLOUT, stream=None, policy=None):
+        self.n, self.R, self.IN = n, rollout, beams + 5
+        self.stream = _stream(stream)
+        h = ctypes.c_void_p()
+        call("racer_trainer_create", n, beams, rollout, self.stream, ctypes.byref(h))
+        self.handle = h
+        b = TrainerBuffers()
+        call("racer_trainer_get_buffers", h, ctypes.byref(b))
+        self.batch = B = b.batch
+        R, IN = rollout, self.IN
+        P = H * IN + H * HA + OUT * HA + 2
+        s = self.stream
+        self.obs = DevArray(b.obs, (R + 1, IN, n), owner=self, stream=s)
+        self.actions = DevArray(b.actions, (R, 2, n), owner=self, stream=s)
+        for name in ("logp", "value", "reward", "done", "advantage"):
+            setattr(self, name, DevArray(getattr(b, name), (R, n), owner=self, stream=s))
+        self.x = DevArray(b.x, (IN, B), owner=self, stream=s)
+        self.d3 = DevArray(b.d3, (OUT + 3, B), owner=self, stream=s)
+        self.d2 = DevArray(b.d2, (HA, B), owner=self, stream=s)
+        self.d1 = DevArray(b.d1, (HA, B), owner=self, stream=s)
+        self.grad = DevArray(b.grad, (P,), owner=self, stream=s)
+        self.first = DevArray(b.first, (P,), owner=self, stream=s)
+        self.second = DevArray(b.second, (P,), owner=self, stream=s)
+        self.stats = DevArray(b.stats, (5,), owner=self, stream=s)
+        self.acts = Activations(None, B, handle=b.acts)
+
+    def __del__(self):
+        if getattr(self, "handle", None):
+            load_library().racer_trainer_destroy(self.handle)
+            self.handle = None
+
+    def rollout(self, sim, policy, acts, iteration):
+        r = ctypes.c_float()
+        call("racer_trainer_rollout", self.handle, sim.handle, policy.handle, acts.handle, iteration, ctypes.byref(r))
+        return r.value
+
+    def update(self, policy):
+        kl = ctypes.c_float()
+        call("racer_trainer_update", self.handle, policy.handle, ctypes.byref(kl))
+        return kl.value
+
+    def minibatch(self, policy, m, adv_mean, adv_scale):
+        call("racer_trainer_minibatch", self.handle, policy.handle, m, float(adv_mean), float(adv_scale))
+
+
+def save(policy, path, iteration):
+    call("racer_policy_save", policy.handle, str(path).encode(), iteration)
+
+
+def load(policy, path):
+    it = ctypes.c_int()
+    call("racer_policy_load", policy.handle, str(path).encode(), ctypes.byref(it))
+    return it.value
+
+
+class Runner:
+    """A device, n cars on a track and a policy driving them (main.mojo:22-124)."""
+
+    def __init__(self, track, n, beams=108, seed=42, policy_seed=42, stream=None):
+        self.sim = Sim(track, n, seed, beams=beams, stream=stream)
+        self.policy = Policy(policy_seed, beams=beams, stream=self.sim.stream)
+        self.acts = Activations(self.policy, n)
+        self.scratch = DevArray.empty((2, n))  # log probabilities and values
+        self.sim.reset()
+
+    def step(self, deterministic, t):
+        call("racer_runner_step", self.sim.handle, self.policy.handle, self.acts.handle, self.scratch.c,
+             int(deterministic), t)
+
+    def rollout(self, steps, deterministic=False, step0=0):
+        """`steps` Runner steps replayed from one CUDA graph."""
+        call("racer_rollout", self.sim.handle, self.policy.handle, self.acts.handle, self.scratch.c, steps,
+             int(deterministic), step0)
+
+    def synchronize(self):
+        call("racer_synchronize", self.sim.stream)
+
+    def rollout_kernel_count(self, steps, deterministic=False):
+        count = ctypes.c_int64()
+        call("racer_rollout_kernel_count", self.sim.handle, self.policy.handle, self.acts.handle, self.scratch.c,
+             steps, int(deterministic), ctypes.byref(count))
+        return count.value
+
+    def profile_sim(self, reps):
+        """Mean physics and lidar kernel times (ms) and the probe iterations of one lidar pass."""
+        phys, lid, iters = ctypes.c_float(), ctypes.c_float(), ctypes.c_int64()
+        call("racer_sim_profile", self.sim.handle, self.sim.actions.c, reps, ctypes.byref(phys), ctypes.byref(lid),
+             ctypes.byref(iters))
+        return phys.value, lid.value, iters.value
+
+    def benchmark(self, steps, warmup=10):
+        """main.mojo:82-92: n cars; ms/step; transitions/s."""
+        for t in range(warmup):
+            self.step(False, t)
+        self.synchronize()
+        start = time.perf_counter()
+        for t in range(steps):
+            self.step(False, t)
+        self.synchronize()
+        ms = (time.perf_counter() - start) * 1000 / steps
+        return ms, self.sim.n * 1000 / ms
+
+    def evaluate(self, steps):
+        """main.mojo:70-80: reward per step and crashes per car, deterministic actions."""
+        reward, crashes = 0.0, 0
+        for t in range(steps):
+            self.step(True, t)
+            reward += float(self.sim.reward.numpy().astype(np.float64).sum())
+            crashes += int((self.sim.done.numpy() == CRASH).sum())
+        n = self.sim.n
+        return reward / (n * steps), crashes / n
+
+    def train(self, iterations, path, resume="", rollout=ROLLOUT, log=print):
+        """main.mojo:54-68: rollout + update per iteration, checkpoint every 100."""
+        trainer = Trainer(self.sim.n, beams=self.sim.beams, rollout=rollout, stream=self.sim.stream)
+        first = load(self.policy, resume) if resume else 0
+        start = time.perf_counter()
+        for iteration in range(first, first + iterations):
+            reward = trainer.rollout(self.sim, self.policy, self.acts, iteration)
+            kl = trainer.update(self.policy)
+            if not np.isfinite(kl):
+                raise RacerError("training diverged (nonfinite KL)")
+            log(f"iteration {iteration + 1} reward/step {reward} KL {kl}")
+            if (iteration + 1) % 100 == 0:
+                save(self.policy, path, iteration + 1)
+        save(self.policy, path, first + iterations)
+        rate = self.sim.n * rollout * iterations / (time.perf_counter() - start)
+        log(f"Saved {path} ; {rate} training transitions/s")
+        return rate

@@ -96,6 +96,9 @@ int racer_policy_forward(racer_policy* policy, const float* x_dev, racer_acts* a
  * W0/W1/W2 entries of grad [P]. */
 int racer_policy_backward(racer_policy* policy, const float* x_dev, racer_acts* acts, const float* d3_dev,
                           float* d2_dev, float* d1_dev, float* grad_dev);
+/* Error word of the policy's tensor-core kernels (0 = none; nonzero when a
+ * bounded wait on the tensor core timed out). Synchronises the policy's stream. */
+int racer_policy_status(racer_policy* policy, int* code);
 /* save/load (racer/ppo.mojo:341-355): one float32 .npy holding [iteration, theta]. */
 int racer_policy_save(racer_policy* policy, const char* path, int iteration);
 int racer_policy_load(racer_policy* policy, const char* path, int* iteration);

@@ -42,6 +42,7 @@ def test_policy_forward(beams, cols):
         a, b = getattr(ga, name).numpy(), getattr(ca, name)
         assert np.all(np.abs(a - b) <= FWD_ATOL + FWD_RTOL * np.abs(b)), (name, np.abs(a - b).max())
     assert np.all(ga.h1.numpy()[64] == 1) and np.all(ga.h2.numpy()[64] == 1)
+    assert g.status() == 0
 
 
 def test_gae_bit_exact_and_gradient_and_update():

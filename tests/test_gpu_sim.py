@@ -60,14 +60,15 @@ def test_timeouts_and_crashes_respawn_bit_exact():
     gpu.reset()
     cpu.reset()
     s = cpu.state.copy()
-    s[O.STEPS] = np.float32(2995)  # every episode times out within a few steps
+    s[O.STEPS, 1::2] = np.float32(2995)  # odd cars time out within a few steps
+    s[O.HEADING, 0::2] += np.float32(np.pi / 2)  # even cars face the wall, 1.3 m away
     gpu.state.write(s)
     cpu.state[:] = s
-    act = np.stack([np.linspace(-1, 1, n), np.ones(n)]).astype(np.float32)  # hard steering into walls
+    act = np.stack([np.zeros(n), np.ones(n)]).astype(np.float32)  # full throttle
     gpu.actions.write(act)
     cpu.actions[:] = act
     seen = set()
-    for step in range(40):
+    for step in range(60):
         gpu.step(gpu.actions, gpu.reward, gpu.done, gpu.obs)
         cpu.step(cpu.actions, cpu.reward, cpu.done, cpu.obs)
         check_sim(gpu, cpu, f"step {step} ")

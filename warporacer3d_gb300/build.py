@@ -24,6 +24,7 @@ UNITS = {
     "sim.cu": EXACT,
     "ppo.cu": EXACT,
     "mlp.cu": [],
+    "mlp_tc.cu": EXACT,
     "policy.cu": [],
     "api.cu": [],
 }

@@ -358,8 +358,14 @@ int racer_acts_buffers(racer_acts* a, float** h1, float** h2, float** o) {
   return 0;
 }
 
-static int forward_on(racer_policy* p, const float* x, racer_acts* a, cudaStream_t st) {
-  return policy_forward(p, x, a->cols, a->h1, a->h2, a->o, st);
+static int forward_on(racer_policy* p, const float* x, racer_acts* a, cudaStream_t st,
+                      const SampleArgs* sa = nullptr, int write_hidden = 1) {
+  return policy_forward(p, x, a->cols, a->h1, a->h2, a->o, write_hidden, sa, st);
+}
+
+int racer_policy_status(racer_policy* p, int* code) {
+  RACER_ARG(p && code, "racer_policy_status: null argument");
+  return policy_status(p, code);
 }
 
 int racer_policy_forward(racer_policy* p, const float* x, racer_acts* a) {
@@ -534,10 +540,15 @@ int racer_trainer_rollout(racer_trainer* tr, racer_sim* s, racer_policy* p, race
   const float* logstd = policy_theta(p) + policy_params(p) - 2;
   RACER_TRY(cudaMemcpyAsync(tr->obs, s->obs, IN * n * sizeof(float), cudaMemcpyDeviceToDevice, st));
   for (size_t t = 0; t < R; ++t) {
-    int rc = forward_on(p, tr->obs + t * IN * n, a, st);
+    SampleArgs sa;
+    sa.seed = s->seed;
+    sa.log_std = logstd;
+    sa.actions = tr->actions + t * 2 * n;
+    sa.logp = tr->logp + t * n;
+    sa.value = tr->value + t * n;
+    sa.step_add = (int64_t)iteration * (int64_t)R + (int64_t)t;
+    int rc = forward_on(p, tr->obs + t * IN * n, a, st, &sa, 0);
     if (rc) return rc;
-    launch_sample((int)n, s->seed, a->o, logstd, tr->actions + t * 2 * n, tr->logp + t * n, tr->value + t * n, 0,
-                  nullptr, (int64_t)iteration * (int64_t)R + (int64_t)t, st);
     if ((rc = sim_step_on(s, tr->actions + t * 2 * n, tr->reward + t * n, tr->done + t * n, tr->obs + (t + 1) * IN * n,
                           nullptr, st)))
       return rc;
@@ -609,10 +620,17 @@ int racer_trainer_update(racer_trainer* tr, racer_policy* p, float* kl) {
 
 static int runner_step_on(racer_sim* s, racer_policy* p, racer_acts* a, float* scratch, int det,
                           const int64_t* base, int64_t add, cudaStream_t st) {
-  const float* logstd = policy_theta(p) + policy_params(p) - 2;
-  int rc = forward_on(p, s->obs, a, st);
+  SampleArgs sa;
+  sa.seed = s->seed;
+  sa.log_std = policy_theta(p) + policy_params(p) - 2;
+  sa.actions = s->actions;
+  sa.logp = scratch;
+  sa.value = scratch + s->n;
+  sa.deterministic = det;
+  sa.step_base = base;
+  sa.step_add = add;
+  int rc = forward_on(p, s->obs, a, st, &sa, 0);
   if (rc) return rc;
-  launch_sample(s->n, s->seed, a->o, logstd, s->actions, scratch, scratch + s->n, det, base, add, st);
   return sim_step_on(s, s->actions, s->reward, s->done, s->obs, nullptr, st);
 }
 

@@ -1,0 +1,243 @@
+// Policy forward on the tcgen05 tensor cores (racer/ppo.mojo:108-111), BF16
+// operands with FP32 accumulation in TMEM, all three layers fused per tile of
+// 128 samples:
+//
+//   layer 1  D[128, 64]  = X^T[128, IN] . W0^T   (K = IN padded to 64k)
+//   layer 2  D[128, 64]  = [h1 | 1][128, 128] . W1^T (K = 65 padded to 128)
+//   layer 3  D[128, 16]  = [h2 | 1][128, 128] . W2^T (N = 3 padded to 16)
+//
+// X arrives feature-major FP32 [IN, cols] (the reference's layout); the CTA's
+// four warps load it coalesced along the samples, convert to BF16 and store
+// the transposed K-major tile into 128B-swizzled shared memory (two stages,
+// overlapped with the MMAs of the previous k-block). W0 k-blocks and the
+// whole of W1/W2 come from pre-swizzled BF16 copies made by k_pack_weights
+// whenever theta changes. One thread issues the MMAs; tcgen05.commit signals
+// an mbarrier; every thread then reads its row of the accumulator with
+// tcgen05.ld, applies tanh and writes the next layer's operand. The last
+// epilogue can sample the Gaussian actions in place (racer/sim.mojo:337-346),
+// saving a launch per environment step.
+//
+// Built with --fmad=false so the fused sampling matches the standalone kernel.
+#include <cuda_bf16.h>
+
+#include "common.cuh"
+#include "mlp_tc.h"
+#include "sample.cuh"
+#include "tc.cuh"
+
+namespace racer {
+namespace {
+
+constexpr int TILE = 128;
+constexpr int A_BYTES = TILE * 128;  // 128 rows x 64 bf16
+constexpr int B_BYTES = 64 * 128;    // 64 rows x 64 bf16
+constexpr int OFF_A = 0;
+constexpr int OFF_B = OFF_A + 2 * A_BYTES;
+constexpr int OFF_H = OFF_B + 2 * B_BYTES;
+constexpr int OFF_W1 = OFF_H + 2 * A_BYTES;
+constexpr int OFF_W2 = OFF_W1 + 2 * B_BYTES;
+constexpr int OFF_BAR = OFF_W2 + 2 * 16 * 128;
+// + alignment slack, + 16 KB so that every descriptor-addressed read stays inside the allocation
+constexpr int SMEM_BYTES = OFF_BAR + 64 + 1024 + 16384;
+
+__global__ void __launch_bounds__(TILE) k_mlp_fwd(const float* __restrict__ x, int in, int cols,
+                                                  const uint4* __restrict__ w0s, int kblocks,
+                                                  const uint4* __restrict__ w1s, const uint4* __restrict__ w2s,
+                                                  float* h1g, float* h2g, float* og, int write_hidden,
+                                                  SampleArgs sa, int* err) {
+  extern __shared__ uint8_t smem_raw[];
+  const uint32_t raw = tc::smem_u32(smem_raw);
+  uint8_t* smem = smem_raw + (((raw + 1023u) & ~1023u) - raw);
+  uint8_t* As = smem + OFF_A;
+  uint8_t* Bs = smem + OFF_B;
+  uint8_t* Hs = smem + OFF_H;
+  uint64_t* bars = reinterpret_cast<uint64_t*>(smem + OFF_BAR);
+  uint32_t* tslot = reinterpret_cast<uint32_t*>(smem + OFF_BAR + 32);
+
+  const int tid = threadIdx.x, warp = tid >> 5;
+  const int c = blockIdx.x * TILE + tid;
+  const bool live = c < cols;
+
+  if (tid == 0) {
+    tc::mbar_init(&bars[0], 1);
+    tc::mbar_init(&bars[1], 1);
+    tc::mbar_init(&bars[2], 1);
+    tc::fence_barrier_init();
+  }
+  if (warp == 0) {
+    tc::tmem_alloc(tslot, 64);
+    tc::tmem_relinquish();
+  }
+  {  // W1 (2 x 8 KB) and W2 (2 x 2 KB), resident for the whole tile
+    uint4* w1 = reinterpret_cast<uint4*>(smem + OFF_W1);
+    uint4* w2 = reinterpret_cast<uint4*>(smem + OFF_W2);
+    for (int e = tid; e < 2 * B_BYTES / 16; e += TILE) w1[e] = __ldg(w1s + e);
+    for (int e = tid; e < 2 * 16 * 128 / 16; e += TILE) w2[e] = __ldg(w2s + e);
+  }
+  tc::fence_proxy_async_smem();
+  tc::tc_fence_before();
+  __syncthreads();
+  tc::tc_fence_after();
+  const uint32_t tmem = *tslot;
+  const uint32_t trow = tmem + ((uint32_t)(warp * 32) << 16);
+  const uint32_t id64 = tc::idesc_bf16(TILE, 64), id16 = tc::idesc_bf16(TILE, 16);
+  bool ok = true;
+
+  // ---- layer 1: K loop over 64-wide blocks of the inputs, two smem stages ----
+  for (int kb = 0; kb < kblocks; ++kb) {
+    const int s = kb & 1;
+    if (kb >= 2 && !tc::mbar_wait(&bars[s], ((kb - 2) >> 1) & 1)) ok = false;
+    uint8_t* A = As + s * A_BYTES;
+    float v[64];
+#pragma unroll
+    for (int q = 0; q < 64; ++q) {
+      int f = kb * 64 + q;
+      v[q] = (live && f < in) ? __ldg(x + (long)f * cols + c) : 0.0f;
+    }
+#pragma unroll
+    for (int j = 0; j < 8; ++j) {
+      uint4 pk = make_uint4(tc::pack_bf16(v[8 * j], v[8 * j + 1]), tc::pack_bf16(v[8 * j + 2], v[8 * j + 3]),
+                            tc::pack_bf16(v[8 * j + 4], v[8 * j + 5]), tc::pack_bf16(v[8 * j + 6], v[8 * j + 7]));
+      *reinterpret_cast<uint4*>(A + tid * 128 + ((j ^ (tid & 7)) << 4)) = pk;
+    }
+    uint4* B = reinterpret_cast<uint4*>(Bs + s * B_BYTES);
+    const uint4* src = w0s + (long)kb * (B_BYTES / 16);
+    for (int e = tid; e < B_BYTES / 16; e += TILE) B[e] = __ldg(src + e);
+    tc::fence_proxy_async_smem();
+    tc::tc_fence_before();
+    __syncthreads();
+    if (tid == 0) {
+      tc::tc_fence_after();
+      const uint32_t a = tc::smem_u32(A), b = tc::smem_u32(Bs + s * B_BYTES);
+#pragma unroll
+      for (int k = 0; k < 4; ++k)
+        tc::mma_bf16(tmem, tc::sdesc_sw128(a + 32 * k), tc::sdesc_sw128(b + 32 * k), id64, (kb | k) ? 1u : 0u);
+      tc::mma_commit(&bars[s]);
+    }
+  }
+  {
+    const int last = kblocks - 1;
+    if (!tc::mbar_wait(&bars[last & 1], (last >> 1) & 1)) ok = false;
+  }
+  tc::tc_fence_after();
+
+  float acc[64];
+  // ---- epilogues 1 and 2: tanh, then the next layer's K-major operand [h | 1 | 0...] ----
+  for (int layer = 0; layer < 2; ++layer) {
+#pragma unroll
+    for (int q = 0; q < 4; ++q) tc::tmem_ld16(trow + 16 * q, acc + 16 * q);
+    tc::tmem_wait_ld();
+#pragma unroll
+    for (int q = 0; q < 64; ++q) acc[q] = tc::tanh_fast(acc[q]);
+#pragma unroll
+    for (int j = 0; j < 8; ++j) {
+      uint4 pk = make_uint4(tc::pack_bf16(acc[8 * j], acc[8 * j + 1]), tc::pack_bf16(acc[8 * j + 2], acc[8 * j + 3]),
+                            tc::pack_bf16(acc[8 * j + 4], acc[8 * j + 5]),
+                            tc::pack_bf16(acc[8 * j + 6], acc[8 * j + 7]));
+      *reinterpret_cast<uint4*>(Hs + tid * 128 + ((j ^ (tid & 7)) << 4)) = pk;
+      uint4 hi = j == 0 ? make_uint4(tc::pack_bf16(1.0f, 0.0f), 0u, 0u, 0u) : make_uint4(0u, 0u, 0u, 0u);
+      *reinterpret_cast<uint4*>(Hs + A_BYTES + tid * 128 + ((j ^ (tid & 7)) << 4)) = hi;
+    }
+    if (write_hidden && live) {
+      float* hg = layer == 0 ? h1g : h2g;
+#pragma unroll
+      for (int q = 0; q < 64; ++q) hg[(long)q * cols + c] = acc[q];
+    }
+    tc::fence_proxy_async_smem();
+    tc::tc_fence_before();
+    __syncthreads();
+    if (tid == 0) {
+      tc::tc_fence_after();
+      const uint32_t h = tc::smem_u32(Hs);
+      const uint32_t w = tc::smem_u32(smem + (layer == 0 ? OFF_W1 : OFF_W2));
+      const uint32_t wstride = layer == 0 ? B_BYTES : 16 * 128;
+#pragma unroll
+      for (int kb = 0; kb < 2; ++kb)
+#pragma unroll
+        for (int k = 0; k < 4; ++k)
+          tc::mma_bf16(tmem, tc::sdesc_sw128(h + kb * A_BYTES + 32 * k), tc::sdesc_sw128(w + kb * wstride + 32 * k),
+                       layer == 0 ? id64 : id16, (kb | k) ? 1u : 0u);
+      tc::mma_commit(&bars[2]);
+    }
+    if (!tc::mbar_wait(&bars[2], layer)) ok = false;
+    tc::tc_fence_after();
+  }
+
+  // ---- epilogue 3: the three outputs, optionally the sampled actions ----
+  float o[4];
+  tc::tmem_ld4(trow, o);
+  tc::tmem_wait_ld();
+  if (live) {
+    og[c] = o[0];
+    og[(long)cols + c] = o[1];
+    og[2L * cols + c] = o[2];
+    if (sa.actions) {
+      int64_t step = (sa.step_base ? *sa.step_base : 0) + sa.step_add;
+      sample_car(cols, c, sa.seed, o[0], o[1], o[2], sa.log_std, sa.actions, sa.logp, sa.value, sa.deterministic,
+                 step);
+    }
+  }
+  tc::tc_fence_before();
+  __syncthreads();
+  if (warp == 0) tc::tmem_dealloc(tmem, 64);
+  if (!ok && tid == 0) atomicExch(err, 1);
+}
+
+// theta -> pre-swizzled BF16 operand images: W0 [kblocks][64 x 64], W1 [2][64 x 64] (K = 65 padded),
+// W2 [2][16 x 64] (rows 3..15 and K >= 65 zero).
+__global__ void k_pack_weights(const float* __restrict__ theta, int in, int kblocks, __nv_bfloat16* w0s,
+                               __nv_bfloat16* w1s, __nv_bfloat16* w2s) {
+  const long n0 = (long)kblocks * 64 * 64, n1 = 2L * 64 * 64, n2 = 2L * 16 * 64;
+  const int w1 = H * in, w2 = w1 + H * HA;
+  for (long e = (long)blockIdx.x * blockDim.x + threadIdx.x; e < n0 + n1 + n2; e += (long)gridDim.x * blockDim.x) {
+    if (e < n0) {
+      int kb = (int)(e / 4096), r = (int)((e / 64) % 64), kk = (int)(e % 64), k = kb * 64 + kk;
+      float v = k < in ? theta[(long)r * in + k] : 0.0f;
+      w0s[((long)kb * 8192 + tc::sw128_offset(r, kk)) / 2] = __float2bfloat16_rn(v);
+    } else if (e < n0 + n1) {
+      long f = e - n0;
+      int kb = (int)(f / 4096), r = (int)((f / 64) % 64), kk = (int)(f % 64), k = kb * 64 + kk;
+      float v = k < HA ? theta[w1 + r * HA + k] : 0.0f;
+      w1s[((long)kb * 8192 + tc::sw128_offset(r, kk)) / 2] = __float2bfloat16_rn(v);
+    } else {
+      long f = e - n0 - n1;
+      int kb = (int)(f / 1024), r = (int)((f / 64) % 16), kk = (int)(f % 64), k = kb * 64 + kk;
+      float v = (r < OUT && k < HA) ? theta[w2 + r * HA + k] : 0.0f;
+      w2s[((long)kb * 2048 + tc::sw128_offset(r, kk)) / 2] = __float2bfloat16_rn(v);
+    }
+  }
+}
+
+}  // namespace
+
+size_t mlp_pack_bytes(int in) {
+  int kb = (in + 63) / 64;
+  return (size_t)kb * 8192 + 2 * 8192 + 2 * 2048;
+}
+
+void launch_pack_weights(const float* theta, int in, uint8_t* pack, cudaStream_t st) {
+  int kb = (in + 63) / 64;
+  auto* w0 = reinterpret_cast<__nv_bfloat16*>(pack);
+  auto* w1 = reinterpret_cast<__nv_bfloat16*>(pack + (size_t)kb * 8192);
+  auto* w2 = reinterpret_cast<__nv_bfloat16*>(pack + (size_t)kb * 8192 + 2 * 8192);
+  k_pack_weights<<<152, 256, 0, st>>>(theta, in, kb, w0, w1, w2);
+}
+
+cudaError_t launch_mlp_fwd(const float* x, int in, int cols, const uint8_t* pack, float* h1, float* h2, float* o,
+                           int write_hidden, const SampleArgs& sa, int* err, cudaStream_t st) {
+  static bool configured = false;
+  if (!configured) {
+    cudaError_t e = cudaFuncSetAttribute(k_mlp_fwd, cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM_BYTES);
+    if (e != cudaSuccess) return e;
+    configured = true;
+  }
+  int kb = (in + 63) / 64;
+  const uint4* w0 = reinterpret_cast<const uint4*>(pack);
+  const uint4* w1 = reinterpret_cast<const uint4*>(pack + (size_t)kb * 8192);
+  const uint4* w2 = reinterpret_cast<const uint4*>(pack + (size_t)kb * 8192 + 2 * 8192);
+  k_mlp_fwd<<<(cols + TILE - 1) / TILE, TILE, SMEM_BYTES, st>>>(x, in, cols, w0, kb, w1, w2, h1, h2, o, write_hidden,
+                                                                  sa, err);
+  return cudaGetLastError();
+}
+
+}  // namespace racer

@@ -1,0 +1,26 @@
+// tcgen05 policy forward (mlp_tc.cu).
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+namespace racer {
+
+// Optional Gaussian sampling fused into the forward's epilogue
+// (racer/sim.mojo:337-346); disabled when actions is null.
+struct SampleArgs {
+  uint64_t seed = 0;
+  const float* log_std = nullptr;
+  float* actions = nullptr;
+  float* logp = nullptr;
+  float* value = nullptr;
+  int deterministic = 0;
+  const int64_t* step_base = nullptr;
+  int64_t step_add = 0;
+};
+
+size_t mlp_pack_bytes(int in);
+void launch_pack_weights(const float* theta, int in, uint8_t* pack, cudaStream_t st);
+cudaError_t launch_mlp_fwd(const float* x, int in, int cols, const uint8_t* pack, float* h1, float* h2, float* o,
+                           int write_hidden, const SampleArgs& sa, int* err, cudaStream_t st);
+
+}  // namespace racer

@@ -11,6 +11,8 @@ struct racer_policy {
   int in = 0, p = 0;
   float* theta = nullptr;
   float* scratch = nullptr;  // split-K partials of the weight gradients
+  uint8_t* pack = nullptr;   // pre-swizzled BF16 operand images of W0, W1, W2
+  int* err = nullptr;        // device error word of the tensor-core kernels
   cudaStream_t st = nullptr;
   bool owned = false;
 };
@@ -28,6 +30,9 @@ int policy_new(int in_rows, void* stream, racer_policy** out) {
   RACER_TRY(cudaMalloc((void**)&p->theta, (size_t)p->p * sizeof(float)));
   RACER_TRY(cudaMemset(p->theta, 0, (size_t)p->p * sizeof(float)));
   RACER_TRY(cudaMalloc((void**)&p->scratch, backward_scratch_floats(in_rows, 0) * sizeof(float)));
+  RACER_TRY(cudaMalloc((void**)&p->pack, mlp_pack_bytes(in_rows)));
+  RACER_TRY(cudaMalloc((void**)&p->err, sizeof(int)));
+  RACER_TRY(cudaMemset(p->err, 0, sizeof(int)));
   *out = p;
   return 0;
 }
@@ -36,6 +41,8 @@ void policy_delete(racer_policy* p) {
   if (!p) return;
   cudaFree(p->theta);
   cudaFree(p->scratch);
+  cudaFree(p->pack);
+  cudaFree(p->err);
   if (p->owned) cudaStreamDestroy(p->st);
   delete p;
 }
@@ -46,21 +53,29 @@ int policy_inputs(racer_policy* p) { return p->in; }
 cudaStream_t policy_stream(racer_policy* p) { return p->st; }
 int policy_refresh(racer_policy* p) { return policy_refresh_on(p, p->st); }
 int policy_refresh_on(racer_policy* p, cudaStream_t st) {
-  (void)p;
-  (void)st;
+  launch_pack_weights(p->theta, p->in, p->pack, st);
+  cudaError_t err = cudaGetLastError();
+  if (err != cudaSuccess) {
+    racer_host::set_error(std::string("policy weight pack: ") + cudaGetErrorString(err));
+    return 2;
+  }
   return 0;
 }
 
-int policy_forward(racer_policy* p, const float* x, int cols, float* h1, float* h2, float* o, cudaStream_t st) {
-  const int in = p->in, w1 = H * in, w2 = w1 + H * HA;
-  launch_sgemm(p->theta, in, x, cols, h1, cols, H, cols, in, 1, st);
-  launch_sgemm(p->theta + w1, HA, h1, cols, h2, cols, H, cols, HA, 1, st);
-  launch_sgemm(p->theta + w2, HA, h2, cols, o, cols, OUT, cols, HA, 0, st);
-  cudaError_t err = cudaGetLastError();
+int policy_forward(racer_policy* p, const float* x, int cols, float* h1, float* h2, float* o, int write_hidden,
+                   const SampleArgs* sa, cudaStream_t st) {
+  SampleArgs none;
+  cudaError_t err = launch_mlp_fwd(x, p->in, cols, p->pack, h1, h2, o, write_hidden, sa ? *sa : none, p->err, st);
   if (err != cudaSuccess) {
     racer_host::set_error(std::string("policy forward: ") + cudaGetErrorString(err));
     return 2;
   }
+  return 0;
+}
+
+int policy_status(racer_policy* p, int* code) {
+  RACER_TRY(cudaStreamSynchronize(p->st));
+  RACER_TRY(cudaMemcpy(code, p->err, sizeof(int), cudaMemcpyDeviceToHost));
   return 0;
 }
 

@@ -19,6 +19,7 @@
 #include "kernels.h"
 #include "philox.h"
 #include "rmath.h"
+#include "sample.cuh"
 
 namespace racer {
 namespace {
@@ -298,17 +299,8 @@ __global__ void k_sample(int n, uint64_t seed, const float* output, const float*
   int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
   int64_t step = (step_base ? *step_base : 0) + step_add;
-  float noise[4];
-  philox::normal4(seed + 1, (uint64_t)i, (uint64_t)step, noise);
-  float probability = 0.0f;
-  for (int a = 0; a < 2; ++a) {
-    float z = deterministic ? 0.0f : noise[a];
-    float ls = log_std[a];
-    actions[(long)a * n + i] = output[(long)a * n + i] + rmath::expf_(ls) * z;
-    probability -= ((0.5f * z) * z + ls) + HALF_LOG_2PI;
-  }
-  logp[i] = probability;
-  value[i] = output[2L * n + i];
+  sample_car(n, i, seed, output[i], output[(long)n + i], output[2L * n + i], log_std, actions, logp, value,
+             deterministic, step);
 }
 
 __global__ void k_add_i64(int64_t* p, int64_t v) {

@@ -162,6 +162,12 @@ class Policy:
     def sync(self):
         call("racer_policy_sync", self.handle)
 
+    def status(self):
+        """Error word of the tensor-core kernels (0 = none)."""
+        code = ctypes.c_int()
+        call("racer_policy_status", self.handle, ctypes.byref(code))
+        return code.value
+
     def forward(self, x, acts):
         call("racer_policy_forward", self.handle, x.c, acts.handle)
 

@@ -87,6 +87,7 @@ struct racer_sim {
   float* d_track = nullptr;
   float2* d_cl = nullptr;
   float2* beam_dir = nullptr;
+  float4* ray = nullptr;  // [2, n] per-car lidar frame written by the physics kernel
   float *state = nullptr, *obs = nullptr, *actions = nullptr, *reward = nullptr, *done = nullptr;
   int64_t* step_base = nullptr;
   cudaStream_t st = nullptr;
@@ -194,7 +195,7 @@ int racer_sim_create(const float* track, size_t len, int n, uint64_t seed, int b
   if ((rc = dalloc(&s->d_track, len)) || (rc = dalloc(&s->d_cl, cl.size())) || (rc = dalloc(&s->beam_dir, beams)) ||
       (rc = dalloc(&s->state, (size_t)STATE * n)) || (rc = dalloc(&s->obs, (size_t)s->in_rows * n)) ||
       (rc = dalloc(&s->actions, 2 * (size_t)n)) || (rc = dalloc(&s->reward, n)) || (rc = dalloc(&s->done, n)) ||
-      (rc = dalloc(&s->step_base, 1))) {
+      (rc = dalloc(&s->step_base, 1)) || (rc = dalloc(&s->ray, 2 * (size_t)n))) {
     racer_sim_destroy(s);
     return rc;
   }
@@ -217,6 +218,7 @@ int racer_sim_create(const float* track, size_t len, int n, uint64_t seed, int b
   t.x0 = track[2];
   t.y0 = track[3];
   t.cell = track[4];
+  t.inv_cell = 1.0f / track[4];
   t.spacing = track[6];
   t.slope = track[8];
   t.nxf = (float)nx;
@@ -232,6 +234,7 @@ int racer_sim_destroy(racer_sim* s) {
   cudaFree(s->d_track);
   cudaFree(s->d_cl);
   cudaFree(s->beam_dir);
+  cudaFree(s->ray);
   cudaFree(s->state);
   cudaFree(s->obs);
   cudaFree(s->actions);
@@ -256,8 +259,8 @@ int racer_sim_get_buffers(racer_sim* s, racer_sim_buffers* out) {
 
 static int sim_step_on(racer_sim* s, const float* actions, float* reward, float* done, float* obs, int32_t* iters,
                        cudaStream_t st) {
-  launch_advance(s->t, s->state, actions, reward, done, obs, s->n, s->beams, s->seed, st);
-  launch_lidar(s->t, s->state, obs, s->n, s->beams, s->beam_dir, iters, st);
+  launch_advance(s->t, s->state, actions, reward, done, obs, s->n, s->beams, s->seed, s->ray, st);
+  launch_lidar(s->t, s->ray, obs, s->n, s->beams, s->beam_dir, iters, st);
   RACER_LAUNCHED();
   return 0;
 }
@@ -712,9 +715,9 @@ int racer_sim_profile(racer_sim* s, const float* actions, int reps, float* physi
   for (auto& e : ev) RACER_TRY(cudaEventCreate(&e));
   for (int r = 0; r < reps; ++r) {
     RACER_TRY(cudaEventRecord(ev[3 * r], st));
-    launch_advance(s->t, s->state, actions, s->reward, s->done, s->obs, s->n, s->beams, s->seed, st);
+    launch_advance(s->t, s->state, actions, s->reward, s->done, s->obs, s->n, s->beams, s->seed, s->ray, st);
     RACER_TRY(cudaEventRecord(ev[3 * r + 1], st));
-    launch_lidar(s->t, s->state, s->obs, s->n, s->beams, s->beam_dir, nullptr, st);
+    launch_lidar(s->t, s->ray, s->obs, s->n, s->beams, s->beam_dir, nullptr, st);
     RACER_TRY(cudaEventRecord(ev[3 * r + 2], st));
   }
   RACER_LAUNCHED();
@@ -723,7 +726,7 @@ int racer_sim_profile(racer_sim* s, const float* actions, int reps, float* physi
   RACER_TRY(cudaMalloc((void**)&iters, (size_t)s->beams * s->n * sizeof(int32_t)));
   RACER_TRY(cudaMalloc((void**)&total, sizeof(unsigned long long)));
   RACER_TRY(cudaMemsetAsync(total, 0, sizeof(unsigned long long), st));
-  launch_lidar(s->t, s->state, s->obs, s->n, s->beams, s->beam_dir, iters, st);
+  launch_lidar(s->t, s->ray, s->obs, s->n, s->beams, s->beam_dir, iters, st);
   k_sum_i32<<<152, 256, 0, st>>>(iters, (long)s->beams * s->n, total);
   RACER_LAUNCHED();
   unsigned long long host_total = 0;

@@ -41,6 +41,7 @@ struct TrackDev {
   const float2* cl;
   int nx, ny, waypoints, layers;
   float x0, y0, cell, spacing, slope;
+  float inv_cell;  // RN(1 / cell), for the division-free cell index
   float nxf, nyf;
   long route;
 };

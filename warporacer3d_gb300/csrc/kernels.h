@@ -9,9 +9,10 @@ namespace racer {
 
 // sim.cu (bit-exact simulator kernels)
 void launch_spawn(const TrackDev& t, float* state, float* actions, int n, uint64_t seed, cudaStream_t st);
+// ray [2, n] float4: the per-car lidar frame the physics kernel leaves for the lidar.
 void launch_advance(const TrackDev& t, float* state, const float* actions, float* reward, float* done, float* obs,
-                    int n, int beams, uint64_t seed, cudaStream_t st);
-void launch_lidar(const TrackDev& t, const float* state, float* obs, int n, int beams, const float2* beam_dir,
+                    int n, int beams, uint64_t seed, float4* ray, cudaStream_t st);
+void launch_lidar(const TrackDev& t, const float4* ray, float* obs, int n, int beams, const float2* beam_dir,
                   int* iters, cudaStream_t st);
 int lidar_max_iters(const TrackDev& t);
 void launch_sample(int n, uint64_t seed, const float* output, const float* log_std, float* actions, float* logp,
@@ -40,5 +41,7 @@ void launch_sgemm(const float* A, int lda, const float* B, int ldb, float* C, in
 void launch_backward(int in, const float* theta, const float* x, int cols, const float* h1, const float* h2,
                      const float* d3, float* d2, float* d1, float* grad, float* scratch, cudaStream_t st);
 size_t backward_scratch_floats(int in, int cols);
+// Scratch floats launch_backward actually touches for these sizes (<= backward_scratch_floats).
+size_t backward_scratch_needed(int in, int cols);
 
 }  // namespace racer

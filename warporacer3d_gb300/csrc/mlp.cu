@@ -136,6 +136,20 @@ size_t backward_scratch_floats(int in, int cols) {
   return (size_t)2 * 152 * BM * BN;
 }
 
+// Floats of split-K partials one weight-gradient GEMM [M, N] over K uses (0 when unsplit).
+static size_t split_need(int M, int N, int K) {
+  int tiles = ((N + BN - 1) / BN) * ((M + BM - 1) / BM);
+  int splits = splits_for(K, tiles);
+  if (splits <= 1) return 0;
+  int kper = ((K + splits - 1) / splits + BK - 1) / BK * BK;
+  splits = (K + kper - 1) / kper;
+  return (size_t)splits * M * N;
+}
+
+size_t backward_scratch_needed(int in, int cols) {
+  return std::max(split_need(H, in, cols), std::max(split_need(H, HA, cols), split_need(OUT, HA, cols)));
+}
+
 // racer/ppo.mojo:113-138: d3 [3, cols] -> d2, d1 [HA, cols], grad[W0|W1|W2].
 void launch_backward(int in, const float* theta, const float* x, int cols, const float* h1, const float* h2,
                      const float* d3, float* d2, float* d1, float* grad, float* scratch, cudaStream_t st) {

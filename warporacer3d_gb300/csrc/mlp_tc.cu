@@ -29,158 +29,178 @@ namespace racer {
 namespace {
 
 constexpr int TILE = 128;
-constexpr int A_BYTES = TILE * 128;  // 128 rows x 64 bf16
-constexpr int B_BYTES = 64 * 128;    // 64 rows x 64 bf16
-constexpr int OFF_A = 0;
-constexpr int OFF_B = OFF_A + 2 * A_BYTES;
-constexpr int OFF_H = OFF_B + 2 * B_BYTES;
-constexpr int OFF_W1 = OFF_H + 2 * A_BYTES;
+constexpr int GROUPS = 4;                          // producer groups, one k-block in flight each
+constexpr int THREADS = (GROUPS * 4 + 1) * 32;     // 16 producer warps + 1 MMA warp
+constexpr int MMA_WARP = GROUPS * 4;
+constexpr int A_BYTES = TILE * 128;                // 128 rows x 64 bf16
+constexpr int B_BYTES = 64 * 128;                  // 64 rows x 64 bf16
+constexpr int OFF_A = 0;                           // GROUPS x A; H = [h | 1 | 0] reuses A[0], A[1]
+constexpr int OFF_B = OFF_A + GROUPS * A_BYTES;
+constexpr int OFF_W1 = OFF_B + GROUPS * B_BYTES;
 constexpr int OFF_W2 = OFF_W1 + 2 * B_BYTES;
 constexpr int OFF_BAR = OFF_W2 + 2 * 16 * 128;
-// + alignment slack, + 16 KB so that every descriptor-addressed read stays inside the allocation
-constexpr int SMEM_BYTES = OFF_BAR + 64 + 1024 + 16384;
+// + barriers, + alignment slack, + 16 KB so every descriptor-addressed read stays inside the allocation
+constexpr int SMEM_BYTES = OFF_BAR + 128 + 1024 + 16384;
 
-__global__ void __launch_bounds__(TILE) k_mlp_fwd(const float* __restrict__ x, int in, int cols,
-                                                  const uint4* __restrict__ w0s, int kblocks,
-                                                  const uint4* __restrict__ w1s, const uint4* __restrict__ w2s,
-                                                  float* h1g, float* h2g, float* og, int write_hidden,
-                                                  SampleArgs sa, int* err) {
+// Grid: one CTA per 128 samples. Warps 0-15 form four producer groups; group
+// g loads k-blocks g, g+4, g+8, ... of X (thread = sample row) and of W0 into
+// stage g, then arrives on full[g]. Warp 16 waits on full[kb % 4], issues the
+// four K=16 MMAs of the block and commits to empty[kb % 4]; after the last
+// block it commits to `done`. Warps 0-3 (TMEM lanes 0-127) then run the
+// epilogues and issue layers 2 and 3.
+__global__ void __launch_bounds__(THREADS, 1) k_mlp_fwd(const float* __restrict__ x, int in, int cols,
+                                                        const uint4* __restrict__ w0s, int kblocks,
+                                                        const uint4* __restrict__ w1s,
+                                                        const uint4* __restrict__ w2s, float* h1g, float* h2g,
+                                                        float* og, int write_hidden, SampleArgs sa, int* err) {
   extern __shared__ uint8_t smem_raw[];
   const uint32_t raw = tc::smem_u32(smem_raw);
   uint8_t* smem = smem_raw + (((raw + 1023u) & ~1023u) - raw);
-  uint8_t* As = smem + OFF_A;
-  uint8_t* Bs = smem + OFF_B;
-  uint8_t* Hs = smem + OFF_H;
-  uint64_t* bars = reinterpret_cast<uint64_t*>(smem + OFF_BAR);
-  uint32_t* tslot = reinterpret_cast<uint32_t*>(smem + OFF_BAR + 32);
+  uint64_t* full = reinterpret_cast<uint64_t*>(smem + OFF_BAR);
+  uint64_t* empty = full + GROUPS;
+  uint64_t* done = empty + GROUPS;
+  uint32_t* tslot = reinterpret_cast<uint32_t*>(done + 1);
 
   const int tid = threadIdx.x, warp = tid >> 5;
-  const int c = blockIdx.x * TILE + tid;
+  const int r = tid & (TILE - 1);  // sample row of a producer or epilogue thread
+  const int c = blockIdx.x * TILE + r;
   const bool live = c < cols;
 
   if (tid == 0) {
-    tc::mbar_init(&bars[0], 1);
-    tc::mbar_init(&bars[1], 1);
-    tc::mbar_init(&bars[2], 1);
+    for (int g = 0; g < GROUPS; ++g) {
+      tc::mbar_init(&full[g], TILE);
+      tc::mbar_init(&empty[g], 1);
+    }
+    tc::mbar_init(done, 1);
     tc::fence_barrier_init();
   }
-  if (warp == 0) {
+  if (warp == MMA_WARP) {
     tc::tmem_alloc(tslot, 64);
     tc::tmem_relinquish();
   }
   {  // W1 (2 x 8 KB) and W2 (2 x 2 KB), resident for the whole tile
     uint4* w1 = reinterpret_cast<uint4*>(smem + OFF_W1);
     uint4* w2 = reinterpret_cast<uint4*>(smem + OFF_W2);
-    for (int e = tid; e < 2 * B_BYTES / 16; e += TILE) w1[e] = __ldg(w1s + e);
-    for (int e = tid; e < 2 * 16 * 128 / 16; e += TILE) w2[e] = __ldg(w2s + e);
+    for (int e = tid; e < 2 * B_BYTES / 16; e += THREADS) w1[e] = __ldg(w1s + e);
+    for (int e = tid; e < 2 * 16 * 128 / 16; e += THREADS) w2[e] = __ldg(w2s + e);
   }
   tc::fence_proxy_async_smem();
   tc::tc_fence_before();
   __syncthreads();
   tc::tc_fence_after();
   const uint32_t tmem = *tslot;
-  const uint32_t trow = tmem + ((uint32_t)(warp * 32) << 16);
   const uint32_t id64 = tc::idesc_bf16(TILE, 64), id16 = tc::idesc_bf16(TILE, 16);
   bool ok = true;
 
-  // ---- layer 1: K loop over 64-wide blocks of the inputs, two smem stages ----
-  for (int kb = 0; kb < kblocks; ++kb) {
-    const int s = kb & 1;
-    if (kb >= 2 && !tc::mbar_wait(&bars[s], ((kb - 2) >> 1) & 1)) ok = false;
-    uint8_t* A = As + s * A_BYTES;
-    float v[64];
+  if (warp < MMA_WARP) {
+    // ---- producers: layer-1 operands, one k-block per group in flight ----
+    const int g = warp >> 2;
+    uint8_t* A = smem + OFF_A + g * A_BYTES;
+    uint4* B = reinterpret_cast<uint4*>(smem + OFF_B + g * B_BYTES);
+    for (int j = 0;; ++j) {
+      const int kb = g + GROUPS * j;
+      if (kb >= kblocks) break;
+      float v[64];
 #pragma unroll
-    for (int q = 0; q < 64; ++q) {
-      int f = kb * 64 + q;
-      v[q] = (live && f < in) ? __ldg(x + (long)f * cols + c) : 0.0f;
-    }
+      for (int q = 0; q < 64; ++q) {
+        const int f = kb * 64 + q;
+        v[q] = (live && f < in) ? __ldg(x + (long)f * cols + c) : 0.0f;
+      }
+      uint4 wb[4];
+      const uint4* src = w0s + (long)kb * (B_BYTES / 16);
 #pragma unroll
-    for (int j = 0; j < 8; ++j) {
-      uint4 pk = make_uint4(tc::pack_bf16(v[8 * j], v[8 * j + 1]), tc::pack_bf16(v[8 * j + 2], v[8 * j + 3]),
-                            tc::pack_bf16(v[8 * j + 4], v[8 * j + 5]), tc::pack_bf16(v[8 * j + 6], v[8 * j + 7]));
-      *reinterpret_cast<uint4*>(A + tid * 128 + ((j ^ (tid & 7)) << 4)) = pk;
+      for (int e = 0; e < 4; ++e) wb[e] = __ldg(src + r + e * TILE);
+      if (j >= 1 && !tc::mbar_wait(&empty[g], (j - 1) & 1)) ok = false;
+#pragma unroll
+      for (int q = 0; q < 8; ++q) {
+        uint4 pk = make_uint4(tc::pack_bf16(v[8 * q], v[8 * q + 1]), tc::pack_bf16(v[8 * q + 2], v[8 * q + 3]),
+                              tc::pack_bf16(v[8 * q + 4], v[8 * q + 5]), tc::pack_bf16(v[8 * q + 6], v[8 * q + 7]));
+        *reinterpret_cast<uint4*>(A + r * 128 + ((q ^ (r & 7)) << 4)) = pk;
+      }
+#pragma unroll
+      for (int e = 0; e < 4; ++e) B[r + e * TILE] = wb[e];
+      tc::fence_proxy_async_smem();
+      tc::mbar_arrive(&full[g]);
     }
-    uint4* B = reinterpret_cast<uint4*>(Bs + s * B_BYTES);
-    const uint4* src = w0s + (long)kb * (B_BYTES / 16);
-    for (int e = tid; e < B_BYTES / 16; e += TILE) B[e] = __ldg(src + e);
-    tc::fence_proxy_async_smem();
-    tc::tc_fence_before();
-    __syncthreads();
-    if (tid == 0) {
+  } else if ((tid & 31) == 0) {
+    // ---- MMA issuer: layer 1 ----
+    for (int kb = 0; kb < kblocks; ++kb) {
+      const int g = kb % GROUPS;
+      if (!tc::mbar_wait(&full[g], (kb / GROUPS) & 1)) ok = false;
       tc::tc_fence_after();
-      const uint32_t a = tc::smem_u32(A), b = tc::smem_u32(Bs + s * B_BYTES);
+      const uint32_t a = tc::smem_u32(smem + OFF_A + g * A_BYTES), b = tc::smem_u32(smem + OFF_B + g * B_BYTES);
 #pragma unroll
       for (int k = 0; k < 4; ++k)
         tc::mma_bf16(tmem, tc::sdesc_sw128(a + 32 * k), tc::sdesc_sw128(b + 32 * k), id64, (kb | k) ? 1u : 0u);
-      tc::mma_commit(&bars[s]);
+      tc::mma_commit(&empty[g]);
     }
+    tc::mma_commit(done);
   }
-  {
-    const int last = kblocks - 1;
-    if (!tc::mbar_wait(&bars[last & 1], (last >> 1) & 1)) ok = false;
-  }
-  tc::tc_fence_after();
 
-  float acc[64];
-  // ---- epilogues 1 and 2: tanh, then the next layer's K-major operand [h | 1 | 0...] ----
-  for (int layer = 0; layer < 2; ++layer) {
-#pragma unroll
-    for (int q = 0; q < 4; ++q) tc::tmem_ld16(trow + 16 * q, acc + 16 * q);
-    tc::tmem_wait_ld();
-#pragma unroll
-    for (int q = 0; q < 64; ++q) acc[q] = tc::tanh_fast(acc[q]);
-#pragma unroll
-    for (int j = 0; j < 8; ++j) {
-      uint4 pk = make_uint4(tc::pack_bf16(acc[8 * j], acc[8 * j + 1]), tc::pack_bf16(acc[8 * j + 2], acc[8 * j + 3]),
-                            tc::pack_bf16(acc[8 * j + 4], acc[8 * j + 5]),
-                            tc::pack_bf16(acc[8 * j + 6], acc[8 * j + 7]));
-      *reinterpret_cast<uint4*>(Hs + tid * 128 + ((j ^ (tid & 7)) << 4)) = pk;
-      uint4 hi = j == 0 ? make_uint4(tc::pack_bf16(1.0f, 0.0f), 0u, 0u, 0u) : make_uint4(0u, 0u, 0u, 0u);
-      *reinterpret_cast<uint4*>(Hs + A_BYTES + tid * 128 + ((j ^ (tid & 7)) << 4)) = hi;
-    }
-    if (write_hidden && live) {
-      float* hg = layer == 0 ? h1g : h2g;
-#pragma unroll
-      for (int q = 0; q < 64; ++q) hg[(long)q * cols + c] = acc[q];
-    }
-    tc::fence_proxy_async_smem();
-    tc::tc_fence_before();
-    __syncthreads();
-    if (tid == 0) {
-      tc::tc_fence_after();
-      const uint32_t h = tc::smem_u32(Hs);
-      const uint32_t w = tc::smem_u32(smem + (layer == 0 ? OFF_W1 : OFF_W2));
-      const uint32_t wstride = layer == 0 ? B_BYTES : 16 * 128;
-#pragma unroll
-      for (int kb = 0; kb < 2; ++kb)
-#pragma unroll
-        for (int k = 0; k < 4; ++k)
-          tc::mma_bf16(tmem, tc::sdesc_sw128(h + kb * A_BYTES + 32 * k), tc::sdesc_sw128(w + kb * wstride + 32 * k),
-                       layer == 0 ? id64 : id16, (kb | k) ? 1u : 0u);
-      tc::mma_commit(&bars[2]);
-    }
-    if (!tc::mbar_wait(&bars[2], layer)) ok = false;
+  if (warp < 4) {
+    // ---- epilogues (TMEM lanes 0-127 = sample rows): layers 2 and 3 ----
+    const uint32_t trow = tmem + ((uint32_t)(warp * 32) << 16);
+    uint8_t* Hs = smem + OFF_A;
+    if (!tc::mbar_wait(done, 0)) ok = false;
     tc::tc_fence_after();
-  }
-
-  // ---- epilogue 3: the three outputs, optionally the sampled actions ----
-  float o[4];
-  tc::tmem_ld4(trow, o);
-  tc::tmem_wait_ld();
-  if (live) {
-    og[c] = o[0];
-    og[(long)cols + c] = o[1];
-    og[2L * cols + c] = o[2];
-    if (sa.actions) {
-      int64_t step = (sa.step_base ? *sa.step_base : 0) + sa.step_add;
-      sample_car(cols, c, sa.seed, o[0], o[1], o[2], sa.log_std, sa.actions, sa.logp, sa.value, sa.deterministic,
-                 step);
+    float acc[64];
+    for (int layer = 0; layer < 2; ++layer) {
+#pragma unroll
+      for (int q = 0; q < 4; ++q) tc::tmem_ld16(trow + 16 * q, acc + 16 * q);
+      tc::tmem_wait_ld();
+#pragma unroll
+      for (int q = 0; q < 64; ++q) acc[q] = tc::tanh_fast(acc[q]);
+#pragma unroll
+      for (int q = 0; q < 8; ++q) {
+        uint4 pk = make_uint4(tc::pack_bf16(acc[8 * q], acc[8 * q + 1]), tc::pack_bf16(acc[8 * q + 2], acc[8 * q + 3]),
+                              tc::pack_bf16(acc[8 * q + 4], acc[8 * q + 5]),
+                              tc::pack_bf16(acc[8 * q + 6], acc[8 * q + 7]));
+        *reinterpret_cast<uint4*>(Hs + r * 128 + ((q ^ (r & 7)) << 4)) = pk;
+        uint4 hi = q == 0 ? make_uint4(tc::pack_bf16(1.0f, 0.0f), 0u, 0u, 0u) : make_uint4(0u, 0u, 0u, 0u);
+        *reinterpret_cast<uint4*>(Hs + A_BYTES + r * 128 + ((q ^ (r & 7)) << 4)) = hi;
+      }
+      if (write_hidden && live) {
+        float* hg = layer == 0 ? h1g : h2g;
+#pragma unroll
+        for (int q = 0; q < 64; ++q) hg[(long)q * cols + c] = acc[q];
+      }
+      tc::fence_proxy_async_smem();
+      tc::tc_fence_before();
+      tc::named_sync(1, TILE);
+      if (tid == 0) {
+        tc::tc_fence_after();
+        const uint32_t h = tc::smem_u32(Hs);
+        const uint32_t w = tc::smem_u32(smem + (layer == 0 ? OFF_W1 : OFF_W2));
+        const uint32_t wstride = layer == 0 ? B_BYTES : 16 * 128;
+#pragma unroll
+        for (int kb = 0; kb < 2; ++kb)
+#pragma unroll
+          for (int k = 0; k < 4; ++k)
+            tc::mma_bf16(tmem, tc::sdesc_sw128(h + kb * A_BYTES + 32 * k),
+                         tc::sdesc_sw128(w + kb * wstride + 32 * k), layer == 0 ? id64 : id16, (kb | k) ? 1u : 0u);
+        tc::mma_commit(done);
+      }
+      if (!tc::mbar_wait(done, (1 + layer) & 1)) ok = false;
+      tc::tc_fence_after();
+    }
+    float o[4];
+    tc::tmem_ld4(trow, o);
+    tc::tmem_wait_ld();
+    if (live) {
+      og[c] = o[0];
+      og[(long)cols + c] = o[1];
+      og[2L * cols + c] = o[2];
+      if (sa.actions) {
+        int64_t step = (sa.step_base ? *sa.step_base : 0) + sa.step_add;
+        sample_car(cols, c, sa.seed, o[0], o[1], o[2], sa.log_std, sa.actions, sa.logp, sa.value, sa.deterministic,
+                   step);
+      }
     }
   }
   tc::tc_fence_before();
   __syncthreads();
-  if (warp == 0) tc::tmem_dealloc(tmem, 64);
-  if (!ok && tid == 0) atomicExch(err, 1);
+  if (warp == MMA_WARP) tc::tmem_dealloc(tmem, 64);
+  if (!ok) atomicExch(err, 1);
 }
 
 // theta -> pre-swizzled BF16 operand images: W0 [kblocks][64 x 64], W1 [2][64 x 64] (K = 65 padded),
@@ -235,7 +255,7 @@ cudaError_t launch_mlp_fwd(const float* x, int in, int cols, const uint8_t* pack
   const uint4* w0 = reinterpret_cast<const uint4*>(pack);
   const uint4* w1 = reinterpret_cast<const uint4*>(pack + (size_t)kb * 8192);
   const uint4* w2 = reinterpret_cast<const uint4*>(pack + (size_t)kb * 8192 + 2 * 8192);
-  k_mlp_fwd<<<(cols + TILE - 1) / TILE, TILE, SMEM_BYTES, st>>>(x, in, cols, w0, kb, w1, w2, h1, h2, o, write_hidden,
+  k_mlp_fwd<<<(cols + TILE - 1) / TILE, THREADS, SMEM_BYTES, st>>>(x, in, cols, w0, kb, w1, w2, h1, h2, o, write_hidden,
                                                                   sa, err);
   return cudaGetLastError();
 }

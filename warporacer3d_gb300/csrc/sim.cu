@@ -41,13 +41,30 @@ __device__ __forceinline__ void slopes(const Surface& g, float heading, float* a
   *across = -g.sx * s + g.sy * c;
 }
 
+// floor((v - v0) / cell + 0.5), the reference's nearest-cell coordinate
+// (racer/sim.mojo:110-111), without the division in almost every case:
+// u' = (v - v0) * RN(1/cell) + 0.5 differs from the exact u by less than
+// delta = (|u'| + 1) * 2^-20 (the two quotients are within 3 * 2^-24 |q| of
+// each other and each + 0.5 rounds by half an ulp), so when u' is farther
+// than delta from an integer both floors agree; inside that band the IEEE
+// division decides. The result is bit-identical to the division form.
+__device__ __forceinline__ float cell_coord(float v, float v0, float cell, float inv_cell) {
+  float d = v - v0;
+  float u = d * inv_cell + 0.5f;
+  float fl = floorf(u);
+  float g = u - fl;
+  float delta = (fabsf(u) + 1.0f) * 9.5367431640625e-07f;
+  if (g > delta && g < 1.0f - delta) return fl;
+  return floorf(d / cell + 0.5f);
+}
+
 // Nearest-cell index (racer/sim.mojo:108-114); false off the map or for
 // non-finite coordinates.
 __device__ __forceinline__ bool cell_of(const TrackDev& t, float x, float y, long* idx) {
-  float fx = floorf((x - t.x0) / t.cell + 0.5f);
-  float fy = floorf((y - t.y0) / t.cell + 0.5f);
+  float fx = cell_coord(x, t.x0, t.cell, t.inv_cell);
+  float fy = cell_coord(y, t.y0, t.cell, t.inv_cell);
   if (!(fx >= 0.0f && fx < t.nxf && fy >= 0.0f && fy < t.nyf)) return false;
-  *idx = (long)fy * t.nx + (long)fx;
+  *idx = (long)((int)fy * t.nx + (int)fx);
   return true;
 }
 
@@ -175,7 +192,7 @@ __global__ void k_spawn(TrackDev t, float* state, float* actions, int n, uint64_
 // racer/sim.mojo:184-235: one 60 Hz step of car i.
 template <int LAYERS>
 __global__ void k_advance(TrackDev t, float* s, const float* act, float* reward, float* done, float* obs, int n,
-                          int beams, uint64_t seed) {
+                          int beams, uint64_t seed, float4* ray) {
   int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
   V4 p{s[(long)X * n + i], s[(long)Y * n + i], s[(long)HEADING * n + i], s[(long)SPEED * n + i]};
@@ -242,55 +259,66 @@ __global__ void k_advance(TrackDev t, float* s, const float* act, float* reward,
   obs[2L * n + i] = along;
   obs[3L * n + i] = across;
   obs[(long)(beams + 4) * n + i] = 1.0f;
+  // The lidar's per-car frame (racer/sim.mojo:243-249), from the values just
+  // written: origin = position + MOUNT_X forward + MOUNT_Z up, and the
+  // heading's cos/sin with the slopes that tilt the body plane.
+  float ch, sh;
+  rmath::sincosf_(heading, &sh, &ch);
+  ray[i] = make_float4((s[(long)X * n + i] + MOUNT_X * ch) + 0.0f, (s[(long)Y * n + i] + MOUNT_X * sh) + 0.0f,
+                       (s[(long)Z * n + i] + MOUNT_X * along) + MOUNT_Z, ch);
+  ray[n + i] = make_float4(sh, along, across, 0.0f);
 }
 
-// racer/sim.mojo:238-266, one thread per (car, beam). Block = 8 warps; warp w
-// marches 32 consecutive beams of car blockIdx.x * 8 + w, so the lanes of a
-// warp start at one origin and probe neighbouring cells.
+// racer/sim.mojo:238-266: the sphere-traced lidar, one thread per (car, beam).
+// Block = 8 warps; warp w marches 32 consecutive beams of car
+// blockIdx.x * 8 + w, so its lanes start at one origin and probe neighbouring
+// cells (L1 reuse) and finish after similar numbers of probes. The per-car
+// frame comes from the physics kernel (`ray`). Every floating-point operation
+// of a beam is the reference's, in its order; the nearest-cell index avoids
+// the division where that provably gives the same cell (cell_coord), and
+// floor/descent is skipped where min() cannot select it.
 template <int LAYERS>
-__global__ void __launch_bounds__(256) k_lidar(TrackDev t, const float* s, float* obs, int n, int beams,
-                                               const float2* beam_dir, int max_iters, int* iters) {
-  int i = blockIdx.x * 8 + (threadIdx.x >> 5);
-  int b = blockIdx.y * 32 + (threadIdx.x & 31);
-  if (i >= n || b >= beams) return;
-  float heading = s[(long)HEADING * n + i];
-  float sh, ch;
-  rmath::sincosf_(heading, &sh, &ch);
-  float fz = obs[2L * n + i], lz = obs[3L * n + i];
-  float2 az = __ldg(beam_dir + b);  // (cos azimuth, sin azimuth)
-  float dx = az.x * ch + az.y * -sh;
-  float dy = az.x * sh + az.y * ch;
-  float dz = az.x * fz + az.y * lz;
-  float norm = sqrtf((dx * dx + dz * dz) + (dy * dy + 0.0f));
+__global__ void __launch_bounds__(256) k_lidar(TrackDev t, const float4* __restrict__ ray, float* obs, int n,
+                                               int beams, const float2* __restrict__ beam_dir, int max_iters,
+                                               int* iters) {
+  const int car = blockIdx.x * 8 + (threadIdx.x >> 5);
+  const int beam = blockIdx.y * 32 + (threadIdx.x & 31);
+  if (car >= n || beam >= beams) return;
+  const float4 r0 = __ldg(ray + car), r1 = __ldg(ray + n + car);  // (ox, oy, oz, cos h), (sin h, along, across)
+  const float2 az = __ldg(beam_dir + beam);                        // (cos azimuth, sin azimuth)
+  float dx = az.x * r0.w + az.y * -r1.x;
+  float dy = az.x * r1.x + az.y * r0.w;
+  float dz = az.x * r1.y + az.y * r1.z;
+  const float norm = sqrtf((dx * dx + dz * dz) + (dy * dy + 0.0f));
   dx = dx / norm;
   dy = dy / norm;
   dz = dz / norm;
-  float ox = (s[(long)X * n + i] + MOUNT_X * ch) + 0.0f;
-  float oy = (s[(long)Y * n + i] + MOUNT_X * sh) + 0.0f;
-  float oz = (s[(long)Z * n + i] + MOUNT_X * fz) + MOUNT_Z;
-  float horizontal = sqrtf(dx * dx + dy * dy);
-  float descent = (1.5f * t.slope) * horizontal + fmaxf(-dz, 0.0f);
+  const float ox = r0.x, oy = r0.y, oz = r0.z;
+  const float descent = (1.5f * t.slope) * sqrtf(dx * dx + dy * dy) + fmaxf(-dz, 0.0f);
   const float cell = t.cell, min_step = 0.5f * t.cell;
   float tt = 0.0f, last = 0.0f, last_floor = 0.0f, range = -1.0f;
   int count = 0;
   while (tt < RANGE && count < max_iters) {
     ++count;
-    float px = ox + tt * dx, py = oy + tt * dy, pz = oz + tt * dz;
-    Spot spot = probe<LAYERS>(t, px, py, pz);
-    float floor_ = (pz - spot.height) - 0.03f;
-    if (floor_ < 0.0f) {
-      range = fminf(last + ((tt - last) * last_floor) / (last_floor - floor_), RANGE);
+    const float px = ox + tt * dx, py = oy + tt * dy, pz = oz + tt * dz;
+    const Spot spot = probe<LAYERS>(t, px, py, pz);
+    const float fl = (pz - spot.height) - 0.03f;
+    if (fl < 0.0f) {
+      range = fminf(last + ((tt - last) * last_floor) / (last_floor - fl), RANGE);
       break;
     }
-    float step = fminf(spot.clearance - cell, floor_ / descent);
+    const float a = spot.clearance - cell;
+    if (a < min_step) break;  // min(a, fl / descent) <= a < min_step
+    // for descent == 0 the quotient is +inf or NaN (fl >= 0 here) and fminf returns a
+    const float step = descent != 0.0f ? fminf(a, fl / descent) : a;
     if (step < min_step) break;
     last = tt;
-    last_floor = floor_;
+    last_floor = fl;
     tt += step;
   }
   if (range < 0.0f) range = fminf(tt, RANGE);
-  obs[(long)(4 + b) * n + i] = range / RANGE;
-  if (iters) iters[(long)b * n + i] = count;
+  obs[(long)(4 + beam) * n + car] = range / RANGE;
+  if (iters) iters[(long)beam * n + car] = count;
 }
 
 // racer/sim.mojo:323-348. step = *step_base (if given) + step_add.
@@ -315,28 +343,28 @@ void launch_spawn(const TrackDev& t, float* state, float* actions, int n, uint64
 }
 
 void launch_advance(const TrackDev& t, float* state, const float* actions, float* reward, float* done, float* obs,
-                    int n, int beams, uint64_t seed, cudaStream_t st) {
+                    int n, int beams, uint64_t seed, float4* ray, cudaStream_t st) {
   dim3 grid((n + 127) / 128);
   if (t.layers == 1)
-    k_advance<1><<<grid, 128, 0, st>>>(t, state, actions, reward, done, obs, n, beams, seed);
+    k_advance<1><<<grid, 128, 0, st>>>(t, state, actions, reward, done, obs, n, beams, seed, ray);
   else if (t.layers == 2)
-    k_advance<2><<<grid, 128, 0, st>>>(t, state, actions, reward, done, obs, n, beams, seed);
+    k_advance<2><<<grid, 128, 0, st>>>(t, state, actions, reward, done, obs, n, beams, seed, ray);
   else
-    k_advance<0><<<grid, 128, 0, st>>>(t, state, actions, reward, done, obs, n, beams, seed);
+    k_advance<0><<<grid, 128, 0, st>>>(t, state, actions, reward, done, obs, n, beams, seed, ray);
 }
 
 int lidar_max_iters(const TrackDev& t) { return (int)ceilf(RANGE / (0.5f * t.cell)) + 2; }
 
-void launch_lidar(const TrackDev& t, const float* state, float* obs, int n, int beams, const float2* beam_dir,
+void launch_lidar(const TrackDev& t, const float4* ray, float* obs, int n, int beams, const float2* beam_dir,
                   int* iters, cudaStream_t st) {
   dim3 grid((n + 7) / 8, (beams + 31) / 32);
   int cap = lidar_max_iters(t);
   if (t.layers == 1)
-    k_lidar<1><<<grid, 256, 0, st>>>(t, state, obs, n, beams, beam_dir, cap, iters);
+    k_lidar<1><<<grid, 256, 0, st>>>(t, ray, obs, n, beams, beam_dir, cap, iters);
   else if (t.layers == 2)
-    k_lidar<2><<<grid, 256, 0, st>>>(t, state, obs, n, beams, beam_dir, cap, iters);
+    k_lidar<2><<<grid, 256, 0, st>>>(t, ray, obs, n, beams, beam_dir, cap, iters);
   else
-    k_lidar<0><<<grid, 256, 0, st>>>(t, state, obs, n, beams, beam_dir, cap, iters);
+    k_lidar<0><<<grid, 256, 0, st>>>(t, ray, obs, n, beams, beam_dir, cap, iters);
 }
 
 void launch_sample(int n, uint64_t seed, const float* output, const float* log_std, float* actions, float* logp,

@@ -96,6 +96,19 @@ int racer_policy_forward(racer_policy* policy, const float* x_dev, racer_acts* a
  * W0/W1/W2 entries of grad [P]. */
 int racer_policy_backward(racer_policy* policy, const float* x_dev, racer_acts* acts, const float* d3_dev,
                           float* d2_dev, float* d1_dev, float* grad_dev);
+/* Policy.backward for callers that cannot allocate device memory (their
+ * device memory belongs to another runtime's allocator, such as a Mojo/MAX
+ * DeviceContext, or to a fixed up-front budget). It has no counterpart in the
+ * reference. Every buffer is the caller's: theta [P] for IN = beams + 5,
+ * x [IN, cols], h1/h2 [65, cols] from a forward, d3 [3, cols]; it writes
+ * d2, d1 [65, cols] and the W0/W1/W2 entries of grad [P], the same values as
+ * racer_policy_backward. The split-K scratch is a 4.75 MiB array inside the
+ * library (one per GPU, held until exit); no call allocates or frees. The
+ * first call on a device resolves the array's address (make it before any
+ * stream capture); calls that overlap on the GPU race on the array. */
+int racer_policy_backward_noalloc(int beams, const float* theta_dev, const float* x_dev, int cols,
+                                  const float* h1_dev, const float* h2_dev, const float* d3_dev, float* d2_dev,
+                                  float* d1_dev, float* grad_dev, void* stream);
 /* Error word of the policy's tensor-core kernels (0 = none; nonzero when a
  * bounded wait on the tensor core timed out). Synchronises the policy's stream. */
 int racer_policy_status(racer_policy* policy, int* code);

@@ -53,6 +53,8 @@ SIGNATURES = {
     "racer_acts_buffers": [c_void_p, P(c_void_p), P(c_void_p), P(c_void_p)],
     "racer_policy_forward": [c_void_p, c_void_p, c_void_p],
     "racer_policy_backward": [c_void_p, c_void_p, c_void_p, c_void_p, c_void_p, c_void_p, c_void_p],
+    "racer_policy_backward_noalloc": [c_int, c_void_p, c_void_p, c_int, c_void_p, c_void_p, c_void_p, c_void_p,
+                                      c_void_p, c_void_p, c_void_p],
     "racer_policy_status": [c_void_p, P(c_int)],
     "racer_policy_save": [c_void_p, ctypes.c_char_p, c_int],
     "racer_policy_load": [c_void_p, ctypes.c_char_p, P(c_int)],

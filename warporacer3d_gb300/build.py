@@ -27,6 +27,7 @@ UNITS = {
     "mlp_tc.cu": EXACT,
     "policy.cu": [],
     "api.cu": [],
+    "noalloc.cu": [],
 }
 
 

@@ -146,6 +146,15 @@ int racer_runner_step(racer_sim* sim, racer_policy* policy, racer_acts* acts, fl
 int racer_rollout(racer_sim* sim, racer_policy* policy, racer_acts* acts, float* scratch_dev, int steps,
                   int deterministic, int64_t step0);
 
+/* ---- dense products (Device.gemm with transpose_b, racer/device.mojo:82-98) ---- */
+/* C[M, N] (float32, row-major, ldc) = A[M, K] . B[N, K]^T on the tcgen05 tensor
+ * cores with BF16 operands (row-major, K contiguous, lda/ldb multiples of 8,
+ * 16-byte aligned) and FP32 accumulation. splits > 1 divides K across CTAs and
+ * needs scratch_dev of splits * M * N floats. err_dev (int, device) is set
+ * nonzero if a bounded wait inside the kernel timed out. */
+int racer_gemm_bf16(const void* a_dev, const void* b_dev, float* c_dev, int M, int N, int K, int lda, int ldb,
+                    int ldc, int splits, float* scratch_dev, int* err_dev, void* stream);
+
 /* ---- measurement ---- */
 /* Kernel launches in the CUDA graph racer_rollout replays for these arguments
  * (captured here if needed), plus the one launch that sets its step offset. */

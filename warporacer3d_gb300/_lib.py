@@ -66,7 +66,9 @@ SIGNATURES = {
     "racer_trainer_minibatch": [c_void_p, c_void_p, c_int, c_float, c_float],
     "racer_runner_step": [c_void_p, c_void_p, c_void_p, c_void_p, c_int, c_int64],
     "racer_rollout": [c_void_p, c_void_p, c_void_p, c_void_p, c_int, c_int, c_int64],
-    "racer_rollout_kernel_count": [c_void_p, c_void_p, c_void_p, c_void_p, c_int, c_int, P(c_int64)],
+    "racer_gemm_bf16": [c_void_p, c_void_p, c_void_p, c_int, c_int, c_int, c_int, c_int, c_int, c_int, c_void_p,
+                        c_void_p, c_void_p],
+    "racer_rollout_kernel_count":[c_void_p, c_void_p, c_void_p, c_void_p, c_int, c_int, P(c_int64)],
     "racer_sim_profile": [c_void_p, c_void_p, c_int, P(c_float), P(c_float), P(c_int64)],
 }
 

@@ -28,6 +28,8 @@ UNITS = {
     "policy.cu": [],
     "api.cu": [],
     "noalloc.cu": [],
+    "tma.cu": [],
+    "gemm.cu": [],
 }
 
 

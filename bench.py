@@ -104,10 +104,11 @@ def peaks():
 
 def dram_traffic_per_launch():
     """Per-launch DRAM bytes of the lidar kernel from the committed ncu summary, if any."""
-    p = ROOT / "profiles" / "lidar_traffic.json"
+    p = ROOT / "profiles" / "lidar_traffic.txt"
     if p.exists():
-        d = json.loads(p.read_text())
-        return d.get("dram_bytes_per_launch")
+        for line in p.read_text().splitlines():
+            if line.startswith("dram_bytes_per_launch:"):
+                return int(line.split(":", 1)[1])
     return None
 
 

@@ -146,6 +146,34 @@ int racer_runner_step(racer_sim* sim, racer_policy* policy, racer_acts* acts, fl
 int racer_rollout(racer_sim* sim, racer_policy* policy, racer_acts* acts, float* scratch_dev, int steps,
                   int deterministic, int64_t step0);
 
+/* ---- learned lidar surrogate (no counterpart in the reference; replaces
+ * racer/sim.mojo:238-266's tracing during rollouts, audited by it) ---- */
+typedef struct racer_surrogate racer_surrogate;
+/* MLP from the lidar frame (origin x, y, z; sin/cos heading; layer one-hot;
+ * constant 1) through three tanh layers of `hidden` (128, 256 or 512) to the
+ * sim's `beams` ranges / 10 m, for the sim's track (at most two layers).
+ * `batch` (a multiple of 128) is the training batch; `seed` the init. */
+int racer_surrogate_create(racer_sim* sim, int hidden, int batch, uint64_t seed, racer_surrogate** out);
+int racer_surrogate_destroy(racer_surrogate* surrogate);
+/* FP32 master parameters W1 [H,8] | W2 [H,H] | b2 [H] | W3 [H,H] | b3 [H] |
+ * W4 [beams,H] | b4 [beams], and their last gradient (device pointers). */
+int racer_surrogate_params(racer_surrogate* surrogate, float** theta_dev, float** grad_dev, long* count, int* hidden);
+/* Training set: `count` poses (a multiple of the batch), uniform over the
+ * drivable cells of every layer, heading uniform in (-pi, pi). */
+int racer_surrogate_set_poses(racer_surrogate* surrogate, long count, uint64_t seed);
+/* Device pointer to the pose set: float4 (x, y, heading, layer) per pose. */
+int racer_surrogate_poses(racer_surrogate* surrogate, void** poses_dev, long* count);
+/* Gradient of the mean squared range error (ranges / 10 m) of the batch of
+ * poses starting at `first`, labelled by the exact tracer; no update.
+ * label_dev_out (optional) gets the labels [beams, batch]. */
+int racer_surrogate_gradient(racer_surrogate* surrogate, long first, float* mse, float* label_dev_out);
+/* `steps` Adam steps over consecutive batches (cosine decay from lr to lr/100);
+ * returns the last batch's mean squared error and mean absolute error in metres. */
+int racer_surrogate_train(racer_surrogate* surrogate, int steps, float lr, float* last_mse, float* last_mae_m);
+/* Held-out error on `batches` fresh batches drawn with `seed`, surrogate vs exact. */
+int racer_surrogate_evaluate(racer_surrogate* surrogate, int batches, uint64_t seed, float* mae_m, float* rmse_m,
+                             float* max_m, float* frac_over_5cm);
+
 /* ---- dense products (Device.gemm with transpose_b, racer/device.mojo:82-98) ---- */
 /* C[M, N] (float32, row-major, ldc) = A[M, K] . B[N, K]^T on the tcgen05 tensor
  * cores with BF16 operands (row-major, K contiguous, lda/ldb multiples of 8,

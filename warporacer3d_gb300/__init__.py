@@ -10,8 +10,8 @@ from pathlib import Path
 import numpy as np
 
 from ._lib import RacerError, load_library  # noqa: F401
-from .racer import (CRASH, STATE, TIMEOUT, Activations, DevArray, Policy, Runner, Sim, Trainer, load,  # noqa: F401
-                    save)
+from .racer import (CRASH, STATE, TIMEOUT, Activations, DevArray, Policy, Runner, Sim, Surrogate, Trainer,  # noqa: F401
+                    load, save)
 
 TRACKS = Path(__file__).resolve().parent / "tracks"
 

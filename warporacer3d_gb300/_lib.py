@@ -66,7 +66,15 @@ SIGNATURES = {
     "racer_trainer_minibatch": [c_void_p, c_void_p, c_int, c_float, c_float],
     "racer_runner_step": [c_void_p, c_void_p, c_void_p, c_void_p, c_int, c_int64],
     "racer_rollout": [c_void_p, c_void_p, c_void_p, c_void_p, c_int, c_int, c_int64],
-    "racer_gemm_bf16": [c_void_p, c_void_p, c_void_p, c_int, c_int, c_int, c_int, c_int, c_int, c_int, c_void_p,
+    "racer_surrogate_create": [c_void_p, c_int, c_int, c_uint64, P(c_void_p)],
+    "racer_surrogate_destroy": [c_void_p],
+    "racer_surrogate_params": [c_void_p, P(c_void_p), P(c_void_p), P(ctypes.c_long), P(c_int)],
+    "racer_surrogate_set_poses": [c_void_p, ctypes.c_long, c_uint64],
+    "racer_surrogate_poses": [c_void_p, P(c_void_p), P(ctypes.c_long)],
+    "racer_surrogate_gradient": [c_void_p, ctypes.c_long, P(c_float), c_void_p],
+    "racer_surrogate_train": [c_void_p, c_int, c_float, P(c_float), P(c_float)],
+    "racer_surrogate_evaluate": [c_void_p, c_int, c_uint64, P(c_float), P(c_float), P(c_float), P(c_float)],
+    "racer_gemm_bf16":[c_void_p, c_void_p, c_void_p, c_int, c_int, c_int, c_int, c_int, c_int, c_int, c_void_p,
                         c_void_p, c_void_p],
     "racer_rollout_kernel_count":[c_void_p, c_void_p, c_void_p, c_void_p, c_int, c_int, P(c_int64)],
     "racer_sim_profile": [c_void_p, c_void_p, c_int, P(c_float), P(c_float), P(c_int64)],

@@ -30,6 +30,7 @@ UNITS = {
     "noalloc.cu": [],
     "tma.cu": [],
     "gemm.cu": [],
+    "surrogate.cu": [],
 }
 
 

@@ -19,6 +19,7 @@
 #include "../../include/racer.h"
 #include "common.cuh"
 #include "kernels.h"
+#include "objects.h"
 #include "policy_fwd.h"
 
 namespace racer_host {
@@ -78,23 +79,6 @@ __global__ void k_set_i64(int64_t* p, int64_t v) {
 }
 
 }  // namespace
-
-struct racer_sim {
-  int n = 0, beams = 0, in_rows = 0;
-  uint64_t seed = 0;
-  size_t track_len = 0;
-  TrackDev t{};
-  float* d_track = nullptr;
-  float2* d_cl = nullptr;
-  float2* beam_dir = nullptr;
-  float4* ray = nullptr;  // [2, n] per-car lidar frame written by the physics kernel
-  float *state = nullptr, *obs = nullptr, *actions = nullptr, *reward = nullptr, *done = nullptr;
-  int64_t* step_base = nullptr;
-  cudaStream_t st = nullptr;
-  bool owned = false;
-  std::map<std::tuple<const void*, const void*, const void*, int, int>, cudaGraphExec_t> graphs;
-  std::map<std::tuple<const void*, const void*, const void*, int, int>, size_t> graph_kernels;
-};
 
 struct racer_acts {
   int cols = 0;

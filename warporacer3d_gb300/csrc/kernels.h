@@ -15,6 +15,8 @@ void launch_advance(const TrackDev& t, float* state, const float* actions, float
 void launch_lidar(const TrackDev& t, const float4* ray, float* obs, int n, int beams, const float2* beam_dir,
                   int* iters, cudaStream_t st);
 int lidar_max_iters(const TrackDev& t);
+// poses [count] (x, y, heading, layer) -> ray [2, count]: the frame of a car at rest there.
+void launch_pose_frames(const TrackDev& t, const float4* poses, int count, float4* ray, cudaStream_t st);
 void launch_sample(int n, uint64_t seed, const float* output, const float* log_std, float* actions, float* logp,
                    float* value, int deterministic, const int64_t* step_base, int64_t step_add, cudaStream_t st);
 void launch_add_i64(int64_t* p, int64_t v, cudaStream_t st);

@@ -1,0 +1,29 @@
+// Internal definitions of the C-ABI objects shared by the library's host
+// translation units (api.cu, surrogate.cu).
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <map>
+#include <tuple>
+
+#include "../../include/racer.h"
+#include "common.cuh"
+
+// Sim (racer/sim.mojo:269-289): track, cars and their buffers on one stream.
+struct racer_sim {
+  int n = 0, beams = 0, in_rows = 0;
+  uint64_t seed = 0;
+  size_t track_len = 0;
+  racer::TrackDev t{};
+  float* d_track = nullptr;
+  float2* d_cl = nullptr;
+  float2* beam_dir = nullptr;
+  float4* ray = nullptr;  // [2, n] per-car lidar frame written by the physics kernel
+  float *state = nullptr, *obs = nullptr, *actions = nullptr, *reward = nullptr, *done = nullptr;
+  int64_t* step_base = nullptr;
+  cudaStream_t st = nullptr;
+  bool owned = false;
+  std::map<std::tuple<const void*, const void*, const void*, int, int>, cudaGraphExec_t> graphs;
+  std::map<std::tuple<const void*, const void*, const void*, int, int>, size_t> graph_kernels;
+};

@@ -261,12 +261,32 @@ __global__ void k_advance(TrackDev t, float* s, const float* act, float* reward,
   obs[(long)(beams + 4) * n + i] = 1.0f;
   // The lidar's per-car frame (racer/sim.mojo:243-249), from the values just
   // written: origin = position + MOUNT_X forward + MOUNT_Z up, and the
-  // heading's cos/sin with the slopes that tilt the body plane.
+  // heading's cos/sin with the slopes that tilt the body plane; .w of the
+  // second half carries the car's layer (surrogate input).
   float ch, sh;
   rmath::sincosf_(heading, &sh, &ch);
-  ray[i] = make_float4((s[(long)X * n + i] + MOUNT_X * ch) + 0.0f, (s[(long)Y * n + i] + MOUNT_X * sh) + 0.0f,
-                       (s[(long)Z * n + i] + MOUNT_X * along) + MOUNT_Z, ch);
-  ray[n + i] = make_float4(sh, along, across, 0.0f);
+  const float sx = s[(long)X * n + i], sy = s[(long)Y * n + i], sz = s[(long)Z * n + i];
+  ray[i] = make_float4((sx + MOUNT_X * ch) + 0.0f, (sy + MOUNT_X * sh) + 0.0f, (sz + MOUNT_X * along) + MOUNT_Z, ch);
+  ray[n + i] = make_float4(sh, along, across, (float)probe<LAYERS>(t, sx, sy, sz).layer);
+}
+
+// The lidar frame of a car at rest on a layer (racer/sim.mojo:229-234,
+// 243-249): pose (x, y, heading, layer) -> z = the layer's bilinear height,
+// the slopes along and across the heading, and the same frame k_advance
+// writes. Used to label surrogate training poses with the exact tracer.
+__global__ void k_pose_frames(TrackDev t, const float4* __restrict__ poses, int count, float4* ray) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= count) return;
+  const float4 p = poses[i];
+  const int layer = (int)p.w;
+  const Surface g = surface(t, layer, p.x, p.y);
+  float along, across;
+  slopes(g, p.z, &along, &across);
+  float ch, sh;
+  rmath::sincosf_(p.z, &sh, &ch);
+  ray[i] = make_float4((p.x + MOUNT_X * ch) + 0.0f, (p.y + MOUNT_X * sh) + 0.0f, (g.height + MOUNT_X * along) + MOUNT_Z,
+                       ch);
+  ray[count + i] = make_float4(sh, along, across, (float)layer);
 }
 
 // racer/sim.mojo:238-266: the sphere-traced lidar, one thread per (car, beam).
@@ -365,6 +385,10 @@ void launch_lidar(const TrackDev& t, const float4* ray, float* obs, int n, int b
     k_lidar<2><<<grid, 256, 0, st>>>(t, ray, obs, n, beams, beam_dir, cap, iters);
   else
     k_lidar<0><<<grid, 256, 0, st>>>(t, ray, obs, n, beams, beam_dir, cap, iters);
+}
+
+void launch_pose_frames(const TrackDev& t, const float4* poses, int count, float4* ray, cudaStream_t st) {
+  k_pose_frames<<<(count + 127) / 128, 128, 0, st>>>(t, poses, count, ray);
 }
 
 void launch_sample(int n, uint64_t seed, const float* output, const float* log_std, float* actions, float* logp,

@@ -1,0 +1,736 @@
+// Learned lidar surrogate: a per-track MLP from the lidar's ray frame to all
+// beam ranges, trained on the GPU against the exact sphere tracer.
+//
+// Network (one hidden width H, default 512):
+//   inputs  f = (x', y', z, sin h, cos h, [layer == 0], [layer == 1], 1)
+//           with (x, y, z) the lidar origin, x', y' scaled to [-1, 1] over the map
+//   h1 = tanh(W1 f)            W1 [H, 8] (the constant input is its bias)
+//   h2 = tanh(W2 h1 + b2)      W2 [H, H]
+//   h3 = tanh(W3 h2 + b3)      W3 [H, H]
+//   y  = W4 h3 + b4            W4 [beams, H]; y = range / RANGE per beam
+// Activations are sample-major BF16 for the forward GEMMs and also written
+// feature-major (batch contiguous) for the weight-gradient GEMMs; every GEMM
+// is the generic tcgen05 kernel (BF16 operands by TMA, FP32 accumulation in
+// TMEM) with an epilogue that applies tanh/bias, the loss gradient, the tanh
+// derivative or the split-K partial store. Master weights and Adam are FP32.
+//
+// Training poses are uniform over the drivable cells (clearance > 0) of every
+// layer with uniform heading; their labels come from the exact tracer
+// (k_pose_frames + k_lidar) batch by batch, so the labels are never stored.
+#include <cuda_bf16.h>
+
+#include <cmath>
+#include <string>
+#include <vector>
+
+#include "../../include/racer.h"
+#include "common.cuh"
+#include "gemm_epi.cuh"
+#include "gemm_tc.cuh"
+#include "kernels.h"
+#include "objects.h"
+#include "philox.h"
+#include "tma.h"
+
+using bf16 = __nv_bfloat16;
+
+namespace racer {
+namespace {
+
+constexpr int NIN = 8;
+
+struct Norm {
+  float xc, inv_xs, yc, inv_ys;
+};
+
+__device__ __forceinline__ float warp_sum(float v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  return v;
+}
+
+// H = tanh(v + bias) -> sample-major hs [M, lds] and feature-major hf [N, ldf] (either may be null).
+struct EpiTanhOut {
+  bf16* hs;
+  int lds;
+  bf16* hf;
+  int ldf;
+  const float* bias;
+  int M, N;
+  __device__ void operator()(int m, int n, const float* v) const {
+    if (m >= M) return;
+    float h[16];
+#pragma unroll
+    for (int j = 0; j < 16; ++j) h[j] = (n + j < N) ? tc::tanh_fast(v[j] + (bias ? bias[n + j] : 0.0f)) : 0.0f;
+    if (hs && n < N) {  // N is a multiple of 16: a chunk is wholly inside or outside
+      uint4 a = make_uint4(tc::pack_bf16(h[0], h[1]), tc::pack_bf16(h[2], h[3]), tc::pack_bf16(h[4], h[5]),
+                           tc::pack_bf16(h[6], h[7]));
+      uint4 b = make_uint4(tc::pack_bf16(h[8], h[9]), tc::pack_bf16(h[10], h[11]), tc::pack_bf16(h[12], h[13]),
+                           tc::pack_bf16(h[14], h[15]));
+      uint4* dst = reinterpret_cast<uint4*>(hs + (long)m * lds + n);
+      dst[0] = a;
+      dst[1] = b;
+    }
+    if (hf) {
+#pragma unroll
+      for (int j = 0; j < 16; ++j)
+        if (n + j < N) hf[(long)(n + j) * ldf + m] = __float2bfloat16_rn(h[j]);
+    }
+  }
+};
+
+// Output layer in training: y = v + b4, e = y - target, g = scale * e (MSE gradient).
+// Writes g sample-major [M, ldgs] and feature-major [npad rows, ldgf] (zero past N),
+// accumulates the bias gradient and the sums of e^2 and |e|.
+struct EpiLoss {
+  const float* target;  // [N, ldt] feature-major
+  int ldt;
+  const float* bias;
+  int M, N;
+  float scale;
+  bf16* gs;
+  int ldgs;
+  bf16* gf;
+  int ldgf;
+  float* dbias;
+  double* sums;
+  int npad;  // columns stored (a multiple of 16; past N they are zero)
+  __device__ void operator()(int m, int n, const float* v) const {
+    const bool row = m < M;
+    float g[16], se = 0.0f, ae = 0.0f;
+#pragma unroll
+    for (int j = 0; j < 16; ++j) {
+      g[j] = 0.0f;
+      if (row && n + j < N) {
+        float e = (v[j] + bias[n + j]) - target[(long)(n + j) * ldt + m];
+        se += e * e;
+        ae += fabsf(e);
+        g[j] = scale * e;
+      }
+    }
+    if (row && n < npad) {
+      uint4 a = make_uint4(tc::pack_bf16(g[0], g[1]), tc::pack_bf16(g[2], g[3]), tc::pack_bf16(g[4], g[5]),
+                           tc::pack_bf16(g[6], g[7]));
+      uint4 b = make_uint4(tc::pack_bf16(g[8], g[9]), tc::pack_bf16(g[10], g[11]), tc::pack_bf16(g[12], g[13]),
+                           tc::pack_bf16(g[14], g[15]));
+      uint4* dst = reinterpret_cast<uint4*>(gs + (long)m * ldgs + n);
+      dst[0] = a;
+      dst[1] = b;
+#pragma unroll
+      for (int j = 0; j < 16; ++j) gf[(long)(n + j) * ldgf + m] = __float2bfloat16_rn(g[j]);
+    }
+#pragma unroll
+    for (int j = 0; j < 16; ++j) {
+      float s = warp_sum(g[j]);
+      if ((threadIdx.x & 31) == 0 && n + j < N) atomicAdd(dbias + n + j, s);
+    }
+    se = warp_sum(se);
+    ae = warp_sum(ae);
+    if ((threadIdx.x & 31) == 0) {
+      atomicAdd(sums, (double)se);
+      atomicAdd(sums + 1, (double)ae);
+    }
+  }
+};
+
+// Back through tanh: g = v * (1 - h^2) with h from hs [M, ldh]; writes gs (optional) and gf,
+// accumulates the bias gradient (optional).
+struct EpiDTanh {
+  const bf16* hs;
+  int ldh;
+  bf16* gs;
+  int ldgs;
+  bf16* gf;
+  int ldgf;
+  float* dbias;
+  int M, N;
+  __device__ void operator()(int m, int n, const float* v) const {
+    const bool row = m < M;
+    float g[16];
+#pragma unroll
+    for (int j = 0; j < 16; ++j) {
+      g[j] = 0.0f;
+      if (row && n + j < N) {
+        float h = __bfloat162float(hs[(long)m * ldh + n + j]);
+        g[j] = v[j] * (1.0f - h * h);
+      }
+    }
+    if (row && n < N) {
+      if (gs) {
+        uint4 a = make_uint4(tc::pack_bf16(g[0], g[1]), tc::pack_bf16(g[2], g[3]), tc::pack_bf16(g[4], g[5]),
+                             tc::pack_bf16(g[6], g[7]));
+        uint4 b = make_uint4(tc::pack_bf16(g[8], g[9]), tc::pack_bf16(g[10], g[11]), tc::pack_bf16(g[12], g[13]),
+                             tc::pack_bf16(g[14], g[15]));
+        uint4* dst = reinterpret_cast<uint4*>(gs + (long)m * ldgs + n);
+        dst[0] = a;
+        dst[1] = b;
+      }
+#pragma unroll
+      for (int j = 0; j < 16; ++j)
+        if (n + j < N) gf[(long)(n + j) * ldgf + m] = __float2bfloat16_rn(g[j]);
+    }
+    if (dbias) {
+#pragma unroll
+      for (int j = 0; j < 16; ++j) {
+        float s = warp_sum(g[j]);
+        if ((threadIdx.x & 31) == 0 && n + j < N) atomicAdd(dbias + n + j, s);
+      }
+    }
+  }
+};
+
+// Inference output: out[(n) * ldo + m] = clamp(v + b4, 0, 1) (feature-major, the obs rows of the
+// beams), and the smallest predicted range of each row into minr (as ordered uint bits).
+struct EpiInfer {
+  float* out;
+  int ldo;
+  const float* bias;
+  int M, N;
+  unsigned* minr;
+  __device__ void operator()(int m, int n, const float* v) const {
+    if (m >= M) return;
+    float lo = 1.0f;
+#pragma unroll
+    for (int j = 0; j < 16; ++j) {
+      if (n + j < N) {
+        float y = fminf(fmaxf(v[j] + bias[n + j], 0.0f), 1.0f);
+        out[(long)(n + j) * ldo + m] = y;
+        lo = fminf(lo, y);
+      }
+    }
+    if (minr) atomicMin(minr + m, __float_as_uint(lo));
+  }
+};
+
+// ray frames [2, count] -> inputs, sample-major x [count, 8] and feature-major xf [8, count].
+__global__ void k_features(const float4* __restrict__ ray, int count, Norm nm, bf16* x, bf16* xf) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= count) return;
+  const float4 r0 = ray[i], r1 = ray[count + i];
+  float f[NIN] = {(r0.x - nm.xc) * nm.inv_xs, (r0.y - nm.yc) * nm.inv_ys, r0.z, r1.x, r0.w,
+                  r1.w == 0.0f ? 1.0f : 0.0f, r1.w == 1.0f ? 1.0f : 0.0f, 1.0f};
+  uint4 pk = make_uint4(tc::pack_bf16(f[0], f[1]), tc::pack_bf16(f[2], f[3]), tc::pack_bf16(f[4], f[5]),
+                        tc::pack_bf16(f[6], f[7]));
+  *reinterpret_cast<uint4*>(x + (long)i * NIN) = pk;
+  if (xf)
+    for (int k = 0; k < NIN; ++k) xf[(long)k * count + i] = __float2bfloat16_rn(f[k]);
+}
+
+// Poses uniform over drivable (cell, layer) pairs, jittered inside the cell, heading uniform.
+__global__ void k_sample_poses(const int2* cells, int ncells, int count, uint64_t seed, TrackDev t, float4* poses) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= count) return;
+  float u[4];
+  philox::uniform4(seed, (uint64_t)i, 7, u);
+  int k = min((int)(u[0] * (float)ncells), ncells - 1);
+  int2 c = cells[k];
+  int ix = c.x % t.nx, iy = c.x / t.nx;
+  float x = t.x0 + ((float)ix + u[1] - 0.5f) * t.cell;
+  float y = t.y0 + ((float)iy + u[2] - 0.5f) * t.cell;
+  float h = (2.0f * u[3] - 1.0f) * PI_F;
+  poses[i] = make_float4(x, y, h, (float)c.y);
+}
+
+// Sum of split-K partials into a row-major [Mreal, N] gradient block.
+__global__ void k_reduce_splits(const float* P, int splits, long mn, int N, int Mreal, float* out) {
+  long e = (long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= (long)Mreal * N) return;
+  float acc = 0.0f;
+  for (int z = 0; z < splits; ++z) acc += P[(long)z * mn + e];
+  out[e] = acc;
+}
+
+// theta -> BF16 operand images (row-major and transposed), zero past `beams` rows/cols of W4.
+struct Layout {
+  int H, beams, npad;
+  long w1, w2, b2, w3, b3, w4, b4, total;
+};
+
+__global__ void k_refresh(const float* __restrict__ th, Layout L, bf16* w1b, bf16* w2b, bf16* w3b, bf16* w4b,
+                          bf16* w2t, bf16* w3t, bf16* w4t) {
+  const int H = L.H;
+  const long n1 = (long)H * NIN, n2 = (long)H * H, n4 = (long)L.npad * H;
+  for (long e = (long)blockIdx.x * blockDim.x + threadIdx.x; e < n1 + 2 * n2 + n4;
+       e += (long)gridDim.x * blockDim.x) {
+    if (e < n1) {
+      w1b[e] = __float2bfloat16_rn(th[L.w1 + e]);
+    } else if (e < n1 + n2) {
+      long f = e - n1;
+      int o = (int)(f / H), i = (int)(f % H);
+      bf16 v = __float2bfloat16_rn(th[L.w2 + f]);
+      w2b[f] = v;
+      w2t[(long)i * H + o] = v;
+    } else if (e < n1 + 2 * n2) {
+      long f = e - n1 - n2;
+      int o = (int)(f / H), i = (int)(f % H);
+      bf16 v = __float2bfloat16_rn(th[L.w3 + f]);
+      w3b[f] = v;
+      w3t[(long)i * H + o] = v;
+    } else {
+      long f = e - n1 - 2 * n2;
+      int o = (int)(f / H), i = (int)(f % H);
+      bf16 v = __float2bfloat16_rn(o < L.beams ? th[L.w4 + (long)o * H + i] : 0.0f);
+      w4b[f] = v;
+      w4t[(long)i * L.npad + o] = v;
+    }
+  }
+}
+
+__global__ void k_init_params(float* th, Layout L, uint64_t seed) {
+  for (long e = (long)blockIdx.x * blockDim.x + threadIdx.x; e < L.total; e += (long)gridDim.x * blockDim.x) {
+    float z[4];
+    philox::normal4(seed, (uint64_t)e, 11, z);
+    float v = 0.0f;
+    if (e < L.w2) v = z[0] * rsqrtf((float)NIN);
+    else if (e < L.b2) v = z[0] * rsqrtf((float)L.H);
+    else if (e < L.w3) v = 0.0f;
+    else if (e < L.b3) v = z[0] * rsqrtf((float)L.H);
+    else if (e < L.w4) v = 0.0f;
+    else if (e < L.b4) v = z[0] * rsqrtf((float)L.H) * 0.5f;
+    else v = 0.3f;  // output bias: a typical normalised range
+    th[e] = v;
+  }
+}
+
+__global__ void k_adam_s(long p, float lr, float c1, float c2, float* th, const float* g, float* m1, float* m2) {
+  for (long i = (long)blockIdx.x * blockDim.x + threadIdx.x; i < p; i += (long)gridDim.x * blockDim.x) {
+    float gi = g[i];
+    float a = 0.9f * m1[i] + 0.1f * gi;
+    float b = 0.999f * m2[i] + 0.001f * gi * gi;
+    m1[i] = a;
+    m2[i] = b;
+    th[i] -= lr * (a / c1) / (sqrtf(b / c2) + 1e-8f);
+  }
+}
+
+// |pred - exact| statistics over [beams, count] (both feature-major rows of ranges / RANGE):
+// sums[0] += sum |e|, sums[1] += sum e^2, max in bits, count of |e| > 5 cm.
+__global__ void k_compare(const float* pred, const float* exact, long total, double* sums, unsigned* maxbits,
+                          unsigned long long* over) {
+  double a = 0.0, s = 0.0;
+  float mx = 0.0f;
+  unsigned long long ov = 0;
+  for (long i = (long)blockIdx.x * blockDim.x + threadIdx.x; i < total; i += (long)gridDim.x * blockDim.x) {
+    float e = fabsf(pred[i] - exact[i]) * RANGE;
+    a += e;
+    s += (double)e * e;
+    mx = fmaxf(mx, e);
+    ov += e > 0.05f;
+  }
+  atomicAdd(sums, a);
+  atomicAdd(sums + 1, s);
+  atomicMax(maxbits, __float_as_uint(mx));
+  atomicAdd(over, ov);
+}
+
+}  // namespace
+}  // namespace racer
+
+using namespace racer;
+
+struct SurrogateActs {  // activation buffers and tensor maps for one row count M
+  int M = 0;
+  bf16 *x = nullptr, *xf = nullptr, *h1s = nullptr, *h2s = nullptr, *h3s = nullptr;
+  bf16 *h1f = nullptr, *h2f = nullptr, *h3f = nullptr;
+  bf16 *g4s = nullptr, *g4f = nullptr, *g3s = nullptr, *g3f = nullptr, *g2s = nullptr, *g2f = nullptr,
+       *g1f = nullptr;
+  CUtensorMap tx, th1, th2, th3, tg4s, tg3s, tg2s;          // A operands (M rows)
+  CUtensorMap tg4f, tg3f, tg2f, tg1f, th3f, th2f, th1f, txf;  // weight-gradient operands (K = M)
+};
+
+struct racer_surrogate {
+  racer_sim* sim = nullptr;
+  Layout L{};
+  Norm nm{};
+  int batch = 0;
+  cudaStream_t st = nullptr;
+  float *theta = nullptr, *grad = nullptr, *m1 = nullptr, *m2 = nullptr;
+  bf16 *w1b = nullptr, *w2b = nullptr, *w3b = nullptr, *w4b = nullptr, *w2t = nullptr, *w3t = nullptr,
+       *w4t = nullptr;
+  CUtensorMap tw1, tw2, tw3, tw4, tw2t, tw3t, tw4t;  // B operands
+  int2* cells = nullptr;
+  int ncells = 0;
+  float4* poses = nullptr;
+  int npose = 0;
+  float4* ray = nullptr;   // [2, batch]
+  float* label = nullptr;  // [4 + beams, batch] (rows 4.. are the exact ranges / RANGE)
+  float* pred = nullptr;   // [beams, batch]
+  float* scratch = nullptr;
+  size_t scratch_floats = 0;
+  double* sums = nullptr;    // loss sums / compare sums
+  unsigned* maxbits = nullptr;
+  unsigned long long* over = nullptr;
+  int* err = nullptr;
+  SurrogateActs train;
+  int step = 0;
+};
+
+namespace {
+
+template <typename T>
+int salloc(T** p, size_t count) {
+  RACER_TRY(cudaMalloc((void**)p, count * sizeof(T) + 64));
+  RACER_TRY(cudaMemset(*p, 0, count * sizeof(T) + 64));
+  return 0;
+}
+
+int make_acts(racer_surrogate* s, SurrogateActs* a, int M, bool training) {
+  const int H = s->L.H, NP = s->L.npad;
+  a->M = M;
+  int rc = 0;
+  if ((rc = salloc(&a->x, (size_t)M * NIN)) || (rc = salloc(&a->h1s, (size_t)M * H)) ||
+      (rc = salloc(&a->h2s, (size_t)M * H)) || (rc = salloc(&a->h3s, (size_t)M * H)))
+    return rc;
+  if ((rc = make_tmap_bf16(&a->tx, a->x, M, NIN, NIN, 128)) || (rc = make_tmap_bf16(&a->th1, a->h1s, M, H, H, 128)) ||
+      (rc = make_tmap_bf16(&a->th2, a->h2s, M, H, H, 128)))
+    return rc;
+  if ((rc = make_tmap_bf16(&a->th3, a->h3s, M, H, H, 128))) return rc;
+  if (!training) return 0;
+  if ((M % 8) != 0) {
+    racer_host::set_error("surrogate: the training batch must be a multiple of 8");
+    return 1;
+  }
+  if ((rc = salloc(&a->xf, (size_t)NIN * M)) || (rc = salloc(&a->h1f, (size_t)H * M)) ||
+      (rc = salloc(&a->h2f, (size_t)H * M)) || (rc = salloc(&a->h3f, (size_t)H * M)) ||
+      (rc = salloc(&a->g4s, (size_t)M * NP)) || (rc = salloc(&a->g4f, (size_t)NP * M)) ||
+      (rc = salloc(&a->g3s, (size_t)M * H)) || (rc = salloc(&a->g3f, (size_t)H * M)) ||
+      (rc = salloc(&a->g2s, (size_t)M * H)) || (rc = salloc(&a->g2f, (size_t)H * M)) ||
+      (rc = salloc(&a->g1f, (size_t)H * M)))
+    return rc;
+  if ((rc = make_tmap_bf16(&a->tg4s, a->g4s, M, NP, NP, 128)) || (rc = make_tmap_bf16(&a->tg3s, a->g3s, M, H, H, 128)) ||
+      (rc = make_tmap_bf16(&a->tg2s, a->g2s, M, H, H, 128)) || (rc = make_tmap_bf16(&a->tg4f, a->g4f, NP, M, M, 128)) ||
+      (rc = make_tmap_bf16(&a->tg3f, a->g3f, H, M, M, 128)) || (rc = make_tmap_bf16(&a->tg2f, a->g2f, H, M, M, 128)) ||
+      (rc = make_tmap_bf16(&a->tg1f, a->g1f, H, M, M, 128)) || (rc = make_tmap_bf16(&a->th3f, a->h3f, H, M, M, 256)) ||
+      (rc = make_tmap_bf16(&a->th2f, a->h2f, H, M, M, 256)) || (rc = make_tmap_bf16(&a->th1f, a->h1f, H, M, M, 256)) ||
+      (rc = make_tmap_bf16(&a->txf, a->xf, NIN, M, M, 64)))
+    return rc;
+  return 0;
+}
+
+void free_acts(SurrogateActs* a) {
+  for (bf16* p : {a->x, a->xf, a->h1s, a->h2s, a->h3s, a->h1f, a->h2f, a->h3f, a->g4s, a->g4f, a->g3s, a->g3f, a->g2s,
+                  a->g2f, a->g1f})
+    cudaFree(p);
+}
+
+#define SURR_CHECK(expr)                                                                  \
+  do {                                                                                    \
+    cudaError_t e_ = (expr);                                                              \
+    if (e_ != cudaSuccess) {                                                              \
+      racer_host::set_error(std::string("surrogate: ") + #expr + ": " + cudaGetErrorString(e_)); \
+      return 2;                                                                           \
+    }                                                                                     \
+  } while (0)
+
+// Forward of M rows already featurised in a->x; the last layer uses `out` (inference).
+int forward(racer_surrogate* s, SurrogateActs* a, bool training, const EpiInfer* out) {
+  const int H = s->L.H, M = a->M;
+  const float* th = s->theta;
+  cudaStream_t st = s->st;
+  SURR_CHECK(gemm_launch<256>(a->tx, s->tw1, M, H, 1, 1, EpiTanhOut{a->h1s, H, training ? a->h1f : nullptr, M, nullptr, M, H},
+                              s->err, st));
+  SURR_CHECK(gemm_launch<256>(a->th1, s->tw2, M, H, H / 64, 1,
+                              EpiTanhOut{a->h2s, H, training ? a->h2f : nullptr, M, th + s->L.b2, M, H}, s->err, st));
+  SURR_CHECK(gemm_launch<256>(a->th2, s->tw3, M, H, H / 64, 1,
+                              EpiTanhOut{a->h3s, H, training ? a->h3f : nullptr, M, th + s->L.b3, M, H}, s->err, st));
+  if (out) SURR_CHECK(gemm_launch<256>(a->th3, s->tw4, M, s->L.beams, H / 64, 1, *out, s->err, st));
+  return 0;
+}
+
+// BN must equal the row box of tb's tensor map (256 for the hidden activations, 64 for the inputs).
+template <int BN>
+int wgrad(racer_surrogate* s, const CUtensorMap& ta, const CUtensorMap& tb, int Mpad, int Mreal, int N, long off) {
+  const int kblocks = (s->batch + 63) / 64;
+  const int tiles = ((Mpad + 127) / 128) * ((N + BN - 1) / BN);
+  int splits = std::max(1, std::min(kblocks, 2 * 148 / std::max(1, tiles)));
+  const int per = (kblocks + splits - 1) / splits;
+  splits = (kblocks + per - 1) / per;
+  if ((size_t)splits * Mpad * N > s->scratch_floats) {
+    racer_host::set_error("surrogate: split-K scratch too small");
+    return 1;
+  }
+  EpiSplitF32 epi{s->scratch, (long)Mpad * N, Mpad, N};
+  SURR_CHECK(gemm_launch<BN>(ta, tb, Mpad, N, kblocks, splits, epi, s->err, s->st));
+  long count = (long)Mreal * N;
+  k_reduce_splits<<<(unsigned)((count + 255) / 256), 256, 0, s->st>>>(s->scratch, splits, (long)Mpad * N, N, Mreal,
+                                                                       s->grad + off);
+  SURR_CHECK(cudaGetLastError());
+  return 0;
+}
+
+// Labels and features for batch rows taken from the pose set starting at `first`.
+int prepare(racer_surrogate* s, SurrogateActs* a, long first) {
+  racer_sim* sim = s->sim;
+  const int B = a->M;
+  const float4* poses = s->poses + first;
+  launch_pose_frames(sim->t, poses, B, s->ray, s->st);
+  launch_lidar(sim->t, s->ray, s->label, B, sim->beams, sim->beam_dir, nullptr, s->st);
+  k_features<<<(B + 127) / 128, 128, 0, s->st>>>(s->ray, B, s->nm, a->x, a->xf);
+  SURR_CHECK(cudaGetLastError());
+  return 0;
+}
+
+// Gradient of the mean squared error over the batch into s->grad; loss sums into s->sums.
+int gradient(racer_surrogate* s, long first) {
+  SurrogateActs* a = &s->train;
+  const int H = s->L.H, B = a->M, NP = s->L.npad, beams = s->L.beams;
+  int rc = prepare(s, a, first);
+  if (rc) return rc;
+  SURR_CHECK(cudaMemsetAsync(s->grad + s->L.b2, 0, H * sizeof(float), s->st));
+  SURR_CHECK(cudaMemsetAsync(s->grad + s->L.b3, 0, H * sizeof(float), s->st));
+  SURR_CHECK(cudaMemsetAsync(s->grad + s->L.b4, 0, beams * sizeof(float), s->st));
+  SURR_CHECK(cudaMemsetAsync(s->sums, 0, 2 * sizeof(double), s->st));
+  if ((rc = forward(s, a, true, nullptr))) return rc;
+  EpiLoss loss{s->label + 4L * B, B, s->theta + s->L.b4, B, beams, 2.0f / ((float)B * (float)beams),
+               a->g4s, NP, a->g4f, B, s->grad + s->L.b4, s->sums, NP};
+  SURR_CHECK(gemm_launch<256>(a->th3, s->tw4, B, NP, H / 64, 1, loss, s->err, s->st));
+  SURR_CHECK(gemm_launch<256>(a->tg4s, s->tw4t, B, H, NP / 64, 1,
+                              EpiDTanh{a->h3s, H, a->g3s, H, a->g3f, B, s->grad + s->L.b3, B, H}, s->err, s->st));
+  SURR_CHECK(gemm_launch<256>(a->tg3s, s->tw3t, B, H, H / 64, 1,
+                              EpiDTanh{a->h2s, H, a->g2s, H, a->g2f, B, s->grad + s->L.b2, B, H}, s->err, s->st));
+  SURR_CHECK(gemm_launch<256>(a->tg2s, s->tw2t, B, H, H / 64, 1,
+                              EpiDTanh{a->h1s, H, nullptr, H, a->g1f, B, nullptr, B, H}, s->err, s->st));
+  if ((rc = wgrad<256>(s, a->tg4f, a->th3f, NP, beams, H, s->L.w4))) return rc;
+  if ((rc = wgrad<256>(s, a->tg3f, a->th2f, H, H, H, s->L.w3))) return rc;
+  if ((rc = wgrad<256>(s, a->tg2f, a->th1f, H, H, H, s->L.w2))) return rc;
+  if ((rc = wgrad<64>(s, a->tg1f, a->txf, H, H, NIN, s->L.w1))) return rc;
+  return 0;
+}
+
+int refresh(racer_surrogate* s) {
+  k_refresh<<<296, 256, 0, s->st>>>(s->theta, s->L, s->w1b, s->w2b, s->w3b, s->w4b, s->w2t, s->w3t, s->w4t);
+  SURR_CHECK(cudaGetLastError());
+  return 0;
+}
+
+}  // namespace
+
+extern "C" {
+
+int racer_surrogate_create(racer_sim* sim, int hidden, int batch, uint64_t seed, racer_surrogate** out) {
+  using racer_host::set_error;
+  if (!sim || !out || (hidden != 128 && hidden != 256 && hidden != 512) || batch < 128 || (batch % 128)) {
+    set_error("racer_surrogate_create: hidden must be 128, 256 or 512 and batch a positive multiple of 128");
+    return 1;
+  }
+  if (sim->t.layers > 2) {
+    set_error("racer_surrogate_create: the surrogate's inputs encode at most two layers");
+    return 1;
+  }
+  racer_surrogate* s = new racer_surrogate();
+  s->sim = sim;
+  s->st = sim->st;
+  s->batch = batch;
+  Layout& L = s->L;
+  L.H = hidden;
+  L.beams = sim->beams;
+  L.npad = (sim->beams + 63) / 64 * 64;
+  L.w1 = 0;
+  L.w2 = L.w1 + (long)hidden * NIN;
+  L.b2 = L.w2 + (long)hidden * hidden;
+  L.w3 = L.b2 + hidden;
+  L.b3 = L.w3 + (long)hidden * hidden;
+  L.w4 = L.b3 + hidden;
+  L.b4 = L.w4 + (long)sim->beams * hidden;
+  L.total = L.b4 + sim->beams;
+  const TrackDev& t = sim->t;
+  const float hx = 0.5f * (float)(t.nx - 1) * t.cell, hy = 0.5f * (float)(t.ny - 1) * t.cell;
+  s->nm = Norm{t.x0 + hx, 1.0f / hx, t.y0 + hy, 1.0f / hy};
+  const int H = hidden, NP = L.npad;
+  int rc = 0;
+  s->scratch_floats = (size_t)2 * 148 * 128 * 256 + (size_t)NP * H;
+  if ((rc = salloc(&s->theta, L.total)) || (rc = salloc(&s->grad, L.total)) || (rc = salloc(&s->m1, L.total)) ||
+      (rc = salloc(&s->m2, L.total)) || (rc = salloc(&s->w1b, (size_t)H * NIN)) || (rc = salloc(&s->w2b, (size_t)H * H)) ||
+      (rc = salloc(&s->w3b, (size_t)H * H)) || (rc = salloc(&s->w4b, (size_t)NP * H)) ||
+      (rc = salloc(&s->w2t, (size_t)H * H)) || (rc = salloc(&s->w3t, (size_t)H * H)) ||
+      (rc = salloc(&s->w4t, (size_t)H * NP)) || (rc = salloc(&s->ray, 2 * (size_t)batch)) ||
+      (rc = salloc(&s->label, (size_t)(4 + sim->beams) * batch)) || (rc = salloc(&s->pred, (size_t)sim->beams * batch)) ||
+      (rc = salloc(&s->scratch, s->scratch_floats)) || (rc = salloc(&s->sums, 4)) || (rc = salloc(&s->maxbits, 1)) ||
+      (rc = salloc(&s->over, 1)) || (rc = salloc(&s->err, 1))) {
+    racer_surrogate_destroy(s);
+    return rc;
+  }
+  if ((rc = make_tmap_bf16(&s->tw1, s->w1b, H, NIN, NIN, 256)) || (rc = make_tmap_bf16(&s->tw2, s->w2b, H, H, H, 256)) ||
+      (rc = make_tmap_bf16(&s->tw3, s->w3b, H, H, H, 256)) || (rc = make_tmap_bf16(&s->tw4, s->w4b, NP, H, H, 256)) ||
+      (rc = make_tmap_bf16(&s->tw2t, s->w2t, H, H, H, 256)) || (rc = make_tmap_bf16(&s->tw3t, s->w3t, H, H, H, 256)) ||
+      (rc = make_tmap_bf16(&s->tw4t, s->w4t, H, NP, NP, 256)) || (rc = make_acts(s, &s->train, batch, true))) {
+    racer_surrogate_destroy(s);
+    return rc;
+  }
+  // drivable (cell, layer) pairs from the track's clearance grids
+  std::vector<float> clear((size_t)t.nx * t.ny);
+  std::vector<int2> cells;
+  for (int l = 0; l < t.layers; ++l) {
+    cudaMemcpy(clear.data(), sim->d_track + 12 + (size_t)(3 * l) * t.nx * t.ny, clear.size() * sizeof(float),
+               cudaMemcpyDeviceToHost);
+    for (size_t k = 0; k < clear.size(); ++k)
+      if (clear[k] > 0.0f) cells.push_back(make_int2((int)k, l));
+  }
+  if (cells.empty()) {
+    set_error("racer_surrogate_create: the track has no drivable cell");
+    racer_surrogate_destroy(s);
+    return 1;
+  }
+  s->ncells = (int)cells.size();
+  if ((rc = salloc(&s->cells, cells.size()))) {
+    racer_surrogate_destroy(s);
+    return rc;
+  }
+  cudaMemcpy(s->cells, cells.data(), cells.size() * sizeof(int2), cudaMemcpyHostToDevice);
+  k_init_params<<<296, 256, 0, s->st>>>(s->theta, L, seed);
+  if ((rc = refresh(s))) {
+    racer_surrogate_destroy(s);
+    return rc;
+  }
+  RACER_TRY(cudaStreamSynchronize(s->st));
+  *out = s;
+  return 0;
+}
+
+int racer_surrogate_destroy(racer_surrogate* s) {
+  if (!s) return 0;
+  for (void* p : {(void*)s->theta, (void*)s->grad, (void*)s->m1, (void*)s->m2, (void*)s->w1b, (void*)s->w2b,
+                  (void*)s->w3b, (void*)s->w4b, (void*)s->w2t, (void*)s->w3t, (void*)s->w4t, (void*)s->cells,
+                  (void*)s->poses, (void*)s->ray, (void*)s->label, (void*)s->pred, (void*)s->scratch, (void*)s->sums,
+                  (void*)s->maxbits, (void*)s->over, (void*)s->err})
+    cudaFree(p);
+  free_acts(&s->train);
+  delete s;
+  return 0;
+}
+
+int racer_surrogate_params(racer_surrogate* s, float** theta, float** grad, long* count, int* hidden) {
+  if (!s) {
+    racer_host::set_error("racer_surrogate_params: null surrogate");
+    return 1;
+  }
+  if (theta) *theta = s->theta;
+  if (grad) *grad = s->grad;
+  if (count) *count = s->L.total;
+  if (hidden) *hidden = s->L.H;
+  return 0;
+}
+
+// The training set: `count` poses (a multiple of the batch) drawn with `seed`.
+int racer_surrogate_set_poses(racer_surrogate* s, long count, uint64_t seed) {
+  if (!s || count < s->batch || (count % s->batch)) {
+    racer_host::set_error("racer_surrogate_set_poses: count must be a positive multiple of the batch");
+    return 1;
+  }
+  cudaFree(s->poses);
+  s->poses = nullptr;
+  if (int rc = salloc(&s->poses, (size_t)count)) return rc;
+  s->npose = (int)count;
+  k_sample_poses<<<(unsigned)((count + 255) / 256), 256, 0, s->st>>>(s->cells, s->ncells, (int)count, seed, s->sim->t,
+                                                                       s->poses);
+  RACER_TRY(cudaGetLastError());
+  return 0;
+}
+
+// Poses (x, y, heading, layer) of the training set, for inspection.
+int racer_surrogate_poses(racer_surrogate* s, void** poses, long* count) {
+  if (!s) {
+    racer_host::set_error("racer_surrogate_poses: null surrogate");
+    return 1;
+  }
+  if (poses) *poses = s->poses;
+  if (count) *count = s->npose;
+  return 0;
+}
+
+// Gradient of the batch starting at pose `first` (no update); labels stay in the label buffer.
+int racer_surrogate_gradient(racer_surrogate* s, long first, float* mse, float* label_dev_out) {
+  if (!s || !s->poses || first < 0 || first + s->batch > s->npose) {
+    racer_host::set_error("racer_surrogate_gradient: set poses first; the batch must lie inside the pose set");
+    return 1;
+  }
+  if (int rc = gradient(s, first)) return rc;
+  if (label_dev_out)
+    RACER_TRY(cudaMemcpyAsync(label_dev_out, s->label + 4L * s->batch, (size_t)s->L.beams * s->batch * sizeof(float),
+                              cudaMemcpyDeviceToDevice, s->st));
+  double sums[2];
+  RACER_TRY(cudaMemcpyAsync(sums, s->sums, sizeof sums, cudaMemcpyDeviceToHost, s->st));
+  RACER_TRY(cudaStreamSynchronize(s->st));
+  if (mse) *mse = (float)(sums[0] / ((double)s->batch * s->L.beams));
+  return 0;
+}
+
+// `steps` Adam steps over consecutive batches of the pose set; lr decays by cosine to lr/100.
+int racer_surrogate_train(racer_surrogate* s, int steps, float lr, float* last_mse, float* last_mae_m) {
+  if (!s || !s->poses || steps < 1 || !(lr > 0)) {
+    racer_host::set_error("racer_surrogate_train: set poses first; steps >= 1, lr > 0");
+    return 1;
+  }
+  const int per_epoch = s->npose / s->batch;
+  for (int k = 0; k < steps; ++k) {
+    long first = (long)(s->step % per_epoch) * s->batch;
+    if (int rc = gradient(s, first)) return rc;
+    s->step += 1;
+    const float frac = (float)k / (float)steps;
+    const float rate = lr * (0.01f + 0.99f * 0.5f * (1.0f + cosf(3.14159265f * frac)));
+    const float c1 = 1.0f - powf(0.9f, (float)s->step), c2 = 1.0f - powf(0.999f, (float)s->step);
+    k_adam_s<<<592, 256, 0, s->st>>>(s->L.total, rate, c1, c2, s->theta, s->grad, s->m1, s->m2);
+    RACER_TRY(cudaGetLastError());
+    if (int rc = refresh(s)) return rc;
+  }
+  double sums[2];
+  RACER_TRY(cudaMemcpyAsync(sums, s->sums, sizeof sums, cudaMemcpyDeviceToHost, s->st));
+  RACER_TRY(cudaStreamSynchronize(s->st));
+  const double total = (double)s->batch * s->L.beams;
+  if (last_mse) *last_mse = (float)(sums[0] / total);
+  if (last_mae_m) *last_mae_m = (float)(sums[1] / total * RANGE);
+  return 0;
+}
+
+// Held-out error: `batches` fresh batches of poses drawn with `seed`, surrogate vs exact tracer.
+int racer_surrogate_evaluate(racer_surrogate* s, int batches, uint64_t seed, float* mae_m, float* rmse_m, float* max_m,
+                             float* frac_over_5cm) {
+  if (!s || batches < 1) {
+    racer_host::set_error("racer_surrogate_evaluate: bad argument");
+    return 1;
+  }
+  float4* keep = s->poses;
+  int keep_n = s->npose;
+  s->poses = nullptr;
+  int rc = racer_surrogate_set_poses(s, (long)batches * s->batch, seed);
+  if (rc) {
+    s->poses = keep;
+    s->npose = keep_n;
+    return rc;
+  }
+  RACER_TRY(cudaMemsetAsync(s->sums + 2, 0, 2 * sizeof(double), s->st));
+  RACER_TRY(cudaMemsetAsync(s->maxbits, 0, sizeof(unsigned), s->st));
+  RACER_TRY(cudaMemsetAsync(s->over, 0, sizeof(unsigned long long), s->st));
+  SurrogateActs* a = &s->train;
+  const int B = s->batch;
+  for (int k = 0; k < batches && !rc; ++k) {
+    if ((rc = prepare(s, a, (long)k * B))) break;
+    EpiInfer inf{s->pred, B, s->theta + s->L.b4, B, s->L.beams, nullptr};
+    if ((rc = forward(s, a, false, &inf))) break;
+    k_compare<<<296, 256, 0, s->st>>>(s->pred, s->label + 4L * B, (long)s->L.beams * B, s->sums + 2, s->maxbits,
+                                      s->over);
+  }
+  cudaFree(s->poses);
+  s->poses = keep;
+  s->npose = keep_n;
+  if (rc) return rc;
+  double sums[2];
+  unsigned mx = 0;
+  unsigned long long over = 0;
+  RACER_TRY(cudaMemcpyAsync(sums, s->sums + 2, sizeof sums, cudaMemcpyDeviceToHost, s->st));
+  RACER_TRY(cudaMemcpyAsync(&mx, s->maxbits, sizeof mx, cudaMemcpyDeviceToHost, s->st));
+  RACER_TRY(cudaMemcpyAsync(&over, s->over, sizeof over, cudaMemcpyDeviceToHost, s->st));
+  RACER_TRY(cudaStreamSynchronize(s->st));
+  const double total = (double)batches * B * s->L.beams;
+  if (mae_m) *mae_m = (float)(sums[0] / total);
+  if (rmse_m) *rmse_m = (float)std::sqrt(sums[1] / total);
+  if (max_m) {
+    float f;
+    memcpy(&f, &mx, sizeof f);
+    *max_m = f;
+  }
+  if (frac_over_5cm) *frac_over_5cm = (float)((double)over / total);
+  return 0;
+}
+
+}  // extern "C"

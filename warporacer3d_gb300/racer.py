@@ -248,6 +248,60 @@ class Trainer:
         call("racer_trainer_minibatch", self.handle, policy.handle, m, float(adv_mean), float(adv_scale))
 
 
+class Surrogate:
+    """Learned lidar for one sim's track: lidar frame -> all beam ranges (BF16 MLP on tcgen05)."""
+
+    def __init__(self, sim, hidden=512, batch=8192, seed=0):
+        self.sim = sim
+        h = ctypes.c_void_p()
+        call("racer_surrogate_create", sim.handle, hidden, batch, seed, ctypes.byref(h))
+        self.handle = h
+        self.batch, self.hidden = batch, hidden
+        th, gr, count = ctypes.c_void_p(), ctypes.c_void_p(), ctypes.c_long()
+        call("racer_surrogate_params", h, ctypes.byref(th), ctypes.byref(gr), ctypes.byref(count), None)
+        self.theta = DevArray(th.value, (count.value,), owner=self, stream=sim.stream)
+        self.grad = DevArray(gr.value, (count.value,), owner=self, stream=sim.stream)
+
+    def __del__(self):
+        if getattr(self, "handle", None):
+            load_library().racer_surrogate_destroy(self.handle)
+            self.handle = None
+
+    def layout(self):
+        H, beams, n = self.hidden, self.sim.beams, 8
+        sizes = [("W1", (H, n)), ("W2", (H, H)), ("b2", (H,)), ("W3", (H, H)), ("b3", (H,)), ("W4", (beams, H)),
+                 ("b4", (beams,))]
+        out, off = {}, 0
+        for name, shape in sizes:
+            out[name] = (off, shape)
+            off += int(np.prod(shape))
+        return out
+
+    def set_poses(self, count, seed=1):
+        call("racer_surrogate_set_poses", self.handle, count, seed)
+
+    def poses(self):
+        p, count = ctypes.c_void_p(), ctypes.c_long()
+        call("racer_surrogate_poses", self.handle, ctypes.byref(p), ctypes.byref(count))
+        return DevArray(p.value, (count.value, 4), owner=self, stream=self.sim.stream)
+
+    def gradient(self, first=0, labels=None):
+        mse = ctypes.c_float()
+        call("racer_surrogate_gradient", self.handle, first, ctypes.byref(mse), labels.c if labels else None)
+        return mse.value
+
+    def train(self, steps, lr=1e-3):
+        mse, mae = ctypes.c_float(), ctypes.c_float()
+        call("racer_surrogate_train", self.handle, steps, lr, ctypes.byref(mse), ctypes.byref(mae))
+        return mse.value, mae.value
+
+    def evaluate(self, batches=4, seed=12345):
+        """Held-out error against the exact tracer: MAE, RMSE, max (metres) and fraction of beams off by > 5 cm."""
+        out = [ctypes.c_float() for _ in range(4)]
+        call("racer_surrogate_evaluate", self.handle, batches, seed, *[ctypes.byref(o) for o in out])
+        return tuple(o.value for o in out)
+
+
 def save(policy, path, iteration):
     call("racer_policy_save", policy.handle, str(path).encode(), iteration)
 

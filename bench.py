@@ -48,6 +48,7 @@ def parse():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-surrogate", action="store_true")
     return ap.parse_args()
 
 
@@ -132,6 +133,52 @@ def cpu_baseline(track, seconds=12.0, max_steps=200, threads=None):
     return {"value": CARS * steps / dt, "unit": "env-steps/s", "cores": threads, "kind": "port",
             "sample": f"{steps} env steps of {CARS} cars on {TRACK} at {BEAMS} beams (Runner.step: policy forward, "
                       f"sampling, physics, lidar) in {dt:.1f} s"}
+
+
+SURR_CARS, SURR_STEPS, SURR_REPS, SURR_TRAIN_STEPS = 65536, 32, 3, 20000
+
+
+def surrogate_section(torch, W, track, stream, flush):
+    """Learned lidar on bridge at 65536 cars: exact FP32 rollout vs BF16 surrogate rollout
+    (audit every 16th step, exact fallback under 0.5 m), both device-timed like `value`."""
+    exact = W.Runner(track, SURR_CARS, beams=BEAMS, seed=7, stream=stream)
+    learned = W.Runner(track, SURR_CARS, beams=BEAMS, seed=7, stream=stream)
+    sur = W.Surrogate(learned.sim, hidden=512, batch=8192, seed=1)
+    sur.set_poses(1 << 22, seed=2)
+    t0 = time.perf_counter()
+    sur.train(SURR_TRAIN_STEPS, lr=2e-3)
+    torch.cuda.synchronize()
+    train_s = time.perf_counter() - t0
+    heldout = sur.evaluate(8, 99)
+
+    def timed(run):
+        run(0)
+        torch.cuda.synchronize()
+        ms = 0.0
+        for k in range(SURR_REPS):
+            with torch.cuda.stream(stream):
+                flush.zero_()
+                a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                a.record(stream)
+                run((k + 1) * SURR_STEPS)
+                b.record(stream)
+            torch.cuda.synchronize()
+            ms += a.elapsed_time(b)
+        return SURR_CARS * SURR_STEPS * SURR_REPS / (ms / 1000.0)
+
+    exact_rate = timed(lambda t0: exact.rollout(SURR_STEPS, False, t0))
+    learned_rate = timed(lambda t0: learned.rollout_surrogate(sur, SURR_STEPS, False, t0, 16, 0.5))
+    mae, rmse, mx, over, fallback = sur.rollout_stats()
+    return {"workload": f"{TRACK}, {SURR_CARS} cars, {BEAMS} beams, {SURR_STEPS}-step rollouts",
+            "exact_fp32_env_steps_per_s": exact_rate, "surrogate_bf16_env_steps_per_s": learned_rate,
+            "speedup": learned_rate / exact_rate, "audit_every": 16, "fallback_m": 0.5,
+            "audited_mae_m": mae, "audited_rmse_m": rmse, "audited_max_m": mx, "audited_frac_over_5cm": over,
+            "fallback_frac": fallback,
+            "heldout_mae_m": heldout[0], "heldout_rmse_m": heldout[1], "heldout_frac_over_5cm": heldout[3],
+            "surrogate": "64 encoded inputs -> 3 x 512 tanh -> 1081, BF16 tcgen05, FP32 Adam",
+            "training": f"{SURR_TRAIN_STEPS} steps x 8192 poses from 2^22 drawn over drivable cells, "
+                        f"exact-tracer labels, {train_s:.1f} s",
+            "target_mae_m": 0.02}
 
 
 def run_reference(args, rank, world):
@@ -261,6 +308,9 @@ def main():
                        "policy": "tanh MLP 1086-64-64-3"},
             "beam_steps_per_s": value * BEAMS, "wall_s": wall, "gpu_launches": kernels_per_rollout * args.steps,
             "clocks": clocks.summary(), "e2e": e2e, "roofline": roofline}
+    if not args.no_surrogate:
+        del runner
+        line["surrogate"] = surrogate_section(torch, W, track, stream, flush)
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline(track)
     if rank == 0:

@@ -150,12 +150,13 @@ int racer_rollout(racer_sim* sim, racer_policy* policy, racer_acts* acts, float*
  * racer/sim.mojo:238-266's tracing during rollouts, audited by it) ---- */
 typedef struct racer_surrogate racer_surrogate;
 /* MLP from the lidar frame (origin x, y, z; sin/cos heading; layer one-hot;
- * constant 1) through three tanh layers of `hidden` (128, 256 or 512) to the
- * sim's `beams` ranges / 10 m, for the sim's track (at most two layers).
+ * constant 1; fixed Fourier features of x, y, z and heading: 64 inputs)
+ * through three tanh layers of `hidden` (128, 256 or 512) to the sim's
+ * `beams` ranges / 10 m, for the sim's track (at most two layers).
  * `batch` (a multiple of 128) is the training batch; `seed` the init. */
 int racer_surrogate_create(racer_sim* sim, int hidden, int batch, uint64_t seed, racer_surrogate** out);
 int racer_surrogate_destroy(racer_surrogate* surrogate);
-/* FP32 master parameters W1 [H,8] | W2 [H,H] | b2 [H] | W3 [H,H] | b3 [H] |
+/* FP32 master parameters W1 [H,64] | W2 [H,H] | b2 [H] | W3 [H,H] | b3 [H] |
  * W4 [beams,H] | b4 [beams], and their last gradient (device pointers). */
 int racer_surrogate_params(racer_surrogate* surrogate, float** theta_dev, float** grad_dev, long* count, int* hidden);
 /* Training set: `count` poses (a multiple of the batch), uniform over the
@@ -173,6 +174,19 @@ int racer_surrogate_train(racer_surrogate* surrogate, int steps, float lr, float
 /* Held-out error on `batches` fresh batches drawn with `seed`, surrogate vs exact. */
 int racer_surrogate_evaluate(racer_surrogate* surrogate, int batches, uint64_t seed, float* mae_m, float* rmse_m,
                              float* max_m, float* frac_over_5cm);
+
+/* `steps` Runner steps from one CUDA graph with the lidar rows of the
+ * observations predicted by `surrogate` (built for this sim): every
+ * `audit_every`-th step (0 = never) is traced exactly for all cars and the
+ * prediction error accumulated; on the other steps each car whose smallest
+ * predicted range is below `fallback_m` metres is traced exactly. */
+int racer_rollout_surrogate(racer_sim* sim, racer_policy* policy, racer_acts* acts, float* scratch_dev,
+                            racer_surrogate* surrogate, int steps, int deterministic, int64_t step0, int audit_every,
+                            float fallback_m);
+/* Audited error (metres) and the fraction of non-audit car-steps that fell
+ * back to the exact tracer, since the last reset (reset != 0 clears them). */
+int racer_surrogate_rollout_stats(racer_surrogate* surrogate, float* mae_m, float* rmse_m, float* max_m,
+                                  float* frac_over_5cm, float* fallback_frac, int reset);
 
 /* ---- dense products (Device.gemm with transpose_b, racer/device.mojo:82-98) ---- */
 /* C[M, N] (float32, row-major, ldc) = A[M, K] . B[N, K]^T on the tcgen05 tensor

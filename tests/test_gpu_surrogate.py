@@ -82,9 +82,19 @@ def test_gradient_matches_float64_backprop():
     fr = rest_frames(track, poses)
     nx, ny, x0, y0, cell = track[0], track[1], track[2], track[3], track[4]
     hx, hy = np.float32(0.5) * np.float32(nx - 1) * cell, np.float32(0.5) * np.float32(ny - 1) * cell
-    feats = np.stack([(fr[:, 3] - (x0 + hx)) * (np.float32(1) / hx), (fr[:, 4] - (y0 + hy)) * (np.float32(1) / hy),
-                      fr[:, 5], fr[:, 6], fr[:, 7], poses[:, 3] == 0, poses[:, 3] == 1, np.ones(B)], 1)
-    X = bf16(feats.astype(np.float32))
+    xn = (fr[:, 3] - (x0 + hx)) * (np.float32(1) / hx)
+    yn = (fr[:, 4] - (y0 + hy)) * (np.float32(1) / hy)
+    z, sh, ch = fr[:, 5], fr[:, 6], fr[:, 7]
+    cols = [xn, yn, z, sh, ch, poses[:, 3] == 0, poses[:, 3] == 1, np.ones(B)]
+    for k in range(10):
+        a, b = np.pi * 2.0 ** k * xn.astype(np.float64), np.pi * 2.0 ** k * yn.astype(np.float64)
+        cols += [np.sin(a), np.cos(a), np.sin(b), np.cos(b)]
+    h = np.arctan2(sh.astype(np.float64), ch.astype(np.float64))
+    for j in range(2, 6):
+        cols += [np.sin(j * h), np.cos(j * h)]
+    cols += [np.sin(np.pi * z), np.cos(np.pi * z), np.sin(2 * np.pi * z), np.cos(2 * np.pi * z)]
+    cols += [np.zeros(B)] * 4
+    X = bf16(np.stack(cols, 1).astype(np.float32))
     Wb = {k: bf16(P[k]) for k in ("W1", "W2", "W3", "W4")}
     h1 = bf16(np.tanh(X @ Wb["W1"].T))
     h2 = bf16(np.tanh(h1 @ Wb["W2"].T + P["b2"]))
@@ -101,6 +111,40 @@ def test_gradient_matches_float64_backprop():
         g = grad[o:o + int(np.prod(s))].reshape(s)
         rel = np.linalg.norm(g - r) / np.linalg.norm(r)
         assert rel < 2e-2, (k, rel)
+
+
+@pytest.mark.parametrize("audit_every,fallback_m", [(1, 0.5), (0, 100.0)])
+def test_fully_exact_surrogate_rollout_equals_exact_rollout(audit_every, fallback_m):
+    """Audit on every step, or a fallback threshold every car crosses: the rollout is the exact one."""
+    track = W.track("bridge")
+    n = 512
+    exact = W.Runner(track, n, beams=1081, seed=3)
+    sur_run = W.Runner(track, n, beams=1081, seed=3)
+    sur = W.Surrogate(sur_run.sim, hidden=128, batch=1024, seed=1)
+    exact.rollout(6, False, 40)
+    sur_run.rollout_surrogate(sur, 6, False, 40, audit_every=audit_every, fallback_m=fallback_m)
+    sur_run.synchronize()
+    for name in ("state", "obs", "reward", "done", "actions"):
+        assert np.array_equal(getattr(exact.sim, name).numpy(), getattr(sur_run.sim, name).numpy()), name
+    mae, rmse, mx, over, fb = sur.rollout_stats()
+    if audit_every:
+        assert mae > 0 and rmse >= mae and mx >= rmse
+    else:
+        assert fb == 1.0
+
+
+def test_surrogate_rollout_stats_and_fallback():
+    track = W.track("bridge")
+    run = W.Runner(track, 1024, beams=1081, seed=5)
+    sur = W.Surrogate(run.sim, hidden=128, batch=1024, seed=1)
+    sur.set_poses(1 << 14, seed=2)
+    sur.train(50, lr=1e-3)
+    run.rollout_surrogate(sur, 8, audit_every=4, fallback_m=0.5)
+    mae, rmse, mx, over, fb = sur.rollout_stats(reset=True)
+    assert np.isfinite([mae, rmse, mx, over, fb]).all() and mae > 0 and 0 <= fb <= 1
+    o = run.sim.obs.numpy()
+    assert np.isfinite(o).all() and (o[4:-1] >= 0).all() and (o[4:-1] <= 1).all()
+    assert sur.rollout_stats()[0] == 0.0  # reset
 
 
 def test_training_reduces_heldout_error():

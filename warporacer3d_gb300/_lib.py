@@ -74,6 +74,9 @@ SIGNATURES = {
     "racer_surrogate_gradient": [c_void_p, ctypes.c_long, P(c_float), c_void_p],
     "racer_surrogate_train": [c_void_p, c_int, c_float, P(c_float), P(c_float)],
     "racer_surrogate_evaluate": [c_void_p, c_int, c_uint64, P(c_float), P(c_float), P(c_float), P(c_float)],
+    "racer_rollout_surrogate": [c_void_p, c_void_p, c_void_p, c_void_p, c_void_p, c_int, c_int, c_int64, c_int,
+                                c_float],
+    "racer_surrogate_rollout_stats": [c_void_p, P(c_float), P(c_float), P(c_float), P(c_float), P(c_float), c_int],
     "racer_gemm_bf16":[c_void_p, c_void_p, c_void_p, c_int, c_int, c_int, c_int, c_int, c_int, c_int, c_void_p,
                         c_void_p, c_void_p],
     "racer_rollout_kernel_count":[c_void_p, c_void_p, c_void_p, c_void_p, c_int, c_int, P(c_int64)],

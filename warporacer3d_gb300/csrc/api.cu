@@ -21,6 +21,7 @@
 #include "kernels.h"
 #include "objects.h"
 #include "policy_fwd.h"
+#include "surrogate.h"
 
 namespace racer_host {
 static thread_local std::string g_error;
@@ -215,6 +216,7 @@ int racer_sim_create(const float* track, size_t len, int n, uint64_t seed, int b
 int racer_sim_destroy(racer_sim* s) {
   if (!s) return 0;
   for (auto& kv : s->graphs) cudaGraphExecDestroy(kv.second);
+  for (auto& kv : s->surrogate_graphs) cudaGraphExecDestroy(kv.second);
   cudaFree(s->d_track);
   cudaFree(s->d_cl);
   cudaFree(s->beam_dir);
@@ -605,8 +607,11 @@ int racer_trainer_update(racer_trainer* tr, racer_policy* p, float* kl) {
 
 // ---------------- Runner ----------------
 
+// One Runner step (main.mojo:40-48). With a surrogate, the lidar rows come
+// from it (audited by, or falling back to, the exact tracer).
 static int runner_step_on(racer_sim* s, racer_policy* p, racer_acts* a, float* scratch, int det,
-                          const int64_t* base, int64_t add, cudaStream_t st) {
+                          const int64_t* base, int64_t add, cudaStream_t st, racer_surrogate* sur = nullptr,
+                          bool audit = false, float fallback = 0.0f) {
   SampleArgs sa;
   sa.seed = s->seed;
   sa.log_std = policy_theta(p) + policy_params(p) - 2;
@@ -618,7 +623,44 @@ static int runner_step_on(racer_sim* s, racer_policy* p, racer_acts* a, float* s
   sa.step_add = add;
   int rc = forward_on(p, s->obs, a, st, &sa, 0);
   if (rc) return rc;
-  return sim_step_on(s, s->actions, s->reward, s->done, s->obs, nullptr, st);
+  if (!sur) return sim_step_on(s, s->actions, s->reward, s->done, s->obs, nullptr, st);
+  launch_advance(s->t, s->state, s->actions, s->reward, s->done, s->obs, s->n, s->beams, s->seed, s->ray, st);
+  RACER_LAUNCHED();
+  return surrogate_lidar(sur, s, s->obs, audit, fallback, st);
+}
+
+int racer_rollout_surrogate(racer_sim* s, racer_policy* p, racer_acts* a, float* scratch, racer_surrogate* sur,
+                            int steps, int det, int64_t step0, int audit_every, float fallback_m) {
+  RACER_ARG(s && p && a && scratch && sur && steps >= 1 && audit_every >= 0, "racer_rollout_surrogate: bad argument");
+  RACER_ARG(a->cols == s->n && policy_inputs(p) == s->in_rows, "racer_rollout_surrogate: sizes differ");
+  if (int rc = surrogate_prepare(sur, s)) return rc;
+  const float fallback = fallback_m / RANGE;
+  auto key = std::make_tuple((const void*)p, (const void*)a, (const void*)scratch, steps, det, (const void*)sur,
+                             audit_every, fallback);
+  auto it = s->surrogate_graphs.find(key);
+  int audits = 0;
+  for (int k = 0; k < steps; ++k) audits += audit_every > 0 && k % audit_every == 0;
+  if (it == s->surrogate_graphs.end()) {
+    cudaGraph_t g;
+    RACER_TRY(cudaStreamBeginCapture(s->st, cudaStreamCaptureModeThreadLocal));
+    int rc = 0;
+    for (int k = 0; k < steps && !rc; ++k)
+      rc = runner_step_on(s, p, a, scratch, det, s->step_base, k, s->st, sur, audit_every > 0 && k % audit_every == 0,
+                          fallback);
+    cudaError_t end = cudaStreamEndCapture(s->st, &g);
+    if (rc) return rc;
+    RACER_TRY(end);
+    cudaGraphExec_t exec;
+    cudaError_t inst = cudaGraphInstantiate(&exec, g, 0);
+    cudaGraphDestroy(g);
+    RACER_TRY(inst);
+    it = s->surrogate_graphs.emplace(key, exec).first;
+  }
+  k_set_i64<<<1, 32, 0, s->st>>>(s->step_base, step0);
+  RACER_LAUNCHED();
+  RACER_TRY(cudaGraphLaunch(it->second, s->st));
+  surrogate_account(sur, s, steps, audits);
+  return 0;
 }
 
 int racer_runner_step(racer_sim* s, racer_policy* p, racer_acts* a, float* scratch, int det, int64_t t) {

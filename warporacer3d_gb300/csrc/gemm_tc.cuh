@@ -113,17 +113,26 @@ __global__ void __launch_bounds__(192, 1)
   if (!ok) atomicExch(err, 1);
 }
 
+// Sets the kernel's shared-memory limit once (call before capturing a launch into a graph).
+template <int BN, typename Epi>
+cudaError_t gemm_configure() {
+  static bool configured = false;
+  if (!configured) {
+    cudaError_t e =
+        cudaFuncSetAttribute(k_gemm<BN, Epi>, cudaFuncAttributeMaxDynamicSharedMemorySize, GemmCfg<BN>::SMEM);
+    if (e != cudaSuccess) return e;
+    configured = true;
+  }
+  return cudaSuccess;
+}
+
 // Launch over an M x N output with K = kblocks * 64 split into `splits` ranges.
 template <int BN, typename Epi>
 cudaError_t gemm_launch(const CUtensorMap& ta, const CUtensorMap& tb, int M, int N, int kblocks, int splits,
                         const Epi& epi, int* err, cudaStream_t st) {
   using C = GemmCfg<BN>;
-  static bool configured = false;
-  if (!configured) {
-    cudaError_t e = cudaFuncSetAttribute(k_gemm<BN, Epi>, cudaFuncAttributeMaxDynamicSharedMemorySize, C::SMEM);
-    if (e != cudaSuccess) return e;
-    configured = true;
-  }
+  cudaError_t ce = gemm_configure<BN, Epi>();
+  if (ce != cudaSuccess) return ce;
   if (splits < 1) splits = 1;
   const int per = (kblocks + splits - 1) / splits;
   splits = (kblocks + per - 1) / per;

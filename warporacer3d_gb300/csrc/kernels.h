@@ -12,8 +12,12 @@ void launch_spawn(const TrackDev& t, float* state, float* actions, int n, uint64
 // ray [2, n] float4: the per-car lidar frame the physics kernel leaves for the lidar.
 void launch_advance(const TrackDev& t, float* state, const float* actions, float* reward, float* done, float* obs,
                     int n, int beams, uint64_t seed, float4* ray, cudaStream_t st);
+// With `list` set, only the cars list[0 .. *list_count) (list_max at most) are traced.
 void launch_lidar(const TrackDev& t, const float4* ray, float* obs, int n, int beams, const float2* beam_dir,
-                  int* iters, cudaStream_t st);
+                  int* iters, cudaStream_t st, const int* list = nullptr, const int* list_count = nullptr,
+                  int list_max = 0);
+// Cars whose smallest predicted range (ordered uint bits of a nonnegative float) is below threshold.
+void launch_select_cars(const unsigned* minr, int n, float threshold, int* list, int* count, cudaStream_t st);
 int lidar_max_iters(const TrackDev& t);
 // poses [count] (x, y, heading, layer) -> ray [2, count]: the frame of a car at rest there.
 void launch_pose_frames(const TrackDev& t, const float4* poses, int count, float4* ray, cudaStream_t st);

@@ -26,4 +26,7 @@ struct racer_sim {
   bool owned = false;
   std::map<std::tuple<const void*, const void*, const void*, int, int>, cudaGraphExec_t> graphs;
   std::map<std::tuple<const void*, const void*, const void*, int, int>, size_t> graph_kernels;
+  // rollouts with the learned lidar: (policy, acts, scratch, steps, det, surrogate, audit_every, fallback)
+  std::map<std::tuple<const void*, const void*, const void*, int, int, const void*, int, float>, cudaGraphExec_t>
+      surrogate_graphs;
 };

@@ -15,6 +15,8 @@
 // kept unchanged and, for the probes, repacked per cell as
 // [ny * nx][layers] float2 (clearance, height): one 16-byte load answers a
 // two-layer probe.
+#include <string.h>
+
 #include "common.cuh"
 #include "kernels.h"
 #include "philox.h"
@@ -300,9 +302,13 @@ __global__ void k_pose_frames(TrackDev t, const float4* __restrict__ poses, int 
 template <int LAYERS>
 __global__ void __launch_bounds__(256) k_lidar(TrackDev t, const float4* __restrict__ ray, float* obs, int n,
                                                int beams, const float2* __restrict__ beam_dir, int max_iters,
-                                               int* iters) {
-  const int car = blockIdx.x * 8 + (threadIdx.x >> 5);
+                                               int* iters, const int* __restrict__ list, const int* list_count) {
+  int car = blockIdx.x * 8 + (threadIdx.x >> 5);
   const int beam = blockIdx.y * 32 + (threadIdx.x & 31);
+  if (list) {  // only the listed cars (surrogate fallback)
+    if (car >= *list_count) return;
+    car = list[car];
+  }
   if (car >= n || beam >= beams) return;
   const float4 r0 = __ldg(ray + car), r1 = __ldg(ray + n + car);  // (ox, oy, oz, cos h), (sin h, along, across)
   const float2 az = __ldg(beam_dir + beam);                        // (cos azimuth, sin azimuth)
@@ -376,15 +382,27 @@ void launch_advance(const TrackDev& t, float* state, const float* actions, float
 int lidar_max_iters(const TrackDev& t) { return (int)ceilf(RANGE / (0.5f * t.cell)) + 2; }
 
 void launch_lidar(const TrackDev& t, const float4* ray, float* obs, int n, int beams, const float2* beam_dir,
-                  int* iters, cudaStream_t st) {
-  dim3 grid((n + 7) / 8, (beams + 31) / 32);
+                  int* iters, cudaStream_t st, const int* list, const int* list_count, int list_max) {
+  dim3 grid(((list ? list_max : n) + 7) / 8, (beams + 31) / 32);
+  if (grid.x == 0) return;
   int cap = lidar_max_iters(t);
   if (t.layers == 1)
-    k_lidar<1><<<grid, 256, 0, st>>>(t, ray, obs, n, beams, beam_dir, cap, iters);
+    k_lidar<1><<<grid, 256, 0, st>>>(t, ray, obs, n, beams, beam_dir, cap, iters, list, list_count);
   else if (t.layers == 2)
-    k_lidar<2><<<grid, 256, 0, st>>>(t, ray, obs, n, beams, beam_dir, cap, iters);
+    k_lidar<2><<<grid, 256, 0, st>>>(t, ray, obs, n, beams, beam_dir, cap, iters, list, list_count);
   else
-    k_lidar<0><<<grid, 256, 0, st>>>(t, ray, obs, n, beams, beam_dir, cap, iters);
+    k_lidar<0><<<grid, 256, 0, st>>>(t, ray, obs, n, beams, beam_dir, cap, iters, list, list_count);
+}
+
+__global__ void k_select_cars(const unsigned* minr, int n, unsigned threshold_bits, int* list, int* count) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n && minr[i] < threshold_bits) list[atomicAdd(count, 1)] = i;
+}
+
+void launch_select_cars(const unsigned* minr, int n, float threshold, int* list, int* count, cudaStream_t st) {
+  unsigned bits;
+  memcpy(&bits, &threshold, sizeof bits);
+  k_select_cars<<<(n + 255) / 256, 256, 0, st>>>(minr, n, bits, list, count);
 }
 
 void launch_pose_frames(const TrackDev& t, const float4* poses, int count, float4* ray, cudaStream_t st) {

@@ -2,9 +2,10 @@
 // beam ranges, trained on the GPU against the exact sphere tracer.
 //
 // Network (one hidden width H, default 512):
-//   inputs  f = (x', y', z, sin h, cos h, [layer == 0], [layer == 1], 1)
-//           with (x, y, z) the lidar origin, x', y' scaled to [-1, 1] over the map
-//   h1 = tanh(W1 f)            W1 [H, 8] (the constant input is its bias)
+//   inputs  f = encode(x', y', z, sin h, cos h, layer): the frame itself, a
+//           constant 1 and fixed Fourier features (k_features), 64 values;
+//           (x, y, z) is the lidar origin, x', y' scaled to [-1, 1] over the map
+//   h1 = tanh(W1 f)            W1 [H, 64] (the constant input is its bias)
 //   h2 = tanh(W2 h1 + b2)      W2 [H, H]
 //   h3 = tanh(W3 h2 + b3)      W3 [H, H]
 //   y  = W4 h3 + b4            W4 [beams, H]; y = range / RANGE per beam
@@ -37,7 +38,7 @@ using bf16 = __nv_bfloat16;
 namespace racer {
 namespace {
 
-constexpr int NIN = 8;
+constexpr int NIN = 64;  // encoded inputs (see k_features)
 
 struct Norm {
   float xc, inv_xs, yc, inv_ys;
@@ -202,17 +203,51 @@ struct EpiInfer {
   }
 };
 
-// ray frames [2, count] -> inputs, sample-major x [count, 8] and feature-major xf [8, count].
+// ray frames [2, count] -> encoded inputs, sample-major x [count, 64] and feature-major xf [64, count]:
+//   0..7    x', y', z, sin h, cos h, [layer 0], [layer 1], 1
+//   8..47   sin/cos(2^k pi x'), sin/cos(2^k pi y') for k = 0..9  (Fourier features,
+//           Tancik et al. 2020: a plain MLP on raw coordinates fits the
+//           high-frequency range field far too slowly)
+//   48..55  sin/cos(j h) for j = 2..5
+//   56..59  sin/cos(pi z), sin/cos(2 pi z)
+//   60..63  0
+__device__ __forceinline__ void encode(float xn, float yn, float z, float sh, float ch, float layer, float* f) {
+  f[0] = xn;
+  f[1] = yn;
+  f[2] = z;
+  f[3] = sh;
+  f[4] = ch;
+  f[5] = layer == 0.0f ? 1.0f : 0.0f;
+  f[6] = layer == 1.0f ? 1.0f : 0.0f;
+  f[7] = 1.0f;
+  float scale = 1.0f;
+#pragma unroll
+  for (int k = 0; k < 10; ++k) {
+    sincospif(scale * xn, &f[8 + 4 * k], &f[9 + 4 * k]);
+    sincospif(scale * yn, &f[10 + 4 * k], &f[11 + 4 * k]);
+    scale *= 2.0f;
+  }
+  const float h = atan2f(sh, ch);
+#pragma unroll
+  for (int j = 2; j <= 5; ++j) sincosf((float)j * h, &f[48 + 2 * (j - 2)], &f[49 + 2 * (j - 2)]);
+  sincospif(z, &f[56], &f[57]);
+  sincospif(2.0f * z, &f[58], &f[59]);
+  f[60] = f[61] = f[62] = f[63] = 0.0f;
+}
+
 __global__ void k_features(const float4* __restrict__ ray, int count, Norm nm, bf16* x, bf16* xf) {
   int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= count) return;
   const float4 r0 = ray[i], r1 = ray[count + i];
-  float f[NIN] = {(r0.x - nm.xc) * nm.inv_xs, (r0.y - nm.yc) * nm.inv_ys, r0.z, r1.x, r0.w,
-                  r1.w == 0.0f ? 1.0f : 0.0f, r1.w == 1.0f ? 1.0f : 0.0f, 1.0f};
-  uint4 pk = make_uint4(tc::pack_bf16(f[0], f[1]), tc::pack_bf16(f[2], f[3]), tc::pack_bf16(f[4], f[5]),
-                        tc::pack_bf16(f[6], f[7]));
-  *reinterpret_cast<uint4*>(x + (long)i * NIN) = pk;
+  float f[NIN];
+  encode((r0.x - nm.xc) * nm.inv_xs, (r0.y - nm.yc) * nm.inv_ys, r0.z, r1.x, r0.w, r1.w, f);
+  uint4* row = reinterpret_cast<uint4*>(x + (long)i * NIN);
+#pragma unroll
+  for (int q = 0; q < NIN / 8; ++q)
+    row[q] = make_uint4(tc::pack_bf16(f[8 * q], f[8 * q + 1]), tc::pack_bf16(f[8 * q + 2], f[8 * q + 3]),
+                        tc::pack_bf16(f[8 * q + 4], f[8 * q + 5]), tc::pack_bf16(f[8 * q + 6], f[8 * q + 7]));
   if (xf)
+#pragma unroll
     for (int k = 0; k < NIN; ++k) xf[(long)k * count + i] = __float2bfloat16_rn(f[k]);
 }
 
@@ -363,6 +398,16 @@ struct racer_surrogate {
   int* err = nullptr;
   SurrogateActs train;
   int step = 0;
+  // rollout inference for the sim's cars (allocated on first use)
+  SurrogateActs infer;
+  unsigned* minr = nullptr;  // [n] smallest predicted range per car (uint bits)
+  int* list = nullptr;       // [n] fallback cars
+  int* list_count = nullptr;
+  float* exact = nullptr;    // [4 + beams, n] audit ranges
+  double* rsums = nullptr;   // audit sum |e|, sum e^2 (metres)
+  unsigned* rmax = nullptr;
+  unsigned long long* rcount = nullptr;  // [0] beams over 5 cm, [1] fallback cars
+  double audited_beams = 0, car_steps = 0;
 };
 
 namespace {
@@ -595,6 +640,10 @@ int racer_surrogate_destroy(racer_surrogate* s) {
                   (void*)s->maxbits, (void*)s->over, (void*)s->err})
     cudaFree(p);
   free_acts(&s->train);
+  free_acts(&s->infer);
+  for (void* p : {(void*)s->minr, (void*)s->list, (void*)s->list_count, (void*)s->exact, (void*)s->rsums,
+                  (void*)s->rmax, (void*)s->rcount})
+    cudaFree(p);
   delete s;
   return 0;
 }
@@ -733,4 +782,108 @@ int racer_surrogate_evaluate(racer_surrogate* s, int batches, uint64_t seed, flo
   return 0;
 }
 
+// Rollout statistics since the last reset: audited error (metres) and the
+// fraction of car-steps that fell back to the exact tracer.
+int racer_surrogate_rollout_stats(racer_surrogate* s, float* mae_m, float* rmse_m, float* max_m,
+                                  float* frac_over_5cm, float* fallback_frac, int reset) {
+  if (!s) {
+    racer_host::set_error("racer_surrogate_rollout_stats: null surrogate");
+    return 1;
+  }
+  double sums[2] = {0, 0};
+  unsigned mx = 0;
+  unsigned long long counts[2] = {0, 0};
+  if (s->rsums) {
+    RACER_TRY(cudaMemcpyAsync(sums, s->rsums, sizeof sums, cudaMemcpyDeviceToHost, s->st));
+    RACER_TRY(cudaMemcpyAsync(&mx, s->rmax, sizeof mx, cudaMemcpyDeviceToHost, s->st));
+    RACER_TRY(cudaMemcpyAsync(counts, s->rcount, sizeof counts, cudaMemcpyDeviceToHost, s->st));
+  }
+  RACER_TRY(cudaStreamSynchronize(s->st));
+  const double beams = s->audited_beams > 0 ? s->audited_beams : 1.0;
+  if (mae_m) *mae_m = (float)(sums[0] / beams);
+  if (rmse_m) *rmse_m = (float)std::sqrt(sums[1] / beams);
+  if (max_m) {
+    float f;
+    memcpy(&f, &mx, sizeof f);
+    *max_m = f;
+  }
+  if (frac_over_5cm) *frac_over_5cm = (float)((double)counts[0] / beams);
+  if (fallback_frac) *fallback_frac = (float)(s->car_steps > 0 ? (double)counts[1] / s->car_steps : 0.0);
+  if (reset && s->rsums) {
+    RACER_TRY(cudaMemsetAsync(s->rsums, 0, 2 * sizeof(double), s->st));
+    RACER_TRY(cudaMemsetAsync(s->rmax, 0, sizeof(unsigned), s->st));
+    RACER_TRY(cudaMemsetAsync(s->rcount, 0, 2 * sizeof(unsigned long long), s->st));
+    s->audited_beams = s->car_steps = 0;
+  }
+  return 0;
+}
+
 }  // extern "C"
+
+// ---- rollout integration (used by racer_rollout_surrogate in api.cu) ----
+
+int surrogate_prepare(racer_surrogate* s, racer_sim* sim) {
+  if (s->sim != sim) {
+    racer_host::set_error("surrogate: built for a different sim");
+    return 1;
+  }
+  if (s->infer.M == sim->n) return 0;
+  if (s->infer.M) {
+    racer_host::set_error("surrogate: the sim's car count changed");
+    return 1;
+  }
+  const int n = sim->n;
+  int rc = 0;
+  SURR_CHECK((gemm_configure<256, EpiTanhOut>()));
+  SURR_CHECK((gemm_configure<256, EpiInfer>()));
+  if ((rc = make_acts(s, &s->infer, n, false)) || (rc = salloc(&s->minr, (size_t)n)) ||
+      (rc = salloc(&s->list, (size_t)n)) || (rc = salloc(&s->list_count, 1)) ||
+      (rc = salloc(&s->exact, (size_t)(4 + sim->beams) * n)) || (rc = salloc(&s->rsums, 2)) ||
+      (rc = salloc(&s->rmax, 1)) || (rc = salloc(&s->rcount, 2)))
+    return rc;
+  return 0;
+}
+
+namespace racer {
+namespace {
+__global__ void k_count_fallback(const int* count, unsigned long long* total) {
+  if (threadIdx.x == 0 && blockIdx.x == 0) *total += (unsigned long long)*count;
+}
+}  // namespace
+}  // namespace racer
+
+// The lidar rows of obs for the sim's cars after their physics step: the
+// surrogate's prediction, replaced by the exact tracer for every car on an
+// audit step (with the error accumulated), else for the cars whose smallest
+// predicted range is below `fallback` (obs units, range / RANGE).
+int surrogate_lidar(racer_surrogate* s, racer_sim* sim, float* obs, bool audit, float fallback, cudaStream_t st) {
+  const int n = sim->n, beams = sim->beams;
+  SurrogateActs* a = &s->infer;
+  k_features<<<(n + 127) / 128, 128, 0, st>>>(sim->ray, n, s->nm, a->x, nullptr);
+  SURR_CHECK(cudaGetLastError());
+  SURR_CHECK(cudaMemsetAsync(s->minr, 0x7f, (size_t)n * sizeof(unsigned), st));
+  EpiInfer inf{obs + 4L * n, n, s->theta + s->L.b4, n, beams, s->minr};
+  cudaStream_t keep = s->st;
+  s->st = st;
+  int rc = forward(s, a, false, &inf);
+  s->st = keep;
+  if (rc) return rc;
+  if (audit) {
+    launch_lidar(sim->t, sim->ray, s->exact, n, beams, sim->beam_dir, nullptr, st);
+    k_compare<<<296, 256, 0, st>>>(obs + 4L * n, s->exact + 4L * n, (long)beams * n, s->rsums, s->rmax, s->rcount);
+    SURR_CHECK(cudaMemcpyAsync(obs + 4L * n, s->exact + 4L * n, (size_t)beams * n * sizeof(float),
+                               cudaMemcpyDeviceToDevice, st));
+  } else if (fallback > 0.0f) {
+    SURR_CHECK(cudaMemsetAsync(s->list_count, 0, sizeof(int), st));
+    launch_select_cars(s->minr, n, fallback, s->list, s->list_count, st);
+    launch_lidar(sim->t, sim->ray, obs, n, beams, sim->beam_dir, nullptr, st, s->list, s->list_count, n);
+    k_count_fallback<<<1, 32, 0, st>>>(s->list_count, s->rcount + 1);
+  }
+  SURR_CHECK(cudaGetLastError());
+  return 0;
+}
+
+void surrogate_account(racer_surrogate* s, racer_sim* sim, int steps, int audits) {
+  s->audited_beams += (double)audits * sim->beams * sim->n;
+  s->car_steps += (double)(steps - audits) * sim->n;
+}

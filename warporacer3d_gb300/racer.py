@@ -268,7 +268,7 @@ class Surrogate:
             self.handle = None
 
     def layout(self):
-        H, beams, n = self.hidden, self.sim.beams, 8
+        H, beams, n = self.hidden, self.sim.beams, 64
         sizes = [("W1", (H, n)), ("W2", (H, H)), ("b2", (H,)), ("W3", (H, H)), ("b3", (H,)), ("W4", (beams, H)),
                  ("b4", (beams,))]
         out, off = {}, 0
@@ -294,6 +294,12 @@ class Surrogate:
         mse, mae = ctypes.c_float(), ctypes.c_float()
         call("racer_surrogate_train", self.handle, steps, lr, ctypes.byref(mse), ctypes.byref(mae))
         return mse.value, mae.value
+
+    def rollout_stats(self, reset=False):
+        """(MAE, RMSE, max error in metres, fraction of audited beams off by > 5 cm, fallback fraction)."""
+        out = [ctypes.c_float() for _ in range(5)]
+        call("racer_surrogate_rollout_stats", self.handle, *[ctypes.byref(o) for o in out], int(reset))
+        return tuple(o.value for o in out)
 
     def evaluate(self, batches=4, seed=12345):
         """Held-out error against the exact tracer: MAE, RMSE, max (metres) and fraction of beams off by > 5 cm."""
@@ -330,6 +336,11 @@ class Runner:
         """`steps` Runner steps replayed from one CUDA graph."""
         call("racer_rollout", self.sim.handle, self.policy.handle, self.acts.handle, self.scratch.c, steps,
              int(deterministic), step0)
+
+    def rollout_surrogate(self, surrogate, steps, deterministic=False, step0=0, audit_every=16, fallback_m=0.5):
+        """`steps` Runner steps with the learned lidar, audited every `audit_every` steps."""
+        call("racer_rollout_surrogate", self.sim.handle, self.policy.handle, self.acts.handle, self.scratch.c,
+             surrogate.handle, steps, int(deterministic), step0, audit_every, fallback_m)
 
     def synchronize(self):
         call("racer_synchronize", self.sim.stream)

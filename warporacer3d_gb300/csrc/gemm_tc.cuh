@@ -15,6 +15,10 @@
 #include "tc.cuh"
 
 namespace racer {
+// Internal linkage: every translation unit that includes this header gets its
+// own kernel instantiations and its own one-time attribute flag, so setting the
+// shared-memory limit always reaches the module that launches the kernel.
+namespace {
 
 template <int BN>
 struct GemmCfg {
@@ -141,4 +145,5 @@ cudaError_t gemm_launch(const CUtensorMap& ta, const CUtensorMap& tb, int M, int
   return cudaGetLastError();
 }
 
+}  // namespace
 }  // namespace racer

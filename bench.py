@@ -49,6 +49,9 @@ def parse():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-surrogate", action="store_true")
+    ap.add_argument("--surrogate-only", action="store_true", help="print only the surrogate section")
+    ap.add_argument("--surrogate-train-steps", type=int, default=None,
+                    help="surrogate training steps (default 20000; fewer only to profile the rollout)")
     return ap.parse_args()
 
 
@@ -138,7 +141,7 @@ def cpu_baseline(track, seconds=12.0, max_steps=200, threads=None):
 SURR_CARS, SURR_STEPS, SURR_REPS, SURR_TRAIN_STEPS = 65536, 32, 3, 20000
 
 
-def surrogate_section(torch, W, track, stream, flush):
+def surrogate_section(torch, W, track, stream, flush, train_steps=SURR_TRAIN_STEPS):
     """Learned lidar on bridge at 65536 cars: exact FP32 rollout vs BF16 surrogate rollout
     (audit every 16th step, exact fallback under 0.5 m), both device-timed like `value`."""
     exact = W.Runner(track, SURR_CARS, beams=BEAMS, seed=7, stream=stream)
@@ -146,7 +149,7 @@ def surrogate_section(torch, W, track, stream, flush):
     sur = W.Surrogate(learned.sim, hidden=512, batch=8192, seed=1)
     sur.set_poses(1 << 22, seed=2)
     t0 = time.perf_counter()
-    sur.train(SURR_TRAIN_STEPS, lr=2e-3)
+    sur.train(train_steps, lr=2e-3)
     torch.cuda.synchronize()
     train_s = time.perf_counter() - t0
     heldout = sur.evaluate(8, 99)
@@ -176,7 +179,7 @@ def surrogate_section(torch, W, track, stream, flush):
             "fallback_frac": fallback,
             "heldout_mae_m": heldout[0], "heldout_rmse_m": heldout[1], "heldout_frac_over_5cm": heldout[3],
             "surrogate": "64 encoded inputs -> 3 x 512 tanh -> 1081, BF16 tcgen05, FP32 Adam",
-            "training": f"{SURR_TRAIN_STEPS} steps x 8192 poses from 2^22 drawn over drivable cells, "
+            "training": f"{train_steps} steps x 8192 poses from 2^22 drawn over drivable cells, "
                         f"exact-tracer labels, {train_s:.1f} s",
             "target_mae_m": 0.02}
 
@@ -229,8 +232,12 @@ def main():
 
     track = W.track(TRACK)
     stream = torch.cuda.Stream()
-    runner = W.Runner(track, CARS, beams=BEAMS, seed=42 + rank, policy_seed=42, stream=stream)
     flush = torch.empty(L2_FLUSH_BYTES, dtype=torch.uint8, device="cuda")
+    if args.surrogate_only:
+        steps = args.surrogate_train_steps if args.surrogate_train_steps is not None else SURR_TRAIN_STEPS
+        print(json.dumps({"surrogate": surrogate_section(torch, W, track, stream, flush, steps)}), flush=True)
+        return
+    runner = W.Runner(track, CARS, beams=BEAMS, seed=42 + rank, policy_seed=42, stream=stream)
     kernels_per_rollout = runner.rollout_kernel_count(HORIZON_STEPS)
 
     def barrier():
@@ -310,7 +317,8 @@ def main():
             "clocks": clocks.summary(), "e2e": e2e, "roofline": roofline}
     if not args.no_surrogate:
         del runner
-        line["surrogate"] = surrogate_section(torch, W, track, stream, flush)
+        steps = args.surrogate_train_steps if args.surrogate_train_steps is not None else SURR_TRAIN_STEPS
+        line["surrogate"] = surrogate_section(torch, W, track, stream, flush, steps)
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline(track)
     if rank == 0:

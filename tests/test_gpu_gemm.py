@@ -23,7 +23,8 @@ def to_bf16(x):
 
 
 @pytest.mark.parametrize("M,N,K,splits", [(128, 64, 64, 1), (300, 200, 520, 1), (1000, 512, 512, 1),
-                                          (256, 1081, 512, 1), (130, 64, 4096, 8), (8192, 16, 16, 1)])
+                                          (256, 1081, 512, 1), (130, 64, 4096, 8), (8192, 16, 16, 1),
+                                          (8192, 1081, 512, 1), (4096, 512, 1024, 3), (20000, 64, 128, 1)])
 def test_gemm_bf16(M, N, K, splits):
     rng = np.random.default_rng(M + N + K)
     lda = ldb = (K + 7) // 8 * 8

@@ -300,16 +300,32 @@ __global__ void k_pose_frames(TrackDev t, const float4* __restrict__ poses, int 
 // the division where that provably gives the same cell (cell_coord), and
 // floor/descent is skipped where min() cannot select it.
 template <int LAYERS>
+__device__ __forceinline__ void trace(const TrackDev& t, const float4* __restrict__ ray, float* obs, int n,
+                                      const float2* __restrict__ beam_dir, int max_iters, int* iters, int car,
+                                      int beam);
+
+template <int LAYERS>
 __global__ void __launch_bounds__(256) k_lidar(TrackDev t, const float4* __restrict__ ray, float* obs, int n,
                                                int beams, const float2* __restrict__ beam_dir, int max_iters,
                                                int* iters, const int* __restrict__ list, const int* list_count) {
-  int car = blockIdx.x * 8 + (threadIdx.x >> 5);
   const int beam = blockIdx.y * 32 + (threadIdx.x & 31);
-  if (list) {  // only the listed cars (surrogate fallback)
-    if (car >= *list_count) return;
-    car = list[car];
+  if (beam >= beams) return;
+  if (list) {  // only the listed cars (surrogate fallback), grid-stride over the list
+    const int count = *list_count;
+    for (int k = blockIdx.x * 8 + (threadIdx.x >> 5); k < count; k += gridDim.x * 8) {
+      const int car = list[k];
+      if (car < n) trace<LAYERS>(t, ray, obs, n, beam_dir, max_iters, iters, car, beam);
+    }
+    return;
   }
-  if (car >= n || beam >= beams) return;
+  const int car = blockIdx.x * 8 + (threadIdx.x >> 5);
+  if (car < n) trace<LAYERS>(t, ray, obs, n, beam_dir, max_iters, iters, car, beam);
+}
+
+template <int LAYERS>
+__device__ __forceinline__ void trace(const TrackDev& t, const float4* __restrict__ ray, float* obs, int n,
+                                      const float2* __restrict__ beam_dir, int max_iters, int* iters, int car,
+                                      int beam) {
   const float4 r0 = __ldg(ray + car), r1 = __ldg(ray + n + car);  // (ox, oy, oz, cos h), (sin h, along, across)
   const float2 az = __ldg(beam_dir + beam);                        // (cos azimuth, sin azimuth)
   float dx = az.x * r0.w + az.y * -r1.x;
@@ -383,7 +399,8 @@ int lidar_max_iters(const TrackDev& t) { return (int)ceilf(RANGE / (0.5f * t.cel
 
 void launch_lidar(const TrackDev& t, const float4* ray, float* obs, int n, int beams, const float2* beam_dir,
                   int* iters, cudaStream_t st, const int* list, const int* list_count, int list_max) {
-  dim3 grid(((list ? list_max : n) + 7) / 8, (beams + 31) / 32);
+  // a listed subset: a grid of about eight blocks per SM strides over the list
+  dim3 grid(list ? std::min((list_max + 7) / 8, 8 * 152 / ((beams + 31) / 32) + 1) : (n + 7) / 8, (beams + 31) / 32);
   if (grid.x == 0) return;
   int cap = lidar_max_iters(t);
   if (t.layers == 1)

@@ -340,22 +340,31 @@ __global__ void k_adam_s(long p, float lr, float c1, float c2, float* th, const 
 
 // |pred - exact| statistics over [beams, count] (both feature-major rows of ranges / RANGE):
 // sums[0] += sum |e|, sums[1] += sum e^2, max in bits, count of |e| > 5 cm.
+// FP32 per-thread partial sums (a few thousand terms each; FP64 arithmetic is
+// slow on this GPU), combined in FP64 once per thread.
 __global__ void k_compare(const float* pred, const float* exact, long total, double* sums, unsigned* maxbits,
                           unsigned long long* over) {
-  double a = 0.0, s = 0.0;
-  float mx = 0.0f;
-  unsigned long long ov = 0;
+  float a = 0.0f, s = 0.0f, mx = 0.0f;
+  unsigned ov = 0;
   for (long i = (long)blockIdx.x * blockDim.x + threadIdx.x; i < total; i += (long)gridDim.x * blockDim.x) {
     float e = fabsf(pred[i] - exact[i]) * RANGE;
     a += e;
-    s += (double)e * e;
+    s += e * e;
     mx = fmaxf(mx, e);
     ov += e > 0.05f;
   }
-  atomicAdd(sums, a);
-  atomicAdd(sums + 1, s);
-  atomicMax(maxbits, __float_as_uint(mx));
-  atomicAdd(over, ov);
+  a = warp_sum(a);
+  s = warp_sum(s);
+  for (int o = 16; o > 0; o >>= 1) {
+    mx = fmaxf(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+    ov += __shfl_xor_sync(0xffffffffu, ov, o);
+  }
+  if ((threadIdx.x & 31) == 0) {
+    atomicAdd(sums, (double)a);
+    atomicAdd(sums + 1, (double)s);
+    atomicMax(maxbits, __float_as_uint(mx));
+    atomicAdd(over, (unsigned long long)ov);
+  }
 }
 
 }  // namespace
@@ -870,7 +879,7 @@ int surrogate_lidar(racer_surrogate* s, racer_sim* sim, float* obs, bool audit, 
   if (rc) return rc;
   if (audit) {
     launch_lidar(sim->t, sim->ray, s->exact, n, beams, sim->beam_dir, nullptr, st);
-    k_compare<<<296, 256, 0, st>>>(obs + 4L * n, s->exact + 4L * n, (long)beams * n, s->rsums, s->rmax, s->rcount);
+    k_compare<<<1216, 256, 0, st>>>(obs + 4L * n, s->exact + 4L * n, (long)beams * n, s->rsums, s->rmax, s->rcount);
     SURR_CHECK(cudaMemcpyAsync(obs + 4L * n, s->exact + 4L * n, (size_t)beams * n * sizeof(float),
                                cudaMemcpyDeviceToDevice, st));
   } else if (fallback > 0.0f) {

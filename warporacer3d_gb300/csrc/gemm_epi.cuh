@@ -11,7 +11,7 @@ namespace racer {
 struct EpiRowF32 {
   float* C;
   int ldc, M, N;
-  __device__ void operator()(int m, int n, const float* v) const {
+  __device__ void operator()(int m, int n, const float* v, int z) const {
     if (m >= M) return;
 #pragma unroll
     for (int j = 0; j < 16; ++j)
@@ -19,14 +19,14 @@ struct EpiRowF32 {
   }
 };
 
-// Split-K partial: P[z][m][n] with z = blockIdx.z.
+// Split-K partial: P[z][m][n] for split z.
 struct EpiSplitF32 {
   float* P;
   long mn;
   int M, N;
-  __device__ void operator()(int m, int n, const float* v) const {
+  __device__ void operator()(int m, int n, const float* v, int z) const {
     if (m >= M) return;
-    float* row = P + blockIdx.z * mn + (long)m * N;
+    float* row = P + z * mn + (long)m * N;
 #pragma unroll
     for (int j = 0; j < 16; ++j)
       if (n + j < N) row[n + j] = v[j];

@@ -35,7 +35,7 @@ struct GemmCfg {
   static constexpr int THREADS = (2 + EPI_WARPS) * 32;
 };
 
-// Epilogue contract: operator()(m, n, v) with v[0..15] = D[m][n .. n+15], called
+// Epilogue contract: operator()(m, n, v, z) with v[0..15] = D[m][n .. n+15] of split z, called
 // by all 32 lanes of an epilogue warp together (lane = row); callers mask
 // m >= M and n + j >= N themselves.
 template <int BN, typename Epi>
@@ -135,8 +135,8 @@ __global__ void __launch_bounds__(GemmCfg<BN>::THREADS, 1)
 #pragma unroll
             for (int j = 0; j < 32; ++j) v[j] = 0.0f;
           }
-          epi(m, nt * BN + c, v);
-          epi(m, nt * BN + c + 16, v + 16);
+          epi(m, nt * BN + c, v, z);
+          epi(m, nt * BN + c + 16, v + 16, z);
         }
       } else if (half == 0) {  // narrow tiles: the first warp of each quadrant takes all columns
 #pragma unroll 1
@@ -147,7 +147,7 @@ __global__ void __launch_bounds__(GemmCfg<BN>::THREADS, 1)
 #pragma unroll
             for (int j = 0; j < 16; ++j) v[j] = 0.0f;
           }
-          epi(m, nt * BN + c, v);
+          epi(m, nt * BN + c, v, z);
         }
       }
       tc::tc_fence_before();

@@ -58,7 +58,7 @@ struct EpiTanhOut {
   int ldf;
   const float* bias;
   int M, N;
-  __device__ void operator()(int m, int n, const float* v) const {
+  __device__ void operator()(int m, int n, const float* v, int z) const {
     if (m >= M) return;
     float h[16];
 #pragma unroll
@@ -96,7 +96,7 @@ struct EpiLoss {
   float* dbias;
   double* sums;
   int npad;  // columns stored (a multiple of 16; past N they are zero)
-  __device__ void operator()(int m, int n, const float* v) const {
+  __device__ void operator()(int m, int n, const float* v, int z) const {
     const bool row = m < M;
     float g[16], se = 0.0f, ae = 0.0f;
 #pragma unroll
@@ -145,7 +145,7 @@ struct EpiDTanh {
   int ldgf;
   float* dbias;
   int M, N;
-  __device__ void operator()(int m, int n, const float* v) const {
+  __device__ void operator()(int m, int n, const float* v, int z) const {
     const bool row = m < M;
     float g[16];
 #pragma unroll
@@ -188,7 +188,7 @@ struct EpiInfer {
   const float* bias;
   int M, N;
   unsigned* minr;
-  __device__ void operator()(int m, int n, const float* v) const {
+  __device__ void operator()(int m, int n, const float* v, int z) const {
     if (m >= M) return;
     float lo = 1.0f;
 #pragma unroll

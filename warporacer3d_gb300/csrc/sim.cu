@@ -304,13 +304,13 @@ __device__ __forceinline__ void trace(const TrackDev& t, const float4* __restric
                                       const float2* __restrict__ beam_dir, int max_iters, int* iters, int car,
                                       int beam);
 
-template <int LAYERS>
+template <int LAYERS, bool LIST>
 __global__ void __launch_bounds__(256) k_lidar(TrackDev t, const float4* __restrict__ ray, float* obs, int n,
                                                int beams, const float2* __restrict__ beam_dir, int max_iters,
                                                int* iters, const int* __restrict__ list, const int* list_count) {
   const int beam = blockIdx.y * 32 + (threadIdx.x & 31);
   if (beam >= beams) return;
-  if (list) {  // only the listed cars (surrogate fallback), grid-stride over the list
+  if (LIST) {  // only the listed cars (surrogate fallback), grid-stride over the list
     const int count = *list_count;
     for (int k = blockIdx.x * 8 + (threadIdx.x >> 5); k < count; k += gridDim.x * 8) {
       const int car = list[k];
@@ -403,12 +403,21 @@ void launch_lidar(const TrackDev& t, const float4* ray, float* obs, int n, int b
   dim3 grid(list ? std::min((list_max + 7) / 8, 8 * 152 / ((beams + 31) / 32) + 1) : (n + 7) / 8, (beams + 31) / 32);
   if (grid.x == 0) return;
   int cap = lidar_max_iters(t);
-  if (t.layers == 1)
-    k_lidar<1><<<grid, 256, 0, st>>>(t, ray, obs, n, beams, beam_dir, cap, iters, list, list_count);
-  else if (t.layers == 2)
-    k_lidar<2><<<grid, 256, 0, st>>>(t, ray, obs, n, beams, beam_dir, cap, iters, list, list_count);
-  else
-    k_lidar<0><<<grid, 256, 0, st>>>(t, ray, obs, n, beams, beam_dir, cap, iters, list, list_count);
+  if (list) {
+    if (t.layers == 1)
+      k_lidar<1, true><<<grid, 256, 0, st>>>(t, ray, obs, n, beams, beam_dir, cap, iters, list, list_count);
+    else if (t.layers == 2)
+      k_lidar<2, true><<<grid, 256, 0, st>>>(t, ray, obs, n, beams, beam_dir, cap, iters, list, list_count);
+    else
+      k_lidar<0, true><<<grid, 256, 0, st>>>(t, ray, obs, n, beams, beam_dir, cap, iters, list, list_count);
+  } else {
+    if (t.layers == 1)
+      k_lidar<1, false><<<grid, 256, 0, st>>>(t, ray, obs, n, beams, beam_dir, cap, iters, nullptr, nullptr);
+    else if (t.layers == 2)
+      k_lidar<2, false><<<grid, 256, 0, st>>>(t, ray, obs, n, beams, beam_dir, cap, iters, nullptr, nullptr);
+    else
+      k_lidar<0, false><<<grid, 256, 0, st>>>(t, ray, obs, n, beams, beam_dir, cap, iters, nullptr, nullptr);
+  }
 }
 
 __global__ void k_select_cars(const unsigned* minr, int n, unsigned threshold_bits, int* list, int* count) {

@@ -1,54 +1,86 @@
-"""The lidar's fast nearest-cell index is exactly the reference's.
+"""The lidar's division-free shortcuts are exactly the reference's arithmetic.
 
-racer/sim.mojo:110-111 computes ix = floor((x - x0) / cell + 0.5) with a
-binary32 division. The CUDA probe multiplies by r = RN(1 / cell) instead and
-falls back to the division only when u' = (x - x0) * r + 0.5 lies within
-delta = (|u'| + 1) * 2^-20 of an integer. With |q' - q| <= 3 * 2^-24 |q| for
-the two quotients and half an ulp per rounding of the + 0.5, the two values
-of u differ by less than delta, so outside the guard band both floors agree.
-This test replays both formulas in numpy binary32 (IEEE round-to-nearest,
-like the GPU built with --fmad=false) on random coordinates and on
-adversarial ones a few ulps either side of every cell boundary.
+1. Nearest cell. racer/sim.mojo:110-114 computes ix = floor((x - x0) / cell
+   + 0.5) with a binary32 division and tests 0 <= ix < nx. The CUDA probe
+   (sim.cu, cell_of) multiplies by r = RN(1 / cell) instead; when the
+   fractional parts of both u' = (x - x0) * r + 0.5 lie inside
+   0.5 +- band with band = 0.5 - (max(nx, ny) + 3) * 2^-20 it uses floor(u')
+   with an integer bounds test, otherwise the division. The claim: on-map
+   status and cell are always the reference's.
+2. Division skip. The march (sim.cu, trace) evaluates fl / descent only when
+   fl * RN(1 / descent) <= a * (1 + 2^-20); the claim: whenever it skips,
+   RN(fl / descent) >= a, so min(a, fl / descent) = a.
+
+Both are replayed here in numpy binary32 (IEEE round-to-nearest, like the
+GPU built with --fmad=false) on random values and on adversarial ones a few
+ulps either side of every cell boundary.
 """
 import numpy as np
 import pytest
 
 f32 = np.float32
-DELTA = f32(2.0 ** -20)
+TWO_M20 = f32(2.0 ** -20)
 
 
-def exact(x, x0, cell):
-    return np.floor((x - x0) / cell + f32(0.5))
+def exact_cell(v, v0, cell, n):
+    f = np.floor((v - v0) / cell + f32(0.5))
+    on = (f >= 0) & (f < f32(n))
+    return on, np.where(on, f, -1)
 
 
-def fast(x, x0, cell):
+def fast_cell(v, v0, cell, n, nmax):
     r = f32(1) / cell
-    u = (x - x0) * r + f32(0.5)
+    band = f32(0.5) - f32(nmax + 3) * TWO_M20
+    u = (v - v0) * r + f32(0.5)
     fl = np.floor(u)
-    g = u - fl
-    d = (np.abs(u) + f32(1)) * DELTA
-    ok = (g > d) & (g < f32(1) - d)
-    return np.where(ok, fl, exact(x, x0, cell)), ok
+    ok = np.abs((u - fl) - f32(0.5)) < band
+    with np.errstate(invalid="ignore"):
+        i = np.clip(np.nan_to_num(fl, nan=0, posinf=2**31 - 1, neginf=-2**31), -2**31, 2**31 - 1).astype(np.int64)
+    on_fast = (i >= 0) & (i < n)
+    on_ex, idx_ex = exact_cell(v, v0, cell, n)
+    on = np.where(ok, on_fast, on_ex)
+    idx = np.where(ok, np.where(on_fast, i.astype(f32), -1), idx_ex)
+    return on, idx, ok
 
 
-@pytest.mark.parametrize("cell", [0.025, 0.05, 0.1, 0.03, 0.0123, 0.07])
-def test_fast_cell_index_is_exact(cell):
+@pytest.mark.parametrize("cell,n,nmax", [(0.025, 721, 721), (0.025, 441, 721), (0.05, 2048, 2048),
+                                         (0.05, 281, 281), (0.0123, 900, 1400), (0.07, 100, 3000)])
+def test_fast_cell_index_is_exact(cell, n, nmax):
     cell = f32(cell)
-    rng = np.random.default_rng(int(cell * 1e4))
-    for x0 in (f32(-8.9999361), f32(-7.9985256), f32(-1), f32(3.3), f32(-52.1)):
-        ks = np.arange(-40, 2100)
-        base = (x0 + (ks.astype(f32) + f32(0.5)) * cell).astype(f32)
+    rng = np.random.default_rng(int(cell * 1e4) + n)
+    for v0 in (f32(-8.9999361), f32(-5.4998164), f32(-1), f32(3.3), f32(-52.1)):
+        ks = np.arange(-60, n + 60)
+        base = (v0 + (ks.astype(f32) + f32(0.5)) * cell).astype(f32)
         adv = [base]
         up, down = base.copy(), base.copy()
         for _ in range(12):
             up = np.nextafter(up, f32(np.inf))
             down = np.nextafter(down, f32(-np.inf))
             adv += [up, down]
-        uniform = rng.uniform(-60, 120, 400000).astype(f32)
-        xs = np.concatenate(adv + [uniform]).astype(f32)
+        span = float(n) * float(cell)
+        uniform = rng.uniform(float(v0) - 0.3 * span, float(v0) + 1.3 * span, 400000).astype(f32)
+        far = np.array([1e9, -1e9, 3e38, -3e38, np.inf, -np.inf, np.nan], f32)
+        vs = np.concatenate(adv + [uniform, far]).astype(f32)
         with np.errstate(all="ignore"):
-            want = exact(xs, x0, cell)
-            got, ok = fast(xs, x0, cell)
-        assert np.array_equal(got, want)
-        # the guard band is narrow: almost every uniformly placed lookup skips the division
-        assert ok[-uniform.size:].mean() > 0.97
+            on_ex, idx_ex = exact_cell(vs, v0, cell, n)
+            on, idx, ok = fast_cell(vs, v0, cell, n, nmax)
+        assert np.array_equal(on, on_ex)
+        assert np.array_equal(idx[on], idx_ex[on])
+        # the band is narrow: almost every uniformly placed lookup skips the division
+        assert ok[len(vs) - len(far) - len(uniform):len(vs) - len(far)].mean() > 0.97
+
+
+def test_division_skip_is_exact():
+    rng = np.random.default_rng(0)
+    n = 2_000_000
+    a = (rng.uniform(0.0125, 3, n)).astype(f32)
+    descent = np.concatenate([rng.uniform(1e-4, 2, n // 2), 10 ** rng.uniform(-6, 1, n - n // 2)]).astype(f32)
+    # floors near the point where the two terms cross, plus random ones
+    fl = np.where(rng.random(n) < 0.5, a * descent * (1 + rng.normal(0, 1e-6, n)).astype(f32),
+                  rng.uniform(0, 2, n)).astype(f32)
+    fl = np.abs(fl).astype(f32)
+    inv = f32(1) / descent
+    skip = (fl * inv) > (a * f32(1.00000095))
+    q = fl / descent
+    assert np.all(q[skip] >= a[skip])
+    assert skip.any() and (~skip).any()

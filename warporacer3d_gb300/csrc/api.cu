@@ -204,6 +204,7 @@ int racer_sim_create(const float* track, size_t len, int n, uint64_t seed, int b
   t.y0 = track[3];
   t.cell = track[4];
   t.inv_cell = 1.0f / track[4];
+  t.band = 0.5f - (float)((nx > ny ? nx : ny) + 3) * 9.5367431640625e-07f;
   t.spacing = track[6];
   t.slope = track[8];
   t.nxf = (float)nx;

@@ -42,6 +42,7 @@ struct TrackDev {
   int nx, ny, waypoints, layers;
   float x0, y0, cell, spacing, slope;
   float inv_cell;  // RN(1 / cell), for the division-free cell index
+  float band;      // 0.5 - (max(nx, ny) + 3) * 2^-20: fractional parts inside +-band need no division
   float nxf, nyf;
   long route;
 };

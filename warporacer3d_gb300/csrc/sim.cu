@@ -61,8 +61,20 @@ __device__ __forceinline__ float cell_coord(float v, float v0, float cell, float
 }
 
 // Nearest-cell index (racer/sim.mojo:108-114); false off the map or for
-// non-finite coordinates.
+// non-finite coordinates. One guard band serves the whole grid: where
+// |u| <= max(nx, ny) + 2 the bound of cell_coord is below
+// band_delta = (max(nx, ny) + 3) * 2^-20; farther out both floors are off the
+// map. So when both fractional parts clear the band, the fast floors give the
+// reference's answer (NaN and infinities fail the test and take the exact path).
 __device__ __forceinline__ bool cell_of(const TrackDev& t, float x, float y, long* idx) {
+  const float ux = (x - t.x0) * t.inv_cell + 0.5f, uy = (y - t.y0) * t.inv_cell + 0.5f;
+  const float flx = floorf(ux), fly = floorf(uy);
+  if (fabsf((ux - flx) - 0.5f) < t.band && fabsf((uy - fly) - 0.5f) < t.band) {
+    const int ix = (int)flx, iy = (int)fly;  // saturating conversion: far off the map stays off it
+    if ((unsigned)ix >= (unsigned)t.nx || (unsigned)iy >= (unsigned)t.ny) return false;
+    *idx = (long)(iy * t.nx + ix);
+    return true;
+  }
   float fx = cell_coord(x, t.x0, t.cell, t.inv_cell);
   float fy = cell_coord(y, t.y0, t.cell, t.inv_cell);
   if (!(fx >= 0.0f && fx < t.nxf && fy >= 0.0f && fy < t.nyf)) return false;
@@ -305,7 +317,7 @@ __device__ __forceinline__ void trace(const TrackDev& t, const float4* __restric
                                       int beam);
 
 template <int LAYERS, bool LIST>
-__global__ void __launch_bounds__(256) k_lidar(TrackDev t, const float4* __restrict__ ray, float* obs, int n,
+__global__ void __launch_bounds__(256, 8) k_lidar(TrackDev t, const float4* __restrict__ ray, float* obs, int n,
                                                int beams, const float2* __restrict__ beam_dir, int max_iters,
                                                int* iters, const int* __restrict__ list, const int* list_count) {
   const int beam = blockIdx.y * 32 + (threadIdx.x & 31);
@@ -337,6 +349,7 @@ __device__ __forceinline__ void trace(const TrackDev& t, const float4* __restric
   dz = dz / norm;
   const float ox = r0.x, oy = r0.y, oz = r0.z;
   const float descent = (1.5f * t.slope) * sqrtf(dx * dx + dy * dy) + fmaxf(-dz, 0.0f);
+  const float inv_descent = 1.0f / descent;
   const float cell = t.cell, min_step = 0.5f * t.cell;
   float tt = 0.0f, last = 0.0f, last_floor = 0.0f, range = -1.0f;
   int count = 0;
@@ -351,8 +364,13 @@ __device__ __forceinline__ void trace(const TrackDev& t, const float4* __restric
     }
     const float a = spot.clearance - cell;
     if (a < min_step) break;  // min(a, fl / descent) <= a < min_step
-    // for descent == 0 the quotient is +inf or NaN (fl >= 0 here) and fminf returns a
-    const float step = descent != 0.0f ? fminf(a, fl / descent) : a;
+    // For descent == 0 the quotient is +inf or NaN (fl >= 0 here) and fminf
+    // returns a. Otherwise fl * RN(1/descent) is within (1 + 2^-23) of the
+    // exact fl / descent, so a product above a * (1 + 2^-20) proves the
+    // correctly rounded quotient is >= a and min() returns a: the division
+    // is needed only when the floor term may win.
+    float step = a;
+    if (descent != 0.0f && !(fl * inv_descent > a * 1.00000095f)) step = fminf(a, fl / descent);
     if (step < min_step) break;
     last = tt;
     last_floor = fl;

@@ -304,8 +304,8 @@ __global__ void k_pose_frames(TrackDev t, const float4* __restrict__ poses, int 
 }
 
 // racer/sim.mojo:238-266: the sphere-traced lidar, one thread per (car, beam).
-// Block = 8 warps; warp w marches 32 consecutive beams of car
-// blockIdx.x * 8 + w, so its lanes start at one origin and probe neighbouring
+// Block = LIDAR_CARS warps; warp w marches 32 consecutive beams of car
+// blockIdx.x * LIDAR_CARS + w, so its lanes start at one origin and probe neighbouring
 // cells (L1 reuse) and finish after similar numbers of probes. The per-car
 // frame comes from the physics kernel (`ray`). Every floating-point operation
 // of a beam is the reference's, in its order; the nearest-cell index avoids
@@ -316,21 +316,24 @@ __device__ __forceinline__ void trace(const TrackDev& t, const float4* __restric
                                       const float2* __restrict__ beam_dir, int max_iters, int* iters, int car,
                                       int beam);
 
+// Cars per block: small blocks release their slot as soon as their few cars finish.
+constexpr int LIDAR_CARS = 4;
+
 template <int LAYERS, bool LIST>
-__global__ void __launch_bounds__(256, 8) k_lidar(TrackDev t, const float4* __restrict__ ray, float* obs, int n,
+__global__ void __launch_bounds__(LIDAR_CARS * 32, 64 / LIDAR_CARS) k_lidar(TrackDev t, const float4* __restrict__ ray, float* obs, int n,
                                                int beams, const float2* __restrict__ beam_dir, int max_iters,
                                                int* iters, const int* __restrict__ list, const int* list_count) {
   const int beam = blockIdx.y * 32 + (threadIdx.x & 31);
   if (beam >= beams) return;
   if (LIST) {  // only the listed cars (surrogate fallback), grid-stride over the list
     const int count = *list_count;
-    for (int k = blockIdx.x * 8 + (threadIdx.x >> 5); k < count; k += gridDim.x * 8) {
+    for (int k = blockIdx.x * LIDAR_CARS + (threadIdx.x >> 5); k < count; k += gridDim.x * LIDAR_CARS) {
       const int car = list[k];
       if (car < n) trace<LAYERS>(t, ray, obs, n, beam_dir, max_iters, iters, car, beam);
     }
     return;
   }
-  const int car = blockIdx.x * 8 + (threadIdx.x >> 5);
+  const int car = blockIdx.x * LIDAR_CARS + (threadIdx.x >> 5);
   if (car < n) trace<LAYERS>(t, ray, obs, n, beam_dir, max_iters, iters, car, beam);
 }
 
@@ -418,23 +421,25 @@ int lidar_max_iters(const TrackDev& t) { return (int)ceilf(RANGE / (0.5f * t.cel
 void launch_lidar(const TrackDev& t, const float4* ray, float* obs, int n, int beams, const float2* beam_dir,
                   int* iters, cudaStream_t st, const int* list, const int* list_count, int list_max) {
   // a listed subset: a grid of about eight blocks per SM strides over the list
-  dim3 grid(list ? std::min((list_max + 7) / 8, 8 * 152 / ((beams + 31) / 32) + 1) : (n + 7) / 8, (beams + 31) / 32);
+  dim3 grid(list ? std::min((list_max + LIDAR_CARS - 1) / LIDAR_CARS, 16 * 152 / ((beams + 31) / 32) + 1)
+                 : (n + LIDAR_CARS - 1) / LIDAR_CARS,
+            (beams + 31) / 32);
   if (grid.x == 0) return;
   int cap = lidar_max_iters(t);
   if (list) {
     if (t.layers == 1)
-      k_lidar<1, true><<<grid, 256, 0, st>>>(t, ray, obs, n, beams, beam_dir, cap, iters, list, list_count);
+      k_lidar<1, true><<<grid, LIDAR_CARS * 32, 0, st>>>(t, ray, obs, n, beams, beam_dir, cap, iters, list, list_count);
     else if (t.layers == 2)
-      k_lidar<2, true><<<grid, 256, 0, st>>>(t, ray, obs, n, beams, beam_dir, cap, iters, list, list_count);
+      k_lidar<2, true><<<grid, LIDAR_CARS * 32, 0, st>>>(t, ray, obs, n, beams, beam_dir, cap, iters, list, list_count);
     else
-      k_lidar<0, true><<<grid, 256, 0, st>>>(t, ray, obs, n, beams, beam_dir, cap, iters, list, list_count);
+      k_lidar<0, true><<<grid, LIDAR_CARS * 32, 0, st>>>(t, ray, obs, n, beams, beam_dir, cap, iters, list, list_count);
   } else {
     if (t.layers == 1)
-      k_lidar<1, false><<<grid, 256, 0, st>>>(t, ray, obs, n, beams, beam_dir, cap, iters, nullptr, nullptr);
+      k_lidar<1, false><<<grid, LIDAR_CARS * 32, 0, st>>>(t, ray, obs, n, beams, beam_dir, cap, iters, nullptr, nullptr);
     else if (t.layers == 2)
-      k_lidar<2, false><<<grid, 256, 0, st>>>(t, ray, obs, n, beams, beam_dir, cap, iters, nullptr, nullptr);
+      k_lidar<2, false><<<grid, LIDAR_CARS * 32, 0, st>>>(t, ray, obs, n, beams, beam_dir, cap, iters, nullptr, nullptr);
     else
-      k_lidar<0, false><<<grid, 256, 0, st>>>(t, ray, obs, n, beams, beam_dir, cap, iters, nullptr, nullptr);
+      k_lidar<0, false><<<grid, LIDAR_CARS * 32, 0, st>>>(t, ray, obs, n, beams, beam_dir, cap, iters, nullptr, nullptr);
   }
 }
 

@@ -86,6 +86,11 @@ int racer_policy_theta(racer_policy* policy, float** theta_dev, int* p);
 /* Call after writing theta directly (a checkpoint load): refreshes the
  * policy's derived weight copies. */
 int racer_policy_sync(racer_policy* policy);
+/* Precision of the forward, backward and weight-gradient products: 1 (the
+ * default) = BF16 operands on the tcgen05 tensor cores with FP32
+ * accumulation; 0 = FP32 on the CUDA cores (the same-seed comparison run).
+ * Parameters, sampling and Adam stay FP32 either way. */
+int racer_policy_set_precision(racer_policy* policy, int bf16);
 /* Activations.__init__ (racer/ppo.mojo:56-60): h1, h2 [65, cols] with row 64 = 1, o [3, cols]. */
 int racer_acts_create(racer_policy* policy, int cols, racer_acts** out);
 int racer_acts_destroy(racer_acts* acts);
@@ -102,7 +107,8 @@ int racer_policy_backward(racer_policy* policy, const float* x_dev, racer_acts* 
  * reference. Every buffer is the caller's: theta [P] for IN = beams + 5,
  * x [IN, cols], h1/h2 [65, cols] from a forward, d3 [3, cols]; it writes
  * d2, d1 [65, cols] and the W0/W1/W2 entries of grad [P], the same values as
- * racer_policy_backward. The split-K scratch is a 4.75 MiB array inside the
+ * racer_policy_backward in FP32 precision (its CUDA-core split-K products).
+ * The split-K scratch is a 4.75 MiB array inside the
  * library (one per GPU, held until exit); no call allocates or frees. The
  * first call on a device resolves the array's address (make it before any
  * stream capture); calls that overlap on the GPU race on the array. */

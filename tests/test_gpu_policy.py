@@ -45,7 +45,8 @@ def test_policy_forward(beams, cols):
     assert g.status() == 0
 
 
-def test_gae_bit_exact_and_gradient_and_update():
+@pytest.mark.parametrize("precision", ["bf16", "fp32"])
+def test_gae_bit_exact_and_gradient_and_update(precision):
     """tests/test_mojo.mojo:162-215 on the GPU: GAE, FD gradient (GPU tolerance), KL after one update."""
     flat = W.track("flat")
     sim = W.Sim(flat, N, 42)
@@ -55,6 +56,7 @@ def test_gae_bit_exact_and_gradient_and_update():
         s[O.STEPS, i] = np.float32(O.HORIZON - 5 - 7 * i)
     sim.state.write(s)
     policy = W.Policy(42)
+    policy.set_precision(precision)
     acts = W.Activations(policy, N)
     trainer = W.Trainer(N)
     assert np.isfinite(trainer.rollout(sim, policy, acts, 0))
@@ -89,6 +91,37 @@ def test_gae_bit_exact_and_gradient_and_update():
     assert largest > 1e-3
     kl = trainer.update(policy)
     assert np.isfinite(kl) and 0 <= kl < 0.1
+
+
+@pytest.mark.parametrize("beams,cols", [(108, 4096), (1081, 1000)])
+def test_bf16_backward_matches_fp32_backward(beams, cols):
+    """The tensor-core backward (BF16 operands, FP32 accumulation) against the FP32 one on the same
+    inputs: relative Frobenius error per block below 2e-2."""
+    rng = np.random.default_rng(cols)
+    IN = beams + 5
+    x = rng.uniform(-1, 1, (IN, cols)).astype(np.float32)
+    x[-1] = 1
+    xd = W.DevArray.empty((IN, cols))
+    xd.write(x)
+    d3 = W.DevArray.empty((3, cols))
+    d3.write(rng.normal(0, 1e-3, (3, cols)).astype(np.float32))
+    out = {}
+    for precision in ("fp32", "bf16"):
+        p = W.Policy(11, beams=beams)
+        p.set_precision("fp32")  # identical activations for both backward passes
+        acts = W.Activations(p, cols)
+        p.forward(xd, acts)
+        p.set_precision(precision)
+        bufs = [W.DevArray.empty((65, cols)), W.DevArray.empty((65, cols)), W.DevArray.empty((p.P,))]
+        p.backward(xd, acts, d3, *bufs)
+        out[precision] = [b.numpy() for b in bufs]
+        assert p.status() == 0
+        lay = {"W0": (0, p.W1), "W1": (p.W1, p.W2), "W2": (p.W2, p.LOGSTD)}
+    for name, (a, b) in zip(("d2", "d1"), zip(out["bf16"][:2], out["fp32"][:2])):
+        assert np.linalg.norm(a - b) <= 2e-2 * np.linalg.norm(b), name
+    for name, (lo, hi) in lay.items():
+        a, b = out["bf16"][2][lo:hi], out["fp32"][2][lo:hi]
+        assert np.linalg.norm(a - b) <= 2e-2 * np.linalg.norm(b), name
 
 
 def test_runner_graph_matches_steps():

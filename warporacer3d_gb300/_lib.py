@@ -48,6 +48,7 @@ SIGNATURES = {
     "racer_policy_destroy": [c_void_p],
     "racer_policy_theta": [c_void_p, P(c_void_p), P(c_int)],
     "racer_policy_sync": [c_void_p],
+    "racer_policy_set_precision": [c_void_p, c_int],
     "racer_acts_create": [c_void_p, c_int, P(c_void_p)],
     "racer_acts_destroy": [c_void_p],
     "racer_acts_buffers": [c_void_p, P(c_void_p), P(c_void_p), P(c_void_p)],

@@ -26,6 +26,7 @@ UNITS = {
     "mlp.cu": [],
     "mlp_tc.cu": EXACT,
     "policy.cu": [],
+    "policy_tc.cu": [],
     "api.cu": [],
     "noalloc.cu": [],
     "tma.cu": [],

@@ -307,6 +307,11 @@ int racer_policy_theta(racer_policy* p, float** theta, int* count) {
   return 0;
 }
 
+int racer_policy_set_precision(racer_policy* p, int bf16) {
+  RACER_ARG(p, "racer_policy_set_precision: null policy");
+  return policy_set_precision(p, bf16);
+}
+
 int racer_policy_sync(racer_policy* p) {
   RACER_ARG(p, "racer_policy_sync: null policy");
   return policy_refresh(p);

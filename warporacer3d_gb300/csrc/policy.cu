@@ -1,18 +1,27 @@
 // Policy parameters and the forward/backward dispatch (racer/ppo.mojo:63-138).
+//
+// Two precisions: BF16 (default) runs the forward (mlp_tc.cu) and the
+// backward and weight gradients (policy_tc.cu) on the tcgen05 tensor cores
+// with FP32 accumulation; FP32 runs the same products on the CUDA cores
+// (mlp.cu), for the same-seed comparison run of a BF16 training. Parameters
+// and Adam are FP32 in both.
 #include <string>
 
 #include "common.cuh"
 #include "kernels.h"
 #include "policy_fwd.h"
+#include "policy_tc.h"
 
 using namespace racer;
 
 struct racer_policy {
   int in = 0, p = 0;
+  int bf16 = 1;              // precision of the products
   float* theta = nullptr;
-  float* scratch = nullptr;  // split-K partials of the weight gradients
+  float* scratch = nullptr;  // split-K partials of the FP32 weight gradients
   uint8_t* pack = nullptr;   // pre-swizzled BF16 operand images of W0, W1, W2
   int* err = nullptr;        // device error word of the tensor-core kernels
+  BackwardWork* work = nullptr;  // BF16 backward workspace for the last batch size
   cudaStream_t st = nullptr;
   bool owned = false;
 };
@@ -43,6 +52,7 @@ void policy_delete(racer_policy* p) {
   cudaFree(p->scratch);
   cudaFree(p->pack);
   cudaFree(p->err);
+  backward_work_delete(p->work);
   if (p->owned) cudaStreamDestroy(p->st);
   delete p;
 }
@@ -59,13 +69,31 @@ int policy_refresh_on(racer_policy* p, cudaStream_t st) {
     racer_host::set_error(std::string("policy weight pack: ") + cudaGetErrorString(err));
     return 2;
   }
+  if (p->work) return backward_refresh(p->work, p->theta, st);
+  return 0;
+}
+
+int policy_set_precision(racer_policy* p, int bf16) {
+  p->bf16 = bf16 ? 1 : 0;
   return 0;
 }
 
 int policy_forward(racer_policy* p, const float* x, int cols, float* h1, float* h2, float* o, int write_hidden,
                    const SampleArgs* sa, cudaStream_t st) {
-  SampleArgs none;
-  cudaError_t err = launch_mlp_fwd(x, p->in, cols, p->pack, h1, h2, o, write_hidden, sa ? *sa : none, p->err, st);
+  cudaError_t err;
+  if (p->bf16) {
+    SampleArgs none;
+    err = launch_mlp_fwd(x, p->in, cols, p->pack, h1, h2, o, write_hidden, sa ? *sa : none, p->err, st);
+  } else {
+    const int in = p->in, w1 = H * in, w2 = w1 + H * HA;
+    launch_sgemm(p->theta, in, x, cols, h1, cols, H, cols, in, 1, st);
+    launch_sgemm(p->theta + w1, HA, h1, cols, h2, cols, H, cols, HA, 1, st);
+    launch_sgemm(p->theta + w2, HA, h2, cols, o, cols, OUT, cols, HA, 0, st);
+    if (sa && sa->actions)
+      launch_sample(cols, sa->seed, o, sa->log_std, sa->actions, sa->logp, sa->value, sa->deterministic,
+                    sa->step_base, sa->step_add, st);
+    err = cudaGetLastError();
+  }
   if (err != cudaSuccess) {
     racer_host::set_error(std::string("policy forward: ") + cudaGetErrorString(err));
     return 2;
@@ -81,6 +109,15 @@ int policy_status(racer_policy* p, int* code) {
 
 int policy_backward(racer_policy* p, const float* x, int cols, const float* h1, const float* h2, const float* d3,
                     float* d2, float* d1, float* grad, cudaStream_t st) {
+  if (p->bf16) {
+    if (backward_work_cols(p->work) != cols) {
+      backward_work_delete(p->work);
+      p->work = nullptr;
+      if (int rc = backward_work_new(p->in, cols, &p->work)) return rc;
+      if (int rc = backward_refresh(p->work, p->theta, st)) return rc;
+    }
+    return backward_tc(p->work, p->theta, x, h1, h2, d3, d2, d1, grad, p->err, st);
+  }
   launch_backward(p->in, p->theta, x, cols, h1, h2, d3, d2, d1, grad, p->scratch, st);
   cudaError_t err = cudaGetLastError();
   if (err != cudaSuccess) {

@@ -23,3 +23,5 @@ int policy_forward(racer_policy* p, const float* x, int cols, float* h1, float* 
 int policy_status(racer_policy* p, int* code);
 int policy_backward(racer_policy* p, const float* x, int cols, const float* h1, const float* h2, const float* d3,
                     float* d2, float* d1, float* grad, cudaStream_t st);
+// 1: BF16 tensor-core products (default); 0: FP32 CUDA-core products.
+int policy_set_precision(racer_policy* p, int bf16);

@@ -1,0 +1,19 @@
+// BF16 tensor-core backward of the policy MLP (policy_tc.cu).
+#pragma once
+#include <cuda_runtime.h>
+
+namespace racer {
+
+struct BackwardWork;  // BF16 operand copies, tensor maps and split-K scratch for one batch size
+
+int backward_work_new(int in, int cols, BackwardWork** out);
+void backward_work_delete(BackwardWork* w);
+int backward_work_cols(const BackwardWork* w);
+// Rebuild the BF16 W1^T image after theta changed.
+int backward_refresh(BackwardWork* w, const float* theta, cudaStream_t st);
+// x [IN, cols], h1/h2 [65, cols], d3 [3, cols] (FP32, feature-major) -> d2, d1 [65, cols] and the
+// W0/W1/W2 entries of grad.
+int backward_tc(BackwardWork* w, const float* theta, const float* x, const float* h1, const float* h2,
+                const float* d3, float* d2, float* d1, float* grad, int* err, cudaStream_t st);
+
+}  // namespace racer

@@ -162,6 +162,12 @@ class Policy:
     def sync(self):
         call("racer_policy_sync", self.handle)
 
+    def set_precision(self, precision):
+        """'bf16' (tensor cores, FP32 accumulation; default) or 'fp32' (CUDA cores)."""
+        if precision not in ("bf16", "fp32"):
+            raise ValueError(precision)
+        call("racer_policy_set_precision", self.handle, int(precision == "bf16"))
+
     def status(self):
         """Error word of the tensor-core kernels (0 = none)."""
         code = ctypes.c_int()

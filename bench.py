@@ -50,6 +50,8 @@ def parse():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-surrogate", action="store_true")
     ap.add_argument("--surrogate-only", action="store_true", help="print only the surrogate section")
+    ap.add_argument("--no-training", action="store_true")
+    ap.add_argument("--training-iterations", type=int, default=300)
     ap.add_argument("--surrogate-train-steps", type=int, default=None,
                     help="surrogate training steps (default 20000; fewer only to profile the rollout)")
     return ap.parse_args()
@@ -182,6 +184,36 @@ def surrogate_section(torch, W, track, stream, flush, train_steps=SURR_TRAIN_STE
             "training": f"{train_steps} steps x 8192 poses from 2^22 drawn over drivable cells, "
                         f"exact-tracer labels, {train_s:.1f} s",
             "target_mae_m": 0.02}
+
+
+TRAIN_TRACK, TRAIN_CARS, TRAIN_ROLLOUT, TRAIN_BEAMS = "bank", 16384, 64, 108
+
+
+def training_section(W, iterations):
+    """PPO on bank, 16384 cars x 64-step rollouts (batch 262144): BF16 tensor-core products vs a
+    same-seed FP32 run (racer/ppo.mojo:187-337 per iteration; main.mojo:54-68 loop)."""
+    out = {"workload": f"{TRAIN_TRACK}, {TRAIN_CARS} cars x {TRAIN_ROLLOUT}-step rollouts, {TRAIN_BEAMS} beams, "
+                       f"{iterations} iterations of rollout + GAE + 4 epochs x 4 minibatches of clipped PPO + Adam"}
+    track = W.track(TRAIN_TRACK)
+    for precision in ("bf16", "fp32"):
+        runner = W.Runner(track, TRAIN_CARS, beams=TRAIN_BEAMS, seed=42, policy_seed=42)
+        runner.policy.set_precision(precision)
+        trainer = W.Trainer(TRAIN_CARS, beams=TRAIN_BEAMS, rollout=TRAIN_ROLLOUT, stream=runner.sim.stream)
+        rewards, kls = [], []
+        t0 = time.perf_counter()
+        for it in range(iterations):
+            rewards.append(trainer.rollout(runner.sim, runner.policy, runner.acts, it))
+            kls.append(trainer.update(runner.policy))
+        dt = time.perf_counter() - t0
+        k = max(1, min(20, iterations // 5))
+        out[precision] = {"training_transitions_per_s": TRAIN_CARS * TRAIN_ROLLOUT * iterations / dt,
+                          "reward_per_step_first": float(np.mean(rewards[:k])),
+                          "reward_per_step_last": float(np.mean(rewards[-k:])),
+                          "kl_last": float(kls[-1]), "finite": bool(np.isfinite(rewards).all() and np.isfinite(kls).all()),
+                          "seconds": dt}
+    out["return_ratio_bf16_vs_fp32"] = out["bf16"]["reward_per_step_last"] / out["fp32"]["reward_per_step_last"] \
+        if out["fp32"]["reward_per_step_last"] else None
+    return out
 
 
 def run_reference(args, rank, world):
@@ -319,6 +351,8 @@ def main():
         del runner
         steps = args.surrogate_train_steps if args.surrogate_train_steps is not None else SURR_TRAIN_STEPS
         line["surrogate"] = surrogate_section(torch, W, track, stream, flush, steps)
+    if rank == 0 and not args.no_training:
+        line["training"] = training_section(W, args.training_iterations)
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline(track)
     if rank == 0:

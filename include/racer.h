@@ -151,6 +151,14 @@ int racer_runner_step(racer_sim* sim, racer_policy* policy, racer_acts* acts, fl
  * offsets are step0, step0 + 1, ... */
 int racer_rollout(racer_sim* sim, racer_policy* policy, racer_acts* acts, float* scratch_dev, int steps,
                   int deterministic, int64_t step0);
+/* Accuracy audit of the binary32 dynamics (no counterpart in the reference):
+ * `steps` Runner steps as racer_runner_step, and after each one a kernel
+ * re-integrates racer/sim.mojo:189-213 in FP64 from the pre-step state and
+ * the same actions for every car that did not end its episode. out[7] (host):
+ * cars audited, then the sums and then the maxima of the position (m),
+ * heading (rad) and speed (m/s) differences. */
+int racer_runner_audit_dynamics(racer_sim* sim, racer_policy* policy, racer_acts* acts, float* scratch_dev,
+                                int deterministic, int steps, int64_t step0, double* out);
 
 /* ---- learned lidar surrogate (no counterpart in the reference; replaces
  * racer/sim.mojo:238-266's tracing during rollouts, audited by it) ---- */

@@ -163,3 +163,62 @@ def test_sample_bit_exact():
         a, lp, v = np.zeros((2, n), np.float32), np.zeros(n, np.float32), np.zeros(n, np.float32)
         cpu.sample(out, ls, a, lp, v, det, step)
         assert same(a_dev.numpy(), a) and same(lp_dev.numpy(), lp) and same(v_dev.numpy(), v)
+
+
+def _rk4_f64_flat(prev, act):
+    """FP64 RK4 of racer/sim.mojo:155-167,189-213 on a level surface (no slope terms)."""
+    G, WB, dt = 9.81, 0.3302, 1.0 / 240.0
+    x, y, h, s = (prev[k].astype(np.float64) for k in (O.X, O.Y, O.HEADING, O.SPEED))
+    steer = prev[O.STEER].astype(np.float64)
+    rate = np.float64(np.clip(act[0], -1, 1).astype(np.float32) * np.float32(3.2))
+    accel = np.float64(np.clip(act[1], -1, 1).astype(np.float32) * np.float32(9.51))
+    load = np.float64(np.float32(1.05) * prev[O.FRICTION]) * G
+
+    def deriv(x, y, h, s, st):
+        v = np.maximum(np.abs(s), 0.5) * np.where(s >= 0, 1.0, -1.0)
+        lateral = np.clip(v * s * np.sin(st) / np.cos(st) / WB, -load, load)
+        lon = np.sqrt(np.maximum(load * load - lateral * lateral, 0))
+        return s * np.cos(h), s * np.sin(h), lateral / v, np.clip(accel, -lon, lon)
+
+    for _ in range(4):
+        k1 = deriv(x, y, h, s, steer)
+        k2 = deriv(x + k1[0] * dt / 2, y + k1[1] * dt / 2, h + k1[2] * dt / 2, s + k1[3] * dt / 2, steer + rate * dt / 2)
+        k3 = deriv(x + k2[0] * dt / 2, y + k2[1] * dt / 2, h + k2[2] * dt / 2, s + k2[3] * dt / 2, steer + rate * dt / 2)
+        k4 = deriv(x + k3[0] * dt, y + k3[1] * dt, h + k3[2] * dt, s + k3[3] * dt, steer + rate * dt)
+        x, y, h, s = ((p + (a + 2 * (b + c) + d) * dt / 6) for p, a, b, c, d in zip((x, y, h, s), k1, k2, k3, k4))
+        s = np.clip(s, -5.0, 5.0)
+        steer = np.clip(steer + rate * dt, -0.4189, 0.4189)
+    return x, y, h, s
+
+
+def test_rk4_audit_matches_numpy_fp64_on_flat():
+    """The FP64 audit kernel's statistics equal a numpy FP64 re-integration of the same step."""
+    n = 512
+    run = W.Runner(W.track("flat"), n, beams=108, seed=9)
+    for t in range(30):
+        run.step(False, t)
+    prev = run.sim.state.numpy()
+    stats = run.audit_dynamics(1, step0=30)
+    nxt, done, act = run.sim.state.numpy(), run.sim.done.numpy(), run.sim.actions.numpy()
+    x, y, h, s = _rk4_f64_flat(prev, act)
+    keep = done == 0
+    dh = nxt[O.HEADING].astype(np.float64) - h
+    dh -= 2 * np.pi * np.rint(dh / (2 * np.pi))
+    pos = np.hypot(nxt[O.X] - x, nxt[O.Y] - y)[keep]
+    head, spd = np.abs(dh)[keep], np.abs(nxt[O.SPEED] - s)[keep]
+    assert stats["cars"] == keep.sum() > n // 2
+    for key, ref in (("position", pos), ("heading", head), ("speed", spd)):
+        assert stats[key + "_max_" + ("m" if key == "position" else "rad" if key == "heading" else "mps")] == \
+            pytest.approx(ref.max(), rel=1e-3, abs=1e-12), key
+        mean = stats[key + "_mean_" + ("m" if key == "position" else "rad" if key == "heading" else "mps")]
+        assert mean == pytest.approx(ref.mean(), rel=1e-3, abs=1e-12), key
+    assert 0 < stats["position_max_m"] < 1e-4
+
+
+def test_rk4_audit_error_bounded_on_bank():
+    """Binary32 RK4 stays within a micrometre-scale distance of FP64 per step on a sloped track."""
+    run = W.Runner(W.track("bank"), 2048, beams=108, seed=4)
+    stats = run.audit_dynamics(40)
+    assert stats["cars"] > 40 * 2048 * 0.9
+    assert stats["position_mean_m"] < 1e-5 and stats["position_max_m"] < 1e-3
+    assert stats["speed_mean_mps"] < 1e-5 and stats["heading_mean_rad"] < 1e-5

@@ -67,6 +67,8 @@ SIGNATURES = {
     "racer_trainer_minibatch": [c_void_p, c_void_p, c_int, c_float, c_float],
     "racer_runner_step": [c_void_p, c_void_p, c_void_p, c_void_p, c_int, c_int64],
     "racer_rollout": [c_void_p, c_void_p, c_void_p, c_void_p, c_int, c_int, c_int64],
+    "racer_runner_audit_dynamics": [c_void_p, c_void_p, c_void_p, c_void_p, c_int, c_int, c_int64,
+                                    P(ctypes.c_double)],
     "racer_surrogate_create": [c_void_p, c_int, c_int, c_uint64, P(c_void_p)],
     "racer_surrogate_destroy": [c_void_p],
     "racer_surrogate_params": [c_void_p, P(c_void_p), P(c_void_p), P(ctypes.c_long), P(c_int)],

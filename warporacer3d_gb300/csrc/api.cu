@@ -675,6 +675,43 @@ int racer_runner_step(racer_sim* s, racer_policy* p, racer_acts* a, float* scrat
   return runner_step_on(s, p, a, scratch, det, nullptr, t, s->st);
 }
 
+int racer_runner_audit_dynamics(racer_sim* s, racer_policy* p, racer_acts* a, float* scratch, int det, int steps,
+                                int64_t step0, double* out) {
+  RACER_ARG(s && p && a && scratch && out && steps >= 1, "racer_runner_audit_dynamics: bad argument");
+  RACER_ARG(a->cols == s->n && policy_inputs(p) == s->in_rows, "racer_runner_audit_dynamics: sizes differ");
+  cudaStream_t st = s->st;
+  float* prev = nullptr;
+  double* stats = nullptr;
+  const size_t state_bytes = (size_t)STATE * s->n * sizeof(float);
+  RACER_TRY(cudaMallocAsync((void**)&prev, state_bytes, st));
+  RACER_TRY(cudaMallocAsync((void**)&stats, 7 * sizeof(double), st));
+  RACER_TRY(cudaMemsetAsync(stats, 0, 7 * sizeof(double), st));
+  int rc = 0;
+  for (int k = 0; k < steps && !rc; ++k) {
+    SampleArgs sa;
+    sa.seed = s->seed;
+    sa.log_std = policy_theta(p) + policy_params(p) - 2;
+    sa.actions = s->actions;
+    sa.logp = scratch;
+    sa.value = scratch + s->n;
+    sa.deterministic = det;
+    sa.step_base = nullptr;
+    sa.step_add = step0 + k;
+    if ((rc = forward_on(p, s->obs, a, st, &sa, 0))) break;
+    RACER_TRY(cudaMemcpyAsync(prev, s->state, state_bytes, cudaMemcpyDeviceToDevice, st));
+    if ((rc = sim_step_on(s, s->actions, s->reward, s->done, s->obs, nullptr, st))) break;
+    launch_rk4_audit(s->t, prev, s->actions, s->state, s->done, s->n, stats, st);
+    RACER_LAUNCHED();
+  }
+  cudaError_t copy = cudaMemcpyAsync(out, stats, 7 * sizeof(double), cudaMemcpyDeviceToHost, st);
+  cudaFreeAsync(prev, st);
+  cudaFreeAsync(stats, st);
+  RACER_TRY(cudaStreamSynchronize(st));
+  if (rc) return rc;
+  RACER_TRY(copy);
+  return 0;
+}
+
 // Captures (once) the graph of `steps` Runner steps for these arguments.
 static int rollout_graph(racer_sim* s, racer_policy* p, racer_acts* a, float* scratch, int steps, int det,
                          cudaGraphExec_t* exec_out, size_t* kernels) {

@@ -19,6 +19,10 @@ void launch_lidar(const TrackDev& t, const float4* ray, float* obs, int n, int b
 // Cars whose smallest predicted range (ordered uint bits of a nonnegative float) is below threshold.
 void launch_select_cars(const unsigned* minr, int n, float threshold, int* list, int* count, cudaStream_t st);
 int lidar_max_iters(const TrackDev& t);
+// FP64 re-integration audit of one physics step: prev/next state [11, n] around the FP32 step,
+// stats [7] doubles (count, sums and maxima of position, heading and speed errors).
+void launch_rk4_audit(const TrackDev& t, const float* prev, const float* actions, const float* next,
+                      const float* done, int n, double* stats, cudaStream_t st);
 // poses [count] (x, y, heading, layer) -> ray [2, count]: the frame of a car at rest there.
 void launch_pose_frames(const TrackDev& t, const float4* poses, int count, float4* ray, cudaStream_t st);
 void launch_sample(int n, uint64_t seed, const float* output, const float* log_std, float* actions, float* logp,

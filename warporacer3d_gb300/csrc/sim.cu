@@ -284,6 +284,76 @@ __global__ void k_advance(TrackDev t, float* s, const float* act, float* reward,
   ray[n + i] = make_float4(sh, along, across, (float)probe<LAYERS>(t, sx, sy, sz).layer);
 }
 
+// FP64 re-integration of racer/sim.mojo:189-213 (the 4 RK4 substeps) for
+// the accuracy audit: the same ODE and parameters in double precision with
+// CUDA's double sin/cos/sqrt; map lookups stay binary32 at the rounded
+// position, as the map itself is binary32.
+__device__ void derivative64(const double* p, double steer, double accel, double grip, double along,
+                             double across, double* out) {
+  const double G = (double)GRAV, WB = (double)WHEELBASE;
+  const double nz = 1.0 / sqrt((1.0 + along * along) + across * across);
+  const double load = (grip * G) * nz;
+  const double v = fmax(fabs(p[3]), 0.5) * (p[3] >= 0.0 ? 1.0 : -1.0);
+  const double slide = (G * across) * nz;
+  const double lateral = fmin(fmax((((v * p[3]) * sin(steer)) / cos(steer)) / WB + slide, -load), load);
+  const double yaw = (lateral - slide) / v;
+  const double longitudinal = sqrt(fmax(load * load - lateral * lateral, 0.0));
+  const double dv = fmin(fmax(accel, -longitudinal), longitudinal) - (G * along) * nz;
+  out[0] = p[3] * cos(p[2]);
+  out[1] = p[3] * sin(p[2]);
+  out[2] = yaw;
+  out[3] = dv;
+}
+
+// Per car that did not end its episode this step: |position|, |heading| and
+// |speed| differences between the FP32 step (next) and the FP64 re-integration
+// from the same state (prev) and actions. stats: [0] count, [1..3] sums,
+// [4..6] maxima (as doubles).
+template <int LAYERS>
+__global__ void k_rk4_f64(TrackDev t, const float* prev, const float* act, const float* next, const float* done,
+                          int n, double* stats) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n || done[i] != 0.0f) return;
+  double p[4] = {prev[(long)X * n + i], prev[(long)Y * n + i], prev[(long)HEADING * n + i],
+                 prev[(long)SPEED * n + i]};
+  Spot spot = probe<LAYERS>(t, (float)p[0], (float)p[1], prev[(long)Z * n + i]);
+  Surface ground = surface(t, spot.layer, (float)p[0], (float)p[1]);
+  double steer = prev[(long)STEER * n + i];
+  const double rate = (double)(clampf_(act[i], -1.0f, 1.0f) * STEER_RATE);
+  const double accel = (double)(clampf_(act[(long)n + i], -1.0f, 1.0f) * ACCEL_MAX);
+  const double grip = (double)(GRIP * prev[(long)FRICTION * n + i]);
+  const double dt = 1.0 / 240.0;
+  for (int sub = 0; sub < SUBSTEPS; ++sub) {
+    const double c = cos(p[2]), s = sin(p[2]);
+    const double along = (double)ground.sx * c + (double)ground.sy * s;
+    const double across = -(double)ground.sx * s + (double)ground.sy * c;
+    double k1[4], k2[4], k3[4], k4[4], q[4];
+    derivative64(p, steer, accel, grip, along, across, k1);
+    for (int j = 0; j < 4; ++j) q[j] = p[j] + k1[j] * (dt / 2);
+    derivative64(q, steer + rate * dt / 2, accel, grip, along, across, k2);
+    for (int j = 0; j < 4; ++j) q[j] = p[j] + k2[j] * (dt / 2);
+    derivative64(q, steer + rate * dt / 2, accel, grip, along, across, k3);
+    for (int j = 0; j < 4; ++j) q[j] = p[j] + k3[j] * dt;
+    derivative64(q, steer + rate * dt, accel, grip, along, across, k4);
+    for (int j = 0; j < 4; ++j) p[j] += (k1[j] + 2 * (k2[j] + k3[j]) + k4[j]) * (dt / 6);
+    p[3] = fmin(fmax(p[3], -(double)SPEED_MAX), (double)SPEED_MAX);
+    steer = fmin(fmax(steer + rate * dt, -(double)STEER_MAX), (double)STEER_MAX);
+    spot = probe<LAYERS>(t, (float)p[0], (float)p[1], spot.height);
+    ground = surface(t, spot.layer, (float)p[0], (float)p[1]);
+  }
+  const double pi = 3.141592653589793;
+  double dh = (double)next[(long)HEADING * n + i] - p[2];
+  dh -= 2 * pi * rint(dh / (2 * pi));
+  const double dx = (double)next[(long)X * n + i] - p[0], dy = (double)next[(long)Y * n + i] - p[1];
+  const double e[3] = {sqrt(dx * dx + dy * dy), fabs(dh), fabs((double)next[(long)SPEED * n + i] - p[3])};
+  atomicAdd(stats, 1.0);
+  for (int k = 0; k < 3; ++k) {
+    atomicAdd(stats + 1 + k, e[k]);
+    unsigned long long* mx = reinterpret_cast<unsigned long long*>(stats + 4 + k);
+    atomicMax(mx, (unsigned long long)__double_as_longlong(e[k]));  // nonnegative doubles order as integers
+  }
+}
+
 // The lidar frame of a car at rest on a layer (racer/sim.mojo:229-234,
 // 243-249): pose (x, y, heading, layer) -> z = the layer's bilinear height,
 // the slopes along and across the heading, and the same frame k_advance
@@ -452,6 +522,17 @@ void launch_select_cars(const unsigned* minr, int n, float threshold, int* list,
   unsigned bits;
   memcpy(&bits, &threshold, sizeof bits);
   k_select_cars<<<(n + 255) / 256, 256, 0, st>>>(minr, n, bits, list, count);
+}
+
+void launch_rk4_audit(const TrackDev& t, const float* prev, const float* actions, const float* next,
+                      const float* done, int n, double* stats, cudaStream_t st) {
+  dim3 grid((n + 127) / 128);
+  if (t.layers == 1)
+    k_rk4_f64<1><<<grid, 128, 0, st>>>(t, prev, actions, next, done, n, stats);
+  else if (t.layers == 2)
+    k_rk4_f64<2><<<grid, 128, 0, st>>>(t, prev, actions, next, done, n, stats);
+  else
+    k_rk4_f64<0><<<grid, 128, 0, st>>>(t, prev, actions, next, done, n, stats);
 }
 
 void launch_pose_frames(const TrackDev& t, const float4* poses, int count, float4* ray, cudaStream_t st) {

@@ -348,6 +348,20 @@ class Runner:
         call("racer_rollout_surrogate", self.sim.handle, self.policy.handle, self.acts.handle, self.scratch.c,
              surrogate.handle, steps, int(deterministic), step0, audit_every, fallback_m)
 
+    def audit_dynamics(self, steps, deterministic=False, step0=0):
+        """`steps` Runner steps, each physics step re-integrated in FP64 from the same state and actions.
+
+        Returns the cars audited and the mean and max position (m), heading (rad) and speed (m/s)
+        differences between the binary32 step and the FP64 one (cars that ended an episode are skipped).
+        """
+        out = (ctypes.c_double * 7)()
+        call("racer_runner_audit_dynamics", self.sim.handle, self.policy.handle, self.acts.handle, self.scratch.c,
+             int(deterministic), steps, step0, out)
+        count = max(out[0], 1.0)
+        return {"cars": int(out[0]), "position_mean_m": out[1] / count, "heading_mean_rad": out[2] / count,
+                "speed_mean_mps": out[3] / count, "position_max_m": out[4], "heading_max_rad": out[5],
+                "speed_max_mps": out[6]}
+
     def synchronize(self):
         call("racer_synchronize", self.sim.stream)
 

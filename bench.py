@@ -36,6 +36,7 @@ sys.path.insert(0, str(ROOT))
 
 METRIC = "env-steps/s at 1081 beams, 1 GB300: exact FP32 vs BF16 surrogate (≤2cm MAE)"
 TRACK, CARS, BEAMS, HORIZON_STEPS = "bridge", 4096, 1081, 1000
+AUDIT_STEPS = 64
 WORKLOAD = (f"{TRACK} (2 layers, 721x441 cells), {CARS} cars, {BEAMS} beams, {HORIZON_STEPS}-env-step rollout "
             "per bench step: policy forward + sampling + RK4 physics + sphere-traced lidar, CUDA graph")
 L2_FLUSH_BYTES = 256 << 20
@@ -347,6 +348,10 @@ def main():
                        "policy": "tanh MLP 1086-64-64-3"},
             "beam_steps_per_s": value * BEAMS, "wall_s": wall, "gpu_launches": kernels_per_rollout * args.steps,
             "clocks": clocks.summary(), "e2e": e2e, "roofline": roofline}
+    audit = runner.audit_dynamics(AUDIT_STEPS, False, 10 ** 9)
+    audit["workload"] = f"{TRACK}, {CARS} cars, {AUDIT_STEPS} policy steps after the timed rollouts"
+    audit["method"] = "each binary32 RK4 step re-integrated in FP64 on the GPU from the same state and actions"
+    line["dynamics_fp64_audit"] = audit
     if not args.no_surrogate:
         del runner
         steps = args.surrogate_train_steps if args.surrogate_train_steps is not None else SURR_TRAIN_STEPS

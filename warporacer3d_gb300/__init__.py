@@ -17,5 +17,10 @@ TRACKS = Path(__file__).resolve().parent / "tracks"
 
 
 def track(name):
-    """A built-in track array (flat, ramp, bank, bridge) as compiled by the reference's racer/track.py."""
+    """A track array: the built-ins flat, ramp, bank and bridge as compiled by the
+    reference's racer/track.py, or "occupancy", the seeded 2048 x 2048 px, 0.05 m
+    corridor map with eight ramps (built on first use and cached)."""
+    if name == "occupancy":
+        from .tracks import occupancy
+        return occupancy.synthetic(0)
     return np.load(TRACKS / f"{name}.npz")["track"]

@@ -222,3 +222,96 @@ def test_rk4_audit_error_bounded_on_bank():
     assert stats["cars"] > 40 * 2048 * 0.9
     assert stats["position_mean_m"] < 1e-5 and stats["position_max_m"] < 1e-3
     assert stats["speed_mean_mps"] < 1e-5 and stats["heading_mean_rad"] < 1e-5
+
+
+GOLDEN_OCCUPANCY = __import__("pathlib").Path(__file__).resolve().parent / "golden" / "occupancy_small.npz"
+
+
+def check_segments(gpu, cpus, what=""):
+    for name in ("state", "obs", "reward", "done"):
+        g = getattr(gpu, name).numpy()
+        for k, cpu in enumerate(cpus):
+            lo, hi = gpu.car0[k], gpu.car0[k + 1]
+            c = getattr(cpu, name)
+            assert same(g[..., lo:hi], c), what + f"segment {k} " + diff_report(name, g[..., lo:hi], c)
+
+
+def segment_tracks():
+    return [W.track("flat"), W.track("bridge"), np.load(GOLDEN_OCCUPANCY)["track"], W.track("ramp")]
+
+
+def test_segments_match_separate_oracle_sims():
+    """A batch of four tracks (one an occupancy-image map with ramps) in one sim: every segment
+    evolves bit for bit like the oracle's sim of that track alone; car counts straddle warps and blocks."""
+    tracks, cars, seeds = segment_tracks(), [96, 70, 45, 33], [5, 6, 7, 8]
+    gpu = W.Sim.segments(tracks, cars, seeds, beams=108)
+    cpus = [O.Sim(t, c, s, beams=108) for t, c, s in zip(tracks, cars, seeds)]
+    gpu.reset()
+    for c in cpus:
+        c.reset()
+    check_segments(gpu, cpus, "reset ")
+    rng = np.random.default_rng(3)
+    for step in range(30):
+        act = rng.uniform(-1.2, 1.2, (2, gpu.n)).astype(np.float32)
+        act[1] = np.abs(act[1]) * (1 if step % 4 else -1)
+        gpu.actions.write(act)
+        for k, c in enumerate(cpus):
+            c.actions[:] = act[:, gpu.car0[k]:gpu.car0[k + 1]]
+            c.step(c.actions, c.reward, c.done, c.obs)
+        gpu.step(gpu.actions, gpu.reward, gpu.done, gpu.obs)
+        check_segments(gpu, cpus, f"step {step} ")
+
+
+def test_lidar_shapes_and_autotune_keep_results():
+    tracks, cars, seeds = segment_tracks(), [64, 40, 72, 20], [1, 2, 3, 4]
+    a = W.Sim.segments(tracks, cars, seeds, beams=108)
+    b = W.Sim.segments(tracks, cars, seeds, beams=108)
+    a.reset()
+    b.reset()
+    rng = np.random.default_rng(5)
+    for shape in ((2, [3, 1, 0, 2]), (8, None), (4, [2, 3, 1, 0]), "auto"):
+        if shape == "auto":
+            cars_per_block, order, ms = b.autotune(3)
+            assert cars_per_block in (2, 4, 8) and sorted(order) == [0, 1, 2, 3] and ms > 0
+            assert b.lidar_shape() == (cars_per_block, order)
+        else:
+            b.set_lidar_shape(*shape)
+        for _ in range(4):
+            act = rng.uniform(-1, 1, (2, a.n)).astype(np.float32)
+            a.actions.write(act)
+            b.actions.write(act)
+            a.step(a.actions, a.reward, a.done, a.obs)
+            b.step(b.actions, b.reward, b.done, b.obs)
+            assert same(a.obs.numpy(), b.obs.numpy()) and same(a.state.numpy(), b.state.numpy())
+    with pytest.raises(W.RacerError):
+        b.set_lidar_shape(3)
+    with pytest.raises(W.RacerError):
+        b.set_lidar_shape(4, [0, 0, 1, 2])
+
+
+def test_synthetic_occupancy_map_bit_exact():
+    """The 2048 x 2048 px corridor map (8 ramps, slope bound 2.5: long marches) at 1081 beams."""
+    track = W.track("occupancy")
+    n = 24
+    gpu, cpu = W.Sim(track, n, 11, beams=1081), O.Sim(track, n, 11, beams=1081)
+    gpu.reset()
+    cpu.reset()
+    check_sim(gpu, cpu, "reset ")
+    act = np.tile(np.array([[0.1], [1.0]], np.float32), (1, n))
+    for step in range(3):
+        gpu.actions.write(act)
+        cpu.actions[:] = act
+        gpu.step(gpu.actions, gpu.reward, gpu.done, gpu.obs)
+        cpu.step(cpu.actions, cpu.reward, cpu.done, cpu.obs)
+        check_sim(gpu, cpu, f"step {step} ")
+
+
+def test_segment_runner_rollout_and_audit():
+    tracks = [W.track("bank"), W.track("bridge")]
+    run = W.Runner.segments(tracks, [300, 212], [1, 2], beams=108)
+    run.rollout(8)
+    run.synchronize()
+    stats = run.audit_dynamics(4, step0=8)
+    assert stats["cars"] > 0.9 * 4 * 512 and stats["position_max_m"] < 1e-4
+    with pytest.raises(W.RacerError):
+        W.Surrogate(run.sim)

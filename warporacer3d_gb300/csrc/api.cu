@@ -11,6 +11,7 @@
 #include <stdio.h>
 #include <string.h>
 
+#include <algorithm>
 #include <map>
 #include <string>
 #include <tuple>
@@ -154,20 +155,9 @@ static int check_track(const float* d, size_t len) {
   return 0;
 }
 
-int racer_sim_create(const float* track, size_t len, int n, uint64_t seed, int beams, void* stream,
-                     racer_sim** out) {
-  RACER_ARG(out, "racer_sim_create: null output");
-  RACER_ARG(n >= 1, "racer_sim_create: n must be positive");
-  RACER_ARG(beams >= 2, "racer_sim_create: beams must be at least 2");
-  if (int rc = check_track(track, len)) return rc;
-  racer_sim* s = new racer_sim();
-  s->n = n;
-  s->beams = beams;
-  s->in_rows = beams + 5;
-  s->seed = seed;
-  s->track_len = len;
-  int rc = 0;
-  if ((rc = own_stream(stream, &s->st, &s->owned))) { delete s; return rc; }
+// Uploads one track (the array unchanged plus the per-cell float2 repack) and
+// fills its device view.
+static int upload_track(const float* track, size_t len, float** d_track, float2** d_cl, TrackDev* t) {
   int nx = (int)track[0], ny = (int)track[1], L = (int)track[7];
   std::vector<float2> cl((size_t)nx * ny * L);
   for (int l = 0; l < L; ++l) {
@@ -175,51 +165,100 @@ int racer_sim_create(const float* track, size_t len, int n, uint64_t seed, int b
     const float* h = c + (size_t)nx * ny;
     for (size_t k = 0; k < (size_t)nx * ny; ++k) cl[k * L + l] = make_float2(c[k], h[k]);
   }
-  std::vector<float2> dirs(beams);
-  beam_table(beams, dirs.data());
-  if ((rc = dalloc(&s->d_track, len)) || (rc = dalloc(&s->d_cl, cl.size())) || (rc = dalloc(&s->beam_dir, beams)) ||
-      (rc = dalloc(&s->state, (size_t)STATE * n)) || (rc = dalloc(&s->obs, (size_t)s->in_rows * n)) ||
-      (rc = dalloc(&s->actions, 2 * (size_t)n)) || (rc = dalloc(&s->reward, n)) || (rc = dalloc(&s->done, n)) ||
-      (rc = dalloc(&s->step_base, 1)) || (rc = dalloc(&s->ray, 2 * (size_t)n))) {
+  if (int rc = dalloc(d_track, len)) return rc;
+  if (int rc = dalloc(d_cl, cl.size())) return rc;
+  RACER_TRY(cudaMemcpy(*d_track, track, len * sizeof(float), cudaMemcpyHostToDevice));
+  RACER_TRY(cudaMemcpy(*d_cl, cl.data(), cl.size() * sizeof(float2), cudaMemcpyHostToDevice));
+  t->d = *d_track;
+  t->cl = *d_cl;
+  t->nx = nx;
+  t->ny = ny;
+  t->waypoints = (int)track[5];
+  t->layers = L;
+  t->x0 = track[2];
+  t->y0 = track[3];
+  t->cell = track[4];
+  t->inv_cell = 1.0f / track[4];
+  t->band = 0.5f - (float)((nx > ny ? nx : ny) + 3) * 9.5367431640625e-07f;
+  t->spacing = track[6];
+  t->slope = track[8];
+  t->nxf = (float)nx;
+  t->nyf = (float)ny;
+  t->route = 12 + 3L * L * nx * ny;
+  return 0;
+}
+
+int racer_sim_create_segments(int count, const float* const* tracks, const size_t* lens, const int* cars,
+                              const uint64_t* seeds, int beams, void* stream, racer_sim** out) {
+  RACER_ARG(out, "racer_sim_create: null output");
+  RACER_ARG(count >= 1 && count <= MAX_SEGMENTS, "racer_sim_create_segments: 1 to 8 segments");
+  RACER_ARG(tracks && lens && cars && seeds, "racer_sim_create_segments: null argument");
+  RACER_ARG(beams >= 2, "racer_sim_create: beams must be at least 2");
+  long total = 0;
+  for (int k = 0; k < count; ++k) {
+    RACER_ARG(cars[k] >= 1, "racer_sim_create: every segment needs at least one car");
+    total += cars[k];
+    if (int rc = check_track(tracks[k], lens[k])) return rc;
+  }
+  RACER_ARG(total <= (1L << 30), "racer_sim_create: too many cars");
+  const int n = (int)total;
+  racer_sim* s = new racer_sim();
+  s->n = n;
+  s->beams = beams;
+  s->in_rows = beams + 5;
+  s->seed = seeds[0];
+  s->track_len = lens[0];
+  int rc = 0;
+  if ((rc = own_stream(stream, &s->st, &s->owned))) { delete s; return rc; }
+  s->seg.count = count;
+  s->seg.car0[0] = 0;
+  s->seg_track.assign(count, nullptr);
+  s->seg_cl.assign(count, nullptr);
+  for (int k = 0; k < count && !rc; ++k) {
+    rc = upload_track(tracks[k], lens[k], &s->seg_track[k], &s->seg_cl[k], &s->seg.t[k]);
+    s->seg.car0[k + 1] = s->seg.car0[k] + cars[k];
+    s->seg.seed[k] = seeds[k];
+    s->seg.max_iters[k] = lidar_max_iters(s->seg.t[k]);
+  }
+  for (int k = count; k < MAX_SEGMENTS; ++k) s->seg.car0[k + 1] = n;
+  if (rc) {
     racer_sim_destroy(s);
     return rc;
   }
-  cudaMemcpy(s->d_track, track, len * sizeof(float), cudaMemcpyHostToDevice);
-  cudaMemcpy(s->d_cl, cl.data(), cl.size() * sizeof(float2), cudaMemcpyHostToDevice);
-  cudaMemcpy(s->beam_dir, dirs.data(), beams * sizeof(float2), cudaMemcpyHostToDevice);
-  cudaError_t err = cudaGetLastError();
+  s->t = s->seg.t[0];
+  s->d_track = s->seg_track[0];
+  s->d_cl = s->seg_cl[0];
+  std::vector<float2> dirs(beams);
+  beam_table(beams, dirs.data());
+  if ((rc = dalloc(&s->beam_dir, beams)) || (rc = dalloc(&s->state, (size_t)STATE * n)) ||
+      (rc = dalloc(&s->obs, (size_t)s->in_rows * n)) || (rc = dalloc(&s->actions, 2 * (size_t)n)) ||
+      (rc = dalloc(&s->reward, n)) || (rc = dalloc(&s->done, n)) || (rc = dalloc(&s->step_base, 1)) ||
+      (rc = dalloc(&s->ray, 2 * (size_t)n))) {
+    racer_sim_destroy(s);
+    return rc;
+  }
+  cudaError_t err = cudaMemcpy(s->beam_dir, dirs.data(), beams * sizeof(float2), cudaMemcpyHostToDevice);
   if (err != cudaSuccess) {
     set_error(std::string("racer_sim_create upload: ") + cudaGetErrorString(err));
     racer_sim_destroy(s);
     return 2;
   }
-  TrackDev& t = s->t;
-  t.d = s->d_track;
-  t.cl = s->d_cl;
-  t.nx = nx;
-  t.ny = ny;
-  t.waypoints = (int)track[5];
-  t.layers = L;
-  t.x0 = track[2];
-  t.y0 = track[3];
-  t.cell = track[4];
-  t.inv_cell = 1.0f / track[4];
-  t.band = 0.5f - (float)((nx > ny ? nx : ny) + 3) * 9.5367431640625e-07f;
-  t.spacing = track[6];
-  t.slope = track[8];
-  t.nxf = (float)nx;
-  t.nyf = (float)ny;
-  t.route = 12 + 3L * L * nx * ny;
   *out = s;
   return 0;
+}
+
+int racer_sim_create(const float* track, size_t len, int n, uint64_t seed, int beams, void* stream,
+                     racer_sim** out) {
+  RACER_ARG(n >= 1, "racer_sim_create: n must be positive");
+  return racer_sim_create_segments(1, &track, &len, &n, &seed, beams, stream, out);
 }
 
 int racer_sim_destroy(racer_sim* s) {
   if (!s) return 0;
   for (auto& kv : s->graphs) cudaGraphExecDestroy(kv.second);
   for (auto& kv : s->surrogate_graphs) cudaGraphExecDestroy(kv.second);
-  cudaFree(s->d_track);
-  cudaFree(s->d_cl);
+  for (float* p : s->seg_track) cudaFree(p);
+  for (float2* p : s->seg_cl) cudaFree(p);
   cudaFree(s->beam_dir);
   cudaFree(s->ray);
   cudaFree(s->state);
@@ -246,15 +285,15 @@ int racer_sim_get_buffers(racer_sim* s, racer_sim_buffers* out) {
 
 static int sim_step_on(racer_sim* s, const float* actions, float* reward, float* done, float* obs, int32_t* iters,
                        cudaStream_t st) {
-  launch_advance(s->t, s->state, actions, reward, done, obs, s->n, s->beams, s->seed, s->ray, st);
-  launch_lidar(s->t, s->ray, obs, s->n, s->beams, s->beam_dir, iters, st);
+  launch_advance(s->seg, s->state, actions, reward, done, obs, s->n, s->beams, s->ray, st);
+  launch_lidar(s->seg, s->shape, s->ray, obs, s->n, s->beams, s->beam_dir, iters, st);
   RACER_LAUNCHED();
   return 0;
 }
 
 int racer_sim_reset(racer_sim* s) {
   RACER_ARG(s, "racer_sim_reset: null sim");
-  launch_spawn(s->t, s->state, s->actions, s->n, s->seed, s->st);
+  launch_spawn(s->seg, s->state, s->actions, s->n, s->st);
   return sim_step_on(s, s->actions, s->reward, s->done, s->obs, nullptr, s->st);
 }
 
@@ -630,7 +669,7 @@ static int runner_step_on(racer_sim* s, racer_policy* p, racer_acts* a, float* s
   int rc = forward_on(p, s->obs, a, st, &sa, 0);
   if (rc) return rc;
   if (!sur) return sim_step_on(s, s->actions, s->reward, s->done, s->obs, nullptr, st);
-  launch_advance(s->t, s->state, s->actions, s->reward, s->done, s->obs, s->n, s->beams, s->seed, s->ray, st);
+  launch_advance(s->seg, s->state, s->actions, s->reward, s->done, s->obs, s->n, s->beams, s->ray, st);
   RACER_LAUNCHED();
   return surrogate_lidar(sur, s, s->obs, audit, fallback, st);
 }
@@ -700,7 +739,7 @@ int racer_runner_audit_dynamics(racer_sim* s, racer_policy* p, racer_acts* a, fl
     if ((rc = forward_on(p, s->obs, a, st, &sa, 0))) break;
     RACER_TRY(cudaMemcpyAsync(prev, s->state, state_bytes, cudaMemcpyDeviceToDevice, st));
     if ((rc = sim_step_on(s, s->actions, s->reward, s->done, s->obs, nullptr, st))) break;
-    launch_rk4_audit(s->t, prev, s->actions, s->state, s->done, s->n, stats, st);
+    launch_rk4_audit(s->seg, prev, s->actions, s->state, s->done, s->n, stats, st);
     RACER_LAUNCHED();
   }
   cudaError_t copy = cudaMemcpyAsync(out, stats, 7 * sizeof(double), cudaMemcpyDeviceToHost, st);
@@ -784,9 +823,9 @@ int racer_sim_profile(racer_sim* s, const float* actions, int reps, float* physi
   for (auto& e : ev) RACER_TRY(cudaEventCreate(&e));
   for (int r = 0; r < reps; ++r) {
     RACER_TRY(cudaEventRecord(ev[3 * r], st));
-    launch_advance(s->t, s->state, actions, s->reward, s->done, s->obs, s->n, s->beams, s->seed, s->ray, st);
+    launch_advance(s->seg, s->state, actions, s->reward, s->done, s->obs, s->n, s->beams, s->ray, st);
     RACER_TRY(cudaEventRecord(ev[3 * r + 1], st));
-    launch_lidar(s->t, s->ray, s->obs, s->n, s->beams, s->beam_dir, nullptr, st);
+    launch_lidar(s->seg, s->shape, s->ray, s->obs, s->n, s->beams, s->beam_dir, nullptr, st);
     RACER_TRY(cudaEventRecord(ev[3 * r + 2], st));
   }
   RACER_LAUNCHED();
@@ -795,7 +834,7 @@ int racer_sim_profile(racer_sim* s, const float* actions, int reps, float* physi
   RACER_TRY(cudaMalloc((void**)&iters, (size_t)s->beams * s->n * sizeof(int32_t)));
   RACER_TRY(cudaMalloc((void**)&total, sizeof(unsigned long long)));
   RACER_TRY(cudaMemsetAsync(total, 0, sizeof(unsigned long long), st));
-  launch_lidar(s->t, s->ray, s->obs, s->n, s->beams, s->beam_dir, iters, st);
+  launch_lidar(s->seg, s->shape, s->ray, s->obs, s->n, s->beams, s->beam_dir, iters, st);
   k_sum_i32<<<152, 256, 0, st>>>(iters, (long)s->beams * s->n, total);
   RACER_LAUNCHED();
   unsigned long long host_total = 0;
@@ -815,6 +854,114 @@ int racer_sim_profile(racer_sim* s, const float* actions, int reps, float* physi
   if (physics_ms) *physics_ms = (float)(phys / reps);
   if (lidar_ms) *lidar_ms = (float)(lid / reps);
   if (probe_iterations) *probe_iterations = (int64_t)host_total;
+  return 0;
+}
+
+// Sum of iters[b * n + c] over all beams b and cars c in [c0, c1).
+__global__ void k_sum_cols(const int32_t* iters, int n, int beams, int c0, int c1, unsigned long long* out) {
+  const long w = c1 - c0, total = w * beams;
+  unsigned long long acc = 0;
+  for (long q = (long)blockIdx.x * blockDim.x + threadIdx.x; q < total; q += (long)gridDim.x * blockDim.x)
+    acc += (unsigned long long)iters[(q / w) * n + c0 + q % w];
+  for (int off = 16; off; off >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, off);
+  if ((threadIdx.x & 31) == 0) atomicAdd(out, acc);
+}
+
+static void drop_graphs(racer_sim* s) {
+  for (auto& kv : s->graphs) cudaGraphExecDestroy(kv.second);
+  for (auto& kv : s->surrogate_graphs) cudaGraphExecDestroy(kv.second);
+  s->graphs.clear();
+  s->graph_kernels.clear();
+  s->surrogate_graphs.clear();
+}
+
+static LidarShape make_shape(int cars, const int* order, int count) {
+  LidarShape shape;
+  shape.cars = cars;
+  for (int j = 0; j < MAX_SEGMENTS; ++j) shape.order[j] = order && j < count ? order[j] : j;
+  return shape;
+}
+
+int racer_sim_set_lidar_shape(racer_sim* s, int cars, const int* order) {
+  RACER_ARG(s, "racer_sim_set_lidar_shape: null sim");
+  LidarShape shape = make_shape(cars, order, s->seg.count);
+  RACER_ARG(lidar_shape_ok(shape), "racer_sim_set_lidar_shape: cars per block must be 2, 4 or 8");
+  if (order) {
+    bool seen[MAX_SEGMENTS] = {};
+    for (int j = 0; j < s->seg.count; ++j) {
+      RACER_ARG(order[j] >= 0 && order[j] < s->seg.count && !seen[order[j]],
+                "racer_sim_set_lidar_shape: order must be a permutation of the segments");
+      seen[order[j]] = true;
+    }
+  }
+  RACER_TRY(cudaStreamSynchronize(s->st));
+  drop_graphs(s);
+  s->shape = shape;
+  return 0;
+}
+
+int racer_sim_get_lidar_shape(racer_sim* s, int* cars, int* order) {
+  RACER_ARG(s, "racer_sim_get_lidar_shape: null sim");
+  if (cars) *cars = s->shape.cars;
+  if (order)
+    for (int j = 0; j < s->seg.count; ++j) order[j] = s->shape.order[j];
+  return 0;
+}
+
+int racer_sim_autotune(racer_sim* s, int reps, int* cars_out, int* order_out, float* best_ms) {
+  RACER_ARG(s && reps >= 1, "racer_sim_autotune: bad argument");
+  cudaStream_t st = s->st;
+  const int count = s->seg.count;
+  // probe iterations per segment, from one counted pass
+  int32_t* iters = nullptr;
+  unsigned long long* sums = nullptr;
+  RACER_TRY(cudaMalloc((void**)&iters, (size_t)s->beams * s->n * sizeof(int32_t)));
+  RACER_TRY(cudaMalloc((void**)&sums, MAX_SEGMENTS * sizeof(unsigned long long)));
+  RACER_TRY(cudaMemsetAsync(sums, 0, MAX_SEGMENTS * sizeof(unsigned long long), st));
+  launch_lidar(s->seg, s->shape, s->ray, s->obs, s->n, s->beams, s->beam_dir, iters, st);
+  for (int k = 0; k < count; ++k)
+    k_sum_cols<<<4 * 152, 256, 0, st>>>(iters, s->n, s->beams, s->seg.car0[k], s->seg.car0[k + 1], sums + k);
+  RACER_LAUNCHED();
+  unsigned long long host[MAX_SEGMENTS] = {};
+  RACER_TRY(cudaMemcpyAsync(host, sums, sizeof host, cudaMemcpyDeviceToHost, st));
+  RACER_TRY(cudaStreamSynchronize(st));
+  cudaFree(iters);
+  cudaFree(sums);
+  int natural[MAX_SEGMENTS], heavy[MAX_SEGMENTS];
+  for (int j = 0; j < MAX_SEGMENTS; ++j) natural[j] = heavy[j] = j;
+  std::stable_sort(heavy, heavy + count, [&](int a, int b) { return host[a] > host[b]; });
+  std::vector<LidarShape> candidates;
+  for (int cars : {2, 4, 8}) {
+    candidates.push_back(make_shape(cars, natural, count));
+    if (count > 1 && !std::equal(natural, natural + count, heavy)) candidates.push_back(make_shape(cars, heavy, count));
+  }
+  cudaEvent_t a, b;
+  RACER_TRY(cudaEventCreate(&a));
+  RACER_TRY(cudaEventCreate(&b));
+  float best = 1e30f;
+  LidarShape chosen = s->shape;
+  for (const LidarShape& shape : candidates) {
+    launch_lidar(s->seg, shape, s->ray, s->obs, s->n, s->beams, s->beam_dir, nullptr, st);
+    RACER_TRY(cudaEventRecord(a, st));
+    for (int r = 0; r < reps; ++r)
+      launch_lidar(s->seg, shape, s->ray, s->obs, s->n, s->beams, s->beam_dir, nullptr, st);
+    RACER_TRY(cudaEventRecord(b, st));
+    RACER_LAUNCHED();
+    RACER_TRY(cudaEventSynchronize(b));
+    float ms = 0;
+    RACER_TRY(cudaEventElapsedTime(&ms, a, b));
+    if (ms / reps < best) best = ms / reps, chosen = shape;
+  }
+  cudaEventDestroy(a);
+  cudaEventDestroy(b);
+  if (chosen.cars != s->shape.cars || !std::equal(chosen.order, chosen.order + count, s->shape.order)) {
+    drop_graphs(s);
+    s->shape = chosen;
+  }
+  if (cars_out) *cars_out = s->shape.cars;
+  if (order_out)
+    for (int j = 0; j < count; ++j) order_out[j] = s->shape.order[j];
+  if (best_ms) *best_ms = best;
   return 0;
 }
 

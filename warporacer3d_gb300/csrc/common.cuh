@@ -47,6 +47,27 @@ struct TrackDev {
   long route;
 };
 
+// Several tracks in one launch: cars [car0[k], car0[k + 1]) drive on track
+// t[k] and respawn from seed[k], with car index car - car0[k] in their Philox
+// counters, so segment k evolves exactly as a sim of that track alone.
+// Passed by value as a kernel parameter (about 0.8 KB).
+constexpr int MAX_SEGMENTS = 8;
+struct Segments {
+  int count;
+  int car0[MAX_SEGMENTS + 1];
+  int max_iters[MAX_SEGMENTS];
+  uint64_t seed[MAX_SEGMENTS];
+  TrackDev t[MAX_SEGMENTS];
+};
+
+// Launch shape of the lidar: cars per block (one warp each) and the order in
+// which the segments' blocks are laid out along the grid (heavier first lets
+// the light segments fill the tail).
+struct LidarShape {
+  int cars = 4;
+  int order[MAX_SEGMENTS] = {0, 1, 2, 3, 4, 5, 6, 7};
+};
+
 }  // namespace racer
 
 // Host-side error state of the C ABI (one message per thread).

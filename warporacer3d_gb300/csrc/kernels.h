@@ -7,21 +7,28 @@
 
 namespace racer {
 
-// sim.cu (bit-exact simulator kernels)
-void launch_spawn(const TrackDev& t, float* state, float* actions, int n, uint64_t seed, cudaStream_t st);
+// sim.cu (bit-exact simulator kernels). Every car kernel takes the segment
+// table; a one-track sim is a table of one.
+Segments single_segment(const TrackDev& t, int n, uint64_t seed);
+void launch_spawn(const Segments& g, float* state, float* actions, int n, cudaStream_t st);
 // ray [2, n] float4: the per-car lidar frame the physics kernel leaves for the lidar.
-void launch_advance(const TrackDev& t, float* state, const float* actions, float* reward, float* done, float* obs,
-                    int n, int beams, uint64_t seed, float4* ray, cudaStream_t st);
+void launch_advance(const Segments& g, float* state, const float* actions, float* reward, float* done, float* obs,
+                    int n, int beams, float4* ray, cudaStream_t st);
 // With `list` set, only the cars list[0 .. *list_count) (list_max at most) are traced.
+void launch_lidar(const Segments& g, const LidarShape& shape, const float4* ray, float* obs, int n, int beams,
+                  const float2* beam_dir, int* iters, cudaStream_t st, const int* list = nullptr,
+                  const int* list_count = nullptr, int list_max = 0);
+// One track, default shape (surrogate labels and fallback).
 void launch_lidar(const TrackDev& t, const float4* ray, float* obs, int n, int beams, const float2* beam_dir,
                   int* iters, cudaStream_t st, const int* list = nullptr, const int* list_count = nullptr,
                   int list_max = 0);
+bool lidar_shape_ok(const LidarShape& shape);
 // Cars whose smallest predicted range (ordered uint bits of a nonnegative float) is below threshold.
 void launch_select_cars(const unsigned* minr, int n, float threshold, int* list, int* count, cudaStream_t st);
 int lidar_max_iters(const TrackDev& t);
 // FP64 re-integration audit of one physics step: prev/next state [11, n] around the FP32 step,
 // stats [7] doubles (count, sums and maxima of position, heading and speed errors).
-void launch_rk4_audit(const TrackDev& t, const float* prev, const float* actions, const float* next,
+void launch_rk4_audit(const Segments& g, const float* prev, const float* actions, const float* next,
                       const float* done, int n, double* stats, cudaStream_t st);
 // poses [count] (x, y, heading, layer) -> ray [2, count]: the frame of a car at rest there.
 void launch_pose_frames(const TrackDev& t, const float4* poses, int count, float4* ray, cudaStream_t st);

@@ -5,19 +5,25 @@
 #include <stdint.h>
 
 #include <map>
+#include <vector>
 #include <tuple>
 
 #include "../../include/racer.h"
 #include "common.cuh"
 
-// Sim (racer/sim.mojo:269-289): track, cars and their buffers on one stream.
+// Sim (racer/sim.mojo:269-289): cars on one or more tracks (a segment table,
+// one car range per track) and their buffers on one stream.
 struct racer_sim {
   int n = 0, beams = 0, in_rows = 0;
-  uint64_t seed = 0;
+  uint64_t seed = 0;  // sampling seed (the first segment's)
   size_t track_len = 0;
-  racer::TrackDev t{};
-  float* d_track = nullptr;
+  racer::TrackDev t{};  // the first segment's track
+  racer::Segments seg{};
+  racer::LidarShape shape{};
+  float* d_track = nullptr;  // the first segment's uploads (also in seg_track / seg_cl)
   float2* d_cl = nullptr;
+  std::vector<float*> seg_track;
+  std::vector<float2*> seg_cl;
   float2* beam_dir = nullptr;
   float4* ray = nullptr;  // [2, n] per-car lidar frame written by the physics kernel
   float *state = nullptr, *obs = nullptr, *actions = nullptr, *reward = nullptr, *done = nullptr;

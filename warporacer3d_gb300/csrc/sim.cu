@@ -179,11 +179,12 @@ __device__ __forceinline__ V4 axpy(const V4& p, const V4& k, float h) {
   return V4{p.x + k.x * h, p.y + k.y * h, p.h + k.h * h, p.s + k.s * h};
 }
 
-// racer/sim.mojo:170-181
-__device__ void spawn(const TrackDev& t, float* s, int n, int i, uint64_t seed) {
+// racer/sim.mojo:170-181. `local` is the car's index within its track's
+// segment (its Philox counter); i is its column in the batch.
+__device__ void spawn(const TrackDev& t, float* s, int n, int i, int local, uint64_t seed) {
   float episode = s[(long)EPISODE * n + i] + 1.0f;
   float r[4];
-  philox::uniform4(seed, (uint64_t)i, (uint64_t)episode, r);
+  philox::uniform4(seed, (uint64_t)local, (uint64_t)episode, r);
   int w = min((int)(r[0] * (float)t.waypoints), t.waypoints - 1);
   for (int row = 0; row < STATE; ++row) s[(long)row * n + i] = 0.0f;
   s[(long)X * n + i] = waypoint(t, w, 0);
@@ -195,20 +196,27 @@ __device__ void spawn(const TrackDev& t, float* s, int n, int i, uint64_t seed) 
   s[(long)FRICTION * n + i] = 0.85f + 0.3f * r[1];
 }
 
-__global__ void k_spawn(TrackDev t, float* state, float* actions, int n, uint64_t seed) {
+// Segment of car i (segments are few; a short scan).
+__device__ __forceinline__ int segment_of(const Segments& g, int i) {
+  int k = 0;
+  while (k + 1 < g.count && i >= g.car0[k + 1]) ++k;
+  return k;
+}
+
+__global__ void k_spawn(const __grid_constant__ Segments g, float* state, float* actions, int n) {
   int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
-  spawn(t, state, n, i, seed);
+  const int k = segment_of(g, i);
+  spawn(g.t[k], state, n, i, i - g.car0[k], g.seed[k]);
   actions[i] = 0.0f;
   actions[(long)n + i] = 0.0f;
 }
 
-// racer/sim.mojo:184-235: one 60 Hz step of car i.
+// racer/sim.mojo:184-235: one 60 Hz step of car i (segment index local).
 template <int LAYERS>
-__global__ void k_advance(TrackDev t, float* s, const float* act, float* reward, float* done, float* obs, int n,
-                          int beams, uint64_t seed, float4* ray) {
-  int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= n) return;
+__device__ __forceinline__ void advance_car(const TrackDev& t, float* s, const float* act, float* reward, float* done,
+                                            float* obs, int n, int beams, uint64_t seed, float4* ray, int i,
+                                            int local) {
   V4 p{s[(long)X * n + i], s[(long)Y * n + i], s[(long)HEADING * n + i], s[(long)SPEED * n + i]};
   Spot spot = probe<LAYERS>(t, p.x, p.y, s[(long)Z * n + i]);
   Surface ground = surface(t, spot.layer, p.x, p.y);
@@ -259,7 +267,7 @@ __global__ void k_advance(TrackDev t, float* s, const float* act, float* reward,
   done[i] = reason;
   float heading = p.h, speed = p.s;
   if (reason > 0.0f) {
-    spawn(t, s, n, i, seed);
+    spawn(t, s, n, i, local, seed);
     float sx = s[(long)X * n + i], sy = s[(long)Y * n + i];
     ground = surface(t, probe<LAYERS>(t, sx, sy, s[(long)Z * n + i]).layer, sx, sy);
     heading = s[(long)HEADING * n + i];
@@ -282,6 +290,20 @@ __global__ void k_advance(TrackDev t, float* s, const float* act, float* reward,
   const float sx = s[(long)X * n + i], sy = s[(long)Y * n + i], sz = s[(long)Z * n + i];
   ray[i] = make_float4((sx + MOUNT_X * ch) + 0.0f, (sy + MOUNT_X * sh) + 0.0f, (sz + MOUNT_X * along) + MOUNT_Z, ch);
   ray[n + i] = make_float4(sh, along, across, (float)probe<LAYERS>(t, sx, sy, sz).layer);
+}
+
+__global__ void k_advance(const __grid_constant__ Segments g, float* s, const float* act, float* reward, float* done,
+                          float* obs, int n, int beams, float4* ray) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const int k = segment_of(g, i);
+  const TrackDev& t = g.t[k];
+  if (t.layers == 1)
+    advance_car<1>(t, s, act, reward, done, obs, n, beams, g.seed[k], ray, i, i - g.car0[k]);
+  else if (t.layers == 2)
+    advance_car<2>(t, s, act, reward, done, obs, n, beams, g.seed[k], ray, i, i - g.car0[k]);
+  else
+    advance_car<0>(t, s, act, reward, done, obs, n, beams, g.seed[k], ray, i, i - g.car0[k]);
 }
 
 // FP64 re-integration of racer/sim.mojo:189-213 (the 4 RK4 substeps) for
@@ -310,10 +332,8 @@ __device__ void derivative64(const double* p, double steer, double accel, double
 // from the same state (prev) and actions. stats: [0] count, [1..3] sums,
 // [4..6] maxima (as doubles).
 template <int LAYERS>
-__global__ void k_rk4_f64(TrackDev t, const float* prev, const float* act, const float* next, const float* done,
-                          int n, double* stats) {
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= n || done[i] != 0.0f) return;
+__device__ void rk4_f64_car(const TrackDev& t, const float* prev, const float* act, const float* next, int n,
+                            double* stats, int i) {
   double p[4] = {prev[(long)X * n + i], prev[(long)Y * n + i], prev[(long)HEADING * n + i],
                  prev[(long)SPEED * n + i]};
   Spot spot = probe<LAYERS>(t, (float)p[0], (float)p[1], prev[(long)Z * n + i]);
@@ -354,6 +374,19 @@ __global__ void k_rk4_f64(TrackDev t, const float* prev, const float* act, const
   }
 }
 
+__global__ void k_rk4_f64(const __grid_constant__ Segments g, const float* prev, const float* act, const float* next,
+                          const float* done, int n, double* stats) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n || done[i] != 0.0f) return;
+  const TrackDev& t = g.t[segment_of(g, i)];
+  if (t.layers == 1)
+    rk4_f64_car<1>(t, prev, act, next, n, stats, i);
+  else if (t.layers == 2)
+    rk4_f64_car<2>(t, prev, act, next, n, stats, i);
+  else
+    rk4_f64_car<0>(t, prev, act, next, n, stats, i);
+}
+
 // The lidar frame of a car at rest on a layer (racer/sim.mojo:229-234,
 // 243-249): pose (x, y, heading, layer) -> z = the layer's bilinear height,
 // the slopes along and across the heading, and the same frame k_advance
@@ -374,9 +407,9 @@ __global__ void k_pose_frames(TrackDev t, const float4* __restrict__ poses, int 
 }
 
 // racer/sim.mojo:238-266: the sphere-traced lidar, one thread per (car, beam).
-// Block = LIDAR_CARS warps; warp w marches 32 consecutive beams of car
-// blockIdx.x * LIDAR_CARS + w, so its lanes start at one origin and probe neighbouring
-// cells (L1 reuse) and finish after similar numbers of probes. The per-car
+// A block holds a few warps; each warp marches 32 consecutive beams of one
+// car, so its lanes start at one origin and probe neighbouring cells (L1
+// reuse) and finish after similar numbers of probes. The per-car
 // frame comes from the physics kernel (`ray`). Every floating-point operation
 // of a beam is the reference's, in its order; the nearest-cell index avoids
 // the division where that provably gives the same cell (cell_coord), and
@@ -386,25 +419,50 @@ __device__ __forceinline__ void trace(const TrackDev& t, const float4* __restric
                                       const float2* __restrict__ beam_dir, int max_iters, int* iters, int car,
                                       int beam);
 
-// Cars per block: small blocks release their slot as soon as their few cars finish.
-constexpr int LIDAR_CARS = 4;
+// The lidar grid: the blocks of the segment in slot j of the launch order are
+// [block0[j], block0[j + 1]), each covering `cars` consecutive cars of it.
+struct LidarGrid {
+  int order[MAX_SEGMENTS];
+  int block0[MAX_SEGMENTS + 1];
+};
 
-template <int LAYERS, bool LIST>
-__global__ void __launch_bounds__(LIDAR_CARS * 32, 64 / LIDAR_CARS) k_lidar(TrackDev t, const float4* __restrict__ ray, float* obs, int n,
-                                               int beams, const float2* __restrict__ beam_dir, int max_iters,
-                                               int* iters, const int* __restrict__ list, const int* list_count) {
+__device__ __forceinline__ void trace_any(const TrackDev& t, const float4* __restrict__ ray, float* obs, int n,
+                                          const float2* __restrict__ beam_dir, int max_iters, int* iters, int car,
+                                          int beam) {
+  if (t.layers == 1)
+    trace<1>(t, ray, obs, n, beam_dir, max_iters, iters, car, beam);
+  else if (t.layers == 2)
+    trace<2>(t, ray, obs, n, beam_dir, max_iters, iters, car, beam);
+  else
+    trace<0>(t, ray, obs, n, beam_dir, max_iters, iters, car, beam);
+}
+
+// CARS warps per block (one car each): small blocks release their slot as soon
+// as their few cars finish. A block's segment depends on blockIdx only, so the
+// track's fields stay block-uniform.
+template <int CARS, bool LIST>
+__global__ void __launch_bounds__(CARS * 32, (64 / CARS < 32 ? 64 / CARS : 32))
+    k_lidar(const __grid_constant__ Segments g, const __grid_constant__ LidarGrid lg, const float4* __restrict__ ray,
+            float* obs, int n, int beams, const float2* __restrict__ beam_dir, int* iters,
+            const int* __restrict__ list, const int* list_count) {
   const int beam = blockIdx.y * 32 + (threadIdx.x & 31);
   if (beam >= beams) return;
   if (LIST) {  // only the listed cars (surrogate fallback), grid-stride over the list
     const int count = *list_count;
-    for (int k = blockIdx.x * LIDAR_CARS + (threadIdx.x >> 5); k < count; k += gridDim.x * LIDAR_CARS) {
-      const int car = list[k];
-      if (car < n) trace<LAYERS>(t, ray, obs, n, beam_dir, max_iters, iters, car, beam);
+    for (int q = blockIdx.x * CARS + (threadIdx.x >> 5); q < count; q += gridDim.x * CARS) {
+      const int car = list[q];
+      if (car < n) {
+        const int k = segment_of(g, car);
+        trace_any(g.t[k], ray, obs, n, beam_dir, g.max_iters[k], iters, car, beam);
+      }
     }
     return;
   }
-  const int car = blockIdx.x * LIDAR_CARS + (threadIdx.x >> 5);
-  if (car < n) trace<LAYERS>(t, ray, obs, n, beam_dir, max_iters, iters, car, beam);
+  int j = 0;
+  while (j + 1 < g.count && (int)blockIdx.x >= lg.block0[j + 1]) ++j;
+  const int k = lg.order[j];
+  const int car = g.car0[k] + ((int)blockIdx.x - lg.block0[j]) * CARS + (int)(threadIdx.x >> 5);
+  if (car < g.car0[k + 1]) trace_any(g.t[k], ray, obs, n, beam_dir, g.max_iters[k], iters, car, beam);
 }
 
 template <int LAYERS>
@@ -471,46 +529,81 @@ __global__ void k_add_i64(int64_t* p, int64_t v) {
 }  // namespace
 
 // ---- host launchers ----
-void launch_spawn(const TrackDev& t, float* state, float* actions, int n, uint64_t seed, cudaStream_t st) {
-  k_spawn<<<(n + 127) / 128, 128, 0, st>>>(t, state, actions, n, seed);
+Segments single_segment(const TrackDev& t, int n, uint64_t seed) {
+  Segments g{};
+  g.count = 1;
+  g.car0[0] = 0;
+  g.car0[1] = n;
+  g.max_iters[0] = lidar_max_iters(t);
+  g.seed[0] = seed;
+  g.t[0] = t;
+  return g;
 }
 
-void launch_advance(const TrackDev& t, float* state, const float* actions, float* reward, float* done, float* obs,
-                    int n, int beams, uint64_t seed, float4* ray, cudaStream_t st) {
-  dim3 grid((n + 127) / 128);
-  if (t.layers == 1)
-    k_advance<1><<<grid, 128, 0, st>>>(t, state, actions, reward, done, obs, n, beams, seed, ray);
-  else if (t.layers == 2)
-    k_advance<2><<<grid, 128, 0, st>>>(t, state, actions, reward, done, obs, n, beams, seed, ray);
-  else
-    k_advance<0><<<grid, 128, 0, st>>>(t, state, actions, reward, done, obs, n, beams, seed, ray);
+void launch_spawn(const Segments& g, float* state, float* actions, int n, cudaStream_t st) {
+  k_spawn<<<(n + 127) / 128, 128, 0, st>>>(g, state, actions, n);
+}
+
+void launch_advance(const Segments& g, float* state, const float* actions, float* reward, float* done, float* obs,
+                    int n, int beams, float4* ray, cudaStream_t st) {
+  k_advance<<<(n + 127) / 128, 128, 0, st>>>(g, state, actions, reward, done, obs, n, beams, ray);
 }
 
 int lidar_max_iters(const TrackDev& t) { return (int)ceilf(RANGE / (0.5f * t.cell)) + 2; }
 
-void launch_lidar(const TrackDev& t, const float4* ray, float* obs, int n, int beams, const float2* beam_dir,
-                  int* iters, cudaStream_t st, const int* list, const int* list_count, int list_max) {
+// Slots in the shape's order (invalid or repeated entries skipped, missing
+// segments appended in index order) and their block ranges.
+static LidarGrid lidar_grid(const Segments& g, const LidarShape& shape) {
+  LidarGrid lg{};
+  bool used[MAX_SEGMENTS] = {};
+  int slots = 0;
+  for (int j = 0; j < MAX_SEGMENTS; ++j) {
+    const int k = shape.order[j];
+    if (k >= 0 && k < g.count && !used[k]) used[k] = true, lg.order[slots++] = k;
+  }
+  for (int k = 0; k < g.count; ++k)
+    if (!used[k]) lg.order[slots++] = k;
+  lg.block0[0] = 0;
+  for (int j = 0; j < g.count; ++j) {
+    const int k = lg.order[j];
+    lg.block0[j + 1] = lg.block0[j] + (g.car0[k + 1] - g.car0[k] + shape.cars - 1) / shape.cars;
+  }
+  for (int j = g.count; j < MAX_SEGMENTS; ++j) lg.block0[j + 1] = lg.block0[g.count];
+  return lg;
+}
+
+template <int CARS>
+static void lidar_cars(const Segments& g, const LidarShape& shape, const float4* ray, float* obs, int n, int beams,
+                       const float2* beam_dir, int* iters, cudaStream_t st, const int* list, const int* list_count,
+                       int list_max) {
+  const LidarGrid lg = lidar_grid(g, shape);
   // a listed subset: a grid of about eight blocks per SM strides over the list
-  dim3 grid(list ? std::min((list_max + LIDAR_CARS - 1) / LIDAR_CARS, 16 * 152 / ((beams + 31) / 32) + 1)
-                 : (n + LIDAR_CARS - 1) / LIDAR_CARS,
+  dim3 grid(list ? std::min((list_max + CARS - 1) / CARS, 16 * 152 / ((beams + 31) / 32) + 1) : lg.block0[g.count],
             (beams + 31) / 32);
   if (grid.x == 0) return;
-  int cap = lidar_max_iters(t);
-  if (list) {
-    if (t.layers == 1)
-      k_lidar<1, true><<<grid, LIDAR_CARS * 32, 0, st>>>(t, ray, obs, n, beams, beam_dir, cap, iters, list, list_count);
-    else if (t.layers == 2)
-      k_lidar<2, true><<<grid, LIDAR_CARS * 32, 0, st>>>(t, ray, obs, n, beams, beam_dir, cap, iters, list, list_count);
-    else
-      k_lidar<0, true><<<grid, LIDAR_CARS * 32, 0, st>>>(t, ray, obs, n, beams, beam_dir, cap, iters, list, list_count);
-  } else {
-    if (t.layers == 1)
-      k_lidar<1, false><<<grid, LIDAR_CARS * 32, 0, st>>>(t, ray, obs, n, beams, beam_dir, cap, iters, nullptr, nullptr);
-    else if (t.layers == 2)
-      k_lidar<2, false><<<grid, LIDAR_CARS * 32, 0, st>>>(t, ray, obs, n, beams, beam_dir, cap, iters, nullptr, nullptr);
-    else
-      k_lidar<0, false><<<grid, LIDAR_CARS * 32, 0, st>>>(t, ray, obs, n, beams, beam_dir, cap, iters, nullptr, nullptr);
-  }
+  if (list)
+    k_lidar<CARS, true><<<grid, CARS * 32, 0, st>>>(g, lg, ray, obs, n, beams, beam_dir, iters, list, list_count);
+  else
+    k_lidar<CARS, false><<<grid, CARS * 32, 0, st>>>(g, lg, ray, obs, n, beams, beam_dir, iters, nullptr, nullptr);
+}
+
+bool lidar_shape_ok(const LidarShape& shape) { return shape.cars == 2 || shape.cars == 4 || shape.cars == 8; }
+
+void launch_lidar(const Segments& g, const LidarShape& shape, const float4* ray, float* obs, int n, int beams,
+                  const float2* beam_dir, int* iters, cudaStream_t st, const int* list, const int* list_count,
+                  int list_max) {
+  if (shape.cars == 2)
+    lidar_cars<2>(g, shape, ray, obs, n, beams, beam_dir, iters, st, list, list_count, list_max);
+  else if (shape.cars == 8)
+    lidar_cars<8>(g, shape, ray, obs, n, beams, beam_dir, iters, st, list, list_count, list_max);
+  else
+    lidar_cars<4>(g, shape, ray, obs, n, beams, beam_dir, iters, st, list, list_count, list_max);
+}
+
+void launch_lidar(const TrackDev& t, const float4* ray, float* obs, int n, int beams, const float2* beam_dir,
+                  int* iters, cudaStream_t st, const int* list, const int* list_count, int list_max) {
+  launch_lidar(single_segment(t, n, 0), LidarShape{}, ray, obs, n, beams, beam_dir, iters, st, list, list_count,
+               list_max);
 }
 
 __global__ void k_select_cars(const unsigned* minr, int n, unsigned threshold_bits, int* list, int* count) {
@@ -524,15 +617,9 @@ void launch_select_cars(const unsigned* minr, int n, float threshold, int* list,
   k_select_cars<<<(n + 255) / 256, 256, 0, st>>>(minr, n, bits, list, count);
 }
 
-void launch_rk4_audit(const TrackDev& t, const float* prev, const float* actions, const float* next,
+void launch_rk4_audit(const Segments& g, const float* prev, const float* actions, const float* next,
                       const float* done, int n, double* stats, cudaStream_t st) {
-  dim3 grid((n + 127) / 128);
-  if (t.layers == 1)
-    k_rk4_f64<1><<<grid, 128, 0, st>>>(t, prev, actions, next, done, n, stats);
-  else if (t.layers == 2)
-    k_rk4_f64<2><<<grid, 128, 0, st>>>(t, prev, actions, next, done, n, stats);
-  else
-    k_rk4_f64<0><<<grid, 128, 0, st>>>(t, prev, actions, next, done, n, stats);
+  k_rk4_f64<<<(n + 127) / 128, 128, 0, st>>>(g, prev, actions, next, done, n, stats);
 }
 
 void launch_pose_frames(const TrackDev& t, const float4* poses, int count, float4* ray, cudaStream_t st) {

@@ -567,6 +567,10 @@ int racer_surrogate_create(racer_sim* sim, int hidden, int batch, uint64_t seed,
     set_error("racer_surrogate_create: hidden must be 128, 256 or 512 and batch a positive multiple of 128");
     return 1;
   }
+  if (sim->seg.count != 1) {
+    set_error("racer_surrogate_create: a surrogate learns one track; the sim holds several");
+    return 1;
+  }
   if (sim->t.layers > 2) {
     set_error("racer_surrogate_create: the surrogate's inputs encode at most two layers");
     return 1;

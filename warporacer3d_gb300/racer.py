@@ -98,13 +98,34 @@ class Sim:
     """n cars on a track (racer/sim.mojo:269-348)."""
 
     def __init__(self, track, n, seed, beams=108, stream=None):
-        d = np.ascontiguousarray(track, np.float32)
-        self.n, self.seed, self.beams, self.IN = n, seed, beams, beams + 5
+        self._create([track], [n], [seed], beams, stream)
+
+    @classmethod
+    def segments(cls, tracks, cars, seeds, beams=108, stream=None):
+        """Several tracks in one sim: segment k is cars[k] cars on tracks[k] seeded by seeds[k], in columns
+        sum(cars[:k]) .. sum(cars[:k+1]) of every buffer; each launch covers all segments."""
+        self = cls.__new__(cls)
+        self._create(list(tracks), list(cars), list(seeds), beams, stream)
+        return self
+
+    def _create(self, tracks, cars, seeds, beams, stream):
+        if not (len(tracks) == len(cars) == len(seeds)):
+            raise ValueError("tracks, cars and seeds differ in length")
+        arrays = [np.ascontiguousarray(t, np.float32) for t in tracks]
+        k = len(arrays)
+        fp = ctypes.POINTER(ctypes.c_float)
+        ptrs = (fp * k)(*[a.ctypes.data_as(fp) for a in arrays])
+        lens = (ctypes.c_size_t * k)(*[a.size for a in arrays])
+        counts = (ctypes.c_int * k)(*cars)
+        seeds_c = (ctypes.c_uint64 * k)(*seeds)
+        self.n, self.seed, self.beams, self.IN = int(sum(cars)), seeds[0], beams, beams + 5
+        self.cars = list(cars)
+        self.car0 = [int(v) for v in np.concatenate([[0], np.cumsum(cars)])]
         self.stream = _stream(stream)
         h = ctypes.c_void_p()
-        call("racer_sim_create", d.ctypes.data_as(ctypes.POINTER(ctypes.c_float)), d.size, n, seed, beams,
-             self.stream, ctypes.byref(h))
+        call("racer_sim_create_segments", k, ptrs, lens, counts, seeds_c, beams, self.stream, ctypes.byref(h))
         self.handle = h
+        n = self.n
         b = SimBuffers()
         call("racer_sim_get_buffers", h, ctypes.byref(b))
         s = self.stream
@@ -131,6 +152,23 @@ class Sim:
     def sample(self, output, log_std, actions, logp, value, deterministic, step):
         call("racer_sim_sample", self.handle, output.c, log_std.c, actions.c, logp.c, value.c, int(deterministic),
              step)
+
+    def set_lidar_shape(self, cars_per_block, order=None):
+        k = len(self.cars)
+        arr = None if order is None else (ctypes.c_int * k)(*order)
+        call("racer_sim_set_lidar_shape", self.handle, cars_per_block, arr)
+
+    def lidar_shape(self):
+        cars, order = ctypes.c_int(), (ctypes.c_int * len(self.cars))()
+        call("racer_sim_get_lidar_shape", self.handle, ctypes.byref(cars), order)
+        return cars.value, list(order)
+
+    def autotune(self, reps=5):
+        """Times the lidar launch shapes on the current frames; keeps and returns the fastest
+        (cars per block, segment order, mean ms)."""
+        cars, order, ms = ctypes.c_int(), (ctypes.c_int * len(self.cars))(), ctypes.c_float()
+        call("racer_sim_autotune", self.handle, reps, ctypes.byref(cars), order, ctypes.byref(ms))
+        return cars.value, list(order), ms.value
 
 
 class Policy:
@@ -327,12 +365,18 @@ def load(policy, path):
 class Runner:
     """A device, n cars on a track and a policy driving them (main.mojo:22-124)."""
 
-    def __init__(self, track, n, beams=108, seed=42, policy_seed=42, stream=None):
-        self.sim = Sim(track, n, seed, beams=beams, stream=stream)
-        self.policy = Policy(policy_seed, beams=beams, stream=self.sim.stream)
+    def __init__(self, track, n, beams=108, seed=42, policy_seed=42, stream=None, sim=None):
+        self.sim = sim if sim is not None else Sim(track, n, seed, beams=beams, stream=stream)
+        n = self.sim.n
+        self.policy = Policy(policy_seed, beams=self.sim.beams, stream=self.sim.stream)
         self.acts = Activations(self.policy, n)
         self.scratch = DevArray.empty((2, n))  # log probabilities and values
         self.sim.reset()
+
+    @classmethod
+    def segments(cls, tracks, cars, seeds, beams=108, policy_seed=42, stream=None):
+        """One policy driving cars on several tracks at once (Sim.segments)."""
+        return cls(None, None, policy_seed=policy_seed, sim=Sim.segments(tracks, cars, seeds, beams, stream))
 
     def step(self, deterministic, t):
         call("racer_runner_step", self.sim.handle, self.policy.handle, self.acts.handle, self.scratch.c,

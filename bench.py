@@ -52,6 +52,8 @@ def parse():
     ap.add_argument("--no-surrogate", action="store_true")
     ap.add_argument("--surrogate-only", action="store_true", help="print only the surrogate section")
     ap.add_argument("--no-training", action="store_true")
+    ap.add_argument("--no-batched", action="store_true")
+    ap.add_argument("--batched-only", action="store_true", help="print only the batched multi-track section")
     ap.add_argument("--training-iterations", type=int, default=300)
     ap.add_argument("--surrogate-train-steps", type=int, default=None,
                     help="surrogate training steps (default 20000; fewer only to profile the rollout)")
@@ -187,6 +189,64 @@ def surrogate_section(torch, W, track, stream, flush, train_steps=SURR_TRAIN_STE
             "target_mae_m": 0.02}
 
 
+BATCH_TRACKS = ("flat", "ramp", "bank", "bridge", "occupancy")
+BATCH_CARS = (1024, 4096, 16384, 32768, 65536)
+BATCH_STEPS, BATCH_REPS = 16, 3
+
+
+def batched_section(torch, W, stream, flush):
+    """Five tracks with uneven car counts in one sim (one launch per kernel covers every segment), rollouts
+    of BATCH_STEPS env steps from one CUDA graph, after the autotuner picked the lidar launch shape; against
+    the same cars as five one-track sims whose rollout graphs run back to back."""
+    tracks = [W.track(name) for name in BATCH_TRACKS]
+    seeds = [100 + k for k in range(len(tracks))]
+    total = sum(BATCH_CARS)
+    batch = W.Runner.segments(tracks, BATCH_CARS, seeds, beams=BEAMS, policy_seed=42, stream=stream)
+    batch.rollout(BATCH_STEPS, False, 0)  # cars leave the spawn poses
+    torch.cuda.synchronize()
+    default_shape = batch.sim.lidar_shape()
+    default_ms = batch.profile_sim(5)[1]
+    cars_per_block, wide, order, tuned_ms = batch.sim.autotune(5)
+
+    def timed(run):
+        run(0)
+        torch.cuda.synchronize()
+        ms = 0.0
+        for k in range(BATCH_REPS):
+            with torch.cuda.stream(stream):
+                flush.zero_()
+                a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                a.record(stream)
+                run((k + 1) * BATCH_STEPS)
+                b.record(stream)
+            torch.cuda.synchronize()
+            ms += a.elapsed_time(b)
+        return total * BATCH_STEPS * BATCH_REPS / (ms / 1000.0), ms / (BATCH_REPS * BATCH_STEPS)
+
+    batched_rate, batched_ms = timed(lambda t0: batch.rollout(BATCH_STEPS, False, t0))
+    phys_ms, lidar_ms, probes = batch.profile_sim(5)
+    launches = batch.rollout_kernel_count(BATCH_STEPS)
+    del batch
+    separate = [W.Runner(t, c, beams=BEAMS, seed=s, policy_seed=42, stream=stream)
+                for t, c, s in zip(tracks, BATCH_CARS, seeds)]
+    for r in separate:
+        r.rollout(BATCH_STEPS, False, 0)
+    separate_rate, separate_ms = timed(lambda t0: [r.rollout(BATCH_STEPS, False, t0) for r in separate])
+    per_track_lidar = {name: r.profile_sim(3)[1] for name, r in zip(BATCH_TRACKS, separate)}
+    return {"workload": ", ".join(f"{n} {c}" for n, c in zip(BATCH_TRACKS, BATCH_CARS)) +
+                        f" cars ({total} in all), {BEAMS} beams, {BATCH_STEPS}-step rollouts from one CUDA graph",
+            "batched_env_steps_per_s": batched_rate, "batched_ms_per_env_step": batched_ms,
+            "separate_env_steps_per_s": separate_rate, "separate_ms_per_env_step": separate_ms,
+            "speedup": batched_rate / separate_rate,
+            "lidar_shape_default": {"cars_per_block": default_shape[0], "wide": default_shape[1],
+                                    "order": [BATCH_TRACKS[k] for k in default_shape[2]], "ms": default_ms},
+            "lidar_shape_autotuned": {"cars_per_block": cars_per_block, "wide": wide,
+                                      "order": [BATCH_TRACKS[k] for k in order], "ms": tuned_ms},
+            "batched_physics_ms": phys_ms, "batched_lidar_ms": lidar_ms,
+            "probes_per_beam": probes / (total * BEAMS), "kernels_per_rollout": launches,
+            "separate_lidar_ms": per_track_lidar}
+
+
 TRAIN_TRACK, TRAIN_CARS, TRAIN_ROLLOUT, TRAIN_BEAMS = "bank", 16384, 64, 108
 
 
@@ -266,6 +326,9 @@ def main():
     track = W.track(TRACK)
     stream = torch.cuda.Stream()
     flush = torch.empty(L2_FLUSH_BYTES, dtype=torch.uint8, device="cuda")
+    if args.batched_only:
+        print(json.dumps({"batched": batched_section(torch, W, stream, flush)}), flush=True)
+        return
     if args.surrogate_only:
         steps = args.surrogate_train_steps if args.surrogate_train_steps is not None else SURR_TRAIN_STEPS
         print(json.dumps({"surrogate": surrogate_section(torch, W, track, stream, flush, steps)}), flush=True)
@@ -356,6 +419,8 @@ def main():
         del runner
         steps = args.surrogate_train_steps if args.surrogate_train_steps is not None else SURR_TRAIN_STEPS
         line["surrogate"] = surrogate_section(torch, W, track, stream, flush, steps)
+    if not args.no_batched:
+        line["batched"] = batched_section(torch, W, stream, flush)
     if rank == 0 and not args.no_training:
         line["training"] = training_section(W, args.training_iterations)
     if rank == 0 and world == 1 and not args.no_cpu_baseline:

@@ -68,17 +68,20 @@ int racer_sim_create(const float* track, size_t len, int n, uint64_t seed, int b
  * uses seeds[0] over the whole batch. racer_sim_create is the one-segment case. */
 int racer_sim_create_segments(int count, const float* const* tracks, const size_t* lens, const int* cars,
                               const uint64_t* seeds, int beams, void* stream, racer_sim** out);
-/* Lidar launch shape: warps (cars) per block (2, 4 or 8) and the order in
- * which the segments' blocks are laid out (order[0..count)). Set replaces the
- * shape (and drops captured rollout graphs); get reads it. */
-int racer_sim_set_lidar_shape(racer_sim* sim, int cars_per_block, const int* order);
-int racer_sim_get_lidar_shape(racer_sim* sim, int* cars_per_block, int* order);
+/* Lidar launch shape: warps (cars) per block (2, 4 or 8); wide = 1 selects
+ * the variant compiled for 48 resident warps per SM (40 registers a thread)
+ * instead of 64 (32 registers); order[0..count) is the order in which the
+ * segments' blocks are laid out (NULL: index order). Set replaces the shape
+ * (and drops captured rollout graphs); get reads it. */
+int racer_sim_set_lidar_shape(racer_sim* sim, int cars_per_block, int wide, const int* order);
+int racer_sim_get_lidar_shape(racer_sim* sim, int* cars_per_block, int* wide, int* order);
 /* Autotuner: times `reps` lidar launches on the sim's current lidar frames for
- * every cars-per-block in {2, 4, 8} with the segments in index order and
- * heaviest-first (by probe count measured in one counted pass), keeps the
- * fastest shape, and returns it and its mean launch time in ms. The lidar
- * only rewrites obs rows from the frames, so the sim's state is unchanged. */
-int racer_sim_autotune(racer_sim* sim, int reps, int* cars_per_block, int* order, float* best_ms);
+ * every cars-per-block in {2, 4, 8} and both register budgets, with the
+ * segments in index order and heaviest-first (by probe count measured in one
+ * counted pass), keeps the fastest shape, and returns it and its mean launch
+ * time in ms. The lidar only rewrites obs rows from the frames, so the sim's
+ * state is unchanged. */
+int racer_sim_autotune(racer_sim* sim, int reps, int* cars_per_block, int* wide, int* order, float* best_ms);
 int racer_sim_destroy(racer_sim* sim);
 int racer_sim_get_buffers(racer_sim* sim, racer_sim_buffers* out);
 /* Sim.reset (racer/sim.mojo:291-305): spawn every car, then a step at rest. */

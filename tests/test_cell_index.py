@@ -4,7 +4,7 @@
    + 0.5) with a binary32 division and tests 0 <= ix < nx. The CUDA probe
    (sim.cu, cell_of) multiplies by r = RN(1 / cell) instead; when the
    fractional parts of both u' = (x - x0) * r + 0.5 lie inside
-   0.5 +- band with band = 0.5 - (max(nx, ny) + 3) * 2^-20 it uses floor(u')
+   0.5 +- band with band = 0.5 - (max(nx, ny) + 3) * 6 * 2^-24 it uses floor(u')
    with an integer bounds test, otherwise the division. The claim: on-map
    status and cell are always the reference's.
 2. Division skip. The march (sim.cu, trace) evaluates fl / descent only when
@@ -19,7 +19,7 @@ import numpy as np
 import pytest
 
 f32 = np.float32
-TWO_M20 = f32(2.0 ** -20)
+BAND_UNIT = f32(6 * 2.0 ** -24)
 
 
 def exact_cell(v, v0, cell, n):
@@ -30,7 +30,7 @@ def exact_cell(v, v0, cell, n):
 
 def fast_cell(v, v0, cell, n, nmax):
     r = f32(1) / cell
-    band = f32(0.5) - f32(nmax + 3) * TWO_M20
+    band = f32(0.5) - f32(nmax + 3) * BAND_UNIT
     u = (v - v0) * r + f32(0.5)
     fl = np.floor(u)
     ok = np.abs((u - fl) - f32(0.5)) < band
@@ -53,10 +53,15 @@ def test_fast_cell_index_is_exact(cell, n, nmax):
         base = (v0 + (ks.astype(f32) + f32(0.5)) * cell).astype(f32)
         adv = [base]
         up, down = base.copy(), base.copy()
-        for _ in range(12):
+        for _ in range(40):
             up = np.nextafter(up, f32(np.inf))
             down = np.nextafter(down, f32(-np.inf))
             adv += [up, down]
+        # points whose u' lands just inside and outside the band edge
+        edge = f32(nmax + 3) * BAND_UNIT
+        for frac in (edge, -edge):
+            target = (ks.astype(np.float64) + frac.astype(np.float64) * np.array([[0.5], [1.0], [1.5], [2.0]]))
+            adv += list((v0 + (target - 0.5) * np.float64(cell)).astype(f32))
         span = float(n) * float(cell)
         uniform = rng.uniform(float(v0) - 0.3 * span, float(v0) + 1.3 * span, 400000).astype(f32)
         far = np.array([1e9, -1e9, 3e38, -3e38, np.inf, -np.inf, np.nan], f32)
@@ -67,7 +72,7 @@ def test_fast_cell_index_is_exact(cell, n, nmax):
         assert np.array_equal(on, on_ex)
         assert np.array_equal(idx[on], idx_ex[on])
         # the band is narrow: almost every uniformly placed lookup skips the division
-        assert ok[len(vs) - len(far) - len(uniform):len(vs) - len(far)].mean() > 0.97
+        assert ok[len(vs) - len(far) - len(uniform):len(vs) - len(far)].mean() > 0.99
 
 
 def test_division_skip_is_exact():

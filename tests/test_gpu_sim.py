@@ -269,11 +269,11 @@ def test_lidar_shapes_and_autotune_keep_results():
     a.reset()
     b.reset()
     rng = np.random.default_rng(5)
-    for shape in ((2, [3, 1, 0, 2]), (8, None), (4, [2, 3, 1, 0]), "auto"):
+    for shape in ((2, 0, [3, 1, 0, 2]), (8, 1, None), (4, 1, [2, 3, 1, 0]), (2, 1, None), "auto"):
         if shape == "auto":
-            cars_per_block, order, ms = b.autotune(3)
-            assert cars_per_block in (2, 4, 8) and sorted(order) == [0, 1, 2, 3] and ms > 0
-            assert b.lidar_shape() == (cars_per_block, order)
+            cars_per_block, wide, order, ms = b.autotune(3)
+            assert cars_per_block in (2, 4, 8) and wide in (0, 1) and sorted(order) == [0, 1, 2, 3] and ms > 0
+            assert b.lidar_shape() == (cars_per_block, wide, order)
         else:
             b.set_lidar_shape(*shape)
         for _ in range(4):
@@ -286,7 +286,23 @@ def test_lidar_shapes_and_autotune_keep_results():
     with pytest.raises(W.RacerError):
         b.set_lidar_shape(3)
     with pytest.raises(W.RacerError):
-        b.set_lidar_shape(4, [0, 0, 1, 2])
+        b.set_lidar_shape(4, 0, [0, 0, 1, 2])
+    with pytest.raises(W.RacerError):
+        b.set_lidar_shape(4, 2)
+
+
+def test_one_track_lidar_shapes_bit_exact():
+    """Every launch shape of the one-track lidar kernel gives the oracle's ranges."""
+    track = W.track("bridge")
+    n = 50
+    cpu = O.Sim(track, n, 9, beams=1081)
+    cpu.reset()
+    for cars_per_block in (2, 4, 8):
+        for wide in (0, 1):
+            gpu = W.Sim(track, n, 9, beams=1081)
+            gpu.set_lidar_shape(cars_per_block, wide)
+            gpu.reset()
+            check_sim(gpu, cpu, f"shape {cars_per_block}/{wide} ")
 
 
 def test_synthetic_occupancy_map_bit_exact():

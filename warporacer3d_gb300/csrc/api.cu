@@ -179,7 +179,7 @@ static int upload_track(const float* track, size_t len, float** d_track, float2*
   t->y0 = track[3];
   t->cell = track[4];
   t->inv_cell = 1.0f / track[4];
-  t->band = 0.5f - (float)((nx > ny ? nx : ny) + 3) * 9.5367431640625e-07f;
+  t->band = 0.5f - (float)((nx > ny ? nx : ny) + 3) * 3.5762786865234375e-07f;  // 3 * 2^-23
   t->spacing = track[6];
   t->slope = track[8];
   t->nxf = (float)nx;
@@ -875,17 +875,18 @@ static void drop_graphs(racer_sim* s) {
   s->surrogate_graphs.clear();
 }
 
-static LidarShape make_shape(int cars, const int* order, int count) {
+static LidarShape make_shape(int cars, int wide, const int* order, int count) {
   LidarShape shape;
   shape.cars = cars;
+  shape.wide = wide;
   for (int j = 0; j < MAX_SEGMENTS; ++j) shape.order[j] = order && j < count ? order[j] : j;
   return shape;
 }
 
-int racer_sim_set_lidar_shape(racer_sim* s, int cars, const int* order) {
+int racer_sim_set_lidar_shape(racer_sim* s, int cars, int wide, const int* order) {
   RACER_ARG(s, "racer_sim_set_lidar_shape: null sim");
-  LidarShape shape = make_shape(cars, order, s->seg.count);
-  RACER_ARG(lidar_shape_ok(shape), "racer_sim_set_lidar_shape: cars per block must be 2, 4 or 8");
+  LidarShape shape = make_shape(cars, wide, order, s->seg.count);
+  RACER_ARG(lidar_shape_ok(shape), "racer_sim_set_lidar_shape: cars per block must be 2, 4 or 8 and wide 0 or 1");
   if (order) {
     bool seen[MAX_SEGMENTS] = {};
     for (int j = 0; j < s->seg.count; ++j) {
@@ -900,15 +901,16 @@ int racer_sim_set_lidar_shape(racer_sim* s, int cars, const int* order) {
   return 0;
 }
 
-int racer_sim_get_lidar_shape(racer_sim* s, int* cars, int* order) {
+int racer_sim_get_lidar_shape(racer_sim* s, int* cars, int* wide, int* order) {
   RACER_ARG(s, "racer_sim_get_lidar_shape: null sim");
   if (cars) *cars = s->shape.cars;
+  if (wide) *wide = s->shape.wide;
   if (order)
     for (int j = 0; j < s->seg.count; ++j) order[j] = s->shape.order[j];
   return 0;
 }
 
-int racer_sim_autotune(racer_sim* s, int reps, int* cars_out, int* order_out, float* best_ms) {
+int racer_sim_autotune(racer_sim* s, int reps, int* cars_out, int* wide_out, int* order_out, float* best_ms) {
   RACER_ARG(s && reps >= 1, "racer_sim_autotune: bad argument");
   cudaStream_t st = s->st;
   const int count = s->seg.count;
@@ -931,10 +933,12 @@ int racer_sim_autotune(racer_sim* s, int reps, int* cars_out, int* order_out, fl
   for (int j = 0; j < MAX_SEGMENTS; ++j) natural[j] = heavy[j] = j;
   std::stable_sort(heavy, heavy + count, [&](int a, int b) { return host[a] > host[b]; });
   std::vector<LidarShape> candidates;
-  for (int cars : {2, 4, 8}) {
-    candidates.push_back(make_shape(cars, natural, count));
-    if (count > 1 && !std::equal(natural, natural + count, heavy)) candidates.push_back(make_shape(cars, heavy, count));
-  }
+  for (int cars : {2, 4, 8})
+    for (int wide : {0, 1}) {
+      candidates.push_back(make_shape(cars, wide, natural, count));
+      if (count > 1 && !std::equal(natural, natural + count, heavy))
+        candidates.push_back(make_shape(cars, wide, heavy, count));
+    }
   cudaEvent_t a, b;
   RACER_TRY(cudaEventCreate(&a));
   RACER_TRY(cudaEventCreate(&b));
@@ -954,11 +958,13 @@ int racer_sim_autotune(racer_sim* s, int reps, int* cars_out, int* order_out, fl
   }
   cudaEventDestroy(a);
   cudaEventDestroy(b);
-  if (chosen.cars != s->shape.cars || !std::equal(chosen.order, chosen.order + count, s->shape.order)) {
+  if (chosen.cars != s->shape.cars || chosen.wide != s->shape.wide ||
+      !std::equal(chosen.order, chosen.order + count, s->shape.order)) {
     drop_graphs(s);
     s->shape = chosen;
   }
   if (cars_out) *cars_out = s->shape.cars;
+  if (wide_out) *wide_out = s->shape.wide;
   if (order_out)
     for (int j = 0; j < count; ++j) order_out[j] = s->shape.order[j];
   if (best_ms) *best_ms = best;

@@ -14,11 +14,10 @@ void launch_spawn(const Segments& g, float* state, float* actions, int n, cudaSt
 // ray [2, n] float4: the per-car lidar frame the physics kernel leaves for the lidar.
 void launch_advance(const Segments& g, float* state, const float* actions, float* reward, float* done, float* obs,
                     int n, int beams, float4* ray, cudaStream_t st);
-// With `list` set, only the cars list[0 .. *list_count) (list_max at most) are traced.
 void launch_lidar(const Segments& g, const LidarShape& shape, const float4* ray, float* obs, int n, int beams,
-                  const float2* beam_dir, int* iters, cudaStream_t st, const int* list = nullptr,
-                  const int* list_count = nullptr, int list_max = 0);
-// One track, default shape (surrogate labels and fallback).
+                  const float2* beam_dir, int* iters, cudaStream_t st);
+// One track, default shape (surrogate labels and fallback). With `list` set,
+// only the cars list[0 .. *list_count) (list_max at most) are traced.
 void launch_lidar(const TrackDev& t, const float4* ray, float* obs, int n, int beams, const float2* beam_dir,
                   int* iters, cudaStream_t st, const int* list = nullptr, const int* list_count = nullptr,
                   int list_max = 0);

@@ -61,11 +61,17 @@ __device__ __forceinline__ float cell_coord(float v, float v0, float cell, float
 }
 
 // Nearest-cell index (racer/sim.mojo:108-114); false off the map or for
-// non-finite coordinates. One guard band serves the whole grid: where
-// |u| <= max(nx, ny) + 2 the bound of cell_coord is below
-// band_delta = (max(nx, ny) + 3) * 2^-20; farther out both floors are off the
-// map. So when both fractional parts clear the band, the fast floors give the
-// reference's answer (NaN and infinities fail the test and take the exact path).
+// non-finite coordinates. One guard band serves the whole grid. With
+// d = RN(v - v0), the reference's u = RN(RN(d / cell) + 0.5) and
+// u' = RN(RN(d * RN(1/cell)) + 0.5): the two quotients differ by at most
+// (3 * 2^-24 + 2^-48) |d / cell| and each + 0.5 rounds by at most
+// 2^-24 |u|, so |u' - u| <= 2^-24 (5 U + 2) where |u'| <= U. Where
+// U <= M + 2 (M = max(nx, ny)) that is below delta = (M + 3) * 6 * 2^-24,
+// even after the fractional part's own rounding (at most 2^-26); farther out
+// both floors are off the map. So when both fractional parts lie more than
+// delta from an integer (|frac - 0.5| < band = 0.5 - delta), the fast floors
+// give the reference's answer (NaN and infinities fail the test and take the
+// exact path).
 __device__ __forceinline__ bool cell_of(const TrackDev& t, float x, float y, long* idx) {
   const float ux = (x - t.x0) * t.inv_cell + 0.5f, uy = (y - t.y0) * t.inv_cell + 0.5f;
   const float flx = floorf(ux), fly = floorf(uy);
@@ -437,27 +443,43 @@ __device__ __forceinline__ void trace_any(const TrackDev& t, const float4* __res
     trace<0>(t, ray, obs, n, beam_dir, max_iters, iters, car, beam);
 }
 
-// CARS warps per block (one car each): small blocks release their slot as soon
-// as their few cars finish. A block's segment depends on blockIdx only, so the
-// track's fields stay block-uniform.
-template <int CARS, bool LIST>
-__global__ void __launch_bounds__(CARS * 32, (64 / CARS < 32 ? 64 / CARS : 32))
-    k_lidar(const __grid_constant__ Segments g, const __grid_constant__ LidarGrid lg, const float4* __restrict__ ray,
-            float* obs, int n, int beams, const float2* __restrict__ beam_dir, int* iters,
-            const int* __restrict__ list, const int* list_count) {
+// Resident blocks per SM a lidar kernel is compiled for: all 64 warp slots
+// (32 registers a thread) or, for the wide variant, 48 of them (40 registers).
+constexpr int lidar_min_blocks(int cars, bool wide) {
+  return (wide ? 48 : 64) / cars < 32 ? (wide ? 48 : 64) / cars : 32;
+}
+
+// One track: its fields are kernel parameters, read as constant operands.
+// CARS warps per block (one car each): small blocks release their slot as
+// soon as their few cars finish.
+template <int LAYERS, int CARS, bool WIDE, bool LIST>
+__global__ void __launch_bounds__(CARS * 32, lidar_min_blocks(CARS, WIDE))
+    k_lidar_track(TrackDev t, int max_iters, const float4* __restrict__ ray, float* obs, int n, int beams,
+                  const float2* __restrict__ beam_dir, int* iters, const int* __restrict__ list,
+                  const int* list_count) {
   const int beam = blockIdx.y * 32 + (threadIdx.x & 31);
   if (beam >= beams) return;
   if (LIST) {  // only the listed cars (surrogate fallback), grid-stride over the list
     const int count = *list_count;
     for (int q = blockIdx.x * CARS + (threadIdx.x >> 5); q < count; q += gridDim.x * CARS) {
       const int car = list[q];
-      if (car < n) {
-        const int k = segment_of(g, car);
-        trace_any(g.t[k], ray, obs, n, beam_dir, g.max_iters[k], iters, car, beam);
-      }
+      if (car < n) trace<LAYERS>(t, ray, obs, n, beam_dir, max_iters, iters, car, beam);
     }
     return;
   }
+  const int car = blockIdx.x * CARS + (threadIdx.x >> 5);
+  if (car < n) trace<LAYERS>(t, ray, obs, n, beam_dir, max_iters, iters, car, beam);
+}
+
+// Several tracks: a block's segment depends on blockIdx only, so the track's
+// fields are block-uniform.
+template <int CARS, bool WIDE>
+__global__ void __launch_bounds__(CARS * 32, lidar_min_blocks(CARS, WIDE))
+    k_lidar_segments(const __grid_constant__ Segments g, const __grid_constant__ LidarGrid lg,
+                     const float4* __restrict__ ray, float* obs, int n, int beams,
+                     const float2* __restrict__ beam_dir, int* iters) {
+  const int beam = blockIdx.y * 32 + (threadIdx.x & 31);
+  if (beam >= beams) return;
   int j = 0;
   while (j + 1 < g.count && (int)blockIdx.x >= lg.block0[j + 1]) ++j;
   const int k = lg.order[j];
@@ -572,38 +594,71 @@ static LidarGrid lidar_grid(const Segments& g, const LidarShape& shape) {
   return lg;
 }
 
-template <int CARS>
-static void lidar_cars(const Segments& g, const LidarShape& shape, const float4* ray, float* obs, int n, int beams,
-                       const float2* beam_dir, int* iters, cudaStream_t st, const int* list, const int* list_count,
-                       int list_max) {
-  const LidarGrid lg = lidar_grid(g, shape);
-  // a listed subset: a grid of about eight blocks per SM strides over the list
-  dim3 grid(list ? std::min((list_max + CARS - 1) / CARS, 16 * 152 / ((beams + 31) / 32) + 1) : lg.block0[g.count],
-            (beams + 31) / 32);
-  if (grid.x == 0) return;
-  if (list)
-    k_lidar<CARS, true><<<grid, CARS * 32, 0, st>>>(g, lg, ray, obs, n, beams, beam_dir, iters, list, list_count);
-  else
-    k_lidar<CARS, false><<<grid, CARS * 32, 0, st>>>(g, lg, ray, obs, n, beams, beam_dir, iters, nullptr, nullptr);
+template <int LAYERS, int CARS, bool WIDE>
+static void lidar_track(const TrackDev& t, int max_iters, const float4* ray, float* obs, int n, int beams,
+                        const float2* beam_dir, int* iters, cudaStream_t st) {
+  dim3 grid((n + CARS - 1) / CARS, (beams + 31) / 32);
+  k_lidar_track<LAYERS, CARS, WIDE, false>
+      <<<grid, CARS * 32, 0, st>>>(t, max_iters, ray, obs, n, beams, beam_dir, iters, nullptr, nullptr);
 }
 
-bool lidar_shape_ok(const LidarShape& shape) { return shape.cars == 2 || shape.cars == 4 || shape.cars == 8; }
+template <int CARS, bool WIDE>
+static void lidar_shape(const Segments& g, const LidarShape& shape, const float4* ray, float* obs, int n, int beams,
+                        const float2* beam_dir, int* iters, cudaStream_t st) {
+  if (g.count == 1) {
+    const TrackDev& t = g.t[0];
+    if (t.layers == 1)
+      lidar_track<1, CARS, WIDE>(t, g.max_iters[0], ray, obs, n, beams, beam_dir, iters, st);
+    else if (t.layers == 2)
+      lidar_track<2, CARS, WIDE>(t, g.max_iters[0], ray, obs, n, beams, beam_dir, iters, st);
+    else
+      lidar_track<0, CARS, WIDE>(t, g.max_iters[0], ray, obs, n, beams, beam_dir, iters, st);
+    return;
+  }
+  const LidarGrid lg = lidar_grid(g, shape);
+  dim3 grid(lg.block0[g.count], (beams + 31) / 32);
+  k_lidar_segments<CARS, WIDE><<<grid, CARS * 32, 0, st>>>(g, lg, ray, obs, n, beams, beam_dir, iters);
+}
+
+bool lidar_shape_ok(const LidarShape& shape) {
+  return (shape.cars == 2 || shape.cars == 4 || shape.cars == 8) && (shape.wide == 0 || shape.wide == 1);
+}
 
 void launch_lidar(const Segments& g, const LidarShape& shape, const float4* ray, float* obs, int n, int beams,
-                  const float2* beam_dir, int* iters, cudaStream_t st, const int* list, const int* list_count,
-                  int list_max) {
+                  const float2* beam_dir, int* iters, cudaStream_t st) {
+  if (g.count < 1 || g.car0[g.count] == 0) return;
+  const bool wide = shape.wide == 1;
   if (shape.cars == 2)
-    lidar_cars<2>(g, shape, ray, obs, n, beams, beam_dir, iters, st, list, list_count, list_max);
+    wide ? lidar_shape<2, true>(g, shape, ray, obs, n, beams, beam_dir, iters, st)
+         : lidar_shape<2, false>(g, shape, ray, obs, n, beams, beam_dir, iters, st);
   else if (shape.cars == 8)
-    lidar_cars<8>(g, shape, ray, obs, n, beams, beam_dir, iters, st, list, list_count, list_max);
+    wide ? lidar_shape<8, true>(g, shape, ray, obs, n, beams, beam_dir, iters, st)
+         : lidar_shape<8, false>(g, shape, ray, obs, n, beams, beam_dir, iters, st);
   else
-    lidar_cars<4>(g, shape, ray, obs, n, beams, beam_dir, iters, st, list, list_count, list_max);
+    wide ? lidar_shape<4, true>(g, shape, ray, obs, n, beams, beam_dir, iters, st)
+         : lidar_shape<4, false>(g, shape, ray, obs, n, beams, beam_dir, iters, st);
 }
 
 void launch_lidar(const TrackDev& t, const float4* ray, float* obs, int n, int beams, const float2* beam_dir,
                   int* iters, cudaStream_t st, const int* list, const int* list_count, int list_max) {
-  launch_lidar(single_segment(t, n, 0), LidarShape{}, ray, obs, n, beams, beam_dir, iters, st, list, list_count,
-               list_max);
+  const int max_iters = lidar_max_iters(t);
+  if (!list) {
+    launch_lidar(single_segment(t, n, 0), LidarShape{}, ray, obs, n, beams, beam_dir, iters, st);
+    return;
+  }
+  // a listed subset: a grid of about eight blocks per SM strides over the list
+  constexpr int CARS = 4;
+  dim3 grid(std::min((list_max + CARS - 1) / CARS, 16 * 152 / ((beams + 31) / 32) + 1), (beams + 31) / 32);
+  if (grid.x == 0) return;
+  if (t.layers == 1)
+    k_lidar_track<1, CARS, false, true>
+        <<<grid, CARS * 32, 0, st>>>(t, max_iters, ray, obs, n, beams, beam_dir, iters, list, list_count);
+  else if (t.layers == 2)
+    k_lidar_track<2, CARS, false, true>
+        <<<grid, CARS * 32, 0, st>>>(t, max_iters, ray, obs, n, beams, beam_dir, iters, list, list_count);
+  else
+    k_lidar_track<0, CARS, false, true>
+        <<<grid, CARS * 32, 0, st>>>(t, max_iters, ray, obs, n, beams, beam_dir, iters, list, list_count);
 }
 
 __global__ void k_select_cars(const unsigned* minr, int n, unsigned threshold_bits, int* list, int* count) {

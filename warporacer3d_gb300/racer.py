@@ -153,22 +153,23 @@ class Sim:
         call("racer_sim_sample", self.handle, output.c, log_std.c, actions.c, logp.c, value.c, int(deterministic),
              step)
 
-    def set_lidar_shape(self, cars_per_block, order=None):
+    def set_lidar_shape(self, cars_per_block, wide=0, order=None):
         k = len(self.cars)
         arr = None if order is None else (ctypes.c_int * k)(*order)
-        call("racer_sim_set_lidar_shape", self.handle, cars_per_block, arr)
+        call("racer_sim_set_lidar_shape", self.handle, cars_per_block, wide, arr)
 
     def lidar_shape(self):
-        cars, order = ctypes.c_int(), (ctypes.c_int * len(self.cars))()
-        call("racer_sim_get_lidar_shape", self.handle, ctypes.byref(cars), order)
-        return cars.value, list(order)
+        """(cars per block, wide register budget 0/1, segment order)."""
+        cars, wide, order = ctypes.c_int(), ctypes.c_int(), (ctypes.c_int * len(self.cars))()
+        call("racer_sim_get_lidar_shape", self.handle, ctypes.byref(cars), ctypes.byref(wide), order)
+        return cars.value, wide.value, list(order)
 
     def autotune(self, reps=5):
         """Times the lidar launch shapes on the current frames; keeps and returns the fastest
-        (cars per block, segment order, mean ms)."""
-        cars, order, ms = ctypes.c_int(), (ctypes.c_int * len(self.cars))(), ctypes.c_float()
-        call("racer_sim_autotune", self.handle, reps, ctypes.byref(cars), order, ctypes.byref(ms))
-        return cars.value, list(order), ms.value
+        (cars per block, wide, segment order, mean ms)."""
+        cars, wide, order, ms = ctypes.c_int(), ctypes.c_int(), (ctypes.c_int * len(self.cars))(), ctypes.c_float()
+        call("racer_sim_autotune", self.handle, reps, ctypes.byref(cars), ctypes.byref(wide), order, ctypes.byref(ms))
+        return cars.value, wide.value, list(order), ms.value
 
 
 class Policy:

@@ -206,7 +206,7 @@ def batched_section(torch, W, stream, flush):
     torch.cuda.synchronize()
     default_shape = batch.sim.lidar_shape()
     default_ms = batch.profile_sim(5)[1]
-    cars_per_block, wide, order, tuned_ms = batch.sim.autotune(5)
+    tuned, tuned_ms = batch.sim.autotune(5)
 
     def timed(run):
         run(0)
@@ -238,10 +238,9 @@ def batched_section(torch, W, stream, flush):
             "batched_env_steps_per_s": batched_rate, "batched_ms_per_env_step": batched_ms,
             "separate_env_steps_per_s": separate_rate, "separate_ms_per_env_step": separate_ms,
             "speedup": batched_rate / separate_rate,
-            "lidar_shape_default": {"cars_per_block": default_shape[0], "wide": default_shape[1],
-                                    "order": [BATCH_TRACKS[k] for k in default_shape[2]], "ms": default_ms},
-            "lidar_shape_autotuned": {"cars_per_block": cars_per_block, "wide": wide,
-                                      "order": [BATCH_TRACKS[k] for k in order], "ms": tuned_ms},
+            "lidar_shape_default": dict(default_shape, order=[BATCH_TRACKS[k] for k in default_shape["order"]],
+                                        ms=default_ms),
+            "lidar_shape_autotuned": dict(tuned, order=[BATCH_TRACKS[k] for k in tuned["order"]], ms=tuned_ms),
             "batched_physics_ms": phys_ms, "batched_lidar_ms": lidar_ms,
             "probes_per_beam": probes / (total * BEAMS), "kernels_per_rollout": launches,
             "separate_lidar_ms": per_track_lidar}

@@ -68,20 +68,30 @@ int racer_sim_create(const float* track, size_t len, int n, uint64_t seed, int b
  * uses seeds[0] over the whole batch. racer_sim_create is the one-segment case. */
 int racer_sim_create_segments(int count, const float* const* tracks, const size_t* lens, const int* cars,
                               const uint64_t* seeds, int beams, void* stream, racer_sim** out);
-/* Lidar launch shape: warps (cars) per block (2, 4 or 8); wide = 1 selects
- * the variant compiled for 48 resident warps per SM (40 registers a thread)
- * instead of 64 (32 registers); order[0..count) is the order in which the
- * segments' blocks are laid out (NULL: index order). Set replaces the shape
- * (and drops captured rollout graphs); get reads it. */
-int racer_sim_set_lidar_shape(racer_sim* sim, int cars_per_block, int wide, const int* order);
-int racer_sim_get_lidar_shape(racer_sim* sim, int* cars_per_block, int* wide, int* order);
-/* Autotuner: times `reps` lidar launches on the sim's current lidar frames for
- * every cars-per-block in {2, 4, 8} and both register budgets, with the
- * segments in index order and heaviest-first (by probe count measured in one
- * counted pass), keeps the fastest shape, and returns it and its mean launch
- * time in ms. The lidar only rewrites obs rows from the frames, so the sim's
- * state is unchanged. */
-int racer_sim_autotune(racer_sim* sim, int reps, int* cars_per_block, int* wide, int* order, float* best_ms);
+/* Lidar launch shape (no counterpart in the reference). cars_per_block: cars
+ * (warps) per block, 2, 4 or 8. wide: 1 selects the kernel compiled for 48
+ * resident warps per SM (40 registers a thread) instead of 64 (32 registers).
+ * split (several segments only): 0 = one launch covering every segment
+ * through the segment table; 1 = each segment's one-track kernel on its own
+ * stream, forked from and joined into the sim's stream (parallel branches of
+ * a captured rollout graph). order[0..count): the segments' order in the grid
+ * (split = 0) or their launch order (split = 1). Setting a different shape
+ * drops the sim's captured rollout graphs. */
+typedef struct {
+  int cars_per_block;
+  int wide;
+  int split;
+  int order[8];
+} racer_lidar_shape;
+int racer_sim_set_lidar_shape(racer_sim* sim, const racer_lidar_shape* shape);
+int racer_sim_get_lidar_shape(racer_sim* sim, racer_lidar_shape* shape);
+/* Autotuner: times `reps` lidar passes on the sim's current lidar frames for
+ * every cars_per_block, wide and (with several segments) split, with the
+ * segments in index order and heaviest-first (by probe iterations counted in
+ * one pass), keeps the fastest shape and returns it with its mean time in
+ * ms. The lidar only rewrites obs rows from the frames: the sim's state is
+ * unchanged. */
+int racer_sim_autotune(racer_sim* sim, int reps, racer_lidar_shape* best, float* best_ms);
 int racer_sim_destroy(racer_sim* sim);
 int racer_sim_get_buffers(racer_sim* sim, racer_sim_buffers* out);
 /* Sim.reset (racer/sim.mojo:291-305): spawn every car, then a step at rest. */

@@ -269,13 +269,15 @@ def test_lidar_shapes_and_autotune_keep_results():
     a.reset()
     b.reset()
     rng = np.random.default_rng(5)
-    for shape in ((2, 0, [3, 1, 0, 2]), (8, 1, None), (4, 1, [2, 3, 1, 0]), (2, 1, None), "auto"):
+    shapes = [(2, 0, 0, [3, 1, 0, 2]), (8, 1, 0, None), (4, 1, 1, [2, 3, 1, 0]), (2, 0, 1, None), "auto"]
+    for shape in shapes:
         if shape == "auto":
-            cars_per_block, wide, order, ms = b.autotune(3)
-            assert cars_per_block in (2, 4, 8) and wide in (0, 1) and sorted(order) == [0, 1, 2, 3] and ms > 0
-            assert b.lidar_shape() == (cars_per_block, wide, order)
+            best, ms = b.autotune(3)
+            assert best["cars_per_block"] in (2, 4, 8) and best["wide"] in (0, 1) and best["split"] in (0, 1)
+            assert sorted(best["order"]) == [0, 1, 2, 3] and ms > 0 and b.lidar_shape() == best
         else:
             b.set_lidar_shape(*shape)
+            assert b.lidar_shape()["order"] == (shape[3] or [0, 1, 2, 3])
         for _ in range(4):
             act = rng.uniform(-1, 1, (2, a.n)).astype(np.float32)
             a.actions.write(act)
@@ -286,9 +288,21 @@ def test_lidar_shapes_and_autotune_keep_results():
     with pytest.raises(W.RacerError):
         b.set_lidar_shape(3)
     with pytest.raises(W.RacerError):
-        b.set_lidar_shape(4, 0, [0, 0, 1, 2])
+        b.set_lidar_shape(4, 0, 0, [0, 0, 1, 2])
     with pytest.raises(W.RacerError):
         b.set_lidar_shape(4, 2)
+
+
+def test_split_lidar_in_captured_rollouts():
+    """Rollout graphs captured with per-segment lidar branches give the segment-table launch's results."""
+    tracks, cars, seeds = segment_tracks(), [64, 40, 72, 20], [1, 2, 3, 4]
+    runs = [W.Runner.segments(tracks, cars, seeds, beams=108) for _ in range(2)]
+    runs[1].sim.set_lidar_shape(2, 0, 1, [2, 0, 3, 1])
+    for r in runs:
+        r.rollout(12, False, 0)
+        r.rollout(12, False, 12)
+    assert same(runs[0].sim.obs.numpy(), runs[1].sim.obs.numpy())
+    assert same(runs[0].sim.state.numpy(), runs[1].sim.state.numpy())
 
 
 def test_one_track_lidar_shapes_bit_exact():
@@ -300,7 +314,7 @@ def test_one_track_lidar_shapes_bit_exact():
     for cars_per_block in (2, 4, 8):
         for wide in (0, 1):
             gpu = W.Sim(track, n, 9, beams=1081)
-            gpu.set_lidar_shape(cars_per_block, wide)
+            gpu.set_lidar_shape(cars_per_block, wide, 0)
             gpu.reset()
             check_sim(gpu, cpu, f"shape {cars_per_block}/{wide} ")
 

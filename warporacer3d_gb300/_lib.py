@@ -24,6 +24,10 @@ class SimBuffers(ctypes.Structure):
                 ("done", c_void_p), ("track", c_void_p)]
 
 
+class LidarShape(ctypes.Structure):
+    _fields_ = [("cars_per_block", c_int), ("wide", c_int), ("split", c_int), ("order", c_int * 8)]
+
+
 class TrainerBuffers(ctypes.Structure):
     _fields_ = [(name, c_void_p) for name in ("obs", "actions", "logp", "value", "reward", "done", "advantage", "x",
                                               "d3", "d2", "d1", "grad", "first", "second", "stats", "acts")] + \
@@ -40,9 +44,9 @@ SIGNATURES = {
     "racer_sim_create": [P(c_float), c_size_t, c_int, c_uint64, c_int, c_void_p, P(c_void_p)],
     "racer_sim_create_segments": [c_int, P(P(c_float)), P(c_size_t), P(c_int), P(c_uint64), c_int, c_void_p,
                                   P(c_void_p)],
-    "racer_sim_set_lidar_shape": [c_void_p, c_int, c_int, P(c_int)],
-    "racer_sim_get_lidar_shape": [c_void_p, P(c_int), P(c_int), P(c_int)],
-    "racer_sim_autotune": [c_void_p, c_int, P(c_int), P(c_int), P(c_int), P(c_float)],
+    "racer_sim_set_lidar_shape": [c_void_p, P(LidarShape)],
+    "racer_sim_get_lidar_shape": [c_void_p, P(LidarShape)],
+    "racer_sim_autotune": [c_void_p, c_int, P(LidarShape), P(c_float)],
     "racer_sim_destroy": [c_void_p],
     "racer_sim_get_buffers": [c_void_p, P(SimBuffers)],
     "racer_sim_reset": [c_void_p],

@@ -257,6 +257,9 @@ int racer_sim_destroy(racer_sim* s) {
   if (!s) return 0;
   for (auto& kv : s->graphs) cudaGraphExecDestroy(kv.second);
   for (auto& kv : s->surrogate_graphs) cudaGraphExecDestroy(kv.second);
+  for (cudaStream_t a : s->aux) cudaStreamDestroy(a);
+  for (cudaEvent_t e : s->join) cudaEventDestroy(e);
+  if (s->fork) cudaEventDestroy(s->fork);
   for (float* p : s->seg_track) cudaFree(p);
   for (float2* p : s->seg_cl) cudaFree(p);
   cudaFree(s->beam_dir);
@@ -283,12 +286,59 @@ int racer_sim_get_buffers(racer_sim* s, racer_sim_buffers* out) {
   return 0;
 }
 
+// Launch order of the segments under `shape` (a permutation; entries out of
+// range or repeated are skipped and missing segments appended).
+static void segment_order(const racer_sim* s, const LidarShape& shape, int* order) {
+  bool used[MAX_SEGMENTS] = {};
+  int slots = 0;
+  for (int j = 0; j < MAX_SEGMENTS; ++j) {
+    const int k = shape.order[j];
+    if (k >= 0 && k < s->seg.count && !used[k]) used[k] = true, order[slots++] = k;
+  }
+  for (int k = 0; k < s->seg.count; ++k)
+    if (!used[k]) order[slots++] = k;
+}
+
+// The lidar over every segment: one segment-table launch, or (split) each
+// segment's one-track kernel on its own stream, forked from and joined back
+// into `st` (parallel branches when captured into a graph).
+static int lidar_on(racer_sim* s, const LidarShape& shape, float* obs, int32_t* iters, cudaStream_t st) {
+  if (s->seg.count == 1 || !shape.split) {
+    launch_lidar(s->seg, shape, s->ray, obs, s->n, s->beams, s->beam_dir, iters, st);
+    RACER_LAUNCHED();
+    return 0;
+  }
+  const int extra = s->seg.count - 1;
+  if ((int)s->aux.size() < extra) {
+    if (!s->fork) RACER_TRY(cudaEventCreateWithFlags(&s->fork, cudaEventDisableTiming));
+    while ((int)s->aux.size() < extra) {
+      cudaStream_t a;
+      cudaEvent_t e;
+      RACER_TRY(cudaStreamCreateWithFlags(&a, cudaStreamNonBlocking));
+      s->aux.push_back(a);
+      RACER_TRY(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+      s->join.push_back(e);
+    }
+  }
+  int order[MAX_SEGMENTS];
+  segment_order(s, shape, order);
+  RACER_TRY(cudaEventRecord(s->fork, st));
+  launch_lidar_segment(s->seg, order[0], shape, s->ray, obs, s->n, s->beams, s->beam_dir, iters, st);
+  for (int j = 1; j <= extra; ++j) {
+    RACER_TRY(cudaStreamWaitEvent(s->aux[j - 1], s->fork, 0));
+    launch_lidar_segment(s->seg, order[j], shape, s->ray, obs, s->n, s->beams, s->beam_dir, iters, s->aux[j - 1]);
+    RACER_TRY(cudaEventRecord(s->join[j - 1], s->aux[j - 1]));
+  }
+  for (int j = 1; j <= extra; ++j) RACER_TRY(cudaStreamWaitEvent(st, s->join[j - 1], 0));
+  RACER_LAUNCHED();
+  return 0;
+}
+
 static int sim_step_on(racer_sim* s, const float* actions, float* reward, float* done, float* obs, int32_t* iters,
                        cudaStream_t st) {
   launch_advance(s->seg, s->state, actions, reward, done, obs, s->n, s->beams, s->ray, st);
-  launch_lidar(s->seg, s->shape, s->ray, obs, s->n, s->beams, s->beam_dir, iters, st);
   RACER_LAUNCHED();
-  return 0;
+  return lidar_on(s, s->shape, obs, iters, st);
 }
 
 int racer_sim_reset(racer_sim* s) {
@@ -825,7 +875,7 @@ int racer_sim_profile(racer_sim* s, const float* actions, int reps, float* physi
     RACER_TRY(cudaEventRecord(ev[3 * r], st));
     launch_advance(s->seg, s->state, actions, s->reward, s->done, s->obs, s->n, s->beams, s->ray, st);
     RACER_TRY(cudaEventRecord(ev[3 * r + 1], st));
-    launch_lidar(s->seg, s->shape, s->ray, s->obs, s->n, s->beams, s->beam_dir, nullptr, st);
+    if (int rc = lidar_on(s, s->shape, s->obs, nullptr, st)) return rc;
     RACER_TRY(cudaEventRecord(ev[3 * r + 2], st));
   }
   RACER_LAUNCHED();
@@ -834,7 +884,7 @@ int racer_sim_profile(racer_sim* s, const float* actions, int reps, float* physi
   RACER_TRY(cudaMalloc((void**)&iters, (size_t)s->beams * s->n * sizeof(int32_t)));
   RACER_TRY(cudaMalloc((void**)&total, sizeof(unsigned long long)));
   RACER_TRY(cudaMemsetAsync(total, 0, sizeof(unsigned long long), st));
-  launch_lidar(s->seg, s->shape, s->ray, s->obs, s->n, s->beams, s->beam_dir, iters, st);
+  if (int rc = lidar_on(s, s->shape, s->obs, iters, st)) return rc;
   k_sum_i32<<<152, 256, 0, st>>>(iters, (long)s->beams * s->n, total);
   RACER_LAUNCHED();
   unsigned long long host_total = 0;
@@ -875,42 +925,55 @@ static void drop_graphs(racer_sim* s) {
   s->surrogate_graphs.clear();
 }
 
-static LidarShape make_shape(int cars, int wide, const int* order, int count) {
+static LidarShape from_api(const racer_lidar_shape& in) {
   LidarShape shape;
-  shape.cars = cars;
-  shape.wide = wide;
-  for (int j = 0; j < MAX_SEGMENTS; ++j) shape.order[j] = order && j < count ? order[j] : j;
+  shape.cars = in.cars_per_block;
+  shape.wide = in.wide;
+  shape.split = in.split;
+  for (int j = 0; j < MAX_SEGMENTS; ++j) shape.order[j] = in.order[j];
   return shape;
 }
 
-int racer_sim_set_lidar_shape(racer_sim* s, int cars, int wide, const int* order) {
-  RACER_ARG(s, "racer_sim_set_lidar_shape: null sim");
-  LidarShape shape = make_shape(cars, wide, order, s->seg.count);
-  RACER_ARG(lidar_shape_ok(shape), "racer_sim_set_lidar_shape: cars per block must be 2, 4 or 8 and wide 0 or 1");
-  if (order) {
-    bool seen[MAX_SEGMENTS] = {};
-    for (int j = 0; j < s->seg.count; ++j) {
-      RACER_ARG(order[j] >= 0 && order[j] < s->seg.count && !seen[order[j]],
-                "racer_sim_set_lidar_shape: order must be a permutation of the segments");
-      seen[order[j]] = true;
-    }
+static void to_api(const racer_sim* s, const LidarShape& shape, racer_lidar_shape* out) {
+  out->cars_per_block = shape.cars;
+  out->wide = shape.wide;
+  out->split = shape.split;
+  int order[MAX_SEGMENTS];
+  segment_order(s, shape, order);
+  for (int j = 0; j < MAX_SEGMENTS; ++j) out->order[j] = j < s->seg.count ? order[j] : -1;
+}
+
+static bool same_shape(const racer_sim* s, const LidarShape& a, const LidarShape& b) {
+  int oa[MAX_SEGMENTS], ob[MAX_SEGMENTS];
+  segment_order(s, a, oa);
+  segment_order(s, b, ob);
+  return a.cars == b.cars && a.wide == b.wide && a.split == b.split && std::equal(oa, oa + s->seg.count, ob);
+}
+
+int racer_sim_set_lidar_shape(racer_sim* s, const racer_lidar_shape* in) {
+  RACER_ARG(s && in, "racer_sim_set_lidar_shape: null argument");
+  LidarShape shape = from_api(*in);
+  RACER_ARG(lidar_shape_ok(shape) && (shape.split == 0 || shape.split == 1),
+            "racer_sim_set_lidar_shape: cars per block must be 2, 4 or 8, wide and split 0 or 1");
+  bool seen[MAX_SEGMENTS] = {};
+  for (int j = 0; j < s->seg.count; ++j) {
+    RACER_ARG(in->order[j] >= 0 && in->order[j] < s->seg.count && !seen[in->order[j]],
+              "racer_sim_set_lidar_shape: order must be a permutation of the segments");
+    seen[in->order[j]] = true;
   }
   RACER_TRY(cudaStreamSynchronize(s->st));
-  drop_graphs(s);
+  if (!same_shape(s, shape, s->shape)) drop_graphs(s);
   s->shape = shape;
   return 0;
 }
 
-int racer_sim_get_lidar_shape(racer_sim* s, int* cars, int* wide, int* order) {
-  RACER_ARG(s, "racer_sim_get_lidar_shape: null sim");
-  if (cars) *cars = s->shape.cars;
-  if (wide) *wide = s->shape.wide;
-  if (order)
-    for (int j = 0; j < s->seg.count; ++j) order[j] = s->shape.order[j];
+int racer_sim_get_lidar_shape(racer_sim* s, racer_lidar_shape* out) {
+  RACER_ARG(s && out, "racer_sim_get_lidar_shape: null argument");
+  to_api(s, s->shape, out);
   return 0;
 }
 
-int racer_sim_autotune(racer_sim* s, int reps, int* cars_out, int* wide_out, int* order_out, float* best_ms) {
+int racer_sim_autotune(racer_sim* s, int reps, racer_lidar_shape* best_out, float* best_ms) {
   RACER_ARG(s && reps >= 1, "racer_sim_autotune: bad argument");
   cudaStream_t st = s->st;
   const int count = s->seg.count;
@@ -920,7 +983,7 @@ int racer_sim_autotune(racer_sim* s, int reps, int* cars_out, int* wide_out, int
   RACER_TRY(cudaMalloc((void**)&iters, (size_t)s->beams * s->n * sizeof(int32_t)));
   RACER_TRY(cudaMalloc((void**)&sums, MAX_SEGMENTS * sizeof(unsigned long long)));
   RACER_TRY(cudaMemsetAsync(sums, 0, MAX_SEGMENTS * sizeof(unsigned long long), st));
-  launch_lidar(s->seg, s->shape, s->ray, s->obs, s->n, s->beams, s->beam_dir, iters, st);
+  if (int rc = lidar_on(s, s->shape, s->obs, iters, st)) return rc;
   for (int k = 0; k < count; ++k)
     k_sum_cols<<<4 * 152, 256, 0, st>>>(iters, s->n, s->beams, s->seg.car0[k], s->seg.car0[k + 1], sums + k);
   RACER_LAUNCHED();
@@ -929,28 +992,33 @@ int racer_sim_autotune(racer_sim* s, int reps, int* cars_out, int* wide_out, int
   RACER_TRY(cudaStreamSynchronize(st));
   cudaFree(iters);
   cudaFree(sums);
-  int natural[MAX_SEGMENTS], heavy[MAX_SEGMENTS];
-  for (int j = 0; j < MAX_SEGMENTS; ++j) natural[j] = heavy[j] = j;
+  int heavy[MAX_SEGMENTS];
+  for (int j = 0; j < MAX_SEGMENTS; ++j) heavy[j] = j;
   std::stable_sort(heavy, heavy + count, [&](int a, int b) { return host[a] > host[b]; });
   std::vector<LidarShape> candidates;
   for (int cars : {2, 4, 8})
-    for (int wide : {0, 1}) {
-      candidates.push_back(make_shape(cars, wide, natural, count));
-      if (count > 1 && !std::equal(natural, natural + count, heavy))
-        candidates.push_back(make_shape(cars, wide, heavy, count));
-    }
+    for (int wide : {0, 1})
+      for (int split : {0, 1})
+        for (int sorted : {0, 1}) {
+          if (count == 1 && (split || sorted)) continue;
+          LidarShape shape;
+          shape.cars = cars;
+          shape.wide = wide;
+          shape.split = split;
+          for (int j = 0; j < MAX_SEGMENTS; ++j) shape.order[j] = sorted ? heavy[j] : j;
+          candidates.push_back(shape);
+        }
   cudaEvent_t a, b;
   RACER_TRY(cudaEventCreate(&a));
   RACER_TRY(cudaEventCreate(&b));
   float best = 1e30f;
   LidarShape chosen = s->shape;
   for (const LidarShape& shape : candidates) {
-    launch_lidar(s->seg, shape, s->ray, s->obs, s->n, s->beams, s->beam_dir, nullptr, st);
+    if (int rc = lidar_on(s, shape, s->obs, nullptr, st)) return rc;
     RACER_TRY(cudaEventRecord(a, st));
     for (int r = 0; r < reps; ++r)
-      launch_lidar(s->seg, shape, s->ray, s->obs, s->n, s->beams, s->beam_dir, nullptr, st);
+      if (int rc = lidar_on(s, shape, s->obs, nullptr, st)) return rc;
     RACER_TRY(cudaEventRecord(b, st));
-    RACER_LAUNCHED();
     RACER_TRY(cudaEventSynchronize(b));
     float ms = 0;
     RACER_TRY(cudaEventElapsedTime(&ms, a, b));
@@ -958,15 +1026,9 @@ int racer_sim_autotune(racer_sim* s, int reps, int* cars_out, int* wide_out, int
   }
   cudaEventDestroy(a);
   cudaEventDestroy(b);
-  if (chosen.cars != s->shape.cars || chosen.wide != s->shape.wide ||
-      !std::equal(chosen.order, chosen.order + count, s->shape.order)) {
-    drop_graphs(s);
-    s->shape = chosen;
-  }
-  if (cars_out) *cars_out = s->shape.cars;
-  if (wide_out) *wide_out = s->shape.wide;
-  if (order_out)
-    for (int j = 0; j < count; ++j) order_out[j] = s->shape.order[j];
+  if (!same_shape(s, chosen, s->shape)) drop_graphs(s);
+  s->shape = chosen;
+  if (best_out) to_api(s, s->shape, best_out);
   if (best_ms) *best_ms = best;
   return 0;
 }

@@ -63,9 +63,13 @@ struct Segments {
 // Launch shape of the lidar: cars per block (one warp each) and the order in
 // which the segments' blocks are laid out along the grid (heavier first lets
 // the light segments fill the tail).
+// With several segments, split = 1 launches each segment's one-track kernel
+// on its own stream (parallel branches of a captured graph) instead of one
+// segment-table launch; `order` is then the launch order.
 struct LidarShape {
   int cars = 2;  // measured fastest on every built-in track and the occupancy map
   int wide = 0;  // 1: compiled for 48 resident warps per SM (40 registers) instead of 64 (32)
+  int split = 0;
   int order[MAX_SEGMENTS] = {0, 1, 2, 3, 4, 5, 6, 7};
 };
 

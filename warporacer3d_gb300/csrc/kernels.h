@@ -16,6 +16,9 @@ void launch_advance(const Segments& g, float* state, const float* actions, float
                     int n, int beams, float4* ray, cudaStream_t st);
 void launch_lidar(const Segments& g, const LidarShape& shape, const float4* ray, float* obs, int n, int beams,
                   const float2* beam_dir, int* iters, cudaStream_t st);
+// The lidar of segment k alone (its one-track kernel), for per-segment launches on parallel streams.
+void launch_lidar_segment(const Segments& g, int k, const LidarShape& shape, const float4* ray, float* obs, int n,
+                          int beams, const float2* beam_dir, int* iters, cudaStream_t st);
 // One track, default shape (surrogate labels and fallback). With `list` set,
 // only the cars list[0 .. *list_count) (list_max at most) are traced.
 void launch_lidar(const TrackDev& t, const float4* ray, float* obs, int n, int beams, const float2* beam_dir,

@@ -24,6 +24,10 @@ struct racer_sim {
   float2* d_cl = nullptr;
   std::vector<float*> seg_track;
   std::vector<float2*> seg_cl;
+  // per-segment lidar launches (LidarShape::split): streams and events of the fork/join
+  std::vector<cudaStream_t> aux;
+  std::vector<cudaEvent_t> join;
+  cudaEvent_t fork = nullptr;
   float2* beam_dir = nullptr;
   float4* ray = nullptr;  // [2, n] per-car lidar frame written by the physics kernel
   float *state = nullptr, *obs = nullptr, *actions = nullptr, *reward = nullptr, *done = nullptr;

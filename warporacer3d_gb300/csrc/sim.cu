@@ -449,13 +449,13 @@ constexpr int lidar_min_blocks(int cars, bool wide) {
   return (wide ? 48 : 64) / cars < 32 ? (wide ? 48 : 64) / cars : 32;
 }
 
-// One track: its fields are kernel parameters, read as constant operands.
-// CARS warps per block (one car each): small blocks release their slot as
-// soon as their few cars finish.
+// One track (cars [c0, c1) of the batch): its fields are kernel parameters,
+// read as constant operands. CARS warps per block (one car each): small
+// blocks release their slot as soon as their few cars finish.
 template <int LAYERS, int CARS, bool WIDE, bool LIST>
 __global__ void __launch_bounds__(CARS * 32, lidar_min_blocks(CARS, WIDE))
-    k_lidar_track(TrackDev t, int max_iters, const float4* __restrict__ ray, float* obs, int n, int beams,
-                  const float2* __restrict__ beam_dir, int* iters, const int* __restrict__ list,
+    k_lidar_track(TrackDev t, int max_iters, const float4* __restrict__ ray, float* obs, int n, int c0, int c1,
+                  int beams, const float2* __restrict__ beam_dir, int* iters, const int* __restrict__ list,
                   const int* list_count) {
   const int beam = blockIdx.y * 32 + (threadIdx.x & 31);
   if (beam >= beams) return;
@@ -467,8 +467,8 @@ __global__ void __launch_bounds__(CARS * 32, lidar_min_blocks(CARS, WIDE))
     }
     return;
   }
-  const int car = blockIdx.x * CARS + (threadIdx.x >> 5);
-  if (car < n) trace<LAYERS>(t, ray, obs, n, beam_dir, max_iters, iters, car, beam);
+  const int car = c0 + (int)blockIdx.x * CARS + (int)(threadIdx.x >> 5);
+  if (car < c1) trace<LAYERS>(t, ray, obs, n, beam_dir, max_iters, iters, car, beam);
 }
 
 // Several tracks: a block's segment depends on blockIdx only, so the track's
@@ -595,24 +595,32 @@ static LidarGrid lidar_grid(const Segments& g, const LidarShape& shape) {
 }
 
 template <int LAYERS, int CARS, bool WIDE>
-static void lidar_track(const TrackDev& t, int max_iters, const float4* ray, float* obs, int n, int beams,
-                        const float2* beam_dir, int* iters, cudaStream_t st) {
-  dim3 grid((n + CARS - 1) / CARS, (beams + 31) / 32);
+static void lidar_track(const TrackDev& t, int max_iters, const float4* ray, float* obs, int n, int c0, int c1,
+                        int beams, const float2* beam_dir, int* iters, cudaStream_t st) {
+  dim3 grid((c1 - c0 + CARS - 1) / CARS, (beams + 31) / 32);
+  if (grid.x == 0) return;
   k_lidar_track<LAYERS, CARS, WIDE, false>
-      <<<grid, CARS * 32, 0, st>>>(t, max_iters, ray, obs, n, beams, beam_dir, iters, nullptr, nullptr);
+      <<<grid, CARS * 32, 0, st>>>(t, max_iters, ray, obs, n, c0, c1, beams, beam_dir, iters, nullptr, nullptr);
+}
+
+template <int CARS, bool WIDE>
+static void lidar_segment(const Segments& g, int k, const float4* ray, float* obs, int n, int beams,
+                          const float2* beam_dir, int* iters, cudaStream_t st) {
+  const TrackDev& t = g.t[k];
+  const int c0 = g.car0[k], c1 = g.car0[k + 1];
+  if (t.layers == 1)
+    lidar_track<1, CARS, WIDE>(t, g.max_iters[k], ray, obs, n, c0, c1, beams, beam_dir, iters, st);
+  else if (t.layers == 2)
+    lidar_track<2, CARS, WIDE>(t, g.max_iters[k], ray, obs, n, c0, c1, beams, beam_dir, iters, st);
+  else
+    lidar_track<0, CARS, WIDE>(t, g.max_iters[k], ray, obs, n, c0, c1, beams, beam_dir, iters, st);
 }
 
 template <int CARS, bool WIDE>
 static void lidar_shape(const Segments& g, const LidarShape& shape, const float4* ray, float* obs, int n, int beams,
                         const float2* beam_dir, int* iters, cudaStream_t st) {
   if (g.count == 1) {
-    const TrackDev& t = g.t[0];
-    if (t.layers == 1)
-      lidar_track<1, CARS, WIDE>(t, g.max_iters[0], ray, obs, n, beams, beam_dir, iters, st);
-    else if (t.layers == 2)
-      lidar_track<2, CARS, WIDE>(t, g.max_iters[0], ray, obs, n, beams, beam_dir, iters, st);
-    else
-      lidar_track<0, CARS, WIDE>(t, g.max_iters[0], ray, obs, n, beams, beam_dir, iters, st);
+    lidar_segment<CARS, WIDE>(g, 0, ray, obs, n, beams, beam_dir, iters, st);
     return;
   }
   const LidarGrid lg = lidar_grid(g, shape);
@@ -639,6 +647,21 @@ void launch_lidar(const Segments& g, const LidarShape& shape, const float4* ray,
          : lidar_shape<4, false>(g, shape, ray, obs, n, beams, beam_dir, iters, st);
 }
 
+void launch_lidar_segment(const Segments& g, int k, const LidarShape& shape, const float4* ray, float* obs, int n,
+                          int beams, const float2* beam_dir, int* iters, cudaStream_t st) {
+  if (k < 0 || k >= g.count) return;
+  const bool wide = shape.wide == 1;
+  if (shape.cars == 2)
+    wide ? lidar_segment<2, true>(g, k, ray, obs, n, beams, beam_dir, iters, st)
+         : lidar_segment<2, false>(g, k, ray, obs, n, beams, beam_dir, iters, st);
+  else if (shape.cars == 8)
+    wide ? lidar_segment<8, true>(g, k, ray, obs, n, beams, beam_dir, iters, st)
+         : lidar_segment<8, false>(g, k, ray, obs, n, beams, beam_dir, iters, st);
+  else
+    wide ? lidar_segment<4, true>(g, k, ray, obs, n, beams, beam_dir, iters, st)
+         : lidar_segment<4, false>(g, k, ray, obs, n, beams, beam_dir, iters, st);
+}
+
 void launch_lidar(const TrackDev& t, const float4* ray, float* obs, int n, int beams, const float2* beam_dir,
                   int* iters, cudaStream_t st, const int* list, const int* list_count, int list_max) {
   const int max_iters = lidar_max_iters(t);
@@ -652,13 +675,13 @@ void launch_lidar(const TrackDev& t, const float4* ray, float* obs, int n, int b
   if (grid.x == 0) return;
   if (t.layers == 1)
     k_lidar_track<1, CARS, false, true>
-        <<<grid, CARS * 32, 0, st>>>(t, max_iters, ray, obs, n, beams, beam_dir, iters, list, list_count);
+        <<<grid, CARS * 32, 0, st>>>(t, max_iters, ray, obs, n, 0, n, beams, beam_dir, iters, list, list_count);
   else if (t.layers == 2)
     k_lidar_track<2, CARS, false, true>
-        <<<grid, CARS * 32, 0, st>>>(t, max_iters, ray, obs, n, beams, beam_dir, iters, list, list_count);
+        <<<grid, CARS * 32, 0, st>>>(t, max_iters, ray, obs, n, 0, n, beams, beam_dir, iters, list, list_count);
   else
     k_lidar_track<0, CARS, false, true>
-        <<<grid, CARS * 32, 0, st>>>(t, max_iters, ray, obs, n, beams, beam_dir, iters, list, list_count);
+        <<<grid, CARS * 32, 0, st>>>(t, max_iters, ray, obs, n, 0, n, beams, beam_dir, iters, list, list_count);
 }
 
 __global__ void k_select_cars(const unsigned* minr, int n, unsigned threshold_bits, int* list, int* count) {

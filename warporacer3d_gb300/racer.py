@@ -17,7 +17,7 @@ import time
 
 import numpy as np
 
-from ._lib import RacerError, SimBuffers, TrainerBuffers, call, load_library
+from ._lib import LidarShape, RacerError, SimBuffers, TrainerBuffers, call, load_library
 
 STATE = 11
 X, Y, Z, HEADING, SPEED, STEER, STEPS, PROGRESS, EPISODE, FRICTION, RETURN = range(11)
@@ -153,23 +153,29 @@ class Sim:
         call("racer_sim_sample", self.handle, output.c, log_std.c, actions.c, logp.c, value.c, int(deterministic),
              step)
 
-    def set_lidar_shape(self, cars_per_block, wide=0, order=None):
-        k = len(self.cars)
-        arr = None if order is None else (ctypes.c_int * k)(*order)
-        call("racer_sim_set_lidar_shape", self.handle, cars_per_block, wide, arr)
+    def set_lidar_shape(self, cars_per_block, wide=0, split=0, order=None):
+        """Lidar launch shape: cars per block (2, 4, 8), the 40-register variant (wide), per-segment
+        launches on parallel streams (split) and the segments' order (default: index order)."""
+        order = list(range(len(self.cars))) if order is None else list(order)
+        shape = LidarShape(cars_per_block, wide, split, (ctypes.c_int * 8)(*(order + [-1] * (8 - len(order)))))
+        call("racer_sim_set_lidar_shape", self.handle, ctypes.byref(shape))
+
+    @staticmethod
+    def _shape(shape):
+        return {"cars_per_block": shape.cars_per_block, "wide": shape.wide, "split": shape.split,
+                "order": [k for k in shape.order if k >= 0]}
 
     def lidar_shape(self):
-        """(cars per block, wide register budget 0/1, segment order)."""
-        cars, wide, order = ctypes.c_int(), ctypes.c_int(), (ctypes.c_int * len(self.cars))()
-        call("racer_sim_get_lidar_shape", self.handle, ctypes.byref(cars), ctypes.byref(wide), order)
-        return cars.value, wide.value, list(order)
+        shape = LidarShape()
+        call("racer_sim_get_lidar_shape", self.handle, ctypes.byref(shape))
+        return self._shape(shape)
 
     def autotune(self, reps=5):
-        """Times the lidar launch shapes on the current frames; keeps and returns the fastest
-        (cars per block, wide, segment order, mean ms)."""
-        cars, wide, order, ms = ctypes.c_int(), ctypes.c_int(), (ctypes.c_int * len(self.cars))(), ctypes.c_float()
-        call("racer_sim_autotune", self.handle, reps, ctypes.byref(cars), ctypes.byref(wide), order, ctypes.byref(ms))
-        return cars.value, wide.value, list(order), ms.value
+        """Times every lidar launch shape on the current frames; keeps the fastest and returns it
+        with its mean time in ms."""
+        shape, ms = LidarShape(), ctypes.c_float()
+        call("racer_sim_autotune", self.handle, reps, ctypes.byref(shape), ctypes.byref(ms))
+        return self._shape(shape), ms.value
 
 
 class Policy:

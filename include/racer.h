@@ -75,12 +75,16 @@ int racer_sim_create_segments(int count, const float* const* tracks, const size_
  * through the segment table; 1 = each segment's one-track kernel on its own
  * stream, forked from and joined into the sim's stream (parallel branches of
  * a captured rollout graph). order[0..count): the segments' order in the grid
- * (split = 0) or their launch order (split = 1). Setting a different shape
+ * (split = 0) or their launch order (split = 1). dynamic (one-track sims and
+ * split launches): 1 = a persistent grid per segment whose warps take (car,
+ * 32-beam group) units from an atomic counter instead of a fixed block per
+ * group of cars (cars_per_block is then unused). Setting a different shape
  * drops the sim's captured rollout graphs. */
 typedef struct {
   int cars_per_block;
   int wide;
   int split;
+  int dynamic;
   int order[8];
 } racer_lidar_shape;
 int racer_sim_set_lidar_shape(racer_sim* sim, const racer_lidar_shape* shape);

@@ -269,7 +269,8 @@ def test_lidar_shapes_and_autotune_keep_results():
     a.reset()
     b.reset()
     rng = np.random.default_rng(5)
-    shapes = [(2, 0, 0, [3, 1, 0, 2]), (8, 1, 0, None), (4, 1, 1, [2, 3, 1, 0]), (2, 0, 1, None), "auto"]
+    shapes = [(2, 0, 0, [3, 1, 0, 2]), (8, 1, 0, None), (4, 1, 1, [2, 3, 1, 0]), (2, 0, 1, None),
+              (2, 0, 1, [1, 0, 2, 3], 1), (2, 1, 1, None, 1), "auto"]
     for shape in shapes:
         if shape == "auto":
             best, ms = b.autotune(3)
@@ -297,7 +298,7 @@ def test_split_lidar_in_captured_rollouts():
     """Rollout graphs captured with per-segment lidar branches give the segment-table launch's results."""
     tracks, cars, seeds = segment_tracks(), [64, 40, 72, 20], [1, 2, 3, 4]
     runs = [W.Runner.segments(tracks, cars, seeds, beams=108) for _ in range(2)]
-    runs[1].sim.set_lidar_shape(2, 0, 1, [2, 0, 3, 1])
+    runs[1].sim.set_lidar_shape(2, 0, 1, [2, 0, 3, 1], 1)
     for r in runs:
         r.rollout(12, False, 0)
         r.rollout(12, False, 12)
@@ -311,12 +312,12 @@ def test_one_track_lidar_shapes_bit_exact():
     n = 50
     cpu = O.Sim(track, n, 9, beams=1081)
     cpu.reset()
-    for cars_per_block in (2, 4, 8):
+    for cars_per_block, dynamic in ((2, 0), (4, 0), (8, 0), (2, 1)):
         for wide in (0, 1):
             gpu = W.Sim(track, n, 9, beams=1081)
-            gpu.set_lidar_shape(cars_per_block, wide, 0)
+            gpu.set_lidar_shape(cars_per_block, wide, 0, None, dynamic)
             gpu.reset()
-            check_sim(gpu, cpu, f"shape {cars_per_block}/{wide} ")
+            check_sim(gpu, cpu, f"shape {cars_per_block}/{wide}/{dynamic} ")
 
 
 def test_synthetic_occupancy_map_bit_exact():

@@ -25,7 +25,8 @@ class SimBuffers(ctypes.Structure):
 
 
 class LidarShape(ctypes.Structure):
-    _fields_ = [("cars_per_block", c_int), ("wide", c_int), ("split", c_int), ("order", c_int * 8)]
+    _fields_ = [("cars_per_block", c_int), ("wide", c_int), ("split", c_int), ("dynamic", c_int),
+                ("order", c_int * 8)]
 
 
 class TrainerBuffers(ctypes.Structure):

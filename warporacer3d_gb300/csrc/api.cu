@@ -237,6 +237,13 @@ int racer_sim_create_segments(int count, const float* const* tracks, const size_
     racer_sim_destroy(s);
     return rc;
   }
+  if ((rc = dalloc(&s->counters, MAX_SEGMENTS))) {
+    racer_sim_destroy(s);
+    return rc;
+  }
+  int device = 0;
+  if (cudaGetDevice(&device) == cudaSuccess)
+    cudaDeviceGetAttribute(&s->sms, cudaDevAttrMultiProcessorCount, device);
   cudaError_t err = cudaMemcpy(s->beam_dir, dirs.data(), beams * sizeof(float2), cudaMemcpyHostToDevice);
   if (err != cudaSuccess) {
     set_error(std::string("racer_sim_create upload: ") + cudaGetErrorString(err));
@@ -257,6 +264,7 @@ int racer_sim_destroy(racer_sim* s) {
   if (!s) return 0;
   for (auto& kv : s->graphs) cudaGraphExecDestroy(kv.second);
   for (auto& kv : s->surrogate_graphs) cudaGraphExecDestroy(kv.second);
+  cudaFree(s->counters);
   for (cudaStream_t a : s->aux) cudaStreamDestroy(a);
   for (cudaEvent_t e : s->join) cudaEventDestroy(e);
   if (s->fork) cudaEventDestroy(s->fork);
@@ -302,7 +310,10 @@ static void segment_order(const racer_sim* s, const LidarShape& shape, int* orde
 // The lidar over every segment: one segment-table launch, or (split) each
 // segment's one-track kernel on its own stream, forked from and joined back
 // into `st` (parallel branches when captured into a graph).
-static int lidar_on(racer_sim* s, const LidarShape& shape, float* obs, int32_t* iters, cudaStream_t st) {
+static int lidar_on(racer_sim* s, const LidarShape& given, float* obs, int32_t* iters, cudaStream_t st) {
+  LidarShape shape = given;
+  shape.counters = s->counters;
+  shape.sms = s->sms;
   if (s->seg.count == 1 || !shape.split) {
     launch_lidar(s->seg, shape, s->ray, obs, s->n, s->beams, s->beam_dir, iters, st);
     RACER_LAUNCHED();
@@ -930,6 +941,7 @@ static LidarShape from_api(const racer_lidar_shape& in) {
   shape.cars = in.cars_per_block;
   shape.wide = in.wide;
   shape.split = in.split;
+  shape.dynamic = in.dynamic;
   for (int j = 0; j < MAX_SEGMENTS; ++j) shape.order[j] = in.order[j];
   return shape;
 }
@@ -938,6 +950,7 @@ static void to_api(const racer_sim* s, const LidarShape& shape, racer_lidar_shap
   out->cars_per_block = shape.cars;
   out->wide = shape.wide;
   out->split = shape.split;
+  out->dynamic = shape.dynamic;
   int order[MAX_SEGMENTS];
   segment_order(s, shape, order);
   for (int j = 0; j < MAX_SEGMENTS; ++j) out->order[j] = j < s->seg.count ? order[j] : -1;
@@ -947,14 +960,16 @@ static bool same_shape(const racer_sim* s, const LidarShape& a, const LidarShape
   int oa[MAX_SEGMENTS], ob[MAX_SEGMENTS];
   segment_order(s, a, oa);
   segment_order(s, b, ob);
-  return a.cars == b.cars && a.wide == b.wide && a.split == b.split && std::equal(oa, oa + s->seg.count, ob);
+  return a.cars == b.cars && a.wide == b.wide && a.split == b.split && a.dynamic == b.dynamic &&
+         std::equal(oa, oa + s->seg.count, ob);
 }
 
 int racer_sim_set_lidar_shape(racer_sim* s, const racer_lidar_shape* in) {
   RACER_ARG(s && in, "racer_sim_set_lidar_shape: null argument");
   LidarShape shape = from_api(*in);
-  RACER_ARG(lidar_shape_ok(shape) && (shape.split == 0 || shape.split == 1),
-            "racer_sim_set_lidar_shape: cars per block must be 2, 4 or 8, wide and split 0 or 1");
+  RACER_ARG(lidar_shape_ok(shape) && (shape.split == 0 || shape.split == 1) &&
+                (shape.dynamic == 0 || shape.dynamic == 1),
+            "racer_sim_set_lidar_shape: cars per block must be 2, 4 or 8, wide, split and dynamic 0 or 1");
   bool seen[MAX_SEGMENTS] = {};
   for (int j = 0; j < s->seg.count; ++j) {
     RACER_ARG(in->order[j] >= 0 && in->order[j] < s->seg.count && !seen[in->order[j]],
@@ -996,15 +1011,18 @@ int racer_sim_autotune(racer_sim* s, int reps, racer_lidar_shape* best_out, floa
   for (int j = 0; j < MAX_SEGMENTS; ++j) heavy[j] = j;
   std::stable_sort(heavy, heavy + count, [&](int a, int b) { return host[a] > host[b]; });
   std::vector<LidarShape> candidates;
-  for (int cars : {2, 4, 8})
-    for (int wide : {0, 1})
-      for (int split : {0, 1})
-        for (int sorted : {0, 1}) {
+  for (int dynamic : {0, 1})
+    for (int cars : {2, 4, 8})
+      for (int wide : {0, 1})
+        for (int split : {0, 1})
+          for (int sorted : {0, 1}) {
           if (count == 1 && (split || sorted)) continue;
+          if (dynamic && (cars != 2 || (count > 1 && !split))) continue;  // per segment; no cars-per-block
           LidarShape shape;
           shape.cars = cars;
           shape.wide = wide;
           shape.split = split;
+          shape.dynamic = dynamic;
           for (int j = 0; j < MAX_SEGMENTS; ++j) shape.order[j] = sorted ? heavy[j] : j;
           candidates.push_back(shape);
         }

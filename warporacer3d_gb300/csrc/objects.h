@@ -28,6 +28,8 @@ struct racer_sim {
   std::vector<cudaStream_t> aux;
   std::vector<cudaEvent_t> join;
   cudaEvent_t fork = nullptr;
+  unsigned* counters = nullptr;  // [MAX_SEGMENTS] unit counters of the dynamic lidar
+  int sms = 152;
   float2* beam_dir = nullptr;
   float4* ray = nullptr;  // [2, n] per-car lidar frame written by the physics kernel
   float *state = nullptr, *obs = nullptr, *actions = nullptr, *reward = nullptr, *done = nullptr;

@@ -471,6 +471,28 @@ __global__ void __launch_bounds__(CARS * 32, lidar_min_blocks(CARS, WIDE))
   if (car < c1) trace<LAYERS>(t, ray, obs, n, beam_dir, max_iters, iters, car, beam);
 }
 
+// Dynamic variant of k_lidar_track: a persistent grid whose warps take
+// (car, 32-beam group) units from `counter` (zero at launch) one at a time,
+// so no warp holds a block slot waiting for a sibling and the last wave has
+// no tail of idle slots.
+template <int LAYERS, bool WIDE>
+__global__ void __launch_bounds__(128, lidar_min_blocks(4, WIDE))
+    k_lidar_dynamic(TrackDev t, int max_iters, const float4* __restrict__ ray, float* obs, int n, int c0, int c1,
+                    int beams, const float2* __restrict__ beam_dir, int* iters, unsigned* counter) {
+  const int groups = (beams + 31) >> 5;
+  const unsigned total = (unsigned)(c1 - c0) * (unsigned)groups;
+  const int lane = threadIdx.x & 31;
+  for (;;) {
+    unsigned unit = 0;
+    if (lane == 0) unit = atomicAdd(counter, 1u);
+    unit = __shfl_sync(0xffffffffu, unit, 0);
+    if (unit >= total) break;
+    const int car = c0 + (int)(unit / (unsigned)groups);
+    const int beam = (int)(unit % (unsigned)groups) * 32 + lane;
+    if (beam < beams) trace<LAYERS>(t, ray, obs, n, beam_dir, max_iters, iters, car, beam);
+  }
+}
+
 // Several tracks: a block's segment depends on blockIdx only, so the track's
 // fields are block-uniform.
 template <int CARS, bool WIDE>
@@ -603,11 +625,33 @@ static void lidar_track(const TrackDev& t, int max_iters, const float4* ray, flo
       <<<grid, CARS * 32, 0, st>>>(t, max_iters, ray, obs, n, c0, c1, beams, beam_dir, iters, nullptr, nullptr);
 }
 
+template <int LAYERS, bool WIDE>
+static void lidar_dynamic(const TrackDev& t, int max_iters, const float4* ray, float* obs, int n, int c0, int c1,
+                          int beams, const float2* beam_dir, int* iters, unsigned* counter, int sms,
+                          cudaStream_t st) {
+  const long units = (long)(c1 - c0) * ((beams + 31) / 32);
+  if (units <= 0) return;
+  const long blocks = std::min<long>((long)sms * lidar_min_blocks(4, WIDE), (units + 3) / 4);
+  cudaMemsetAsync(counter, 0, sizeof(unsigned), st);
+  k_lidar_dynamic<LAYERS, WIDE>
+      <<<(unsigned)blocks, 128, 0, st>>>(t, max_iters, ray, obs, n, c0, c1, beams, beam_dir, iters, counter);
+}
+
 template <int CARS, bool WIDE>
 static void lidar_segment(const Segments& g, int k, const float4* ray, float* obs, int n, int beams,
-                          const float2* beam_dir, int* iters, cudaStream_t st) {
+                          const float2* beam_dir, int* iters, cudaStream_t st, const LidarShape& shape) {
   const TrackDev& t = g.t[k];
   const int c0 = g.car0[k], c1 = g.car0[k + 1];
+  if (shape.dynamic && shape.counters) {
+    unsigned* counter = shape.counters + k;
+    if (t.layers == 1)
+      lidar_dynamic<1, WIDE>(t, g.max_iters[k], ray, obs, n, c0, c1, beams, beam_dir, iters, counter, shape.sms, st);
+    else if (t.layers == 2)
+      lidar_dynamic<2, WIDE>(t, g.max_iters[k], ray, obs, n, c0, c1, beams, beam_dir, iters, counter, shape.sms, st);
+    else
+      lidar_dynamic<0, WIDE>(t, g.max_iters[k], ray, obs, n, c0, c1, beams, beam_dir, iters, counter, shape.sms, st);
+    return;
+  }
   if (t.layers == 1)
     lidar_track<1, CARS, WIDE>(t, g.max_iters[k], ray, obs, n, c0, c1, beams, beam_dir, iters, st);
   else if (t.layers == 2)
@@ -620,7 +664,7 @@ template <int CARS, bool WIDE>
 static void lidar_shape(const Segments& g, const LidarShape& shape, const float4* ray, float* obs, int n, int beams,
                         const float2* beam_dir, int* iters, cudaStream_t st) {
   if (g.count == 1) {
-    lidar_segment<CARS, WIDE>(g, 0, ray, obs, n, beams, beam_dir, iters, st);
+    lidar_segment<CARS, WIDE>(g, 0, ray, obs, n, beams, beam_dir, iters, st, shape);
     return;
   }
   const LidarGrid lg = lidar_grid(g, shape);
@@ -652,14 +696,14 @@ void launch_lidar_segment(const Segments& g, int k, const LidarShape& shape, con
   if (k < 0 || k >= g.count) return;
   const bool wide = shape.wide == 1;
   if (shape.cars == 2)
-    wide ? lidar_segment<2, true>(g, k, ray, obs, n, beams, beam_dir, iters, st)
-         : lidar_segment<2, false>(g, k, ray, obs, n, beams, beam_dir, iters, st);
+    wide ? lidar_segment<2, true>(g, k, ray, obs, n, beams, beam_dir, iters, st, shape)
+         : lidar_segment<2, false>(g, k, ray, obs, n, beams, beam_dir, iters, st, shape);
   else if (shape.cars == 8)
-    wide ? lidar_segment<8, true>(g, k, ray, obs, n, beams, beam_dir, iters, st)
-         : lidar_segment<8, false>(g, k, ray, obs, n, beams, beam_dir, iters, st);
+    wide ? lidar_segment<8, true>(g, k, ray, obs, n, beams, beam_dir, iters, st, shape)
+         : lidar_segment<8, false>(g, k, ray, obs, n, beams, beam_dir, iters, st, shape);
   else
-    wide ? lidar_segment<4, true>(g, k, ray, obs, n, beams, beam_dir, iters, st)
-         : lidar_segment<4, false>(g, k, ray, obs, n, beams, beam_dir, iters, st);
+    wide ? lidar_segment<4, true>(g, k, ray, obs, n, beams, beam_dir, iters, st, shape)
+         : lidar_segment<4, false>(g, k, ray, obs, n, beams, beam_dir, iters, st, shape);
 }
 
 void launch_lidar(const TrackDev& t, const float4* ray, float* obs, int n, int beams, const float2* beam_dir,

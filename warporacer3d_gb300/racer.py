@@ -153,17 +153,19 @@ class Sim:
         call("racer_sim_sample", self.handle, output.c, log_std.c, actions.c, logp.c, value.c, int(deterministic),
              step)
 
-    def set_lidar_shape(self, cars_per_block, wide=0, split=0, order=None):
+    def set_lidar_shape(self, cars_per_block, wide=0, split=0, order=None, dynamic=0):
         """Lidar launch shape: cars per block (2, 4, 8), the 40-register variant (wide), per-segment
-        launches on parallel streams (split) and the segments' order (default: index order)."""
+        launches on parallel streams (split), the segments' order (default: index order) and the
+        persistent grid with dynamically assigned (car, beam group) units (dynamic)."""
         order = list(range(len(self.cars))) if order is None else list(order)
-        shape = LidarShape(cars_per_block, wide, split, (ctypes.c_int * 8)(*(order + [-1] * (8 - len(order)))))
+        shape = LidarShape(cars_per_block, wide, split, dynamic,
+                           (ctypes.c_int * 8)(*(order + [-1] * (8 - len(order)))))
         call("racer_sim_set_lidar_shape", self.handle, ctypes.byref(shape))
 
     @staticmethod
     def _shape(shape):
         return {"cars_per_block": shape.cars_per_block, "wide": shape.wide, "split": shape.split,
-                "order": [k for k in shape.order if k >= 0]}
+                "dynamic": shape.dynamic, "order": [k for k in shape.order if k >= 0]}
 
     def lidar_shape(self):
         shape = LidarShape()

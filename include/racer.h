@@ -189,6 +189,20 @@ int racer_runner_step(racer_sim* sim, racer_policy* policy, racer_acts* acts, fl
  * offsets are step0, step0 + 1, ... */
 int racer_rollout(racer_sim* sim, racer_policy* policy, racer_acts* acts, float* scratch_dev, int steps,
                   int deterministic, int64_t step0);
+/* Runner.evaluate (main.mojo:70-80): `steps` deterministic Runner steps
+ * (sampling offsets step0, step0 + 1, ...) replayed from one CUDA graph in
+ * which the physics kernel adds every car's reward (FP64) and crash to
+ * per-car sums on the device; one fixed-order reduction and one read at the
+ * end replace the reference's two blocking reads per step. out[0] = reward
+ * per car-step, out[1] = crashes per car. */
+int racer_runner_evaluate(racer_sim* sim, racer_policy* policy, racer_acts* acts, float* scratch_dev, int steps,
+                          int64_t step0, double* out);
+/* Serve snapshot (main.mojo:94-124, without the HTTP bridge and viewer):
+ * state, obs, actions, reward and done of every car, in that order,
+ * (11 + beams + 5 + 4) * n floats, packed on the device and copied to `host`
+ * by one asynchronous copy on the sim's stream (use pinned memory for an
+ * asynchronous copy); synchronize != 0 waits for it. */
+int racer_sim_snapshot(racer_sim* sim, float* host, int synchronize);
 /* Accuracy audit of the binary32 dynamics (no counterpart in the reference):
  * `steps` Runner steps as racer_runner_step, and after each one a kernel
  * re-integrates racer/sim.mojo:189-213 in FP64 from the pre-step state and

@@ -346,3 +346,34 @@ def test_segment_runner_rollout_and_audit():
     assert stats["cars"] > 0.9 * 4 * 512 and stats["position_max_m"] < 1e-4
     with pytest.raises(W.RacerError):
         W.Surrogate(run.sim)
+
+
+def test_device_evaluate_matches_host_loop():
+    """main.mojo:70-80's evaluation: graph-captured with device-side sums equals the host loop
+    that reads reward and done after every step."""
+    a = W.Runner(W.track("ramp"), 300, beams=108, seed=5, policy_seed=8)
+    b = W.Runner(W.track("ramp"), 300, beams=108, seed=5, policy_seed=8)
+    host_reward, host_crashes = a.evaluate(60)
+    dev_reward, dev_crashes = b.evaluate_graph(60)
+    assert dev_reward == pytest.approx(host_reward, rel=1e-12, abs=1e-15)
+    assert dev_crashes == host_crashes
+    assert same(a.sim.state.numpy(), b.sim.state.numpy())
+    # a second call replays the captured graph from the state reached (offsets 60..119)
+    r2, c2 = b.evaluate_graph(60, step0=60)
+    reward, crashes = 0.0, 0  # the host loop over offsets 60..119
+    for t in range(60, 120):
+        a.step(True, t)
+        reward += float(a.sim.reward.numpy().astype(np.float64).sum())
+        crashes += int((a.sim.done.numpy() == W.CRASH).sum())
+    assert r2 == pytest.approx(reward / (300 * 60), rel=1e-12, abs=1e-15) and c2 == crashes / 300
+
+
+def test_snapshot_rows_and_serve_step():
+    run = W.Runner(W.track("bridge"), 70, beams=108, seed=2)
+    snap = run.serve_step(25, 80, reset=False, policy=False, tick=1)
+    sim = run.sim
+    rows = [sim.state.numpy(), sim.obs.numpy(), sim.actions.numpy(), sim.reward.numpy()[None], sim.done.numpy()[None]]
+    assert snap.shape == (11 + 113 + 4, 70) and same(snap, np.concatenate(rows))
+    assert np.all(snap[11 + 113] == np.float32(0.25)) and np.all(snap[11 + 113 + 1] == np.float32(0.8))
+    snap2 = run.serve_step(0, 0, reset=True, policy=True, tick=2)
+    assert same(snap2[:11], sim.state.numpy()) and same(snap2[-1], sim.done.numpy())

@@ -77,6 +77,8 @@ SIGNATURES = {
     "racer_trainer_minibatch": [c_void_p, c_void_p, c_int, c_float, c_float],
     "racer_runner_step": [c_void_p, c_void_p, c_void_p, c_void_p, c_int, c_int64],
     "racer_rollout": [c_void_p, c_void_p, c_void_p, c_void_p, c_int, c_int, c_int64],
+    "racer_runner_evaluate": [c_void_p, c_void_p, c_void_p, c_void_p, c_int, c_int64, P(ctypes.c_double)],
+    "racer_sim_snapshot": [c_void_p, c_void_p, c_int],
     "racer_runner_audit_dynamics": [c_void_p, c_void_p, c_void_p, c_void_p, c_int, c_int, c_int64,
                                     P(ctypes.c_double)],
     "racer_surrogate_create": [c_void_p, c_int, c_int, c_uint64, P(c_void_p)],

@@ -265,6 +265,11 @@ int racer_sim_destroy(racer_sim* s) {
   for (auto& kv : s->graphs) cudaGraphExecDestroy(kv.second);
   for (auto& kv : s->surrogate_graphs) cudaGraphExecDestroy(kv.second);
   cudaFree(s->counters);
+  for (auto& kv : s->eval_graphs) cudaGraphExecDestroy(kv.second);
+  cudaFree(s->eval_reward);
+  cudaFree(s->eval_crash);
+  cudaFree(s->eval_total);
+  cudaFree(s->snapshot);
   for (cudaStream_t a : s->aux) cudaStreamDestroy(a);
   for (cudaEvent_t e : s->join) cudaEventDestroy(e);
   if (s->fork) cudaEventDestroy(s->fork);
@@ -346,8 +351,9 @@ static int lidar_on(racer_sim* s, const LidarShape& given, float* obs, int32_t* 
 }
 
 static int sim_step_on(racer_sim* s, const float* actions, float* reward, float* done, float* obs, int32_t* iters,
-                       cudaStream_t st) {
-  launch_advance(s->seg, s->state, actions, reward, done, obs, s->n, s->beams, s->ray, st);
+                       cudaStream_t st, bool eval = false) {
+  launch_advance(s->seg, s->state, actions, reward, done, obs, s->n, s->beams, s->ray, st,
+                 eval ? s->eval_reward : nullptr, eval ? s->eval_crash : nullptr);
   RACER_LAUNCHED();
   return lidar_on(s, s->shape, obs, iters, st);
 }
@@ -717,7 +723,7 @@ int racer_trainer_update(racer_trainer* tr, racer_policy* p, float* kl) {
 // from it (audited by, or falling back to, the exact tracer).
 static int runner_step_on(racer_sim* s, racer_policy* p, racer_acts* a, float* scratch, int det,
                           const int64_t* base, int64_t add, cudaStream_t st, racer_surrogate* sur = nullptr,
-                          bool audit = false, float fallback = 0.0f) {
+                          bool audit = false, float fallback = 0.0f, bool eval = false) {
   SampleArgs sa;
   sa.seed = s->seed;
   sa.log_std = policy_theta(p) + policy_params(p) - 2;
@@ -729,7 +735,7 @@ static int runner_step_on(racer_sim* s, racer_policy* p, racer_acts* a, float* s
   sa.step_add = add;
   int rc = forward_on(p, s->obs, a, st, &sa, 0);
   if (rc) return rc;
-  if (!sur) return sim_step_on(s, s->actions, s->reward, s->done, s->obs, nullptr, st);
+  if (!sur) return sim_step_on(s, s->actions, s->reward, s->done, s->obs, nullptr, st, eval);
   launch_advance(s->seg, s->state, s->actions, s->reward, s->done, s->obs, s->n, s->beams, s->ray, st);
   RACER_LAUNCHED();
   return surrogate_lidar(sur, s, s->obs, audit, fallback, st);
@@ -809,6 +815,110 @@ int racer_runner_audit_dynamics(racer_sim* s, racer_policy* p, racer_acts* a, fl
   RACER_TRY(cudaStreamSynchronize(st));
   if (rc) return rc;
   RACER_TRY(copy);
+  return 0;
+}
+
+// Totals of the per-car evaluation sums in a fixed order (one block): the
+// result does not depend on scheduling.
+__global__ void k_eval_total(const double* reward, const int* crash, int n, double* out) {
+  __shared__ double sr[1024];
+  __shared__ long long sc[1024];
+  double r = 0;
+  long long c = 0;
+  for (int i = threadIdx.x; i < n; i += blockDim.x) {
+    r += reward[i];
+    c += crash[i];
+  }
+  sr[threadIdx.x] = r;
+  sc[threadIdx.x] = c;
+  __syncthreads();
+  for (int w = blockDim.x / 2; w > 0; w >>= 1) {
+    if ((int)threadIdx.x < w) {
+      sr[threadIdx.x] += sr[threadIdx.x + w];
+      sc[threadIdx.x] += sc[threadIdx.x + w];
+    }
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) {
+    out[0] = sr[0];
+    out[1] = (double)sc[0];
+  }
+}
+
+int racer_runner_evaluate(racer_sim* s, racer_policy* p, racer_acts* a, float* scratch, int steps, int64_t step0,
+                          double* out) {
+  RACER_ARG(s && p && a && scratch && out && steps >= 1, "racer_runner_evaluate: bad argument");
+  RACER_ARG(a->cols == s->n && policy_inputs(p) == s->in_rows, "racer_runner_evaluate: sizes differ");
+  cudaStream_t st = s->st;
+  if (!s->eval_reward) {
+    int rc = 0;
+    if ((rc = dalloc(&s->eval_reward, s->n)) || (rc = dalloc(&s->eval_crash, s->n)) ||
+        (rc = dalloc(&s->eval_total, 2)))
+      return rc;
+  }
+  RACER_TRY(cudaMemsetAsync(s->eval_reward, 0, (size_t)s->n * sizeof(double), st));
+  RACER_TRY(cudaMemsetAsync(s->eval_crash, 0, (size_t)s->n * sizeof(int), st));
+  auto key = std::make_tuple((const void*)p, (const void*)a, (const void*)scratch, steps);
+  auto it = s->eval_graphs.find(key);
+  if (it == s->eval_graphs.end()) {
+    cudaGraph_t g;
+    RACER_TRY(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
+    int rc = 0;
+    for (int k = 0; k < steps && !rc; ++k)
+      rc = runner_step_on(s, p, a, scratch, 1, s->step_base, k, st, nullptr, false, 0.0f, true);
+    cudaError_t end = cudaStreamEndCapture(st, &g);
+    if (rc) return rc;
+    RACER_TRY(end);
+    cudaGraphExec_t exec;
+    cudaError_t inst = cudaGraphInstantiate(&exec, g, 0);
+    cudaGraphDestroy(g);
+    RACER_TRY(inst);
+    it = s->eval_graphs.emplace(key, exec).first;
+  }
+  k_set_i64<<<1, 32, 0, st>>>(s->step_base, step0);
+  RACER_LAUNCHED();
+  RACER_TRY(cudaGraphLaunch(it->second, st));
+  k_eval_total<<<1, 1024, 0, st>>>(s->eval_reward, s->eval_crash, s->n, s->eval_total);
+  RACER_LAUNCHED();
+  double host[2];
+  RACER_TRY(cudaMemcpyAsync(host, s->eval_total, sizeof host, cudaMemcpyDeviceToHost, st));
+  RACER_TRY(cudaStreamSynchronize(st));
+  out[0] = host[0] / ((double)s->n * steps);
+  out[1] = host[1] / (double)s->n;
+  return 0;
+}
+
+// [state | obs | actions | reward | done] of every car, row after row.
+__global__ void k_pack_snapshot(const float* state, const float* obs, const float* actions, const float* reward,
+                                const float* done, long n, int in_rows, float* out) {
+  const long total = (STATE + in_rows + 4) * n;
+  for (long q = (long)blockIdx.x * blockDim.x + threadIdx.x; q < total; q += (long)gridDim.x * blockDim.x) {
+    const long row = q / n, col = q % n;
+    float v;
+    if (row < STATE)
+      v = state[q];
+    else if (row < STATE + in_rows)
+      v = obs[q - STATE * n];
+    else if (row < STATE + in_rows + 2)
+      v = actions[q - (STATE + in_rows) * n];
+    else if (row == STATE + in_rows + 2)
+      v = reward[col];
+    else
+      v = done[col];
+    out[q] = v;
+  }
+}
+
+int racer_sim_snapshot(racer_sim* s, float* host, int synchronize) {
+  RACER_ARG(s && host, "racer_sim_snapshot: null argument");
+  const size_t count = (size_t)(STATE + s->in_rows + 4) * s->n;
+  if (!s->snapshot)
+    if (int rc = dalloc(&s->snapshot, count)) return rc;
+  k_pack_snapshot<<<4 * s->sms, 256, 0, s->st>>>(s->state, s->obs, s->actions, s->reward, s->done, s->n,
+                                                  s->in_rows, s->snapshot);
+  RACER_LAUNCHED();
+  RACER_TRY(cudaMemcpyAsync(host, s->snapshot, count * sizeof(float), cudaMemcpyDeviceToHost, s->st));
+  if (synchronize) RACER_TRY(cudaStreamSynchronize(s->st));
   return 0;
 }
 
@@ -931,6 +1041,8 @@ __global__ void k_sum_cols(const int32_t* iters, int n, int beams, int c0, int c
 static void drop_graphs(racer_sim* s) {
   for (auto& kv : s->graphs) cudaGraphExecDestroy(kv.second);
   for (auto& kv : s->surrogate_graphs) cudaGraphExecDestroy(kv.second);
+  for (auto& kv : s->eval_graphs) cudaGraphExecDestroy(kv.second);
+  s->eval_graphs.clear();
   s->graphs.clear();
   s->graph_kernels.clear();
   s->surrogate_graphs.clear();

@@ -11,9 +11,11 @@ namespace racer {
 // table; a one-track sim is a table of one.
 Segments single_segment(const TrackDev& t, int n, uint64_t seed);
 void launch_spawn(const Segments& g, float* state, float* actions, int n, cudaStream_t st);
-// ray [2, n] float4: the per-car lidar frame the physics kernel leaves for the lidar.
+// ray [2, n] float4: the per-car lidar frame the physics kernel leaves for the lidar. With
+// eval_reward / eval_crash [n] set, each car adds its reward and crash to them.
 void launch_advance(const Segments& g, float* state, const float* actions, float* reward, float* done, float* obs,
-                    int n, int beams, float4* ray, cudaStream_t st);
+                    int n, int beams, float4* ray, cudaStream_t st, double* eval_reward = nullptr,
+                    int* eval_crash = nullptr);
 void launch_lidar(const Segments& g, const LidarShape& shape, const float4* ray, float* obs, int n, int beams,
                   const float2* beam_dir, int* iters, cudaStream_t st);
 // The lidar of segment k alone (its one-track kernel), for per-segment launches on parallel streams.

@@ -29,6 +29,12 @@ struct racer_sim {
   std::vector<cudaEvent_t> join;
   cudaEvent_t fork = nullptr;
   unsigned* counters = nullptr;  // [MAX_SEGMENTS] unit counters of the dynamic lidar
+  // device-side evaluation: per-car reward (FP64) and crash sums, and the two totals
+  double* eval_reward = nullptr;
+  int* eval_crash = nullptr;
+  double* eval_total = nullptr;
+  std::map<std::tuple<const void*, const void*, const void*, int>, cudaGraphExec_t> eval_graphs;
+  float* snapshot = nullptr;  // [(STATE + IN + 4) * n] staging for one-copy snapshots
   int sms = 152;
   float2* beam_dir = nullptr;
   float4* ray = nullptr;  // [2, n] per-car lidar frame written by the physics kernel

@@ -298,8 +298,10 @@ __device__ __forceinline__ void advance_car(const TrackDev& t, float* s, const f
   ray[n + i] = make_float4(sh, along, across, (float)probe<LAYERS>(t, sx, sy, sz).layer);
 }
 
+// With eval_reward set, each car also adds its reward (FP64) and a crash
+// count to its own accumulators (racer eval's sums, kept on the device).
 __global__ void k_advance(const __grid_constant__ Segments g, float* s, const float* act, float* reward, float* done,
-                          float* obs, int n, int beams, float4* ray) {
+                          float* obs, int n, int beams, float4* ray, double* eval_reward, int* eval_crash) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
   const int k = segment_of(g, i);
@@ -310,6 +312,10 @@ __global__ void k_advance(const __grid_constant__ Segments g, float* s, const fl
     advance_car<2>(t, s, act, reward, done, obs, n, beams, g.seed[k], ray, i, i - g.car0[k]);
   else
     advance_car<0>(t, s, act, reward, done, obs, n, beams, g.seed[k], ray, i, i - g.car0[k]);
+  if (eval_reward) {
+    eval_reward[i] += (double)reward[i];
+    eval_crash[i] += done[i] == (float)CRASH;
+  }
 }
 
 // FP64 re-integration of racer/sim.mojo:189-213 (the 4 RK4 substeps) for
@@ -589,8 +595,9 @@ void launch_spawn(const Segments& g, float* state, float* actions, int n, cudaSt
 }
 
 void launch_advance(const Segments& g, float* state, const float* actions, float* reward, float* done, float* obs,
-                    int n, int beams, float4* ray, cudaStream_t st) {
-  k_advance<<<(n + 127) / 128, 128, 0, st>>>(g, state, actions, reward, done, obs, n, beams, ray);
+                    int n, int beams, float4* ray, cudaStream_t st, double* eval_reward, int* eval_crash) {
+  k_advance<<<(n + 127) / 128, 128, 0, st>>>(g, state, actions, reward, done, obs, n, beams, ray, eval_reward,
+                                             eval_crash);
 }
 
 int lidar_max_iters(const TrackDev& t) { return (int)ceilf(RANGE / (0.5f * t.cell)) + 2; }

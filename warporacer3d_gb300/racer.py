@@ -153,6 +153,16 @@ class Sim:
         call("racer_sim_sample", self.handle, output.c, log_std.c, actions.c, logp.c, value.c, int(deterministic),
              step)
 
+    def snapshot(self, out=None):
+        """state, obs, actions, reward, done of every car as one [(11 + IN + 4), n] float32 array
+        (main.mojo:94-124's serve snapshot), from one device-to-host copy."""
+        rows = STATE + self.IN + 4
+        if out is None:
+            out = np.empty((rows, self.n), np.float32)
+        assert out.dtype == np.float32 and out.size == rows * self.n and out.flags.c_contiguous
+        call("racer_sim_snapshot", self.handle, out.ctypes.data_as(ctypes.c_void_p), 1)
+        return out
+
     def set_lidar_shape(self, cars_per_block, wide=0, split=0, order=None, dynamic=0):
         """Lidar launch shape: cars per block (2, 4, 8), the 40-register variant (wide), per-segment
         launches on parallel streams (split), the segments' order (default: index order) and the
@@ -442,6 +452,28 @@ class Runner:
         self.synchronize()
         ms = (time.perf_counter() - start) * 1000 / steps
         return ms, self.sim.n * 1000 / ms
+
+    def evaluate_graph(self, steps, step0=0):
+        """main.mojo:70-80 on the device: reward per car-step and crashes per car over `steps`
+        deterministic steps replayed from one CUDA graph, with one read at the end."""
+        out = (ctypes.c_double * 2)()
+        call("racer_runner_evaluate", self.sim.handle, self.policy.handle, self.acts.handle, self.scratch.c, steps,
+             step0, out)
+        return out[0], out[1]
+
+    def serve_step(self, steer_pct, throttle_pct, reset, policy, tick):
+        """One request of the reference's serve loop (main.mojo:108-124), headless: optional reset,
+        then a deterministic policy step or the same manual action for every car, then the snapshot."""
+        if reset:
+            self.sim.reset()
+        if policy:
+            self.step(True, tick)
+        else:
+            act = np.empty((2, self.sim.n), np.float32)
+            act[0], act[1] = np.float32(steer_pct) / np.float32(100), np.float32(throttle_pct) / np.float32(100)
+            self.sim.actions.write(act)
+            self.sim.step(self.sim.actions, self.sim.reward, self.sim.done, self.sim.obs)
+        return self.sim.snapshot()
 
     def evaluate(self, steps):
         """main.mojo:70-80: reward per step and crashes per car, deterministic actions."""

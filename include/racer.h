@@ -164,7 +164,8 @@ int racer_policy_load(racer_policy* policy, const char* path, int* iteration);
 typedef struct racer_trainer racer_trainer;
 typedef struct {
   float *obs, *actions, *logp, *value, *reward, *done, *advantage; /* rollout storage */
-  float *x, *d3, *d2, *d1, *grad, *first, *second, *stats;         /* minibatch scratch, Adam, stats[5] */
+  float *x, *d3, *d2, *d1, *grad, *first, *second, *stats;         /* minibatch scratch (x: [4][IN, batch], the
+                                                                      four minibatches' inputs), Adam, stats[5] */
   racer_acts* acts;                                                  /* the minibatch activations */
   int batch;
 } racer_trainer_buffers;

@@ -574,7 +574,7 @@ int racer_trainer_create(int n, int beams, int rollout, void* stream, racer_trai
   size_t R = rollout, IN = tr->in_rows, B = tr->batch, P = (size_t)H * IN + H * HA + OUT * HA + 2;
   if ((rc = dalloc(&tr->obs, (R + 1) * IN * n)) || (rc = dalloc(&tr->actions, R * 2 * n)) ||
       (rc = dalloc(&tr->logp, R * n)) || (rc = dalloc(&tr->value, R * n)) || (rc = dalloc(&tr->reward, R * n)) ||
-      (rc = dalloc(&tr->done, R * n)) || (rc = dalloc(&tr->advantage, R * n)) || (rc = dalloc(&tr->x, IN * B)) ||
+      (rc = dalloc(&tr->done, R * n)) || (rc = dalloc(&tr->advantage, R * n)) || (rc = dalloc(&tr->x, MINIBATCHES * IN * B)) ||
       (rc = dalloc(&tr->d3, (OUT + 3) * B)) || (rc = dalloc(&tr->d2, (size_t)HA * B)) ||
       (rc = dalloc(&tr->d1, (size_t)HA * B)) || (rc = dalloc(&tr->grad, P)) || (rc = dalloc(&tr->first, P)) ||
       (rc = dalloc(&tr->second, P)) || (rc = dalloc(&tr->stats, STATS)) || (rc = dalloc(&tr->red, 4096))) {
@@ -667,17 +667,18 @@ int racer_trainer_rollout(racer_trainer* tr, racer_sim* s, racer_policy* p, race
   return 0;
 }
 
+// One minibatch on the inputs x[m] gathered beforehand (launch_gather_all).
 static int minibatch_on(racer_trainer* tr, racer_policy* p, int m, int use_moments, float adv_mean,
                         float adv_scale) {
   cudaStream_t st = tr->st;
   const int B = tr->batch, IN = tr->in_rows, P = policy_params(p);
   const float* logstd = policy_theta(p) + P - 2;
-  launch_gather(IN, tr->n, B, m, tr->obs, tr->x, st);
-  int rc = forward_on(p, tr->x, tr->acts, st);
+  const float* x = tr->x + (size_t)m * IN * B;
+  int rc = forward_on(p, x, tr->acts, st);
   if (rc) return rc;
   launch_loss(tr->n, B, m, tr->actions, tr->logp, tr->value, tr->advantage, tr->acts->o, logstd,
               tr->stats + ST_ADV, use_moments, adv_mean, adv_scale, tr->d3, st);
-  if ((rc = policy_backward(p, tr->x, B, tr->acts->h1, tr->acts->h2, tr->d3, tr->d2, tr->d1, tr->grad, st)))
+  if ((rc = policy_backward(p, x, B, tr->acts->h1, tr->acts->h2, tr->d3, tr->d2, tr->d1, tr->grad, st)))
     return rc;
   launch_rowsum(tr->d3 + (size_t)OUT * B, 2, B, B, tr->grad + P - 2, tr->red, 0, st);
   launch_rowsum(tr->grad, 1, P, P, tr->stats + ST_NORM, tr->red + 2048, 1, st);
@@ -688,6 +689,8 @@ static int minibatch_on(racer_trainer* tr, racer_policy* p, int m, int use_momen
 int racer_trainer_minibatch(racer_trainer* tr, racer_policy* p, int m, float adv_mean, float adv_scale) {
   RACER_ARG(tr && p && m >= 0 && m < MINIBATCHES, "racer_trainer_minibatch: bad argument");
   RACER_ARG(policy_inputs(p) == tr->in_rows, "racer_trainer_minibatch: policy and trainer sizes differ");
+  launch_gather_all(tr->in_rows, tr->n, tr->rollout, tr->batch, tr->obs, tr->x, tr->st);
+  RACER_LAUNCHED();
   return minibatch_on(tr, p, m, 0, adv_mean, adv_scale);
 }
 
@@ -697,6 +700,9 @@ int racer_trainer_update(racer_trainer* tr, racer_policy* p, float* kl) {
   cudaStream_t st = tr->st;
   const int P = policy_params(p);
   launch_moments(tr->advantage, (long)tr->rollout * tr->n, tr->stats, tr->red, st);
+  // the minibatches' samples are the same in every epoch: gather them once
+  launch_gather_all(tr->in_rows, tr->n, tr->rollout, tr->batch, tr->obs, tr->x, st);
+  RACER_LAUNCHED();
   for (int epoch = 0; epoch < EPOCHS; ++epoch) {
     for (int m = 0; m < MINIBATCHES; ++m) {
       int rc = minibatch_on(tr, p, (m + epoch) % MINIBATCHES, 1, 0.0f, 1.0f);

@@ -21,11 +21,14 @@ void launch_lidar(const Segments& g, const LidarShape& shape, const float4* ray,
 // The lidar of segment k alone (its one-track kernel), for per-segment launches on parallel streams.
 void launch_lidar_segment(const Segments& g, int k, const LidarShape& shape, const float4* ray, float* obs, int n,
                           int beams, const float2* beam_dir, int* iters, cudaStream_t st);
-// One track, default shape (surrogate labels and fallback). With `list` set,
-// only the cars list[0 .. *list_count) (list_max at most) are traced.
+// One track, default shape (surrogate labels).
 void launch_lidar(const TrackDev& t, const float4* ray, float* obs, int n, int beams, const float2* beam_dir,
-                  int* iters, cudaStream_t st, const int* list = nullptr, const int* list_count = nullptr,
-                  int list_max = 0);
+                  int* iters, cudaStream_t st);
+// Only the cars list[0 .. *list_count) (at most list_max; the count is read on the device): a
+// persistent grid pulling (car, beam group) units from `counter` (zeroed here). sms = SM count.
+void launch_lidar_list(const TrackDev& t, const float4* ray, float* obs, int n, int beams, const float2* beam_dir,
+                       const int* list, const int* list_count, int list_max, unsigned* counter, int sms,
+                       cudaStream_t st);
 bool lidar_shape_ok(const LidarShape& shape);
 // Cars whose smallest predicted range (ordered uint bits of a nonnegative float) is below threshold.
 void launch_select_cars(const unsigned* minr, int n, float threshold, int* list, int* count, cudaStream_t st);
@@ -46,6 +49,8 @@ void launch_policy_init(int in, uint64_t seed, float* theta, cudaStream_t st);
 void launch_gae(int n, int rollout, const float* reward, const float* done, const float* value,
                 const float* last_value, float* advantage, cudaStream_t st);
 void launch_gather(int in, int n, int batch, int m, const float* obs, float* x, cudaStream_t st);
+// x [4][in, batch]: every minibatch's inputs from rollout storage obs [rollout + 1][in, n] in one pass.
+void launch_gather_all(int in, int n, int rollout, int batch, const float* obs, float* x, cudaStream_t st);
 void launch_loss(int n, int batch, int m, const float* actions, const float* logp, const float* value,
                  const float* advantage, const float* o, const float* log_std, const float* adv_moments,
                  int use_moments, float adv_mean, float adv_scale, float* d3, cudaStream_t st);

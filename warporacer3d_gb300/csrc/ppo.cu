@@ -164,6 +164,23 @@ void launch_gather(int in, int n, int batch, int m, const float* obs, float* x, 
   k_gather<<<grid, 256, 0, st>>>(in, n, batch, m, obs, x);
 }
 
+// All four minibatches at once (racer/ppo.mojo:259-268's sample order
+// s = b * 4 + m): obs[t][r][i] -> x[m][r][b] with s = t * n + i, m = s % 4,
+// b = s / 4, so every rollout row is read once, coalesced.
+__global__ void k_gather_all(int in, int n, int batch, const float* __restrict__ obs, float* __restrict__ x) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const int r = blockIdx.y, t = blockIdx.z;
+  const long s = (long)t * n + i;
+  x[((s & (MINIBATCHES - 1)) * in + r) * (long)batch + (s >> 2)] = obs[((long)t * in + r) * n + i];
+}
+
+void launch_gather_all(int in, int n, int rollout, int batch, const float* obs, float* x, cudaStream_t st) {
+  static_assert(MINIBATCHES == 4, "the sample split assumes four minibatches");
+  dim3 grid((n + 255) / 256, in, rollout);
+  k_gather_all<<<grid, 256, 0, st>>>(in, n, batch, obs, x);
+}
+
 void launch_loss(int n, int batch, int m, const float* actions, const float* logp, const float* value,
                  const float* advantage, const float* o, const float* log_std, const float* adv_moments,
                  int use_moments, float adv_mean, float adv_scale, float* d3, cudaStream_t st) {

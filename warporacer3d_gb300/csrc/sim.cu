@@ -481,21 +481,25 @@ __global__ void __launch_bounds__(CARS * 32, lidar_min_blocks(CARS, WIDE))
 // (car, 32-beam group) units from `counter` (zero at launch) one at a time,
 // so no warp holds a block slot waiting for a sibling and the last wave has
 // no tail of idle slots.
-template <int LAYERS, bool WIDE>
+// With LIST, the cars are list[0 .. *list_count) (the surrogate's fallback
+// cars, counted on the device), whatever their number.
+template <int LAYERS, bool WIDE, bool LIST>
 __global__ void __launch_bounds__(128, lidar_min_blocks(4, WIDE))
     k_lidar_dynamic(TrackDev t, int max_iters, const float4* __restrict__ ray, float* obs, int n, int c0, int c1,
-                    int beams, const float2* __restrict__ beam_dir, int* iters, unsigned* counter) {
+                    int beams, const float2* __restrict__ beam_dir, int* iters, unsigned* counter,
+                    const int* __restrict__ list, const int* list_count) {
   const int groups = (beams + 31) >> 5;
-  const unsigned total = (unsigned)(c1 - c0) * (unsigned)groups;
+  const unsigned cars = LIST ? (unsigned)min(max(*list_count, 0), n) : (unsigned)(c1 - c0);
+  const unsigned total = cars * (unsigned)groups;
   const int lane = threadIdx.x & 31;
   for (;;) {
     unsigned unit = 0;
     if (lane == 0) unit = atomicAdd(counter, 1u);
     unit = __shfl_sync(0xffffffffu, unit, 0);
     if (unit >= total) break;
-    const int car = c0 + (int)(unit / (unsigned)groups);
+    const int car = LIST ? list[unit / (unsigned)groups] : c0 + (int)(unit / (unsigned)groups);
     const int beam = (int)(unit % (unsigned)groups) * 32 + lane;
-    if (beam < beams) trace<LAYERS>(t, ray, obs, n, beam_dir, max_iters, iters, car, beam);
+    if (beam < beams && (unsigned)car < (unsigned)n) trace<LAYERS>(t, ray, obs, n, beam_dir, max_iters, iters, car, beam);
   }
 }
 
@@ -640,8 +644,8 @@ static void lidar_dynamic(const TrackDev& t, int max_iters, const float4* ray, f
   if (units <= 0) return;
   const long blocks = std::min<long>((long)sms * lidar_min_blocks(4, WIDE), (units + 3) / 4);
   cudaMemsetAsync(counter, 0, sizeof(unsigned), st);
-  k_lidar_dynamic<LAYERS, WIDE>
-      <<<(unsigned)blocks, 128, 0, st>>>(t, max_iters, ray, obs, n, c0, c1, beams, beam_dir, iters, counter);
+  k_lidar_dynamic<LAYERS, WIDE, false><<<(unsigned)blocks, 128, 0, st>>>(t, max_iters, ray, obs, n, c0, c1, beams,
+                                                                          beam_dir, iters, counter, nullptr, nullptr);
 }
 
 template <int CARS, bool WIDE>
@@ -714,25 +718,27 @@ void launch_lidar_segment(const Segments& g, int k, const LidarShape& shape, con
 }
 
 void launch_lidar(const TrackDev& t, const float4* ray, float* obs, int n, int beams, const float2* beam_dir,
-                  int* iters, cudaStream_t st, const int* list, const int* list_count, int list_max) {
+                  int* iters, cudaStream_t st) {
+  launch_lidar(single_segment(t, n, 0), LidarShape{}, ray, obs, n, beams, beam_dir, iters, st);
+}
+
+void launch_lidar_list(const TrackDev& t, const float4* ray, float* obs, int n, int beams, const float2* beam_dir,
+                       const int* list, const int* list_count, int list_max, unsigned* counter, int sms,
+                       cudaStream_t st) {
+  const long units = (long)list_max * ((beams + 31) / 32);
+  if (units <= 0) return;
+  const long blocks = std::min<long>((long)sms * lidar_min_blocks(4, false), (units + 3) / 4);
   const int max_iters = lidar_max_iters(t);
-  if (!list) {
-    launch_lidar(single_segment(t, n, 0), LidarShape{}, ray, obs, n, beams, beam_dir, iters, st);
-    return;
-  }
-  // a listed subset: a grid of about eight blocks per SM strides over the list
-  constexpr int CARS = 4;
-  dim3 grid(std::min((list_max + CARS - 1) / CARS, 16 * 152 / ((beams + 31) / 32) + 1), (beams + 31) / 32);
-  if (grid.x == 0) return;
+  cudaMemsetAsync(counter, 0, sizeof(unsigned), st);
   if (t.layers == 1)
-    k_lidar_track<1, CARS, false, true>
-        <<<grid, CARS * 32, 0, st>>>(t, max_iters, ray, obs, n, 0, n, beams, beam_dir, iters, list, list_count);
+    k_lidar_dynamic<1, false, true><<<(unsigned)blocks, 128, 0, st>>>(t, max_iters, ray, obs, n, 0, n, beams, beam_dir,
+                                                                     nullptr, counter, list, list_count);
   else if (t.layers == 2)
-    k_lidar_track<2, CARS, false, true>
-        <<<grid, CARS * 32, 0, st>>>(t, max_iters, ray, obs, n, 0, n, beams, beam_dir, iters, list, list_count);
+    k_lidar_dynamic<2, false, true><<<(unsigned)blocks, 128, 0, st>>>(t, max_iters, ray, obs, n, 0, n, beams, beam_dir,
+                                                                     nullptr, counter, list, list_count);
   else
-    k_lidar_track<0, CARS, false, true>
-        <<<grid, CARS * 32, 0, st>>>(t, max_iters, ray, obs, n, 0, n, beams, beam_dir, iters, list, list_count);
+    k_lidar_dynamic<0, false, true><<<(unsigned)blocks, 128, 0, st>>>(t, max_iters, ray, obs, n, 0, n, beams, beam_dir,
+                                                                     nullptr, counter, list, list_count);
 }
 
 __global__ void k_select_cars(const unsigned* minr, int n, unsigned threshold_bits, int* list, int* count) {

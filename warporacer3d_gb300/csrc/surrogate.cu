@@ -412,6 +412,7 @@ struct racer_surrogate {
   unsigned* minr = nullptr;  // [n] smallest predicted range per car (uint bits)
   int* list = nullptr;       // [n] fallback cars
   int* list_count = nullptr;
+  unsigned* list_units = nullptr;  // unit counter of the fallback lidar
   float* exact = nullptr;    // [4 + beams, n] audit ranges
   double* rsums = nullptr;   // audit sum |e|, sum e^2 (metres)
   unsigned* rmax = nullptr;
@@ -654,8 +655,8 @@ int racer_surrogate_destroy(racer_surrogate* s) {
     cudaFree(p);
   free_acts(&s->train);
   free_acts(&s->infer);
-  for (void* p : {(void*)s->minr, (void*)s->list, (void*)s->list_count, (void*)s->exact, (void*)s->rsums,
-                  (void*)s->rmax, (void*)s->rcount})
+  for (void* p : {(void*)s->minr, (void*)s->list, (void*)s->list_count, (void*)s->list_units, (void*)s->exact,
+                  (void*)s->rsums, (void*)s->rmax, (void*)s->rcount})
     cudaFree(p);
   delete s;
   return 0;
@@ -850,7 +851,7 @@ int surrogate_prepare(racer_surrogate* s, racer_sim* sim) {
   SURR_CHECK((gemm_configure<256, EpiTanhOut>()));
   SURR_CHECK((gemm_configure<256, EpiInfer>()));
   if ((rc = make_acts(s, &s->infer, n, false)) || (rc = salloc(&s->minr, (size_t)n)) ||
-      (rc = salloc(&s->list, (size_t)n)) || (rc = salloc(&s->list_count, 1)) ||
+      (rc = salloc(&s->list, (size_t)n)) || (rc = salloc(&s->list_count, 1)) || (rc = salloc(&s->list_units, 1)) ||
       (rc = salloc(&s->exact, (size_t)(4 + sim->beams) * n)) || (rc = salloc(&s->rsums, 2)) ||
       (rc = salloc(&s->rmax, 1)) || (rc = salloc(&s->rcount, 2)))
     return rc;
@@ -889,7 +890,8 @@ int surrogate_lidar(racer_surrogate* s, racer_sim* sim, float* obs, bool audit, 
   } else if (fallback > 0.0f) {
     SURR_CHECK(cudaMemsetAsync(s->list_count, 0, sizeof(int), st));
     launch_select_cars(s->minr, n, fallback, s->list, s->list_count, st);
-    launch_lidar(sim->t, sim->ray, obs, n, beams, sim->beam_dir, nullptr, st, s->list, s->list_count, n);
+    launch_lidar_list(sim->t, sim->ray, obs, n, beams, sim->beam_dir, s->list, s->list_count, n, s->list_units,
+                      sim->sms, st);
     k_count_fallback<<<1, 32, 0, st>>>(s->list_count, s->rcount + 1);
   }
   SURR_CHECK(cudaGetLastError());

@@ -282,7 +282,7 @@ class Trainer:
         self.actions = DevArray(b.actions, (R, 2, n), owner=self, stream=s)
         for name in ("logp", "value", "reward", "done", "advantage"):
             setattr(self, name, DevArray(getattr(b, name), (R, n), owner=self, stream=s))
-        self.x = DevArray(b.x, (IN, B), owner=self, stream=s)
+        self.x = DevArray(b.x, (MINIBATCHES, IN, B), owner=self, stream=s)
         self.d3 = DevArray(b.d3, (OUT + 3, B), owner=self, stream=s)
         self.d2 = DevArray(b.d2, (HA, B), owner=self, stream=s)
         self.d1 = DevArray(b.d1, (HA, B), owner=self, stream=s)

@@ -249,30 +249,41 @@ def batched_section(torch, W, stream, flush):
 TRAIN_TRACK, TRAIN_CARS, TRAIN_ROLLOUT, TRAIN_BEAMS = "bank", 16384, 64, 108
 
 
+TRAIN_SEEDS = (42, 43, 44)
+
+
 def training_section(W, iterations):
-    """PPO on bank, 16384 cars x 64-step rollouts (batch 262144): BF16 tensor-core products vs a
-    same-seed FP32 run (racer/ppo.mojo:187-337 per iteration; main.mojo:54-68 loop)."""
+    """PPO on bank, 16384 cars x 64-step rollouts (batch 262144): BF16 tensor-core products vs FP32 from the
+    same seeds (racer/ppo.mojo:187-337 per iteration; main.mojo:54-68 loop). Runs differ in accumulation
+    order, so single trajectories diverge chaotically; three seeds per precision are reported."""
     out = {"workload": f"{TRAIN_TRACK}, {TRAIN_CARS} cars x {TRAIN_ROLLOUT}-step rollouts, {TRAIN_BEAMS} beams, "
-                       f"{iterations} iterations of rollout + GAE + 4 epochs x 4 minibatches of clipped PPO + Adam"}
+                       f"{iterations} iterations of rollout + GAE + 4 epochs x 4 minibatches of clipped PPO + Adam, "
+                       f"seeds {list(TRAIN_SEEDS)}"}
     track = W.track(TRAIN_TRACK)
     for precision in ("bf16", "fp32"):
-        runner = W.Runner(track, TRAIN_CARS, beams=TRAIN_BEAMS, seed=42, policy_seed=42)
-        runner.policy.set_precision(precision)
-        trainer = W.Trainer(TRAIN_CARS, beams=TRAIN_BEAMS, rollout=TRAIN_ROLLOUT, stream=runner.sim.stream)
-        rewards, kls = [], []
-        t0 = time.perf_counter()
-        for it in range(iterations):
-            rewards.append(trainer.rollout(runner.sim, runner.policy, runner.acts, it))
-            kls.append(trainer.update(runner.policy))
-        dt = time.perf_counter() - t0
-        k = max(1, min(20, iterations // 5))
-        out[precision] = {"training_transitions_per_s": TRAIN_CARS * TRAIN_ROLLOUT * iterations / dt,
-                          "reward_per_step_first": float(np.mean(rewards[:k])),
-                          "reward_per_step_last": float(np.mean(rewards[-k:])),
-                          "kl_last": float(kls[-1]), "finite": bool(np.isfinite(rewards).all() and np.isfinite(kls).all()),
-                          "seconds": dt}
-    out["return_ratio_bf16_vs_fp32"] = out["bf16"]["reward_per_step_last"] / out["fp32"]["reward_per_step_last"] \
-        if out["fp32"]["reward_per_step_last"] else None
+        runs = []
+        for seed in TRAIN_SEEDS:
+            runner = W.Runner(track, TRAIN_CARS, beams=TRAIN_BEAMS, seed=seed, policy_seed=seed)
+            runner.policy.set_precision(precision)
+            trainer = W.Trainer(TRAIN_CARS, beams=TRAIN_BEAMS, rollout=TRAIN_ROLLOUT, stream=runner.sim.stream)
+            rewards, kls = [], []
+            t0 = time.perf_counter()
+            for it in range(iterations):
+                rewards.append(trainer.rollout(runner.sim, runner.policy, runner.acts, it))
+                kls.append(trainer.update(runner.policy))
+            dt = time.perf_counter() - t0
+            k = max(1, min(20, iterations // 5))
+            runs.append({"seed": seed, "training_transitions_per_s": TRAIN_CARS * TRAIN_ROLLOUT * iterations / dt,
+                         "reward_per_step_first": float(np.mean(rewards[:k])),
+                         "reward_per_step_last": float(np.mean(rewards[-k:])), "kl_last": float(kls[-1]),
+                         "finite": bool(np.isfinite(rewards).all() and np.isfinite(kls).all()), "seconds": dt})
+            del trainer, runner
+        out[precision] = {"training_transitions_per_s": float(np.mean([r["training_transitions_per_s"] for r in runs])),
+                          "reward_per_step_last_mean": float(np.mean([r["reward_per_step_last"] for r in runs])),
+                          "reward_per_step_first_mean": float(np.mean([r["reward_per_step_first"] for r in runs])),
+                          "runs": runs}
+    last16, last32 = out["bf16"]["reward_per_step_last_mean"], out["fp32"]["reward_per_step_last_mean"]
+    out["return_ratio_bf16_vs_fp32"] = last16 / last32 if last32 else None
     return out
 
 

@@ -55,17 +55,28 @@ __device__ __forceinline__ float bf16_round(float v) { return __bfloat162float(_
 // operands a tensor-core product would see; FP32 accumulation), written as
 // FP32 d2, d1 [65, cols] plus the BF16 operand copies of the weight-gradient
 // GEMMs d2f, d1f [64, ld] and d3f [16, ld] (feature-major).
-__global__ void __launch_bounds__(128) k_dgrad(int in, const float* __restrict__ theta, const float* __restrict__ d3,
-                                               const float* __restrict__ h1, const float* __restrict__ h2, float* d2,
-                                               float* d1, int cols, bf16* d1f, bf16* d2f, bf16* d3f, int ld) {
-  __shared__ __align__(16) float w1t[HA][H];  // w1t[k][r] = bf16(W1[r][k])
+constexpr int DGRAD_THREADS = 128;
+constexpr int DGRAD_SMEM = (HA * H + HA * DGRAD_THREADS) * 4;
+
+__global__ void __launch_bounds__(DGRAD_THREADS) k_dgrad(int in, const float* __restrict__ theta,
+                                                         const float* __restrict__ d3, const float* __restrict__ h1,
+                                                         const float* __restrict__ h2, float* d2, float* d1, int cols,
+                                                         bf16* d1f, bf16* d2f, bf16* d3f, int ld) {
+  extern __shared__ __align__(16) float dg_smem[];
+  float(*w1t)[H] = reinterpret_cast<float(*)[H]>(dg_smem);                          // w1t[k][r] = bf16(W1[r][k])
+  float(*h1s)[DGRAD_THREADS] = reinterpret_cast<float(*)[DGRAD_THREADS]>(dg_smem + HA * H);  // this thread's h1
+  const int j = blockIdx.x * blockDim.x + threadIdx.x;
+  // every h1 load of this sample in flight at once; each thread reads back only its own column
+  if (j < cols) {
+#pragma unroll
+    for (int k = 0; k < HA; ++k) h1s[k][threadIdx.x] = h1[(long)k * cols + j];
+  }
   const float* w1 = theta + H * in;
   for (int e = threadIdx.x; e < H * HA; e += blockDim.x) {
     const int r = e / HA, k = e % HA;
     w1t[k][r] = bf16_round(w1[e]);
   }
   __syncthreads();
-  const int j = blockIdx.x * blockDim.x + threadIdx.x;
   if (j >= cols) return;
   const float* w2 = theta + H * in + H * HA;
   const float e0 = d3[j], e1 = d3[(long)cols + j], e2 = d3[2L * cols + j];
@@ -85,33 +96,49 @@ __global__ void __launch_bounds__(128) k_dgrad(int in, const float* __restrict__
       b[k] = __bfloat162float(vb);
     }
   }
+  constexpr int KU = 5;  // 65 = 13 x 5 output units per pass: five independent loads of h1 in flight
 #pragma unroll 1
-  for (int k = 0; k < HA; ++k) {
-    const float4* w = reinterpret_cast<const float4*>(w1t[k]);
-    float acc = 0.0f;
+  for (int k0 = 0; k0 < HA; k0 += KU) {
+    float acc[KU], a[KU];
+#pragma unroll
+    for (int u = 0; u < KU; ++u) {
+      a[u] = h1s[k0 + u][threadIdx.x];
+      acc[u] = 0.0f;
+    }
 #pragma unroll
     for (int q = 0; q < H / 4; ++q) {
-      const float4 c = w[q];
-      acc += c.x * b[4 * q] + c.y * b[4 * q + 1] + c.z * b[4 * q + 2] + c.w * b[4 * q + 3];
+#pragma unroll
+      for (int u = 0; u < KU; ++u) {
+        const float4 c = reinterpret_cast<const float4*>(w1t[k0 + u])[q];
+        acc[u] += c.x * b[4 * q] + c.y * b[4 * q + 1] + c.z * b[4 * q + 2] + c.w * b[4 * q + 3];
+      }
     }
-    const float a = h1[(long)k * cols + j];
-    const float g = acc * (1.0f - a * a);
-    d1[(long)k * cols + j] = g;
-    if (k < H) d1f[(long)k * ld + j] = __float2bfloat16_rn(g);
+#pragma unroll
+    for (int u = 0; u < KU; ++u) {
+      const int k = k0 + u;
+      const float g = acc[u] * (1.0f - a[u] * a[u]);
+      d1[(long)k * cols + j] = g;
+      if (k < H) d1f[(long)k * ld + j] = __float2bfloat16_rn(g);
+    }
   }
 }
 
 // grad[n * ldg + m] = sum_z P[z][m][n] for m < mreal, n < nreal (the GEMM row
-// m is the weight's input index, column n its output row). Consecutive
-// threads read consecutive n of each partial.
+// m is the weight's input index, column n its output row). One warp per
+// element: lane l sums the partials z = l, l + 32, ... in order, then a fixed
+// shuffle tree adds the lanes (deterministic).
 __global__ void k_wgrad_reduce(const float* __restrict__ P, int splits, int mrows, int nreal, int mreal,
                                float* grad, int ldg) {
   const long total = (long)mreal * nreal;
-  for (long e = (long)blockIdx.x * blockDim.x + threadIdx.x; e < total; e += (long)gridDim.x * blockDim.x) {
+  const int lane = threadIdx.x & 31;
+  const long warps = ((long)gridDim.x * blockDim.x) >> 5;
+  for (long e = ((long)blockIdx.x * blockDim.x + threadIdx.x) >> 5; e < total; e += warps) {
     const int m = (int)(e / nreal), n = (int)(e % nreal);
     float acc = 0.0f;
-    for (int z = 0; z < splits; ++z) acc += P[((long)z * mrows + m) * nreal + n];
-    grad[(long)n * ldg + m] = acc;
+    for (int z = lane; z < splits; z += 32) acc += P[((long)z * mrows + m) * nreal + n];
+#pragma unroll
+    for (int off = 16; off; off >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, off);
+    if (lane == 0) grad[(long)n * ldg + m] = acc;
   }
 }
 
@@ -188,8 +215,8 @@ int wgrad(BackwardWork* w, const CUtensorMap& ta, const CUtensorMap& tb, int mro
   EpiSplitF32 epi{w->scratch, (long)mrows * nreal, mrows, nreal};
   BW_CHECK(gemm_launch<BN>(ta, tb, mrows, nreal, kblocks, splits, epi, err, st));
   const long total = (long)mreal * nreal;
-  k_wgrad_reduce<<<(unsigned)std::min<long>((total + 255) / 256, 1024), 256, 0, st>>>(w->scratch, splits, mrows,
-                                                                                        nreal, mreal, grad, ldg);
+  k_wgrad_reduce<<<(unsigned)std::min<long>((total + 7) / 8, 4096), 256, 0, st>>>(w->scratch, splits, mrows, nreal,
+                                                                                     mreal, grad, ldg);
   BW_CHECK(cudaGetLastError());
   return 0;
 }
@@ -207,7 +234,13 @@ int backward_tc(BackwardWork* w, const float* theta, const float* x, const float
   k_rows_bf16<<<dim3(gx, in), 256, 0, st>>>(x, in, cols, w->xb, ld);
   k_rows_bf16<<<dim3(gx, HA), 256, 0, st>>>(h1, HA, cols, w->h1b, ld);
   k_rows_bf16<<<dim3(gx, HA), 256, 0, st>>>(h2, HA, cols, w->h2b, ld);
-  k_dgrad<<<(cols + 127) / 128, 128, 0, st>>>(in, theta, d3, h1, h2, d2, d1, cols, w->d1f, w->d2f, w->d3f, ld);
+  static bool dgrad_configured = false;
+  if (!dgrad_configured) {
+    BW_CHECK(cudaFuncSetAttribute(k_dgrad, cudaFuncAttributeMaxDynamicSharedMemorySize, DGRAD_SMEM));
+    dgrad_configured = true;
+  }
+  k_dgrad<<<(cols + DGRAD_THREADS - 1) / DGRAD_THREADS, DGRAD_THREADS, DGRAD_SMEM, st>>>(
+      in, theta, d3, h1, h2, d2, d1, cols, w->d1f, w->d2f, w->d3f, ld);
   BW_CHECK(cudaGetLastError());
   int rc;
   if ((rc = wgrad<64>(w, w->txb, w->td1f, in, H, in, grad, in, err, st))) return rc;

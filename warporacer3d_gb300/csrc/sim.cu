@@ -492,14 +492,17 @@ __global__ void __launch_bounds__(128, lidar_min_blocks(4, WIDE))
   const unsigned cars = LIST ? (unsigned)min(max(*list_count, 0), n) : (unsigned)(c1 - c0);
   const unsigned total = cars * (unsigned)groups;
   const int lane = threadIdx.x & 31;
-  for (;;) {
-    unsigned unit = 0;
-    if (lane == 0) unit = atomicAdd(counter, 1u);
-    unit = __shfl_sync(0xffffffffu, unit, 0);
-    if (unit >= total) break;
+  // the next unit is claimed before the current one is traced, so the atomic's
+  // round trip overlaps the march
+  unsigned next = 0;
+  if (lane == 0) next = atomicAdd(counter, 1u);
+  unsigned unit = __shfl_sync(0xffffffffu, next, 0);
+  while (unit < total) {
+    if (lane == 0) next = atomicAdd(counter, 1u);
     const int car = LIST ? list[unit / (unsigned)groups] : c0 + (int)(unit / (unsigned)groups);
     const int beam = (int)(unit % (unsigned)groups) * 32 + lane;
     if (beam < beams && (unsigned)car < (unsigned)n) trace<LAYERS>(t, ray, obs, n, beam_dir, max_iters, iters, car, beam);
+    unit = __shfl_sync(0xffffffffu, next, 0);
   }
 }
 
@@ -727,17 +730,18 @@ void launch_lidar_list(const TrackDev& t, const float4* ray, float* obs, int n, 
                        cudaStream_t st) {
   const long units = (long)list_max * ((beams + 31) / 32);
   if (units <= 0) return;
-  const long blocks = std::min<long>((long)sms * lidar_min_blocks(4, false), (units + 3) / 4);
+  // the 40-register variant: no spills with the list indirection
+  const long blocks = std::min<long>((long)sms * lidar_min_blocks(4, true), (units + 3) / 4);
   const int max_iters = lidar_max_iters(t);
   cudaMemsetAsync(counter, 0, sizeof(unsigned), st);
   if (t.layers == 1)
-    k_lidar_dynamic<1, false, true><<<(unsigned)blocks, 128, 0, st>>>(t, max_iters, ray, obs, n, 0, n, beams, beam_dir,
+    k_lidar_dynamic<1, true, true><<<(unsigned)blocks, 128, 0, st>>>(t, max_iters, ray, obs, n, 0, n, beams, beam_dir,
                                                                      nullptr, counter, list, list_count);
   else if (t.layers == 2)
-    k_lidar_dynamic<2, false, true><<<(unsigned)blocks, 128, 0, st>>>(t, max_iters, ray, obs, n, 0, n, beams, beam_dir,
+    k_lidar_dynamic<2, true, true><<<(unsigned)blocks, 128, 0, st>>>(t, max_iters, ray, obs, n, 0, n, beams, beam_dir,
                                                                      nullptr, counter, list, list_count);
   else
-    k_lidar_dynamic<0, false, true><<<(unsigned)blocks, 128, 0, st>>>(t, max_iters, ray, obs, n, 0, n, beams, beam_dir,
+    k_lidar_dynamic<0, true, true><<<(unsigned)blocks, 128, 0, st>>>(t, max_iters, ray, obs, n, 0, n, beams, beam_dir,
                                                                      nullptr, counter, list, list_count);
 }
 

@@ -53,6 +53,7 @@ def parse():
     ap.add_argument("--surrogate-only", action="store_true", help="print only the surrogate section")
     ap.add_argument("--no-training", action="store_true")
     ap.add_argument("--no-batched", action="store_true")
+    ap.add_argument("--no-config1", action="store_true")
     ap.add_argument("--batched-only", action="store_true", help="print only the batched multi-track section")
     ap.add_argument("--training-iterations", type=int, default=300)
     ap.add_argument("--surrogate-train-steps", type=int, default=None,
@@ -121,14 +122,14 @@ def dram_traffic_per_launch():
     return None
 
 
-def cpu_baseline(track, seconds=12.0, max_steps=200, threads=None):
+def cpu_baseline(track, seconds=12.0, max_steps=200, threads=None, cars=CARS, beams=BEAMS, name=TRACK, seed=42):
     """The CPU restatement (oracle) on this host's cores: Runner steps of the same workload until `seconds`."""
     import oracle as O
     threads = threads or os.cpu_count() or 1
-    sim = O.Sim(track, CARS, 42, beams=BEAMS, threads=threads)
-    pol = O.Policy(42, beams=BEAMS, threads=threads)
-    acts = O.Activations(CARS)
-    logp, value = np.zeros(CARS, np.float32), np.zeros(CARS, np.float32)
+    sim = O.Sim(track, cars, seed, beams=beams, threads=threads)
+    pol = O.Policy(42, beams=beams, threads=threads)
+    acts = O.Activations(cars)
+    logp, value = np.zeros(cars, np.float32), np.zeros(cars, np.float32)
     sim.reset()
     start = time.perf_counter()
     steps = 0
@@ -138,9 +139,36 @@ def cpu_baseline(track, seconds=12.0, max_steps=200, threads=None):
         sim.step(sim.actions, sim.reward, sim.done, sim.obs)
         steps += 1
     dt = time.perf_counter() - start
-    return {"value": CARS * steps / dt, "unit": "env-steps/s", "cores": threads, "kind": "port",
-            "sample": f"{steps} env steps of {CARS} cars on {TRACK} at {BEAMS} beams (Runner.step: policy forward, "
+    return {"value": cars * steps / dt, "unit": "env-steps/s", "cores": threads, "kind": "port",
+            "sample": f"{steps} env steps of {cars} cars on {name} at {beams} beams (Runner.step: policy forward, "
                       f"sampling, physics, lidar) in {dt:.1f} s"}
+
+
+def config1_section(torch, W, stream):
+    """The reference's CPU-runnable benchmark, `racer benchmark ramp cpu 1024 1000` (main.mojo:82-92): ramp,
+    1024 cars, 108 beams, sim seed 0, policy seed 42, 10 warm-up policy steps, then 1000 timed ones; on the
+    GPU replayed from one CUDA graph (device-timed) and as the reference's host loop of per-step calls,
+    and the CPU restatement on all host cores for a bounded sample."""
+    track = W.track("ramp")
+    run = W.Runner(track, 1024, beams=108, seed=0, policy_seed=42, stream=stream)
+    for t in range(10):
+        run.step(False, t)
+    run.rollout(1000, False, 10)  # capture
+    torch.cuda.synchronize()
+    a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    with torch.cuda.stream(stream):
+        a.record(stream)
+        run.rollout(1000, False, 1010)
+        b.record(stream)
+    torch.cuda.synchronize()
+    graph_rate = 1024 * 1000 / (a.elapsed_time(b) / 1000.0)
+    loop_ms, loop_rate = run.benchmark(1000, warmup=10)
+    cpu = cpu_baseline(track, seconds=10.0, max_steps=1000, cars=1024, beams=108, name="ramp", seed=0)
+    return {"workload": "ramp, 1024 cars, 108 beams, 1000 policy steps after 10 warm-up (racer benchmark ramp "
+                        "cpu 1024 1000)",
+            "gpu_graph_env_steps_per_s": graph_rate, "gpu_step_loop_env_steps_per_s": loop_rate,
+            "gpu_step_loop_ms_per_step": loop_ms, "cpu_env_steps_per_s": cpu["value"], "cpu_cores": cpu["cores"],
+            "cpu_sample": cpu["sample"], "gpu_graph_vs_cpu": graph_rate / cpu["value"]}
 
 
 SURR_CARS, SURR_STEPS, SURR_REPS, SURR_TRAIN_STEPS = 65536, 32, 3, 20000
@@ -317,9 +345,8 @@ def run_reference(args, rank, world):
 
 def main():
     args = parse()
-    rank = int(os.environ.get("RANK", "0"))
-    world = int(os.environ.get("WORLD_SIZE", "1"))
-    local = int(os.environ.get("LOCAL_RANK", "0"))
+    from warporacer3d_gb300.replicas import max_over_ranks, replica_seed, topology, whole_job_rate
+    rank, world, local = topology()
     if args.impl == "reference":
         return run_reference(args, rank, world)
 
@@ -343,7 +370,7 @@ def main():
         steps = args.surrogate_train_steps if args.surrogate_train_steps is not None else SURR_TRAIN_STEPS
         print(json.dumps({"surrogate": surrogate_section(torch, W, track, stream, flush, steps)}), flush=True)
         return
-    runner = W.Runner(track, CARS, beams=BEAMS, seed=42 + rank, policy_seed=42, stream=stream)
+    runner = W.Runner(track, CARS, beams=BEAMS, seed=replica_seed(42, rank), policy_seed=42, stream=stream)
     kernels_per_rollout = runner.rollout_kernel_count(HORIZON_STEPS)
 
     def barrier():
@@ -369,13 +396,9 @@ def main():
                 ends[k].record(stream)
         barrier()
         wall = time.perf_counter() - wall0
-    device_ms = sum(s.elapsed_time(e) for s, e in zip(starts, ends))
-    if dist:
-        t = torch.tensor([device_ms], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        device_ms = float(t.item())
+    device_ms = max_over_ranks(sum(s.elapsed_time(e) for s, e in zip(starts, ends)), dist, "cuda")
     env_steps = world * CARS * HORIZON_STEPS * args.steps
-    value = env_steps / (device_ms / 1000.0)
+    value = whole_job_rate(CARS * HORIZON_STEPS * args.steps, world, device_ms / 1000.0)
     ms_per_step = device_ms / args.steps
 
     # end-to-end through the public API with host buffers
@@ -390,11 +413,7 @@ def main():
         out_host[0].copy_(torch.from_numpy(runner.sim.reward.numpy()))
         out_host[1].copy_(torch.from_numpy(runner.sim.done.numpy()))
     barrier()
-    e2e_s = time.perf_counter() - e2e0
-    if dist:
-        t = torch.tensor([e2e_s], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        e2e_s = float(t.item())
+    e2e_s = max_over_ranks(time.perf_counter() - e2e0, dist, "cuda")
     e2e = {"value": env_steps / e2e_s, "unit": "env-steps/s", "h2d_bytes_per_step": 11 * CARS * 4,
            "d2h_bytes_per_step": 2 * CARS * 4}
 
@@ -429,6 +448,8 @@ def main():
         del runner
         steps = args.surrogate_train_steps if args.surrogate_train_steps is not None else SURR_TRAIN_STEPS
         line["surrogate"] = surrogate_section(torch, W, track, stream, flush, steps)
+    if rank == 0 and not args.no_config1:
+        line["config1"] = config1_section(torch, W, stream)
     if not args.no_batched:
         line["batched"] = batched_section(torch, W, stream, flush)
     if rank == 0 and not args.no_training:

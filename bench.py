@@ -57,7 +57,7 @@ def parse():
     ap.add_argument("--batched-only", action="store_true", help="print only the batched multi-track section")
     ap.add_argument("--training-iterations", type=int, default=300)
     ap.add_argument("--surrogate-train-steps", type=int, default=None,
-                    help="surrogate training steps (default 20000; fewer only to profile the rollout)")
+                    help="surrogate training steps (default 60000; fewer only to profile the rollout)")
     return ap.parse_args()
 
 
@@ -171,7 +171,8 @@ def config1_section(torch, W, stream):
             "cpu_sample": cpu["sample"], "gpu_graph_vs_cpu": graph_rate / cpu["value"]}
 
 
-SURR_CARS, SURR_STEPS, SURR_REPS, SURR_TRAIN_STEPS = 65536, 32, 3, 20000
+SURR_CARS, SURR_STEPS, SURR_REPS, SURR_TRAIN_STEPS = 65536, 32, 3, 60000
+SURR_LR, SURR_HUBER_M = 8e-3, 0.02
 
 
 def surrogate_section(torch, W, track, stream, flush, train_steps=SURR_TRAIN_STEPS):
@@ -181,8 +182,9 @@ def surrogate_section(torch, W, track, stream, flush, train_steps=SURR_TRAIN_STE
     learned = W.Runner(track, SURR_CARS, beams=BEAMS, seed=7, stream=stream)
     sur = W.Surrogate(learned.sim, hidden=512, batch=8192, seed=1)
     sur.set_poses(1 << 22, seed=2)
+    sur.set_loss(SURR_HUBER_M)
     t0 = time.perf_counter()
-    sur.train(train_steps, lr=2e-3)
+    sur.train(train_steps, lr=SURR_LR)
     torch.cuda.synchronize()
     train_s = time.perf_counter() - t0
     heldout = sur.evaluate(8, 99)
@@ -212,8 +214,8 @@ def surrogate_section(torch, W, track, stream, flush, train_steps=SURR_TRAIN_STE
             "fallback_frac": fallback,
             "heldout_mae_m": heldout[0], "heldout_rmse_m": heldout[1], "heldout_frac_over_5cm": heldout[3],
             "surrogate": "64 encoded inputs -> 3 x 512 tanh -> 1081, BF16 tcgen05, FP32 Adam",
-            "training": f"{train_steps} steps x 8192 poses from 2^22 drawn over drivable cells, "
-                        f"exact-tracer labels, {train_s:.1f} s",
+            "training": f"{train_steps} Adam steps x 8192 poses from 2^22 drawn over drivable cells, exact-tracer "
+                        f"labels, Huber loss ({SURR_HUBER_M} m), lr {SURR_LR} cosine-decayed, {train_s:.1f} s",
             "target_mae_m": 0.02}
 
 

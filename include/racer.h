@@ -238,6 +238,9 @@ int racer_surrogate_gradient(racer_surrogate* surrogate, long first, float* mse,
 /* `steps` Adam steps over consecutive batches (cosine decay from lr to lr/100);
  * returns the last batch's mean squared error and mean absolute error in metres. */
 int racer_surrogate_train(racer_surrogate* surrogate, int steps, float lr, float* last_mse, float* last_mae_m);
+/* Training loss: huber_m = 0 (the default) is the squared range error; > 0 the
+ * Huber loss with that threshold in metres (gradient clamped beyond it). */
+int racer_surrogate_set_loss(racer_surrogate* surrogate, float huber_m);
 /* Held-out error on `batches` fresh batches drawn with `seed`, surrogate vs exact. */
 int racer_surrogate_evaluate(racer_surrogate* surrogate, int batches, uint64_t seed, float* mae_m, float* rmse_m,
                              float* max_m, float* frac_over_5cm);

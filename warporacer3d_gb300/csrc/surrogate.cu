@@ -95,7 +95,8 @@ struct EpiLoss {
   int ldgf;
   float* dbias;
   double* sums;
-  int npad;  // columns stored (a multiple of 16; past N they are zero)
+  int npad;     // columns stored (a multiple of 16; past N they are zero)
+  float huber;  // > 0: Huber loss with this threshold (range units), its gradient e clamped to +-huber
   __device__ void operator()(int m, int n, const float* v, int z) const {
     const bool row = m < M;
     float g[16], se = 0.0f, ae = 0.0f;
@@ -106,7 +107,7 @@ struct EpiLoss {
         float e = (v[j] + bias[n + j]) - target[(long)(n + j) * ldt + m];
         se += e * e;
         ae += fabsf(e);
-        g[j] = scale * e;
+        g[j] = scale * (huber > 0.0f ? fminf(fmaxf(e, -huber), huber) : e);
       }
     }
     if (row && n < npad) {
@@ -387,6 +388,7 @@ struct racer_surrogate {
   Layout L{};
   Norm nm{};
   int batch = 0;
+  float huber = 0.0f;  // training loss: 0 = squared error, > 0 = Huber threshold (range / 10 m units)
   cudaStream_t st = nullptr;
   float *theta = nullptr, *grad = nullptr, *m1 = nullptr, *m2 = nullptr;
   bf16 *w1b = nullptr, *w2b = nullptr, *w3b = nullptr, *w4b = nullptr, *w2t = nullptr, *w3t = nullptr,
@@ -537,7 +539,7 @@ int gradient(racer_surrogate* s, long first) {
   SURR_CHECK(cudaMemsetAsync(s->sums, 0, 2 * sizeof(double), s->st));
   if ((rc = forward(s, a, true, nullptr))) return rc;
   EpiLoss loss{s->label + 4L * B, B, s->theta + s->L.b4, B, beams, 2.0f / ((float)B * (float)beams),
-               a->g4s, NP, a->g4f, B, s->grad + s->L.b4, s->sums, NP};
+               a->g4s, NP, a->g4f, B, s->grad + s->L.b4, s->sums, NP, s->huber};
   SURR_CHECK(gemm_launch<256>(a->th3, s->tw4, B, NP, H / 64, 1, loss, s->err, s->st));
   SURR_CHECK(gemm_launch<256>(a->tg4s, s->tw4t, B, H, NP / 64, 1,
                               EpiDTanh{a->h3s, H, a->g3s, H, a->g3f, B, s->grad + s->L.b3, B, H}, s->err, s->st));
@@ -687,6 +689,15 @@ int racer_surrogate_set_poses(racer_surrogate* s, long count, uint64_t seed) {
   k_sample_poses<<<(unsigned)((count + 255) / 256), 256, 0, s->st>>>(s->cells, s->ncells, (int)count, seed, s->sim->t,
                                                                        s->poses);
   RACER_TRY(cudaGetLastError());
+  return 0;
+}
+
+int racer_surrogate_set_loss(racer_surrogate* s, float huber_m) {
+  if (!s || !(huber_m >= 0.0f)) {
+    racer_host::set_error("racer_surrogate_set_loss: null surrogate or negative threshold");
+    return 1;
+  }
+  s->huber = huber_m / RANGE;
   return 0;
 }
 

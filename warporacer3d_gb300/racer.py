@@ -353,6 +353,10 @@ class Surrogate:
         call("racer_surrogate_gradient", self.handle, first, ctypes.byref(mse), labels.c if labels else None)
         return mse.value
 
+    def set_loss(self, huber_m=0.0):
+        """0: squared range error; > 0: Huber loss with that threshold in metres."""
+        call("racer_surrogate_set_loss", self.handle, float(huber_m))
+
     def train(self, steps, lr=1e-3):
         mse, mae = ctypes.c_float(), ctypes.c_float()
         call("racer_surrogate_train", self.handle, steps, lr, ctypes.byref(mse), ctypes.byref(mae))

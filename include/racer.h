@@ -241,6 +241,10 @@ int racer_surrogate_train(racer_surrogate* surrogate, int steps, float lr, float
 /* Training loss: huber_m = 0 (the default) is the squared range error; > 0 the
  * Huber loss with that threshold in metres (gradient clamped beyond it). */
 int racer_surrogate_set_loss(racer_surrogate* surrogate, float huber_m);
+/* Rollout inference of a 512-wide surrogate: 1 (the default) = one fused
+ * kernel (all four layers per tile of 128 cars, activations kept on chip);
+ * 0 = four GEMM launches. Both give the same bits. Drops captured rollout graphs. */
+int racer_surrogate_set_fused(racer_surrogate* surrogate, int fused);
 /* Held-out error on `batches` fresh batches drawn with `seed`, surrogate vs exact. */
 int racer_surrogate_evaluate(racer_surrogate* surrogate, int batches, uint64_t seed, float* mae_m, float* rmse_m,
                              float* max_m, float* frac_over_5cm);

@@ -28,6 +28,7 @@
 #include "common.cuh"
 #include "gemm_epi.cuh"
 #include "gemm_tc.cuh"
+#include "surrogate_fused.cuh"
 #include "kernels.h"
 #include "objects.h"
 #include "philox.h"
@@ -389,6 +390,7 @@ struct racer_surrogate {
   Norm nm{};
   int batch = 0;
   float huber = 0.0f;  // training loss: 0 = squared error, > 0 = Huber threshold (range / 10 m units)
+  int fused = 1;       // rollout inference in one fused kernel (hidden width 512)
   cudaStream_t st = nullptr;
   float *theta = nullptr, *grad = nullptr, *m1 = nullptr, *m2 = nullptr;
   bf16 *w1b = nullptr, *w2b = nullptr, *w3b = nullptr, *w4b = nullptr, *w2t = nullptr, *w3t = nullptr,
@@ -692,6 +694,17 @@ int racer_surrogate_set_poses(racer_surrogate* s, long count, uint64_t seed) {
   return 0;
 }
 
+int racer_surrogate_set_fused(racer_surrogate* s, int fused) {
+  if (!s) {
+    racer_host::set_error("racer_surrogate_set_fused: null surrogate");
+    return 1;
+  }
+  s->fused = fused != 0;
+  for (auto& kv : s->sim->surrogate_graphs) cudaGraphExecDestroy(kv.second);
+  s->sim->surrogate_graphs.clear();
+  return 0;
+}
+
 int racer_surrogate_set_loss(racer_surrogate* s, float huber_m) {
   if (!s || !(huber_m >= 0.0f)) {
     racer_host::set_error("racer_surrogate_set_loss: null surrogate or negative threshold");
@@ -887,12 +900,19 @@ int surrogate_lidar(racer_surrogate* s, racer_sim* sim, float* obs, bool audit, 
   k_features<<<(n + 127) / 128, 128, 0, st>>>(sim->ray, n, s->nm, a->x, nullptr);
   SURR_CHECK(cudaGetLastError());
   SURR_CHECK(cudaMemsetAsync(s->minr, 0x7f, (size_t)n * sizeof(unsigned), st));
-  EpiInfer inf{obs + 4L * n, n, s->theta + s->L.b4, n, beams, s->minr};
-  cudaStream_t keep = s->st;
-  s->st = st;
-  int rc = forward(s, a, false, &inf);
-  s->st = keep;
-  if (rc) return rc;
+  if (s->fused && s->L.H == SF_H) {
+    const float* th = s->theta;
+    FusedArgs fa{th + s->L.b2, th + s->L.b3, th + s->L.b4, obs + 4L * n, s->minr, n, beams,
+                 (s->L.npad + 255) / 256, s->err};
+    SURR_CHECK(surrogate_fused_launch(a->tx, s->tw1, s->tw2, s->tw3, s->tw4, fa, sim->sms, st));
+  } else {
+    EpiInfer inf{obs + 4L * n, n, s->theta + s->L.b4, n, beams, s->minr};
+    cudaStream_t keep = s->st;
+    s->st = st;
+    int rc = forward(s, a, false, &inf);
+    s->st = keep;
+    if (rc) return rc;
+  }
   if (audit) {
     launch_lidar(sim->t, sim->ray, s->exact, n, beams, sim->beam_dir, nullptr, st);
     k_compare<<<1216, 256, 0, st>>>(obs + 4L * n, s->exact + 4L * n, (long)beams * n, s->rsums, s->rmax, s->rcount);

@@ -353,6 +353,10 @@ class Surrogate:
         call("racer_surrogate_gradient", self.handle, first, ctypes.byref(mse), labels.c if labels else None)
         return mse.value
 
+    def set_fused(self, fused=True):
+        """Rollout inference in one fused kernel (512-wide) or as four GEMMs; the same bits either way."""
+        call("racer_surrogate_set_fused", self.handle, int(bool(fused)))
+
     def set_loss(self, huber_m=0.0):
         """0: squared range error; > 0: Huber loss with that threshold in metres."""
         call("racer_surrogate_set_loss", self.handle, float(huber_m))

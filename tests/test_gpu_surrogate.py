@@ -162,21 +162,24 @@ def test_training_reduces_heldout_error():
 @pytest.mark.parametrize("cars", [300, 128 * 160 + 37])
 def test_fused_inference_equals_layered_gemms(cars):
     """The fused 512-wide inference kernel (activations kept on chip, output in TMEM chunks) gives the
-    same bits as the four GEMM launches: obs, per-car minimum ranges through the fallback, state.
-    128 * 160 + 37 cars is more tiles than SMs, so CTAs run several tiles."""
-    runs, surs = [], []
+    same bits as the four GEMM launches: obs, the fallback cars picked from the per-car minimum
+    ranges, state. 128 * 160 + 37 cars is more tiles than SMs, so CTAs run several tiles. One
+    trained surrogate serves both (training sums bias gradients with atomics), and the sim's state
+    and observations are restored between the two rollouts."""
+    run = W.Runner(W.track("bridge"), cars, beams=1081, seed=5)
+    sur = W.Surrogate(run.sim, hidden=512, batch=1024, seed=2)
+    sur.set_poses(1 << 14, seed=4)
+    sur.train(30, lr=2e-3)
+    state0, obs0 = run.sim.state.numpy(), run.sim.obs.numpy()
+    out = []
     for fused in (True, False):
-        run = W.Runner(W.track("bridge"), cars, beams=1081, seed=5)
-        sur = W.Surrogate(run.sim, hidden=512, batch=1024, seed=2)
-        sur.set_poses(1 << 14, seed=4)
-        sur.train(30, lr=2e-3)
+        run.sim.state.write(state0)
+        run.sim.obs.write(obs0)
         sur.set_fused(fused)
-        runs.append(run)
-        surs.append(sur)
-    for r, s in zip(runs, surs):
-        r.rollout_surrogate(s, 6, False, 0, 0, 0.5)
-        r.synchronize()
-    a, b = runs
-    assert np.array_equal(a.sim.obs.numpy(), b.sim.obs.numpy())
-    assert np.array_equal(a.sim.state.numpy(), b.sim.state.numpy())
-    assert surs[0].rollout_stats()[4] == surs[1].rollout_stats()[4]  # same fallback fraction
+        sur.rollout_stats(reset=True)
+        run.rollout_surrogate(sur, 6, False, 0, 0, 0.5)
+        run.synchronize()
+        out.append((run.sim.obs.numpy(), run.sim.state.numpy(), sur.rollout_stats()[4]))
+    (obs_f, state_f, fb_f), (obs_l, state_l, fb_l) = out
+    assert np.array_equal(obs_f, obs_l) and np.array_equal(state_f, state_l) and fb_f == fb_l
+    assert 0.0 < fb_f < 1.0

@@ -10,8 +10,10 @@
 // 128B-swizzled): the input block in k-block 0 for layer 1, then each hidden
 // epilogue writes its tanh output there in BF16 as the next layer's A. The
 // output layer runs in 256-column chunks alternating between the two TMEM
-// slots, so the epilogue of chunk c (clamp, obs rows, per-car minimum) overlaps
-// the MMAs of chunk c + 1. The MMAs, their k order and the BF16 rounding of
+// slots, so the epilogue of one chunk (clamp, obs rows, per-car minimum)
+// overlaps the MMAs of the next; each CTA starts at a different chunk so the
+// SMs do not all read the same weight lines at once. The MMAs, their k order
+// and the BF16 rounding of
 // the activations are those of the layer-by-layer GEMMs, so the two paths give
 // the same bits.
 //
@@ -85,8 +87,8 @@ __device__ bool sf_producer(const CUtensorMap* tx, const CUtensorMap* tw1, const
         kb = (f % (2 * SF_KB)) / 2;
         row = 256 * (f & 1);
       } else {
-        const int f = e - 2 - 4 * SF_KB;  // chunk, then k-block
-        map = tw4, row = 256 * (f / SF_KB), kb = f % SF_KB;
+        const int f = e - 2 - 4 * SF_KB;  // chunk position, then k-block
+        map = tw4, row = 256 * ((f / SF_KB + blockIdx.x % nc) % nc), kb = f % SF_KB;
       }
       const uint32_t s = it % SF_STAGES;
       if (it >= (uint32_t)SF_STAGES && !sf_wait(&b.empty[s], ((it / SF_STAGES) - 1) & 1, b.abort)) return false;
@@ -164,6 +166,7 @@ __device__ bool sf_epilogue(uint32_t tmem, uint8_t* abuf, const SfBars& b, const
   const int lane = threadIdx.x & 31;
   const uint32_t lane_addr = (uint32_t)(q * 32) << 16;
   const int r = q * 32 + lane;  // row of the tile
+  const int rot = blockIdx.x % nc;  // output chunks start at a different chunk on each CTA
   uint32_t local = 0;
   float v[32];
   for (int tile = blockIdx.x; tile < tiles; tile += gridDim.x, ++local) {
@@ -174,15 +177,21 @@ __device__ bool sf_epilogue(uint32_t tmem, uint8_t* abuf, const SfBars& b, const
       tc::tc_fence_after();
       const float* bias = layer == 0 ? nullptr : (layer == 1 ? args.b2 : args.b3);
 #pragma unroll 1
-      for (int c = 0; c < 256; c += 32) {
-        tc::tmem_ld32_sync(tmem + lane_addr + 256 * h + c, v);
-        const int col = 256 * h + c;  // first unit of these 32
+      for (int i = 0; i < 8; ++i) {  // columns 32i .. 32i + 31 of this slot
+        const int col = 256 * h + 32 * i;  // first unit of these 32
+        float bb[32];                      // their biases: 16-byte loads issued before the accumulator read
+#pragma unroll
+        for (int q4 = 0; q4 < 8; ++q4) {
+          const float4 t4 = bias ? __ldg(reinterpret_cast<const float4*>(bias + col) + q4) : make_float4(0, 0, 0, 0);
+          bb[4 * q4] = t4.x, bb[4 * q4 + 1] = t4.y, bb[4 * q4 + 2] = t4.z, bb[4 * q4 + 3] = t4.w;
+        }
+        tc::tmem_ld32_sync(tmem + lane_addr + col, v);
         uint8_t* kblock = abuf + (col >> 6) * 16384;
 #pragma unroll
         for (int ch = 0; ch < 4; ++ch) {
           float t[8];
 #pragma unroll
-          for (int j = 0; j < 8; ++j) t[j] = tc::tanh_fast(v[8 * ch + j] + (bias ? bias[col + 8 * ch + j] : 0.0f));
+          for (int j = 0; j < 8; ++j) t[j] = tc::tanh_fast(v[8 * ch + j] + bb[8 * ch + j]);
           const uint4 packed = make_uint4(tc::pack_bf16(t[0], t[1]), tc::pack_bf16(t[2], t[3]),
                                           tc::pack_bf16(t[4], t[5]), tc::pack_bf16(t[6], t[7]));
           *reinterpret_cast<uint4*>(kblock + tc::sw128_offset(r, (col & 63) + 8 * ch)) = packed;
@@ -193,20 +202,31 @@ __device__ bool sf_epilogue(uint32_t tmem, uint8_t* abuf, const SfBars& b, const
       tc::mbar_arrive(b.edone);
     }
     float lo = 1.0f;
-    for (int c = 0; c < nc; ++c) {  // output: chunk c in slot c & 1, this warp's 128 of its 256 columns
-      const int s = c & 1;
-      if (!sf_wait(&b.accfull[s], ((s ? f1 : f0) + 3 + c / 2) & 1, b.abort)) return false;
+    for (int p = 0; p < nc; ++p) {  // output: p-th chunk in slot p & 1, this warp's 128 of its 256 columns
+      const int s = p & 1, c = (p + rot) % nc;
+      if (!sf_wait(&b.accfull[s], ((s ? f1 : f0) + 3 + p / 2) & 1, b.abort)) return false;
       tc::tc_fence_after();
 #pragma unroll 1
-      for (int cc = 0; cc < 128; cc += 32) {
-        tc::tmem_ld32_sync(tmem + lane_addr + 256 * s + 128 * h + cc, v);
-        const int o0 = 256 * c + 128 * h + cc;
+      for (int i = 0; i < 4; ++i) {
+        const int o0 = 256 * c + 128 * h + 32 * i;
+        float bb[32];
+        if (o0 + 32 <= args.beams) {
+#pragma unroll
+          for (int q4 = 0; q4 < 8; ++q4) {
+            const float4 t4 = __ldg(reinterpret_cast<const float4*>(args.b4 + o0) + q4);
+            bb[4 * q4] = t4.x, bb[4 * q4 + 1] = t4.y, bb[4 * q4 + 2] = t4.z, bb[4 * q4 + 3] = t4.w;
+          }
+        } else {
+#pragma unroll
+          for (int j = 0; j < 32; ++j) bb[j] = o0 + j < args.beams ? __ldg(args.b4 + o0 + j) : 0.0f;
+        }
+        tc::tmem_ld32_sync(tmem + lane_addr + 256 * s + 128 * h + 32 * i, v);
         if (m < args.n) {
 #pragma unroll
           for (int j = 0; j < 32; ++j) {
             const int o = o0 + j;
             if (o < args.beams) {
-              const float y = fminf(fmaxf(v[j] + args.b4[o], 0.0f), 1.0f);
+              const float y = fminf(fmaxf(v[j] + bb[j], 0.0f), 1.0f);
               args.out[(long)o * args.n + m] = y;
               lo = fminf(lo, y);
             }

@@ -26,7 +26,7 @@ def test_policy_init_bit_exact():
         assert np.array_equal(g.theta.numpy(), c.theta)
 
 
-@pytest.mark.parametrize("beams,cols", [(108, 1000), (1081, 384)])
+@pytest.mark.parametrize("beams,cols", [(108, 1000), (1081, 384), (2, 1), (2, 129), (1081, 1)])
 def test_policy_forward(beams, cols):
     g = W.Policy(3, beams=beams)
     c = O.Policy(3, beams=beams)

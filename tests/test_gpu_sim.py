@@ -377,3 +377,59 @@ def test_snapshot_rows_and_serve_step():
     assert np.all(snap[11 + 113] == np.float32(0.25)) and np.all(snap[11 + 113 + 1] == np.float32(0.8))
     snap2 = run.serve_step(0, 0, reset=True, policy=True, tick=2)
     assert same(snap2[:11], sim.state.numpy()) and same(snap2[-1], sim.done.numpy())
+
+
+@pytest.mark.parametrize("n,beams,name", [(1, 2, "bridge"), (1, 1081, "ramp"), (33, 2, "bank"), (33, 1081, "bridge")])
+def test_edge_sizes_bit_exact(n, beams, name):
+    """One car, a warp and one, the minimum beam count (2) and the full 1081."""
+    track = W.track(name)
+    gpu, cpu = W.Sim(track, n, 4, beams=beams), O.Sim(track, n, 4, beams=beams)
+    gpu.reset()
+    cpu.reset()
+    rng = np.random.default_rng(n + beams)
+    for step in range(8):
+        act = rng.uniform(-1, 1, (2, n)).astype(np.float32)
+        gpu.actions.write(act)
+        cpu.actions[:] = act
+        gpu.step(gpu.actions, gpu.reward, gpu.done, gpu.obs)
+        cpu.step(cpu.actions, cpu.reward, cpu.done, cpu.obs)
+        check_sim(gpu, cpu, f"step {step} ")
+
+
+def test_car_trajectory_independent_of_batch_size():
+    """Size-independent property at 262144 cars: car i's state depends only on its seed, index and
+    actions, so the first 1000 cars of a 262144-car sim equal a 1000-car sim bit for bit."""
+    track = W.track("ramp")
+    big, small = W.Sim(track, 262144, 8, beams=108), W.Sim(track, 1000, 8, beams=108)
+    big.reset()
+    small.reset()
+    rng = np.random.default_rng(2)
+    for _ in range(6):
+        act = rng.uniform(-1, 1, (2, 262144)).astype(np.float32)
+        big.actions.write(act)
+        small.actions.write(np.ascontiguousarray(act[:, :1000]))
+        big.step(big.actions, big.reward, big.done, big.obs)
+        small.step(small.actions, small.reward, small.done, small.obs)
+    assert same(big.state.numpy()[:, :1000], small.state.numpy())
+    assert same(big.obs.numpy()[:, :1000], small.obs.numpy())
+
+
+def test_eight_segments_bit_exact():
+    """The segment table at its maximum of eight tracks."""
+    names = ["flat", "ramp", "bank", "bridge", "flat", "bridge", "ramp", "bank"]
+    tracks = [W.track(t) for t in names[:7]] + [np.load(GOLDEN_OCCUPANCY)["track"]]
+    cars, seeds = [5, 40, 1, 64, 31, 2, 17, 9], list(range(10, 18))
+    gpu = W.Sim.segments(tracks, cars, seeds, beams=108)
+    cpus = [O.Sim(t, c, s, beams=108) for t, c, s in zip(tracks, cars, seeds)]
+    gpu.reset()
+    for c in cpus:
+        c.reset()
+    rng = np.random.default_rng(9)
+    for step in range(6):
+        act = rng.uniform(-1, 1, (2, gpu.n)).astype(np.float32)
+        gpu.actions.write(act)
+        for k, c in enumerate(cpus):
+            c.actions[:] = act[:, gpu.car0[k]:gpu.car0[k + 1]]
+            c.step(c.actions, c.reward, c.done, c.obs)
+        gpu.step(gpu.actions, gpu.reward, gpu.done, gpu.obs)
+        check_segments(gpu, cpus, f"step {step} ")

@@ -66,3 +66,15 @@ def test_errors_are_reported_without_gpu(lib):
         lib.racer_free(p)
         pytest.skip("GPU present")
     assert rc == 2 and lib.racer_last_error()
+
+
+def test_segment_arguments_checked_on_host(lib):
+    track = W.track("flat")
+    with pytest.raises(W.RacerError, match="1 to 8 segments"):
+        W.Sim.segments([track] * 9, [1] * 9, list(range(9)))
+    with pytest.raises(W.RacerError, match="1 to 8 segments"):
+        W.Sim.segments([], [], [])
+    with pytest.raises(W.RacerError, match="at least one car"):
+        W.Sim.segments([track, track], [4, 0], [1, 2])
+    with pytest.raises(ValueError):
+        W.Sim.segments([track, track], [4], [1, 2])

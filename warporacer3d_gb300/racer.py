@@ -118,7 +118,7 @@ class Sim:
         lens = (ctypes.c_size_t * k)(*[a.size for a in arrays])
         counts = (ctypes.c_int * k)(*cars)
         seeds_c = (ctypes.c_uint64 * k)(*seeds)
-        self.n, self.seed, self.beams, self.IN = int(sum(cars)), seeds[0], beams, beams + 5
+        self.n, self.seed, self.beams, self.IN = int(sum(cars)), (seeds[0] if seeds else 0), beams, beams + 5
         self.cars = list(cars)
         self.car0 = [int(v) for v in np.concatenate([[0], np.cumsum(cars)])]
         self.stream = _stream(stream)

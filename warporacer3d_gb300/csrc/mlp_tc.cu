@@ -29,18 +29,25 @@ namespace racer {
 namespace {
 
 constexpr int TILE = 128;
-constexpr int GROUPS = 4;                          // producer groups, one k-block in flight each
-constexpr int THREADS = (GROUPS * 4 + 1) * 32;     // 16 producer warps + 1 MMA warp
-constexpr int MMA_WARP = GROUPS * 4;
-constexpr int A_BYTES = TILE * 128;                // 128 rows x 64 bf16
-constexpr int B_BYTES = 64 * 128;                  // 64 rows x 64 bf16
-constexpr int OFF_A = 0;                           // GROUPS x A; H = [h | 1 | 0] reuses A[0], A[1]
-constexpr int OFF_B = OFF_A + GROUPS * A_BYTES;
-constexpr int OFF_W1 = OFF_B + GROUPS * B_BYTES;
-constexpr int OFF_W2 = OFF_W1 + 2 * B_BYTES;
-constexpr int OFF_BAR = OFF_W2 + 2 * 16 * 128;
-// + barriers, + alignment slack, + 16 KB so every descriptor-addressed read stays inside the allocation
-constexpr int SMEM_BYTES = OFF_BAR + 128 + 1024 + 16384;
+constexpr int A_BYTES = TILE * 128;  // 128 rows x 64 bf16
+constexpr int B_BYTES = 64 * 128;    // 64 rows x 64 bf16
+
+// GROUPS producer groups of four warps, one k-block in flight each (four for
+// wide inputs; two when the input has at most four k-blocks, which halves the
+// shared memory so two CTAs share an SM), plus one MMA warp.
+template <int GROUPS>
+struct FwdCfg {
+  static constexpr int THREADS = (GROUPS * 4 + 1) * 32;
+  static constexpr int MMA_WARP = GROUPS * 4;
+  static constexpr int OFF_A = 0;  // GROUPS x A; H = [h | 1 | 0] reuses A[0], A[1]
+  static constexpr int OFF_B = OFF_A + GROUPS * A_BYTES;
+  static constexpr int OFF_W1 = OFF_B + GROUPS * B_BYTES;
+  static constexpr int OFF_W2 = OFF_W1 + 2 * B_BYTES;
+  static constexpr int OFF_BAR = OFF_W2 + 2 * 16 * 128;
+  // + barriers, + alignment slack, + 16 KB so every descriptor-addressed read stays inside the allocation
+  static constexpr int SMEM_BYTES = OFF_BAR + 128 + 1024 + 16384;
+  static constexpr int MIN_BLOCKS = GROUPS == 2 ? 2 : 1;
+};
 
 // Grid: one CTA per 128 samples. Warps 0-15 form four producer groups; group
 // g loads k-blocks g, g+4, g+8, ... of X (thread = sample row) and of W0 into
@@ -48,11 +55,16 @@ constexpr int SMEM_BYTES = OFF_BAR + 128 + 1024 + 16384;
 // four K=16 MMAs of the block and commits to empty[kb % 4]; after the last
 // block it commits to `done`. Warps 0-3 (TMEM lanes 0-127) then run the
 // epilogues and issue layers 2 and 3.
-__global__ void __launch_bounds__(THREADS, 1) k_mlp_fwd(const float* __restrict__ x, int in, int cols,
+template <int GROUPS>
+__global__ void __launch_bounds__(FwdCfg<GROUPS>::THREADS, FwdCfg<GROUPS>::MIN_BLOCKS)
+    k_mlp_fwd(const float* __restrict__ x, int in, int cols,
                                                         const uint4* __restrict__ w0s, int kblocks,
                                                         const uint4* __restrict__ w1s,
                                                         const uint4* __restrict__ w2s, float* h1g, float* h2g,
                                                         float* og, int write_hidden, SampleArgs sa, int* err) {
+  using C = FwdCfg<GROUPS>;
+  constexpr int THREADS = C::THREADS, MMA_WARP = C::MMA_WARP, OFF_A = C::OFF_A, OFF_B = C::OFF_B,
+                OFF_W1 = C::OFF_W1, OFF_W2 = C::OFF_W2, OFF_BAR = C::OFF_BAR;
   extern __shared__ uint8_t smem_raw[];
   const uint32_t raw = tc::smem_u32(smem_raw);
   uint8_t* smem = smem_raw + (((raw + 1023u) & ~1023u) - raw);
@@ -243,21 +255,30 @@ void launch_pack_weights(const float* theta, int in, uint8_t* pack, cudaStream_t
   k_pack_weights<<<152, 256, 0, st>>>(theta, in, kb, w0, w1, w2);
 }
 
-cudaError_t launch_mlp_fwd(const float* x, int in, int cols, const uint8_t* pack, float* h1, float* h2, float* o,
-                           int write_hidden, const SampleArgs& sa, int* err, cudaStream_t st) {
+template <int GROUPS>
+static cudaError_t fwd_launch(const float* x, int in, int cols, int kb, const uint4* w0, const uint4* w1,
+                              const uint4* w2, float* h1, float* h2, float* o, int write_hidden, const SampleArgs& sa,
+                              int* err, cudaStream_t st) {
+  using C = FwdCfg<GROUPS>;
   static bool configured = false;
   if (!configured) {
-    cudaError_t e = cudaFuncSetAttribute(k_mlp_fwd, cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM_BYTES);
+    cudaError_t e = cudaFuncSetAttribute(k_mlp_fwd<GROUPS>, cudaFuncAttributeMaxDynamicSharedMemorySize, C::SMEM_BYTES);
     if (e != cudaSuccess) return e;
     configured = true;
   }
+  k_mlp_fwd<GROUPS><<<(cols + TILE - 1) / TILE, C::THREADS, C::SMEM_BYTES, st>>>(x, in, cols, w0, kb, w1, w2, h1, h2,
+                                                                               o, write_hidden, sa, err);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_mlp_fwd(const float* x, int in, int cols, const uint8_t* pack, float* h1, float* h2, float* o,
+                           int write_hidden, const SampleArgs& sa, int* err, cudaStream_t st) {
   int kb = (in + 63) / 64;
   const uint4* w0 = reinterpret_cast<const uint4*>(pack);
   const uint4* w1 = reinterpret_cast<const uint4*>(pack + (size_t)kb * 8192);
   const uint4* w2 = reinterpret_cast<const uint4*>(pack + (size_t)kb * 8192 + 2 * 8192);
-  k_mlp_fwd<<<(cols + TILE - 1) / TILE, THREADS, SMEM_BYTES, st>>>(x, in, cols, w0, kb, w1, w2, h1, h2, o, write_hidden,
-                                                                  sa, err);
-  return cudaGetLastError();
+  if (kb <= 4) return fwd_launch<2>(x, in, cols, kb, w0, w1, w2, h1, h2, o, write_hidden, sa, err, st);
+  return fwd_launch<4>(x, in, cols, kb, w0, w1, w2, h1, h2, o, write_hidden, sa, err, st);
 }
 
 }  // namespace racer

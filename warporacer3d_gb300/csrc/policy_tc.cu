@@ -1,9 +1,8 @@
 // Policy backward (racer/ppo.mojo:113-138) with BF16 operands and FP32
 // accumulation, FP32 outputs in the reference's layouts.
 //
-//   d2 = (W2^T d3) * (1 - h2^2)                   k_dgrad (CUDA cores: K = 3)
-//   d1 = (W1^T d2[:64]) * (1 - h1^2)              k_dgrad, same thread: K = 64 per sample, W1 in shared
-//                                                 memory; operands rounded to BF16 like a tensor-core product
+//   d2 = (W2^T d3) * (1 - h2^2)                   k_dgrad_tc, per sample on the CUDA cores (K = 3)
+//   d1 = (W1^T d2[:64]) * (1 - h1^2)              k_dgrad_tc, per tile of 128 samples on tcgen05 (K = 64)
 //   gW0[r, k] = sum_b d1[r, b] x[k, b]            GEMM D[k, r] = xb[k, :] . d1f[r, :], split-K over b
 //   gW1[r, j] = sum_b d2[r, b] h1[j, b]           GEMM D[j, r] = h1b[j, :] . d2f[r, :], split-K
 //   gW2[r, j] = sum_b d3[r, b] h2[j, b]           GEMM D[j, r] = h2b[j, :] . d3f[r, :], split-K
@@ -11,9 +10,9 @@
 // The three weight gradients (K = batch) run on the tcgen05 tensor cores
 // through the generic TMA-fed kernel of gemm_tc.cuh; their split-K partials
 // are summed in a fixed order and written straight into the theta layout
-// W0 [64, IN] | W1 [64, 65] | W2 [3, 65]. The data-gradient products have
-// K <= 64 and N <= 65 per sample: memory-bound, so they stay on the CUDA
-// cores, fused with the tanh derivatives and the BF16 operand copies.
+// W0 [64, IN] | W1 [64, 65] | W2 [3, 65]. The data gradients are memory-bound
+// (K <= 64): one small kernel per 128 samples fuses them with the tanh
+// derivatives and the BF16 operand copies of the weight-gradient GEMMs.
 #include <cuda_bf16.h>
 
 #include <string>
@@ -48,79 +47,109 @@ __global__ void k_rows_bf16(const float* __restrict__ src, int rows, int cols, b
   }
 }
 
-__device__ __forceinline__ float bf16_round(float v) { return __bfloat162float(__float2bfloat16_rn(v)); }
+// W1^T as a 128B-swizzled K-major BF16 image: row j (input unit, < 64) holds
+// W1[0..63][j], the B operand of the d1 product.
+__global__ void k_pack_w1ts(const float* __restrict__ theta, int in, bf16* w1ts) {
+  const int e = blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= H * H) return;
+  const int j = e / H, r = e % H;
+  w1ts[tc::sw128_offset(j, r) / 2] = __float2bfloat16_rn(theta[H * in + r * HA + j]);
+}
 
-// Per sample j (one thread): d2 = (W2^T d3) * (1 - h2^2) and
-// d1 = (W1^T bf16(d2[:64])) * (1 - h1^2) with W1 rounded to BF16 (the
-// operands a tensor-core product would see; FP32 accumulation), written as
-// FP32 d2, d1 [65, cols] plus the BF16 operand copies of the weight-gradient
-// GEMMs d2f, d1f [64, ld] and d3f [16, ld] (feature-major).
-constexpr int DGRAD_THREADS = 128;
-constexpr int DGRAD_SMEM = (HA * H + HA * DGRAD_THREADS) * 4;
-
-__global__ void __launch_bounds__(DGRAD_THREADS) k_dgrad(int in, const float* __restrict__ theta,
-                                                         const float* __restrict__ d3, const float* __restrict__ h1,
-                                                         const float* __restrict__ h2, float* d2, float* d1, int cols,
-                                                         bf16* d1f, bf16* d2f, bf16* d3f, int ld) {
-  extern __shared__ __align__(16) float dg_smem[];
-  float(*w1t)[H] = reinterpret_cast<float(*)[H]>(dg_smem);                          // w1t[k][r] = bf16(W1[r][k])
-  float(*h1s)[DGRAD_THREADS] = reinterpret_cast<float(*)[DGRAD_THREADS]>(dg_smem + HA * H);  // this thread's h1
-  const int j = blockIdx.x * blockDim.x + threadIdx.x;
-  // every h1 load of this sample in flight at once; each thread reads back only its own column
-  if (j < cols) {
-#pragma unroll
-    for (int k = 0; k < HA; ++k) h1s[k][threadIdx.x] = h1[(long)k * cols + j];
+// Data gradients per tile of 128 samples: each thread computes its sample's
+// d2 = (W2^T d3) * (1 - h2^2) (K = 3, CUDA cores) and writes bf16(d2[:64]) as
+// its row of a 128B-swizzled A tile; one thread issues the
+// four K = 16 MMAs D[128, 64] = A . W1^T into TMEM (64 columns per CTA), and
+// each thread reads its row back for d1 = D * (1 - h1^2).
+// Row 64 of d1 is zero (h1's row 64 is the constant 1).
+__global__ void __launch_bounds__(128, 4)
+    k_dgrad_tc(int in, const float* __restrict__ theta, const uint4* __restrict__ w1ts, const float* __restrict__ d3,
+               const float* __restrict__ h1, const float* __restrict__ h2, float* __restrict__ d2,
+               float* __restrict__ d1, int cols, bf16* __restrict__ d1f, bf16* __restrict__ d2f,
+               bf16* __restrict__ d3f, int ld, int* err) {
+  __shared__ __align__(1024) uint8_t A[128 * 128];
+  __shared__ __align__(1024) uint8_t B[H * 128];
+  __shared__ uint64_t done;
+  __shared__ uint32_t tslot;
+  const int tid = threadIdx.x, warp = tid >> 5;
+  const int j = blockIdx.x * 128 + tid;
+  const bool live = j < cols;
+  if (tid == 0) {
+    tc::mbar_init(&done, 1);
+    tc::fence_barrier_init();
   }
-  const float* w1 = theta + H * in;
-  for (int e = threadIdx.x; e < H * HA; e += blockDim.x) {
-    const int r = e / HA, k = e % HA;
-    w1t[k][r] = bf16_round(w1[e]);
+  if (warp == 0) {
+    tc::tmem_alloc(&tslot, 64);
+    tc::tmem_relinquish();
   }
-  __syncthreads();
-  if (j >= cols) return;
+  for (int e = tid; e < H * 128 / 16; e += 128) reinterpret_cast<uint4*>(B)[e] = __ldg(w1ts + e);
   const float* w2 = theta + H * in + H * HA;
-  const float e0 = d3[j], e1 = d3[(long)cols + j], e2 = d3[2L * cols + j];
-  d3f[j] = __float2bfloat16_rn(e0);
-  d3f[(long)ld + j] = __float2bfloat16_rn(e1);
-  d3f[2L * ld + j] = __float2bfloat16_rn(e2);
-  float b[H];
+  float e0 = 0.0f, e1 = 0.0f, e2 = 0.0f;
+  if (live) {
+    e0 = d3[j], e1 = d3[(long)cols + j], e2 = d3[2L * cols + j];
+    d3f[j] = __float2bfloat16_rn(e0);
+    d3f[(long)ld + j] = __float2bfloat16_rn(e1);
+    d3f[2L * ld + j] = __float2bfloat16_rn(e2);
+  }
+  float hv[HA];  // every h2 load of this sample issued before any store
+#pragma unroll
+  for (int k = 0; k < HA; ++k) hv[k] = live ? h2[(long)k * cols + j] : 0.0f;
+  uint32_t packed[H / 2];
 #pragma unroll
   for (int k = 0; k < HA; ++k) {
     const float acc = w2[k] * e0 + w2[HA + k] * e1 + w2[2 * HA + k] * e2;
-    const float a = h2[(long)k * cols + j];
+    const float a = hv[k];
     const float v = acc * (1.0f - a * a);
-    d2[(long)k * cols + j] = v;
+    if (live) d2[(long)k * cols + j] = v;
     if (k < H) {
       const bf16 vb = __float2bfloat16_rn(v);
-      d2f[(long)k * ld + j] = vb;
-      b[k] = __bfloat162float(vb);
+      if (live) d2f[(long)k * ld + j] = vb;
+      const uint32_t bits = *reinterpret_cast<const uint16_t*>(&vb);
+      packed[k >> 1] = (k & 1) ? (packed[k >> 1] | (bits << 16)) : bits;
     }
   }
-  constexpr int KU = 5;  // 65 = 13 x 5 output units per pass: five independent loads of h1 in flight
-#pragma unroll 1
-  for (int k0 = 0; k0 < HA; k0 += KU) {
-    float acc[KU], a[KU];
 #pragma unroll
-    for (int u = 0; u < KU; ++u) {
-      a[u] = h1s[k0 + u][threadIdx.x];
-      acc[u] = 0.0f;
-    }
+  for (int q = 0; q < 8; ++q)
+    *reinterpret_cast<uint4*>(A + tid * 128 + ((q ^ (tid & 7)) << 4)) =
+        make_uint4(packed[4 * q], packed[4 * q + 1], packed[4 * q + 2], packed[4 * q + 3]);
+  tc::fence_proxy_async_smem();
+  tc::tc_fence_before();
+  __syncthreads();
+  tc::tc_fence_after();
+  const uint32_t tmem = tslot;
+  if (tid == 0) {
+    const uint32_t a = tc::smem_u32(A), b = tc::smem_u32(B), idesc = tc::idesc_bf16(128, H);
 #pragma unroll
-    for (int q = 0; q < H / 4; ++q) {
+    for (int k = 0; k < 4; ++k)
+      tc::mma_bf16(tmem, tc::sdesc_sw128(a + 32 * k), tc::sdesc_sw128(b + 32 * k), idesc, k ? 1u : 0u);
+    tc::mma_commit(&done);
+  }
+  bool ok = tc::mbar_wait(&done, 0);
+  tc::tc_fence_after();
+  float acc[H];
+  const uint32_t trow = tmem + ((uint32_t)(warp * 32) << 16);
 #pragma unroll
-      for (int u = 0; u < KU; ++u) {
-        const float4 c = reinterpret_cast<const float4*>(w1t[k0 + u])[q];
-        acc[u] += c.x * b[4 * q] + c.y * b[4 * q + 1] + c.z * b[4 * q + 2] + c.w * b[4 * q + 3];
+  for (int q = 0; q < 4; ++q) tc::tmem_ld16(trow + 16 * q, acc + 16 * q);
+  tc::tmem_wait_ld();
+  if (live) {
+#pragma unroll
+    for (int k0 = 0; k0 < H; k0 += 32) {  // 32 loads of h1 in flight, then their stores
+      float hh[32];
+#pragma unroll
+      for (int k = 0; k < 32; ++k) hh[k] = h1[(long)(k0 + k) * cols + j];
+#pragma unroll
+      for (int k = 0; k < 32; ++k) {
+        const float g = acc[k0 + k] * (1.0f - hh[k] * hh[k]);
+        d1[(long)(k0 + k) * cols + j] = g;
+        d1f[(long)(k0 + k) * ld + j] = __float2bfloat16_rn(g);
       }
     }
-#pragma unroll
-    for (int u = 0; u < KU; ++u) {
-      const int k = k0 + u;
-      const float g = acc[u] * (1.0f - a[u] * a[u]);
-      d1[(long)k * cols + j] = g;
-      if (k < H) d1f[(long)k * ld + j] = __float2bfloat16_rn(g);
-    }
+    d1[(long)H * cols + j] = 0.0f;
   }
+  tc::tc_fence_before();
+  __syncthreads();
+  if (warp == 0) tc::tmem_dealloc(tmem, 64);
+  if (!ok) atomicExch(err, 1);
 }
 
 // grad[n * ldg + m] = sum_z P[z][m][n] for m < mreal, n < nreal (the GEMM row
@@ -156,6 +185,7 @@ constexpr int MAX_SPLIT_TILES = 296;
 struct BackwardWork {
   int in = 0, cols = 0, ld = 0;
   bf16 *xb = nullptr, *h1b = nullptr, *h2b = nullptr, *d2f = nullptr, *d3f = nullptr, *d1f = nullptr;
+  bf16* w1ts = nullptr;  // swizzled W1^T image for k_dgrad_tc
   float* scratch = nullptr;
   CUtensorMap txb, th1b, th2b, td2f, td3f, td1f;
 };
@@ -170,6 +200,7 @@ int backward_work_new(int in, int cols, BackwardWork** out) {
   if ((rc = walloc(&w->xb, (size_t)in * ld)) || (rc = walloc(&w->h1b, (size_t)HA * ld)) ||
       (rc = walloc(&w->h2b, (size_t)HA * ld)) || (rc = walloc(&w->d2f, (size_t)H * ld)) ||
       (rc = walloc(&w->d3f, (size_t)16 * ld)) || (rc = walloc(&w->d1f, (size_t)H * ld)) ||
+      (rc = walloc(&w->w1ts, (size_t)H * H)) ||
       (rc = walloc(&w->scratch, (size_t)MAX_SPLIT_TILES * 128 * 64))) {
     backward_work_delete(w);
     return rc;
@@ -186,7 +217,7 @@ int backward_work_new(int in, int cols, BackwardWork** out) {
 
 void backward_work_delete(BackwardWork* w) {
   if (!w) return;
-  for (bf16* p : {w->xb, w->h1b, w->h2b, w->d2f, w->d3f, w->d1f}) cudaFree(p);
+  for (bf16* p : {w->xb, w->h1b, w->h2b, w->d2f, w->d3f, w->d1f, w->w1ts}) cudaFree(p);
   cudaFree(w->scratch);
   delete w;
 }
@@ -223,7 +254,8 @@ int wgrad(BackwardWork* w, const CUtensorMap& ta, const CUtensorMap& tb, int mro
 }  // namespace
 
 int backward_refresh(BackwardWork* w, const float* theta, cudaStream_t st) {
-  (void)w, (void)theta, (void)st;  // the backward reads W1 from theta directly
+  k_pack_w1ts<<<(H * H + 255) / 256, 256, 0, st>>>(theta, w->in, w->w1ts);
+  BW_CHECK(cudaGetLastError());
   return 0;
 }
 
@@ -234,13 +266,8 @@ int backward_tc(BackwardWork* w, const float* theta, const float* x, const float
   k_rows_bf16<<<dim3(gx, in), 256, 0, st>>>(x, in, cols, w->xb, ld);
   k_rows_bf16<<<dim3(gx, HA), 256, 0, st>>>(h1, HA, cols, w->h1b, ld);
   k_rows_bf16<<<dim3(gx, HA), 256, 0, st>>>(h2, HA, cols, w->h2b, ld);
-  static bool dgrad_configured = false;
-  if (!dgrad_configured) {
-    BW_CHECK(cudaFuncSetAttribute(k_dgrad, cudaFuncAttributeMaxDynamicSharedMemorySize, DGRAD_SMEM));
-    dgrad_configured = true;
-  }
-  k_dgrad<<<(cols + DGRAD_THREADS - 1) / DGRAD_THREADS, DGRAD_THREADS, DGRAD_SMEM, st>>>(
-      in, theta, d3, h1, h2, d2, d1, cols, w->d1f, w->d2f, w->d3f, ld);
+  k_dgrad_tc<<<(cols + 127) / 128, 128, 0, st>>>(in, theta, reinterpret_cast<const uint4*>(w->w1ts), d3, h1, h2, d2,
+                                                 d1, cols, w->d1f, w->d2f, w->d3f, ld, err);
   BW_CHECK(cudaGetLastError());
   int rc;
   if ((rc = wgrad<64>(w, w->txb, w->td1f, in, H, in, grad, in, err, st))) return rc;

@@ -57,6 +57,11 @@ def test_track_validation_on_host(lib):
         W.Sim(bad, 4, 0)
     with pytest.raises(W.RacerError, match="beams"):
         W.Sim(track, 4, 0, beams=1)
+    for value in (np.nan, np.inf, 2e6):
+        bad = track.copy()
+        bad[12 + 641 * 641 + 7] = value  # a height
+        with pytest.raises(W.RacerError, match="heights"):
+            W.Sim(bad, 4, 0)
 
 
 def test_errors_are_reported_without_gpu(lib):

@@ -151,6 +151,10 @@ static int check_track(const float* d, size_t len) {
       float v = near[k];
       RACER_ARG(v >= 0 && v < (float)w && v == floorf(v), "track: nearest-waypoint grid out of range");
     }
+    // the lidar's probe relies on finite heights of at most 1e6 m (sim.cu, probe)
+    const float* height = d + 12 + (3 * l + 1) * nx * ny;
+    for (size_t k = 0; k < nx * ny; ++k)
+      RACER_ARG(fabsf(height[k]) <= 1e6f, "track: heights must be finite and within 1e6 m");
   }
   return 0;
 }

@@ -89,7 +89,11 @@ __device__ __forceinline__ bool cell_of(const TrackDev& t, float x, float y, lon
 }
 
 // racer/sim.mojo:116-124. LAYERS = 0 reads the layer count from the track.
-template <int LAYERS>
+// The first drivable layer is taken only if |height - z| < 1e30 (the initial
+// gap). GUARD = false drops that test where it cannot fail: grid heights are
+// finite with |h| <= 1e6 (checked on upload) and the caller knows |z| <= 1e20
+// + 10, so the result is the same.
+template <int LAYERS, bool GUARD = true>
 __device__ __forceinline__ Spot probe(const TrackDev& t, float x, float y, float z) {
   long idx;
   if (!cell_of(t, x, y, &idx)) return Spot{0, -1.0f, -1.0f};  // off the map every grid reads -1
@@ -98,7 +102,7 @@ __device__ __forceinline__ Spot probe(const TrackDev& t, float x, float y, float
   if (LAYERS == 2) {
     float4 v = __ldg(reinterpret_cast<const float4*>(t.cl) + idx);
     best = Spot{0, -1.0f, v.y};
-    if (v.x > 0.0f && fabsf(v.y - z) < gap) {
+    if (v.x > 0.0f && (!GUARD || fabsf(v.y - z) < gap)) {
       best = Spot{0, v.x, v.y};
       gap = fabsf(v.y - z);
     }
@@ -106,7 +110,7 @@ __device__ __forceinline__ Spot probe(const TrackDev& t, float x, float y, float
   } else if (LAYERS == 1) {
     float2 v = __ldg(t.cl + idx);
     best = Spot{0, -1.0f, v.y};
-    if (v.x > 0.0f && fabsf(v.y - z) < gap) best = Spot{0, v.x, v.y};
+    if (v.x > 0.0f && (!GUARD || fabsf(v.y - z) < gap)) best = Spot{0, v.x, v.y};
   } else {
     const int L = t.layers;
     const float2* p = t.cl + idx * L;
@@ -186,20 +190,23 @@ __device__ __forceinline__ V4 axpy(const V4& p, const V4& k, float h) {
 }
 
 // racer/sim.mojo:170-181. `local` is the car's index within its track's
-// segment (its Philox counter); i is its column in the batch.
-__device__ void spawn(const TrackDev& t, float* s, int n, int i, int local, uint64_t seed) {
+// segment (its Philox counter); i is its column in the batch. Returns the
+// pose written (x, y, z, heading).
+__device__ float4 spawn(const TrackDev& t, float* s, int n, int i, int local, uint64_t seed) {
   float episode = s[(long)EPISODE * n + i] + 1.0f;
   float r[4];
   philox::uniform4(seed, (uint64_t)local, (uint64_t)episode, r);
   int w = min((int)(r[0] * (float)t.waypoints), t.waypoints - 1);
+  const float4 pose = make_float4(waypoint(t, w, 0), waypoint(t, w, 1), waypoint(t, w, 2), waypoint(t, w, 3));
   for (int row = 0; row < STATE; ++row) s[(long)row * n + i] = 0.0f;
-  s[(long)X * n + i] = waypoint(t, w, 0);
-  s[(long)Y * n + i] = waypoint(t, w, 1);
-  s[(long)Z * n + i] = waypoint(t, w, 2);
-  s[(long)HEADING * n + i] = waypoint(t, w, 3);
+  s[(long)X * n + i] = pose.x;
+  s[(long)Y * n + i] = pose.y;
+  s[(long)Z * n + i] = pose.z;
+  s[(long)HEADING * n + i] = pose.w;
   s[(long)PROGRESS * n + i] = (float)w;
   s[(long)EPISODE * n + i] = episode;
   s[(long)FRICTION * n + i] = 0.85f + 0.3f * r[1];
+  return pose;
 }
 
 // Segment of car i (segments are few; a short scan).
@@ -272,11 +279,16 @@ __device__ __forceinline__ void advance_car(const TrackDev& t, float* s, const f
   reward[i] = score;
   done[i] = reason;
   float heading = p.h, speed = p.s;
+  // the pose the lidar frame starts from: the one just stored, and the layer
+  // the last probe chose (a probe at this cell with the height it returned
+  // selects that layer again)
+  float fx = p.x, fy = p.y, fz = spot.height;
+  int layer = spot.layer;
   if (reason > 0.0f) {
-    spawn(t, s, n, i, local, seed);
-    float sx = s[(long)X * n + i], sy = s[(long)Y * n + i];
-    ground = surface(t, probe<LAYERS>(t, sx, sy, s[(long)Z * n + i]).layer, sx, sy);
-    heading = s[(long)HEADING * n + i];
+    const float4 pose = spawn(t, s, n, i, local, seed);
+    fx = pose.x, fy = pose.y, fz = pose.z, heading = pose.w;
+    layer = probe<LAYERS>(t, fx, fy, fz).layer;
+    ground = surface(t, layer, fx, fy);
     speed = 0.0f;
     steer = 0.0f;
   }
@@ -293,9 +305,8 @@ __device__ __forceinline__ void advance_car(const TrackDev& t, float* s, const f
   // second half carries the car's layer (surrogate input).
   float ch, sh;
   rmath::sincosf_(heading, &sh, &ch);
-  const float sx = s[(long)X * n + i], sy = s[(long)Y * n + i], sz = s[(long)Z * n + i];
-  ray[i] = make_float4((sx + MOUNT_X * ch) + 0.0f, (sy + MOUNT_X * sh) + 0.0f, (sz + MOUNT_X * along) + MOUNT_Z, ch);
-  ray[n + i] = make_float4(sh, along, across, (float)probe<LAYERS>(t, sx, sy, sz).layer);
+  ray[i] = make_float4((fx + MOUNT_X * ch) + 0.0f, (fy + MOUNT_X * sh) + 0.0f, (fz + MOUNT_X * along) + MOUNT_Z, ch);
+  ray[n + i] = make_float4(sh, along, across, (float)layer);
 }
 
 // With eval_reward set, each car also adds its reward (FP64) and a crash
@@ -522,6 +533,10 @@ __global__ void __launch_bounds__(CARS * 32, lidar_min_blocks(CARS, WIDE))
   if (car < g.car0[k + 1]) trace_any(g.t[k], ray, obs, n, beam_dir, g.max_iters[k], iters, car, beam);
 }
 
+template <int LAYERS, bool GUARD>
+__device__ __forceinline__ float march(const TrackDev& t, float ox, float oy, float oz, float dx, float dy, float dz,
+                                       float descent, float inv_descent, int max_iters, int* count_out);
+
 template <int LAYERS>
 __device__ __forceinline__ void trace(const TrackDev& t, const float4* __restrict__ ray, float* obs, int n,
                                       const float2* __restrict__ beam_dir, int max_iters, int* iters, int car,
@@ -538,13 +553,27 @@ __device__ __forceinline__ void trace(const TrackDev& t, const float4* __restric
   const float ox = r0.x, oy = r0.y, oz = r0.z;
   const float descent = (1.5f * t.slope) * sqrtf(dx * dx + dy * dy) + fmaxf(-dz, 0.0f);
   const float inv_descent = 1.0f / descent;
+  int count = 0;
+  // every probe height lies within RANGE of the origin's (|dz| <= 1): with
+  // |oz| <= 1e20 the probe's height guard cannot fail (NaN takes the guarded loop)
+  const float range = fabsf(oz) <= 1e20f
+                          ? march<LAYERS, false>(t, ox, oy, oz, dx, dy, dz, descent, inv_descent, max_iters, &count)
+                          : march<LAYERS, true>(t, ox, oy, oz, dx, dy, dz, descent, inv_descent, max_iters, &count);
+  obs[(long)(4 + beam) * n + car] = range / RANGE;
+  if (iters) iters[(long)beam * n + car] = count;
+}
+
+// The march of one beam (racer/sim.mojo:252-266); returns the range.
+template <int LAYERS, bool GUARD>
+__device__ __forceinline__ float march(const TrackDev& t, float ox, float oy, float oz, float dx, float dy, float dz,
+                                       float descent, float inv_descent, int max_iters, int* count_out) {
   const float cell = t.cell, min_step = 0.5f * t.cell;
   float tt = 0.0f, last = 0.0f, last_floor = 0.0f, range = -1.0f;
   int count = 0;
   while (tt < RANGE && count < max_iters) {
     ++count;
     const float px = ox + tt * dx, py = oy + tt * dy, pz = oz + tt * dz;
-    const Spot spot = probe<LAYERS>(t, px, py, pz);
+    const Spot spot = probe<LAYERS, GUARD>(t, px, py, pz);
     const float fl = (pz - spot.height) - 0.03f;
     if (fl < 0.0f) {
       range = fminf(last + ((tt - last) * last_floor) / (last_floor - fl), RANGE);
@@ -564,9 +593,8 @@ __device__ __forceinline__ void trace(const TrackDev& t, const float4* __restric
     last_floor = fl;
     tt += step;
   }
-  if (range < 0.0f) range = fminf(tt, RANGE);
-  obs[(long)(4 + beam) * n + car] = range / RANGE;
-  if (iters) iters[(long)beam * n + car] = count;
+  *count_out = count;
+  return range < 0.0f ? fminf(tt, RANGE) : range;
 }
 
 // racer/sim.mojo:323-348. step = *step_base (if given) + step_add.

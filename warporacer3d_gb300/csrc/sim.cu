@@ -581,13 +581,14 @@ __device__ __forceinline__ float march(const TrackDev& t, float ox, float oy, fl
     }
     const float a = spot.clearance - cell;
     if (a < min_step) break;  // min(a, fl / descent) <= a < min_step
-    // For descent == 0 the quotient is +inf or NaN (fl >= 0 here) and fminf
-    // returns a. Otherwise fl * RN(1/descent) is within (1 + 2^-23) of the
-    // exact fl / descent, so a product above a * (1 + 2^-20) proves the
-    // correctly rounded quotient is >= a and min() returns a: the division
-    // is needed only when the floor term may win.
+    // fl * RN(1/descent) is within (1 + 2^-23) of the exact fl / descent, so
+    // a product above a * (1 + 2^-20) proves the correctly rounded quotient
+    // is >= a and min() returns a: the division is needed only when the
+    // floor term may win. For descent == 0 (fl >= 0 here) the product is +inf,
+    // which skips, or NaN (fl == 0), where the quotient is NaN too and fminf
+    // returns a: the reference's min(a, fl / 0) either way.
     float step = a;
-    if (descent != 0.0f && !(fl * inv_descent > a * 1.00000095f)) step = fminf(a, fl / descent);
+    if (!(fl * inv_descent > a * 1.00000095f)) step = fminf(a, fl / descent);
     if (step < min_step) break;
     last = tt;
     last_floor = fl;

@@ -96,6 +96,13 @@ int racer_sim_get_lidar_shape(racer_sim* sim, racer_lidar_shape* shape);
  * ms. The lidar only rewrites obs rows from the frames: the sim's state is
  * unchanged. */
 int racer_sim_autotune(racer_sim* sim, int reps, racer_lidar_shape* best, float* best_ms);
+/* Rollout graphs (racer_rollout) as `chains` (1..8) independent chains of
+ * Runner steps over consecutive car ranges (multiples of 128), forked from and
+ * joined into the sim's stream, so one chain's policy forward and physics run
+ * beside another chain's lidar. Cars never interact, so every result is the
+ * one-chain rollout's. Applies to one-track sims with a BF16 policy; drops
+ * captured graphs. */
+int racer_sim_set_chains(racer_sim* sim, int chains);
 int racer_sim_destroy(racer_sim* sim);
 int racer_sim_get_buffers(racer_sim* sim, racer_sim_buffers* out);
 /* Sim.reset (racer/sim.mojo:291-305): spawn every car, then a step at rest. */
@@ -190,6 +197,11 @@ int racer_runner_step(racer_sim* sim, racer_policy* policy, racer_acts* acts, fl
  * offsets are step0, step0 + 1, ... */
 int racer_rollout(racer_sim* sim, racer_policy* policy, racer_acts* acts, float* scratch_dev, int steps,
                   int deterministic, int64_t step0);
+/* Autotuner for the chain count: times `reps` rollouts of `steps` stochastic
+ * Runner steps for 1 to 4 chains (after one warm-up rollout each; the sim
+ * state advances), keeps the fastest and returns it with its env-steps/s. */
+int racer_runner_tune_chains(racer_sim* sim, racer_policy* policy, racer_acts* acts, float* scratch_dev, int steps,
+                             int reps, int* best_chains, float* best_rate);
 /* Runner.evaluate (main.mojo:70-80): `steps` deterministic Runner steps
  * (sampling offsets step0, step0 + 1, ...) replayed from one CUDA graph in
  * which the physics kernel adds every car's reward (FP64) and crash to

@@ -269,6 +269,9 @@ int racer_sim_destroy(racer_sim* s) {
   for (auto& kv : s->graphs) cudaGraphExecDestroy(kv.second);
   for (auto& kv : s->surrogate_graphs) cudaGraphExecDestroy(kv.second);
   cudaFree(s->counters);
+  for (cudaStream_t c : s->chain_st) cudaStreamDestroy(c);
+  for (cudaEvent_t e : s->chain_join) cudaEventDestroy(e);
+  if (s->chain_fork) cudaEventDestroy(s->chain_fork);
   for (auto& kv : s->eval_graphs) cudaGraphExecDestroy(kv.second);
   cudaFree(s->eval_reward);
   cudaFree(s->eval_crash);
@@ -464,8 +467,8 @@ int racer_acts_buffers(racer_acts* a, float** h1, float** h2, float** o) {
 }
 
 static int forward_on(racer_policy* p, const float* x, racer_acts* a, cudaStream_t st,
-                      const SampleArgs* sa = nullptr, int write_hidden = 1) {
-  return policy_forward(p, x, a->cols, a->h1, a->h2, a->o, write_hidden, sa, st);
+                      const SampleArgs* sa = nullptr, int write_hidden = 1, int c0 = 0, int c1 = -1) {
+  return policy_forward(p, x, a->cols, a->h1, a->h2, a->o, write_hidden, sa, st, c0, c1);
 }
 
 int racer_policy_status(racer_policy* p, int* code) {
@@ -731,6 +734,27 @@ int racer_trainer_update(racer_trainer* tr, racer_policy* p, float* kl) {
 
 // One Runner step (main.mojo:40-48). With a surrogate, the lidar rows come
 // from it (audited by, or falling back to, the exact tracer).
+// Cars [c0, c1) only (a rollout chain): policy forward and sampling, physics
+// and the lidar of those cars; every per-car result is the full step's.
+static int runner_step_cars(racer_sim* s, racer_policy* p, racer_acts* a, float* scratch, int det, const int64_t* base,
+                            int64_t add, cudaStream_t st, int c0, int c1) {
+  SampleArgs sa;
+  sa.seed = s->seed;
+  sa.log_std = policy_theta(p) + policy_params(p) - 2;
+  sa.actions = s->actions;
+  sa.logp = scratch;
+  sa.value = scratch + s->n;
+  sa.deterministic = det;
+  sa.step_base = base;
+  sa.step_add = add;
+  if (int rc = forward_on(p, s->obs, a, st, &sa, 0, c0, c1)) return rc;
+  launch_advance(s->seg, s->state, s->actions, s->reward, s->done, s->obs, s->n, s->beams, s->ray, st, nullptr,
+                 nullptr, c0, c1);
+  launch_lidar_cars(s->seg, s->shape, c0, c1, s->ray, s->obs, s->n, s->beams, s->beam_dir, nullptr, st);
+  RACER_LAUNCHED();
+  return 0;
+}
+
 static int runner_step_on(racer_sim* s, racer_policy* p, racer_acts* a, float* scratch, int det,
                           const int64_t* base, int64_t add, cudaStream_t st, racer_surrogate* sur = nullptr,
                           bool audit = false, float fallback = 0.0f, bool eval = false) {
@@ -941,7 +965,30 @@ static int rollout_graph(racer_sim* s, racer_policy* p, racer_acts* a, float* sc
     cudaGraph_t g;
     RACER_TRY(cudaStreamBeginCapture(s->st, cudaStreamCaptureModeThreadLocal));
     int rc = 0;
-    for (int k = 0; k < steps && !rc; ++k) rc = runner_step_on(s, p, a, scratch, det, s->step_base, k, s->st);
+    const int chains = s->chains > 1 && s->seg.count == 1 && policy_is_bf16(p) ? s->chains : 1;
+    if (chains == 1) {
+      for (int k = 0; k < steps && !rc; ++k) rc = runner_step_on(s, p, a, scratch, det, s->step_base, k, s->st);
+    } else {
+      // independent chains over car ranges (multiples of 128, the forward's tile), forked from and joined
+      // into the sim's stream: parallel branches, so one chain's latency-bound kernels run beside
+      // another's lidar
+      int bound[9];
+      for (int c = 0; c <= chains; ++c) bound[c] = c == chains ? s->n : std::min(s->n, (int)((long)s->n * c / chains / 128 * 128));
+      cudaError_t e = cudaEventRecord(s->chain_fork, s->st);
+      for (int c = 1; c < chains && e == cudaSuccess; ++c) e = cudaStreamWaitEvent(s->chain_st[c - 1], s->chain_fork, 0);
+      for (int k = 0; k < steps && !rc && e == cudaSuccess; ++k)
+        for (int c = 0; c < chains && !rc; ++c)
+          rc = runner_step_cars(s, p, a, scratch, det, s->step_base, k, c ? s->chain_st[c - 1] : s->st, bound[c],
+                                bound[c + 1]);
+      for (int c = 1; c < chains && e == cudaSuccess; ++c) {
+        e = cudaEventRecord(s->chain_join[c - 1], s->chain_st[c - 1]);
+        if (e == cudaSuccess) e = cudaStreamWaitEvent(s->st, s->chain_join[c - 1], 0);
+      }
+      if (e != cudaSuccess && !rc) {
+        set_error(std::string("rollout chains: ") + cudaGetErrorString(e));
+        rc = 2;
+      }
+    }
     cudaError_t end = cudaStreamEndCapture(s->st, &g);
     if (rc) return rc;
     RACER_TRY(end);
@@ -975,6 +1022,38 @@ int racer_rollout(racer_sim* s, racer_policy* p, racer_acts* a, float* scratch, 
   k_set_i64<<<1, 32, 0, s->st>>>(s->step_base, step0);
   RACER_LAUNCHED();
   RACER_TRY(cudaGraphLaunch(exec, s->st));
+  return 0;
+}
+
+int racer_runner_tune_chains(racer_sim* s, racer_policy* p, racer_acts* a, float* scratch, int steps, int reps,
+                             int* best_chains, float* best_rate) {
+  RACER_ARG(s && p && a && scratch && steps >= 1 && reps >= 1, "racer_runner_tune_chains: bad argument");
+  cudaEvent_t t0, t1;
+  RACER_TRY(cudaEventCreate(&t0));
+  RACER_TRY(cudaEventCreate(&t1));
+  int best = 1;
+  float rate = 0.0f;
+  const int max_chains = s->seg.count == 1 && policy_is_bf16(p) ? 4 : 1;
+  int64_t step0 = 0;
+  for (int chains = 1; chains <= max_chains; ++chains) {
+    if (int rc = racer_sim_set_chains(s, chains)) return rc;
+    if (int rc = racer_rollout(s, p, a, scratch, steps, 0, step0)) return rc;  // capture and warm up
+    step0 += steps;
+    RACER_TRY(cudaEventRecord(t0, s->st));
+    for (int r = 0; r < reps; ++r, step0 += steps)
+      if (int rc = racer_rollout(s, p, a, scratch, steps, 0, step0)) return rc;
+    RACER_TRY(cudaEventRecord(t1, s->st));
+    RACER_TRY(cudaEventSynchronize(t1));
+    float ms = 0.0f;
+    RACER_TRY(cudaEventElapsedTime(&ms, t0, t1));
+    const float r = (float)((double)s->n * steps * reps / (ms / 1000.0));
+    if (r > rate) rate = r, best = chains;
+  }
+  cudaEventDestroy(t0);
+  cudaEventDestroy(t1);
+  if (int rc = racer_sim_set_chains(s, best)) return rc;
+  if (best_chains) *best_chains = best;
+  if (best_rate) *best_rate = rate;
   return 0;
 }
 
@@ -1084,6 +1163,23 @@ static bool same_shape(const racer_sim* s, const LidarShape& a, const LidarShape
   segment_order(s, b, ob);
   return a.cars == b.cars && a.wide == b.wide && a.split == b.split && a.dynamic == b.dynamic &&
          std::equal(oa, oa + s->seg.count, ob);
+}
+
+int racer_sim_set_chains(racer_sim* s, int chains) {
+  RACER_ARG(s && chains >= 1 && chains <= 8, "racer_sim_set_chains: 1 to 8 chains");
+  RACER_TRY(cudaStreamSynchronize(s->st));
+  if (!s->chain_fork) RACER_TRY(cudaEventCreateWithFlags(&s->chain_fork, cudaEventDisableTiming));
+  while ((int)s->chain_st.size() < chains - 1) {
+    cudaStream_t c;
+    cudaEvent_t e;
+    RACER_TRY(cudaStreamCreateWithFlags(&c, cudaStreamNonBlocking));
+    s->chain_st.push_back(c);
+    RACER_TRY(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+    s->chain_join.push_back(e);
+  }
+  if (chains != s->chains) drop_graphs(s);
+  s->chains = chains;
+  return 0;
 }
 
 int racer_sim_set_lidar_shape(racer_sim* s, const racer_lidar_shape* in) {

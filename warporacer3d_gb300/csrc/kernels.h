@@ -15,7 +15,10 @@ void launch_spawn(const Segments& g, float* state, float* actions, int n, cudaSt
 // eval_reward / eval_crash [n] set, each car adds its reward and crash to them.
 void launch_advance(const Segments& g, float* state, const float* actions, float* reward, float* done, float* obs,
                     int n, int beams, float4* ray, cudaStream_t st, double* eval_reward = nullptr,
-                    int* eval_crash = nullptr);
+                    int* eval_crash = nullptr, int c0 = 0, int c1 = -1);
+// The lidar of cars [c0, c1) of a one-track sim (its one-track kernel, static shapes).
+void launch_lidar_cars(const Segments& g, const LidarShape& shape, int c0, int c1, const float4* ray, float* obs,
+                       int n, int beams, const float2* beam_dir, int* iters, cudaStream_t st);
 void launch_lidar(const Segments& g, const LidarShape& shape, const float4* ray, float* obs, int n, int beams,
                   const float2* beam_dir, int* iters, cudaStream_t st);
 // The lidar of segment k alone (its one-track kernel), for per-segment launches on parallel streams.

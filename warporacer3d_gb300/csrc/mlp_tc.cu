@@ -57,7 +57,7 @@ struct FwdCfg {
 // epilogues and issue layers 2 and 3.
 template <int GROUPS>
 __global__ void __launch_bounds__(FwdCfg<GROUPS>::THREADS, FwdCfg<GROUPS>::MIN_BLOCKS)
-    k_mlp_fwd(const float* __restrict__ x, int in, int cols,
+    k_mlp_fwd(const float* __restrict__ x, int in, int cols, int c0, int c1,
                                                         const uint4* __restrict__ w0s, int kblocks,
                                                         const uint4* __restrict__ w1s,
                                                         const uint4* __restrict__ w2s, float* h1g, float* h2g,
@@ -75,8 +75,8 @@ __global__ void __launch_bounds__(FwdCfg<GROUPS>::THREADS, FwdCfg<GROUPS>::MIN_B
 
   const int tid = threadIdx.x, warp = tid >> 5;
   const int r = tid & (TILE - 1);  // sample row of a producer or epilogue thread
-  const int c = blockIdx.x * TILE + r;
-  const bool live = c < cols;
+  const int c = c0 + (int)blockIdx.x * TILE + r;  // column (sample) of the [rows, cols] buffers
+  const bool live = c < c1;
 
   if (tid == 0) {
     for (int g = 0; g < GROUPS; ++g) {
@@ -256,9 +256,9 @@ void launch_pack_weights(const float* theta, int in, uint8_t* pack, cudaStream_t
 }
 
 template <int GROUPS>
-static cudaError_t fwd_launch(const float* x, int in, int cols, int kb, const uint4* w0, const uint4* w1,
-                              const uint4* w2, float* h1, float* h2, float* o, int write_hidden, const SampleArgs& sa,
-                              int* err, cudaStream_t st) {
+static cudaError_t fwd_launch(const float* x, int in, int cols, int c0, int c1, int kb, const uint4* w0,
+                              const uint4* w1, const uint4* w2, float* h1, float* h2, float* o, int write_hidden,
+                              const SampleArgs& sa, int* err, cudaStream_t st) {
   using C = FwdCfg<GROUPS>;
   static bool configured = false;
   if (!configured) {
@@ -266,19 +266,21 @@ static cudaError_t fwd_launch(const float* x, int in, int cols, int kb, const ui
     if (e != cudaSuccess) return e;
     configured = true;
   }
-  k_mlp_fwd<GROUPS><<<(cols + TILE - 1) / TILE, C::THREADS, C::SMEM_BYTES, st>>>(x, in, cols, w0, kb, w1, w2, h1, h2,
-                                                                               o, write_hidden, sa, err);
+  if (c1 <= c0) return cudaSuccess;
+  k_mlp_fwd<GROUPS><<<(c1 - c0 + TILE - 1) / TILE, C::THREADS, C::SMEM_BYTES, st>>>(x, in, cols, c0, c1, w0, kb, w1, w2,
+                                                                                  h1, h2, o, write_hidden, sa, err);
   return cudaGetLastError();
 }
 
 cudaError_t launch_mlp_fwd(const float* x, int in, int cols, const uint8_t* pack, float* h1, float* h2, float* o,
-                           int write_hidden, const SampleArgs& sa, int* err, cudaStream_t st) {
+                           int write_hidden, const SampleArgs& sa, int* err, cudaStream_t st, int c0, int c1) {
+  if (c1 < 0) c1 = cols;
   int kb = (in + 63) / 64;
   const uint4* w0 = reinterpret_cast<const uint4*>(pack);
   const uint4* w1 = reinterpret_cast<const uint4*>(pack + (size_t)kb * 8192);
   const uint4* w2 = reinterpret_cast<const uint4*>(pack + (size_t)kb * 8192 + 2 * 8192);
-  if (kb <= 4) return fwd_launch<2>(x, in, cols, kb, w0, w1, w2, h1, h2, o, write_hidden, sa, err, st);
-  return fwd_launch<4>(x, in, cols, kb, w0, w1, w2, h1, h2, o, write_hidden, sa, err, st);
+  if (kb <= 4) return fwd_launch<2>(x, in, cols, c0, c1, kb, w0, w1, w2, h1, h2, o, write_hidden, sa, err, st);
+  return fwd_launch<4>(x, in, cols, c0, c1, kb, w0, w1, w2, h1, h2, o, write_hidden, sa, err, st);
 }
 
 }  // namespace racer

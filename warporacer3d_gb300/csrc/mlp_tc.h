@@ -20,7 +20,9 @@ struct SampleArgs {
 
 size_t mlp_pack_bytes(int in);
 void launch_pack_weights(const float* theta, int in, uint8_t* pack, cudaStream_t st);
+// Columns [c0, c1) of the [rows, cols] buffers (c1 < 0: all of them).
 cudaError_t launch_mlp_fwd(const float* x, int in, int cols, const uint8_t* pack, float* h1, float* h2, float* o,
-                           int write_hidden, const SampleArgs& sa, int* err, cudaStream_t st);
+                           int write_hidden, const SampleArgs& sa, int* err, cudaStream_t st, int c0 = 0,
+                           int c1 = -1);
 
 }  // namespace racer

@@ -29,6 +29,11 @@ struct racer_sim {
   std::vector<cudaEvent_t> join;
   cudaEvent_t fork = nullptr;
   unsigned* counters = nullptr;  // [MAX_SEGMENTS] unit counters of the dynamic lidar
+  // rollouts as independent chains over car ranges (parallel branches of the graph)
+  int chains = 1;
+  std::vector<cudaStream_t> chain_st;
+  std::vector<cudaEvent_t> chain_join;
+  cudaEvent_t chain_fork = nullptr;
   // device-side evaluation: per-car reward (FP64) and crash sums, and the two totals
   double* eval_reward = nullptr;
   int* eval_crash = nullptr;

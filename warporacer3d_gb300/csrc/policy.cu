@@ -73,18 +73,25 @@ int policy_refresh_on(racer_policy* p, cudaStream_t st) {
   return 0;
 }
 
+int policy_is_bf16(racer_policy* p) { return p->bf16; }
+
 int policy_set_precision(racer_policy* p, int bf16) {
   p->bf16 = bf16 ? 1 : 0;
   return 0;
 }
 
 int policy_forward(racer_policy* p, const float* x, int cols, float* h1, float* h2, float* o, int write_hidden,
-                   const SampleArgs* sa, cudaStream_t st) {
+                   const SampleArgs* sa, cudaStream_t st, int c0, int c1) {
   cudaError_t err;
+  if (c1 < 0) c1 = cols;
   if (p->bf16) {
     SampleArgs none;
-    err = launch_mlp_fwd(x, p->in, cols, p->pack, h1, h2, o, write_hidden, sa ? *sa : none, p->err, st);
+    err = launch_mlp_fwd(x, p->in, cols, p->pack, h1, h2, o, write_hidden, sa ? *sa : none, p->err, st, c0, c1);
   } else {
+    if (c0 != 0 || c1 != cols) {
+      racer_host::set_error("policy forward: column ranges need the BF16 path");
+      return 1;
+    }
     const int in = p->in, w1 = H * in, w2 = w1 + H * HA;
     launch_sgemm(p->theta, in, x, cols, h1, cols, H, cols, in, 1, st);
     launch_sgemm(p->theta + w1, HA, h1, cols, h2, cols, H, cols, HA, 1, st);

@@ -17,8 +17,11 @@ int policy_refresh(racer_policy* p);
 int policy_refresh_on(racer_policy* p, cudaStream_t st);
 // x [IN, cols] -> h1, h2 [65, cols] (row 64 stays 1; written only if
 // write_hidden), o [3, cols]; with sa->actions set, also the sampled actions.
+// Columns [c0, c1) only (c1 < 0: all; BF16 path only).
 int policy_forward(racer_policy* p, const float* x, int cols, float* h1, float* h2, float* o, int write_hidden,
-                   const racer::SampleArgs* sa, cudaStream_t st);
+                   const racer::SampleArgs* sa, cudaStream_t st, int c0 = 0, int c1 = -1);
+// 1 if the policy computes in BF16 on the tensor cores.
+int policy_is_bf16(racer_policy* p);
 // Device-side error word of the tensor-core kernels (0 = none); synchronises.
 int policy_status(racer_policy* p, int* code);
 int policy_backward(racer_policy* p, const float* x, int cols, const float* h1, const float* h2, const float* d3,

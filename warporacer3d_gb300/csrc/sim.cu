@@ -312,9 +312,10 @@ __device__ __forceinline__ void advance_car(const TrackDev& t, float* s, const f
 // With eval_reward set, each car also adds its reward (FP64) and a crash
 // count to its own accumulators (racer eval's sums, kept on the device).
 __global__ void k_advance(const __grid_constant__ Segments g, float* s, const float* act, float* reward, float* done,
-                          float* obs, int n, int beams, float4* ray, double* eval_reward, int* eval_crash) {
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= n) return;
+                          float* obs, int n, int beams, float4* ray, double* eval_reward, int* eval_crash, int c0,
+                          int c1) {
+  const int i = c0 + (int)(blockIdx.x * blockDim.x + threadIdx.x);
+  if (i >= c1) return;
   const int k = segment_of(g, i);
   const TrackDev& t = g.t[k];
   if (t.layers == 1)
@@ -631,10 +632,15 @@ void launch_spawn(const Segments& g, float* state, float* actions, int n, cudaSt
 }
 
 void launch_advance(const Segments& g, float* state, const float* actions, float* reward, float* done, float* obs,
-                    int n, int beams, float4* ray, cudaStream_t st, double* eval_reward, int* eval_crash) {
-  k_advance<<<(n + 127) / 128, 128, 0, st>>>(g, state, actions, reward, done, obs, n, beams, ray, eval_reward,
-                                             eval_crash);
+                    int n, int beams, float4* ray, cudaStream_t st, double* eval_reward, int* eval_crash, int c0,
+                    int c1) {
+  if (c1 < 0) c1 = n;
+  if (c1 <= c0) return;
+  k_advance<<<(c1 - c0 + 127) / 128, 128, 0, st>>>(g, state, actions, reward, done, obs, n, beams, ray, eval_reward,
+                                                   eval_crash, c0, c1);
 }
+
+
 
 int lidar_max_iters(const TrackDev& t) { return (int)ceilf(RANGE / (0.5f * t.cell)) + 2; }
 
@@ -747,6 +753,28 @@ void launch_lidar_segment(const Segments& g, int k, const LidarShape& shape, con
   else
     wide ? lidar_segment<4, true>(g, k, ray, obs, n, beams, beam_dir, iters, st, shape)
          : lidar_segment<4, false>(g, k, ray, obs, n, beams, beam_dir, iters, st, shape);
+}
+
+void launch_lidar_cars(const Segments& g, const LidarShape& shape, int c0, int c1, const float4* ray, float* obs,
+                       int n, int beams, const float2* beam_dir, int* iters, cudaStream_t st) {
+  if (g.count != 1 || c1 <= c0) return;
+  const TrackDev& t = g.t[0];
+  const bool wide = shape.wide == 1;
+#define RACER_LIDAR_CARS(CARS, WIDE)                                                                         \
+  if (t.layers == 1)                                                                                          \
+    lidar_track<1, CARS, WIDE>(t, g.max_iters[0], ray, obs, n, c0, c1, beams, beam_dir, iters, st);         \
+  else if (t.layers == 2)                                                                                     \
+    lidar_track<2, CARS, WIDE>(t, g.max_iters[0], ray, obs, n, c0, c1, beams, beam_dir, iters, st);         \
+  else                                                                                                        \
+    lidar_track<0, CARS, WIDE>(t, g.max_iters[0], ray, obs, n, c0, c1, beams, beam_dir, iters, st);
+  if (shape.cars == 2) {
+    if (wide) { RACER_LIDAR_CARS(2, true) } else { RACER_LIDAR_CARS(2, false) }
+  } else if (shape.cars == 8) {
+    if (wide) { RACER_LIDAR_CARS(8, true) } else { RACER_LIDAR_CARS(8, false) }
+  } else {
+    if (wide) { RACER_LIDAR_CARS(4, true) } else { RACER_LIDAR_CARS(4, false) }
+  }
+#undef RACER_LIDAR_CARS
 }
 
 void launch_lidar(const TrackDev& t, const float4* ray, float* obs, int n, int beams, const float2* beam_dir,

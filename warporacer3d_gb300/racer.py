@@ -182,6 +182,10 @@ class Sim:
         call("racer_sim_get_lidar_shape", self.handle, ctypes.byref(shape))
         return self._shape(shape)
 
+    def set_chains(self, chains):
+        """Rollout graphs as `chains` independent chains over car ranges (the same results)."""
+        call("racer_sim_set_chains", self.handle, int(chains))
+
     def autotune(self, reps=5):
         """Times every lidar launch shape on the current frames; keeps the fastest and returns it
         with its mean time in ms."""
@@ -432,6 +436,13 @@ class Runner:
         return {"cars": int(out[0]), "position_mean_m": out[1] / count, "heading_mean_rad": out[2] / count,
                 "speed_mean_mps": out[3] / count, "position_max_m": out[4], "heading_max_rad": out[5],
                 "speed_max_mps": out[6]}
+
+    def tune_chains(self, steps=50, reps=3):
+        """Times rollouts with 1 to 4 chains, keeps the fastest; returns (chains, env-steps/s)."""
+        best, rate = ctypes.c_int(), ctypes.c_float()
+        call("racer_runner_tune_chains", self.sim.handle, self.policy.handle, self.acts.handle, self.scratch.c, steps,
+             reps, ctypes.byref(best), ctypes.byref(rate))
+        return best.value, rate.value
 
     def synchronize(self):
         call("racer_synchronize", self.sim.stream)

@@ -299,6 +299,10 @@ def training_section(W, iterations):
         for seed in TRAIN_SEEDS:
             runner = W.Runner(track, TRAIN_CARS, beams=TRAIN_BEAMS, seed=seed, policy_seed=seed)
             runner.policy.set_precision(precision)
+            state, obs = runner.sim.state.numpy(), runner.sim.obs.numpy()
+            chains, _ = runner.tune_chains(32, 2)  # rollout chains (BF16 only), then back to the start state
+            runner.sim.state.write(state)
+            runner.sim.obs.write(obs)
             trainer = W.Trainer(TRAIN_CARS, beams=TRAIN_BEAMS, rollout=TRAIN_ROLLOUT, stream=runner.sim.stream)
             rewards, kls = [], []
             t0 = time.perf_counter()
@@ -307,7 +311,8 @@ def training_section(W, iterations):
                 kls.append(trainer.update(runner.policy))
             dt = time.perf_counter() - t0
             k = max(1, min(20, iterations // 5))
-            runs.append({"seed": seed, "training_transitions_per_s": TRAIN_CARS * TRAIN_ROLLOUT * iterations / dt,
+            runs.append({"seed": seed, "rollout_chains": chains,
+                         "training_transitions_per_s": TRAIN_CARS * TRAIN_ROLLOUT * iterations / dt,
                          "reward_per_step_first": float(np.mean(rewards[:k])),
                          "reward_per_step_last": float(np.mean(rewards[-k:])), "kl_last": float(kls[-1]),
                          "finite": bool(np.isfinite(rewards).all() and np.isfinite(kls).all()), "seconds": dt})

@@ -182,3 +182,21 @@ def test_rollout_chains_match_one_chain(chains):
     for name in ("state", "obs", "actions", "reward", "done"):
         assert np.array_equal(getattr(a.sim, name).numpy(), getattr(b.sim, name).numpy()), name
     assert b.rollout_kernel_count(12) > a.rollout_kernel_count(12)
+
+
+def test_trainer_rollout_with_chains_matches_one_chain():
+    """Trainer.rollout with rollout chains fills the rollout storage with the one-chain bits."""
+    out = []
+    for chains in (1, 3):
+        sim = W.Sim(W.track("bank"), 1000, 3, beams=108)
+        sim.reset()
+        policy = W.Policy(5, beams=108)
+        acts = W.Activations(policy, 1000)
+        sim.set_chains(chains)
+        trainer = W.Trainer(1000, beams=108, rollout=8)
+        reward = trainer.rollout(sim, policy, acts, 0)
+        out.append((reward, trainer.obs.numpy(), trainer.actions.numpy(), trainer.advantage.numpy(),
+                    sim.state.numpy()))
+    for a, b in zip(out[0][1:], out[1][1:]):
+        assert np.array_equal(a, b)
+    assert out[0][0] == out[1][0]

@@ -647,6 +647,14 @@ int racer_trainer_rollout(racer_trainer* tr, racer_sim* s, racer_policy* p, race
   const size_t n = tr->n, IN = tr->in_rows, R = tr->rollout;
   const float* logstd = policy_theta(p) + policy_params(p) - 2;
   RACER_TRY(cudaMemcpyAsync(tr->obs, s->obs, IN * n * sizeof(float), cudaMemcpyDeviceToDevice, st));
+  // with rollout chains (racer_sim_set_chains), each car range steps on its own stream
+  const int chains = s->chains > 1 && s->seg.count == 1 && policy_is_bf16(p) ? s->chains : 1;
+  int bound[9];
+  for (int c = 0; c <= chains; ++c) bound[c] = c == chains ? (int)n : std::min((int)n, (int)((long)n * c / chains / 128 * 128));
+  if (chains > 1) {
+    RACER_TRY(cudaEventRecord(s->chain_fork, st));
+    for (int c = 1; c < chains; ++c) RACER_TRY(cudaStreamWaitEvent(s->chain_st[c - 1], s->chain_fork, 0));
+  }
   for (size_t t = 0; t < R; ++t) {
     SampleArgs sa;
     sa.seed = s->seed;
@@ -655,12 +663,30 @@ int racer_trainer_rollout(racer_trainer* tr, racer_sim* s, racer_policy* p, race
     sa.logp = tr->logp + t * n;
     sa.value = tr->value + t * n;
     sa.step_add = (int64_t)iteration * (int64_t)R + (int64_t)t;
-    int rc = forward_on(p, tr->obs + t * IN * n, a, st, &sa, 0);
-    if (rc) return rc;
-    if ((rc = sim_step_on(s, tr->actions + t * 2 * n, tr->reward + t * n, tr->done + t * n, tr->obs + (t + 1) * IN * n,
-                          nullptr, st)))
-      return rc;
+    if (chains == 1) {
+      int rc = forward_on(p, tr->obs + t * IN * n, a, st, &sa, 0);
+      if (rc) return rc;
+      if ((rc = sim_step_on(s, tr->actions + t * 2 * n, tr->reward + t * n, tr->done + t * n,
+                            tr->obs + (t + 1) * IN * n, nullptr, st)))
+        return rc;
+      continue;
+    }
+    for (int c = 0; c < chains; ++c) {
+      cudaStream_t cs = c ? s->chain_st[c - 1] : st;
+      if (int rc = forward_on(p, tr->obs + t * IN * n, a, cs, &sa, 0, bound[c], bound[c + 1])) return rc;
+      float* obs_next = tr->obs + (t + 1) * IN * n;
+      launch_advance(s->seg, s->state, tr->actions + t * 2 * n, tr->reward + t * n, tr->done + t * n, obs_next,
+                     (int)n, s->beams, s->ray, cs, nullptr, nullptr, bound[c], bound[c + 1]);
+      launch_lidar_cars(s->seg, s->shape, bound[c], bound[c + 1], s->ray, obs_next, (int)n, s->beams, s->beam_dir,
+                        nullptr, cs);
+      RACER_LAUNCHED();
+    }
   }
+  if (chains > 1)
+    for (int c = 1; c < chains; ++c) {
+      RACER_TRY(cudaEventRecord(s->chain_join[c - 1], s->chain_st[c - 1]));
+      RACER_TRY(cudaStreamWaitEvent(st, s->chain_join[c - 1], 0));
+    }
   RACER_TRY(cudaMemcpyAsync(s->obs, tr->obs + R * IN * n, IN * n * sizeof(float), cudaMemcpyDeviceToDevice, st));
   int rc = forward_on(p, tr->obs + R * IN * n, a, st);
   if (rc) return rc;

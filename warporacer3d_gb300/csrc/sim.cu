@@ -127,23 +127,55 @@ __device__ __forceinline__ Spot probe(const TrackDev& t, float x, float y, float
   return best;
 }
 
-// racer/sim.mojo:126-140: bilinear height and its gradient.
-__device__ __forceinline__ Surface surface(const TrackDev& t, int layer, float x, float y) {
+// racer/sim.mojo:126-140: bilinear height and its gradient, in two parts: the
+// cell and weights (independent of the layer) and the corner heights.
+struct SurfaceCell {
+  long base;  // offset of corner (ix, iy) within a layer's height grid
+  float tx, ty;
+};
+
+__device__ __forceinline__ SurfaceCell surface_cell(const TrackDev& t, float x, float y) {
   float fx = (x - t.x0) / t.cell;
   float fy = (y - t.y0) / t.cell;
   float flx = floorf(fx), fly = floorf(fy);
   int ix = flx >= 0.0f ? (flx <= (float)(t.nx - 2) ? (int)flx : t.nx - 2) : 0;
   int iy = fly >= 0.0f ? (fly <= (float)(t.ny - 2) ? (int)fly : t.ny - 2) : 0;
-  float tx = clampf_(fx - (float)ix, 0.0f, 1.0f);
-  float ty = clampf_(fy - (float)iy, 0.0f, 1.0f);
-  const float* hp = t.d + HEADER + (long)(3 * layer + 1) * t.nx * t.ny + (long)iy * t.nx + ix;
-  float h0 = __ldg(hp), h1 = __ldg(hp + 1), h2 = __ldg(hp + t.nx), h3 = __ldg(hp + t.nx + 1);
+  return SurfaceCell{(long)iy * t.nx + ix, clampf_(fx - (float)ix, 0.0f, 1.0f), clampf_(fy - (float)iy, 0.0f, 1.0f)};
+}
+
+__device__ __forceinline__ float4 surface_corners(const TrackDev& t, int layer, long base) {
+  const float* hp = t.d + HEADER + (long)(3 * layer + 1) * t.nx * t.ny + base;
+  return make_float4(__ldg(hp), __ldg(hp + 1), __ldg(hp + t.nx), __ldg(hp + t.nx + 1));
+}
+
+__device__ __forceinline__ Surface surface_blend(const TrackDev& t, const SurfaceCell& c, float4 h) {
+  const float tx = c.tx, ty = c.ty;
   float w0 = (1.0f - tx) * (1.0f - ty), w1 = tx * (1.0f - ty), w2 = (1.0f - tx) * ty, w3 = tx * ty;
   Surface s;
-  s.height = (h0 * w0 + h2 * w2) + (h1 * w1 + h3 * w3);
-  s.sx = ((h1 - h0) * (1.0f - ty) + (h3 - h2) * ty) / t.cell;
-  s.sy = ((h2 - h0) * (1.0f - tx) + (h3 - h1) * tx) / t.cell;
+  s.height = (h.x * w0 + h.z * w2) + (h.y * w1 + h.w * w3);
+  s.sx = ((h.y - h.x) * (1.0f - ty) + (h.w - h.z) * ty) / t.cell;
+  s.sy = ((h.z - h.x) * (1.0f - tx) + (h.w - h.y) * tx) / t.cell;
   return s;
+}
+
+__device__ __forceinline__ Surface surface(const TrackDev& t, int layer, float x, float y) {
+  const SurfaceCell c = surface_cell(t, x, y);
+  return surface_blend(t, c, surface_corners(t, layer, c.base));
+}
+
+// Probe and the surface under the chosen layer. With two layers the corner
+// heights of both layers are loaded alongside the probe and those of the
+// chosen layer blended, so the loads do not wait for the layer.
+template <int LAYERS>
+__device__ __forceinline__ Surface probe_surface(const TrackDev& t, float x, float y, float z, Spot* spot) {
+  if (LAYERS == 2) {
+    const SurfaceCell c = surface_cell(t, x, y);
+    const float4 h0 = surface_corners(t, 0, c.base), h1 = surface_corners(t, 1, c.base);
+    *spot = probe<LAYERS>(t, x, y, z);
+    return surface_blend(t, c, spot->layer ? h1 : h0);
+  }
+  *spot = probe<LAYERS>(t, x, y, z);
+  return surface(t, spot->layer, x, y);
 }
 
 __device__ __forceinline__ float waypoint(const TrackDev& t, long w, int field) {
@@ -231,8 +263,8 @@ __device__ __forceinline__ void advance_car(const TrackDev& t, float* s, const f
                                             float* obs, int n, int beams, uint64_t seed, float4* ray, int i,
                                             int local) {
   V4 p{s[(long)X * n + i], s[(long)Y * n + i], s[(long)HEADING * n + i], s[(long)SPEED * n + i]};
-  Spot spot = probe<LAYERS>(t, p.x, p.y, s[(long)Z * n + i]);
-  Surface ground = surface(t, spot.layer, p.x, p.y);
+  Spot spot;
+  Surface ground = probe_surface<LAYERS>(t, p.x, p.y, s[(long)Z * n + i], &spot);
   float steer = s[(long)STEER * n + i];
   float rate = clampf_(act[i], -1.0f, 1.0f) * STEER_RATE;
   float accel = clampf_(act[(long)n + i], -1.0f, 1.0f) * ACCEL_MAX;
@@ -254,8 +286,7 @@ __device__ __forceinline__ void advance_car(const TrackDev& t, float* s, const f
     p.s = p.s + ((k1.s + 2.0f * (k2.s + k3.s)) + k4.s) * sixth_dt;
     p.s = clampf_(p.s, -SPEED_MAX, SPEED_MAX);
     steer = clampf_(steer + rate * DT, -STEER_MAX, STEER_MAX);
-    spot = probe<LAYERS>(t, p.x, p.y, spot.height);
-    ground = surface(t, spot.layer, p.x, p.y);
+    ground = probe_surface<LAYERS>(t, p.x, p.y, spot.height, &spot);
     crashed = crashed || spot.clearance < HALF_DIAG || ground.sx * ground.sx + ground.sy * ground.sy > 1.0f;
   }
   if (p.h > PI_F) p.h -= TWO_PI_F;

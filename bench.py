@@ -55,6 +55,8 @@ def parse():
     ap.add_argument("--no-batched", action="store_true")
     ap.add_argument("--no-config1", action="store_true")
     ap.add_argument("--batched-only", action="store_true", help="print only the batched multi-track section")
+    ap.add_argument("--no-track-compile", action="store_true")
+    ap.add_argument("--track-compile-only", action="store_true", help="print only the track compilation section")
     ap.add_argument("--training-iterations", type=int, default=300)
     ap.add_argument("--surrogate-train-steps", type=int, default=None,
                     help="surrogate training steps (default 60000; fewer only to profile the rollout)")
@@ -326,6 +328,49 @@ def training_section(W, iterations):
     return out
 
 
+def track_compile_section():
+    """Track compilation (racer/track.py) on the GPU, timed end to end through the Python
+    API (numpy host part, racer_track_ribbon / racer_track_image, assembly) and as the
+    bare C-ABI call on prepared inputs, against the oracle's C++ restatement on the host
+    cores; both must equal each other bit for bit."""
+    import oracle
+    from warporacer3d_gb300.tracks import compile as TC
+    from warporacer3d_gb300.tracks import occupancy
+    lib = __import__("warporacer3d_gb300").load_library()
+    free, loop, ramps, x0, y0 = occupancy.corridor(0)
+    cases = [(n, TC.builtin_route(n), None) for n in ("flat", "ramp", "bank", "bridge")]
+    cases.append(("occupancy_2048", None, (free, loop, x0, y0, 0.05, ramps)))
+    out = {}
+    for name, rib, img in cases:
+        if rib is not None:
+            full, ref = (lambda: TC.ribbon(*rib)), (lambda: oracle.track_ribbon(*rib))
+            inp = TC.RibbonInput(*rib)
+            abi = lambda: TC.ribbon_grids(inp, lib.racer_track_ribbon)
+        else:
+            full, ref = (lambda: TC.compile_image(*img)), (lambda: oracle.track_image(*img))
+            inp = TC.ImageInput(*img)
+            abi = lambda: TC.image_grids(inp, lib.racer_track_image)
+        full()
+        ms, abi_ms = [], []
+        for _ in range(5):
+            t0 = time.perf_counter()
+            a = full()
+            ms.append((time.perf_counter() - t0) * 1e3)
+            t0 = time.perf_counter()
+            abi()
+            abi_ms.append((time.perf_counter() - t0) * 1e3)
+        t0 = time.perf_counter()
+        b = ref()
+        cpu_ms = (time.perf_counter() - t0) * 1e3
+        out[name] = {"gpu_ms": round(statistics.median(ms), 2), "abi_ms": round(statistics.median(abi_ms), 2),
+                     "oracle_ms": round(cpu_ms, 1), "cells": int(a[0]) * int(a[1]), "layers": int(a[7]),
+                     "identical_to_oracle": bool(np.array_equal(a.view(np.uint32), b.view(np.uint32)))}
+    out["oracle_threads"] = os.cpu_count()
+    out["method"] = ("median of 5 compilations after one warm-up; gpu_ms from the route to the packed float32 "
+                     "array, abi_ms the library call alone; the oracle once, OpenMP over cells")
+    return out
+
+
 def run_reference(args, rank, world):
     if rank != 0:
         return
@@ -376,6 +421,9 @@ def main():
     flush = torch.empty(L2_FLUSH_BYTES, dtype=torch.uint8, device="cuda")
     if args.batched_only:
         print(json.dumps({"batched": batched_section(torch, W, stream, flush)}), flush=True)
+        return
+    if args.track_compile_only:
+        print(json.dumps({"track_compile": track_compile_section()}), flush=True)
         return
     if args.surrogate_only:
         steps = args.surrogate_train_steps if args.surrogate_train_steps is not None else SURR_TRAIN_STEPS
@@ -467,6 +515,8 @@ def main():
         line["batched"] = batched_section(torch, W, stream, flush)
     if rank == 0 and not args.no_training:
         line["training"] = training_section(W, args.training_iterations)
+    if rank == 0 and not args.no_track_compile:
+        line["track_compile"] = track_compile_section()
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline(track)
     if rank == 0:

@@ -283,6 +283,32 @@ int racer_surrogate_rollout_stats(racer_surrogate* surrogate, float* mae_m, floa
 int racer_gemm_bf16(const void* a_dev, const void* b_dev, float* c_dev, int M, int N, int K, int lda, int ldb,
                     int ldc, int splits, float* scratch_dev, int* err_dev, void* stream);
 
+/* ---- track compilation (racer/track.py:54-125) ---- */
+/* One ramp box (racer/track.py:111-116): centre, cos and sin of its heading,
+ * length, width, height and rise (the reference's default rise is length / 2). */
+typedef struct racer_ramp {
+  double cx, cy, cos_heading, sin_heading, length, width, height, rise;
+} racer_ramp;
+/* The grids of a ribbon track on the GPU: the per-cell loop of
+ * racer/track.py:73-104 (`ribbon`) and the fill and blur of :108-121 (`pack`).
+ * route [W][3] is the resampled route (racer/track.py:66), cos_h / sin_h the
+ * cos and sin of its headings and grade its z gradient (:67-68), computed as
+ * the reference computes them; x0, y0, nx, ny the grid of :69-71. Writes
+ * grids [layers][3][ny * nx] (clearance, height, waypoint; grids_len >= 6 * nx *
+ * ny) and *layers (1 or 2): the floats between the packed array's header and
+ * route (:122-125), equal to the reference's. Returns 4 if a cell lies under
+ * more than 8 passes of the route, 3 if no cell lies on the road. */
+int racer_track_ribbon(const double* route, const double* cos_h, const double* sin_h, const double* grade,
+                       int waypoints, double half_width, double bank, double x0, double y0, double cell, int nx,
+                       int ny, const double* ramps, int n_ramps, float* grids, int64_t grids_len, int* layers);
+/* The grids of an occupancy-image track on the GPU (racer/track.py:56-58 and
+ * pack :108-121): free [ny * nx] (nonzero = drivable, rows south to north),
+ * route [W][3] the resampled centreline (:54-55). Writes grids [3][ny * nx].
+ * Returns 3 unless the image has both free and occupied cells. */
+int racer_track_image(const uint8_t* free_cells, const double* route, int waypoints, double x0, double y0,
+                      double cell, int nx, int ny, const double* ramps, int n_ramps, float* grids,
+                      int64_t grids_len);
+
 /* ---- measurement ---- */
 /* Kernel launches in the CUDA graph racer_rollout replays for these arguments
  * (captured here if needed), plus the one launch that sets its step offset. */

@@ -12,6 +12,7 @@ restate the reference's Mojo structs around them with the same buffer layout
     Policy       racer/ppo.mojo:63-138
     Trainer      racer/ppo.mojo:141-337   (rollout length is a parameter)
     save / load  racer/ppo.mojo:341-355
+    track_ribbon, track_image   racer/track.py:54-125 (per-cell work, track.cpp)
 
 Parity pins: the reference's own tests (tests/test_mojo.mojo) run against this
 oracle in tests/test_oracle.py with the reference's tolerances. Random streams
@@ -44,15 +45,15 @@ REWARD, ADV, NORM, KL, STATS = 0, 1, 3, 4, 5
 
 
 def build(force=False):
-    """Compile oracle.cpp into _build/liboracle.so with contraction disabled."""
+    """Compile oracle.cpp and track.cpp into _build/liboracle.so with contraction disabled."""
     src = HERE / "oracle.cpp"
-    deps = [src, HERE.parent / "warporacer3d_gb300/csrc/rmath.h", HERE.parent / "warporacer3d_gb300/csrc/philox.h"]
+    deps = [src, HERE / "track.cpp", HERE.parent / "warporacer3d_gb300/csrc/rmath.h", HERE.parent / "warporacer3d_gb300/csrc/philox.h"]
     if not force and LIB.exists() and all(LIB.stat().st_mtime >= d.stat().st_mtime for d in deps):
         return LIB
     BUILD.mkdir(exist_ok=True)
     tmp = BUILD / f"liboracle.{os.getpid()}.so"
     cmd = ["g++", "-O3", "-std=c++17", "-ffp-contract=off", "-fno-fast-math", "-fopenmp", "-fPIC", "-shared",
-           "-o", str(tmp), str(src)]
+           "-o", str(tmp), str(src), str(HERE / "track.cpp")]
     subprocess.run(cmd, check=True)
     os.replace(tmp, LIB)
     return LIB
@@ -335,3 +336,32 @@ def corridor():
     return np.concatenate([np.array(d, np.float32), clear.ravel().astype(np.float32),
                            height.ravel().astype(np.float32), near.ravel().astype(np.float32),
                            np.array(route, np.float32)]).astype(np.float32)
+
+
+def _track_fn(name):
+    from warporacer3d_gb300.tracks import compile as C
+    fn = getattr(lib(), name)
+    fn.restype = ctypes.c_int
+    fn.argtypes = C.RIBBON_ARGS if name == "orc_track_ribbon" else C.IMAGE_ARGS
+    return fn
+
+
+def track_ribbon(route, half_width, bank, cell, ramps=()):
+    """A ribbon track compiled by the oracle (racer/track.py:61-125): same host part as
+    the product's compiler, per-cell work in track.cpp."""
+    from warporacer3d_gb300.tracks import compile as C
+    inp = C.RibbonInput(route, half_width, bank, cell, ramps)
+    rc, grids, layers = C.ribbon_grids(inp, _track_fn("orc_track_ribbon"))
+    if rc:
+        raise RuntimeError(f"orc_track_ribbon failed ({rc})")
+    return C.assemble(inp, grids, layers)
+
+
+def track_image(free, loop, x0, y0, cell, ramps=()):
+    """An occupancy-image track compiled by the oracle (racer/track.py:54-58, 108-125)."""
+    from warporacer3d_gb300.tracks import compile as C
+    inp = C.ImageInput(free, loop, x0, y0, cell, ramps)
+    rc, grids, layers = C.image_grids(inp, _track_fn("orc_track_image"))
+    if rc:
+        raise RuntimeError(f"orc_track_image failed ({rc})")
+    return C.assemble(inp, grids, layers)

@@ -32,6 +32,7 @@ UNITS = {
     "tma.cu": [],
     "gemm.cu": [],
     "surrogate.cu": [],
+    "track.cu": ["--fmad=false", "-ftz=false"],
 }
 
 

@@ -79,6 +79,29 @@ def test_occupancy_2048_equals_oracle():
     assert_bits(ours, oracle.track_image(free, loop, x0, y0, 0.05, ramps), "occupancy 2048")
 
 
+def ring_image(nx, ny=12):
+    """A two-cell-wide ring corridor around a long wall, with its centreline loop as (row, col)."""
+    free = np.zeros((ny, nx), bool)
+    free[2:10, 2:nx - 2] = True
+    free[4:8, 6:nx - 6] = False
+    cols = np.arange(4.0, nx - 4.0)
+    loop = np.concatenate([np.column_stack([np.full(cols.size, 3.0), cols]),
+                           np.column_stack([np.arange(3.0, 9.0), np.full(6, nx - 4.0)]),
+                           np.column_stack([np.full(cols.size, 8.5), cols[::-1]]),
+                           np.column_stack([np.arange(8.0, 3.0, -1.0), np.full(5, 4.0)])])
+    return free, loop
+
+
+@pytest.mark.parametrize("nx", [5000, 18000])
+def test_wide_images_equal_oracle(nx):
+    """Rows wider than 4096 cells take the row pass's large shared-memory path, wider than
+    17066 its global-memory path."""
+    free, loop = ring_image(nx)
+    ramps = [{"center": [nx * 0.005, 0.03], "heading": 0.0, "length": 1.6, "width": 0.04, "height": 0.1}]
+    ours = C.compile_image(free, loop, 0.0, 0.0, 0.01, ramps)
+    assert_bits(ours, oracle.track_image(free, loop, 0.0, 0.0, 0.01, ramps), f"ring {nx}")
+
+
 def test_image_without_walls_is_rejected():
     free, loop, ramps, x0, y0 = occupancy.corridor(**SMALL)
     with pytest.raises(W.RacerError, match="both free and occupied"):

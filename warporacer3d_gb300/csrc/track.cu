@@ -29,6 +29,7 @@
 // and then symmetric pairs from the outermost inward.
 #include <cuda_runtime.h>
 
+#include <climits>
 #include <cmath>
 #include <cstring>
 #include <string>
@@ -65,18 +66,21 @@ struct CellArgs {
 
 __device__ __forceinline__ double cell_x(double x0, double cell, int ix) { return x0 + cell * (double)ix; }
 
-// One cell's passes and nearest waypoints over the candidates `cw` (indices,
-// ascending) with coordinates `cxy` (racer/track.py:73-86).
+// One cell's nearest waypoint (*nearest) and, for a ball query, its passes
+// and the nearest waypoint of each, over the candidates `cw` (indices,
+// ascending) with coordinates `cxy` (racer/track.py:73-86 and 89).
 __device__ int cell_passes(const CellArgs& a, const int* cw, const double2* cxy, int n, double x, double y,
-                           int* out) {
+                           int* out, int* nearest) {
   int pbest[MAX_PASSES];
   double pd[MAX_PASSES];
-  int np = 0, first = -1, last = -10;
+  int np = 0, first = -1, last = -10, best = 0;
+  double bd2 = INFINITY;
   for (int i = 0; i < n; ++i) {
     const int w = cw ? cw[i] : i;
     const double2 r = cxy ? cxy[i] : make_double2(a.route[3 * w], a.route[3 * w + 1]);
     const double dx = r.x - x, dy = r.y - y;
     const double d2 = dx * dx + dy * dy;
+    if (d2 < bd2) bd2 = d2, best = w;
     if (!(d2 <= a.r2)) continue;
     const double d = sqrt(d2);
     if (np == 0 || w - last > 2) {  // a gap of more than 2 starts a new pass
@@ -88,6 +92,7 @@ __device__ int cell_passes(const CellArgs& a, const int* cw, const double2* cxy,
     if (first < 0) first = w;
     last = w;
   }
+  *nearest = best;
   if (np == 0) return 0;
   if (np > 1 && first == 0 && last == a.W - 1) {  // the pass through the seam: its end, then its start
     int bw = pbest[np - 1];
@@ -173,19 +178,10 @@ __global__ void __launch_bounds__(TILE * TILE) k_cells(CellArgs a) {
   const int n = overflow ? a.W : total;
   const int* cw = overflow ? nullptr : s_w;
   const double2* cxy = overflow ? nullptr : s_xy;
-  int best = 0;
-  double bd = INFINITY;
-  for (int i = 0; i < n; ++i) {
-    const int w = cw ? cw[i] : i;
-    const double2 r = cxy ? cxy[i] : make_double2(a.route[3 * w], a.route[3 * w + 1]);
-    const double dx = r.x - x, dy = r.y - y;
-    const double d2 = dx * dx + dy * dy;
-    if (d2 < bd) bd = d2, best = w;
-  }
+  int out[MAX_PASSES], best = 0;
+  const int got = cell_passes(a, cw, cxy, n, x, y, out, &best);
   a.nearest[k] = best;
   if (a.r2 < 0.0) return;
-  int out[MAX_PASSES];
-  const int got = cell_passes(a, cw, cxy, n, x, y, out);
   if (got < 0) {
     atomicExch(a.error, 4);
     a.count[k] = 0;
@@ -252,11 +248,13 @@ __global__ void k_ramps(const RampRow* ramps, int n, double x0, double y0, doubl
   for (int r = 0; r < n; ++r) {
     const RampRow p = ramps[r];
     const double rx = x - p.cx, ry = y - p.cy;
-    const double u = rx * p.c + ry * p.s + p.length / 2;
     const double v = -rx * p.s + ry * p.c;
-    const double q = fmin(u, p.length - u) / p.rise;
-    const double top = p.height * fmin(fmax(q, 0.0), 1.0);
-    const double add = fabs(v) < p.width / 2 ? top : 0.0;
+    double add = 0.0;  // outside the box the reference adds +0.0 too
+    if (fabs(v) < p.width / 2) {
+      const double u = rx * p.c + ry * p.s + p.length / 2;
+      const double q = fmin(u, p.length - u) / p.rise;
+      add = p.height * fmin(fmax(q, 0.0), 1.0);
+    }
     for (int l = 0; l < layers; ++l) height[l * cells + k] += add;
   }
 }
@@ -271,31 +269,46 @@ __global__ void k_mask_image(const unsigned char* free_, long cells, unsigned ch
   if (k < cells) wall[k] = free_[k] == 0, open[k] = free_[k] != 0;
 }
 
-// Per column, the nearest feature row (ties to the lower row), -1 if none.
-__global__ void k_ft_columns(const unsigned char* feature, int ny, int nx, int* fy) {
-  const int x = blockIdx.x * blockDim.x + threadIdx.x;
-  if (x >= nx) return;
-  int prev = -1;
-  for (int y = 0; y < ny; ++y) {
-    if (feature[(long)y * nx + x]) prev = y;
-    fy[(long)y * nx + x] = prev;
+// Per column, the nearest feature row (ties to the lower row), -1 if none: one
+// warp per column, the last feature at or above each row as a running
+// maximum over chunks of 32 rows, then the first at or below as a running
+// minimum from the bottom.
+constexpr int FT_WARPS = 8;
+__global__ void __launch_bounds__(FT_WARPS * 32) k_ft_columns(const unsigned char* feature, int ny, int nx, int* fy) {
+  const int x = blockIdx.x * FT_WARPS + (threadIdx.x >> 5), lane = threadIdx.x & 31;
+  if (x >= nx) return;  // warp-uniform
+  int carry = -1;
+  for (int y0 = 0; y0 < ny; y0 += 32) {
+    const int y = y0 + lane;
+    int p = (y < ny && feature[(long)y * nx + x]) ? y : -1;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const int q = __shfl_up_sync(0xffffffffu, p, o);
+      if (lane >= o) p = max(p, q);
+    }
+    p = max(p, carry);
+    if (y < ny) fy[(long)y * nx + x] = p;
+    carry = __shfl_sync(0xffffffffu, p, 31);
   }
-  int next = -1;
-  for (int y = ny - 1; y >= 0; --y) {
-    if (feature[(long)y * nx + x]) next = y;
-    const int p = fy[(long)y * nx + x];
-    if (next >= 0 && (p < 0 || next - y < y - p)) fy[(long)y * nx + x] = next;
+  int below = INT_MAX;
+  for (int y0 = ((ny - 1) / 32) * 32; y0 >= 0; y0 -= 32) {
+    const int y = y0 + lane;
+    int q = (y < ny && feature[(long)y * nx + x]) ? y : INT_MAX;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const int r = __shfl_down_sync(0xffffffffu, q, o);
+      if (lane + o < 32) q = min(q, r);
+    }
+    q = min(q, below);
+    if (y < ny && q != INT_MAX) {
+      const int p = fy[(long)y * nx + x];
+      if (p < 0 || q - y < y - p) fy[(long)y * nx + x] = q;
+    }
+    below = __shfl_sync(0xffffffffu, q, 0);
   }
 }
 
-// Per row, the lower envelope of the columns' candidates and, for every cell,
-// the flat index of its nearest feature (-1 when the grid has none).
-__global__ void k_ft_rows(const int* fy, int ny, int nx, int* g, int* src) {
-  const int y = blockIdx.x * blockDim.x + threadIdx.x;
-  if (y >= ny) return;
-  const int* row = fy + (long)y * nx;
-  int* gs = g + (long)y * nx;
-  int* out = src + (long)y * nx;
+__device__ void ft_row(const int* row, int y, int nx, int* gs, int* out) {
   int l = -1;
   for (int x = 0; x < nx; ++x) {
     const int fx = row[x];
@@ -327,6 +340,31 @@ __global__ void k_ft_rows(const int* fy, int ny, int nx, int* g, int* src) {
     }
     out[x] = row[gl] * nx + gl;
   }
+}
+
+// Per row, the lower envelope of the columns' candidates and, for every cell,
+// the flat index of its nearest feature (-1 when the grid has none). The
+// envelope is sequential: one thread walks the row, in shared memory when
+// SHARED (a warp per row stages the row, its stack and its output there),
+// else in global memory (`g` holds the stacks).
+template <bool SHARED>
+__global__ void k_ft_rows(const int* fy, int ny, int nx, int* g, int* src) {
+  extern __shared__ int ft_smem[];
+  const int y = SHARED ? blockIdx.x : blockIdx.x * blockDim.x + threadIdx.x;
+  if (y >= ny) return;
+  const int* row = fy + (long)y * nx;
+  int* gs = g + (long)y * nx;
+  int* out = src + (long)y * nx;
+  if (SHARED) {
+    for (int x = threadIdx.x; x < nx; x += 32) ft_smem[x] = row[x];
+    __syncwarp();
+    row = ft_smem, gs = ft_smem + nx, out = ft_smem + 2 * nx;
+    if (threadIdx.x == 0) ft_row(row, y, nx, gs, out);
+    __syncwarp();
+    for (int x = threadIdx.x; x < nx; x += 32) src[(long)y * nx + x] = out[x];
+    return;
+  }
+  ft_row(row, y, nx, gs, out);
 }
 
 __global__ void k_gather(const double* height, const int* src, long cells, double* filled) {
@@ -413,6 +451,22 @@ struct Scratch {
 
 inline unsigned blocks(long n, int t) { return (unsigned)((n + t - 1) / t); }
 
+// The feature transform of `feature` into `src` (flat index of each cell's
+// nearest feature); fy and g are [cells] scratch.
+cudaError_t feature_transform(const unsigned char* feature, int ny, int nx, int* fy, int* g, int* src, cudaStream_t st) {
+  k_ft_columns<<<blocks(nx, FT_WARPS), FT_WARPS * 32, 0, st>>>(feature, ny, nx, fy);
+  const size_t smem = 3 * sizeof(int) * (size_t)nx;
+  if (smem <= 48 * 1024 ||
+      (smem <= 200 * 1024 &&
+       cudaFuncSetAttribute(k_ft_rows<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) == cudaSuccess)) {
+    k_ft_rows<true><<<ny, 32, smem, st>>>(fy, ny, nx, g, src);
+  } else {
+    cudaGetLastError();
+    k_ft_rows<false><<<blocks(ny, 64), 64, 0, st>>>(fy, ny, nx, g, src);
+  }
+  return cudaGetLastError();
+}
+
 #define TRACK_LAUNCH()                                                                            \
   do {                                                                                            \
     cudaError_t e_ = cudaGetLastError();                                                          \
@@ -444,8 +498,7 @@ int pack(Scratch& s, int layers, double* clearance, double* height, const int* w
   const Blur b = blur_weights();
   for (int l = 0; l < layers; ++l) {
     k_mask_road<<<blocks(cells, T), T, 0, st>>>(clearance + l * cells, cells, feature);
-    k_ft_columns<<<blocks(nx, 64), 64, 0, st>>>(feature, ny, nx, fy);
-    k_ft_rows<<<blocks(ny, 64), 64, 0, st>>>(fy, ny, nx, g, src);
+    RACER_TRY(feature_transform(feature, ny, nx, fy, g, src, st));
     TRACK_LAUNCH();
     int first = 0;
     RACER_TRY(cudaMemcpyAsync(&first, src, sizeof(int), cudaMemcpyDeviceToHost, st));
@@ -618,11 +671,9 @@ int racer_track_image(const uint8_t* free_, const double* route, int W, double x
   CellArgs ca{d_route, W, x0, y0, cell, nx, ny, -1.0, nearest, nullptr, nullptr, nullptr, flags + 1};
   k_cells<<<dim3(blocks(nx, TILE), blocks(ny, TILE)), TILE * TILE, 0, st.s>>>(ca);
   k_mask_image<<<blocks(cells, 256), 256, 0, st.s>>>(d_free, cells, wall, open);
-  k_ft_columns<<<blocks(nx, 64), 64, 0, st.s>>>(wall, ny, nx, fy);
-  k_ft_rows<<<blocks(ny, 64), 64, 0, st.s>>>(fy, ny, nx, g, to_wall);
-  k_ft_columns<<<blocks(nx, 64), 64, 0, st.s>>>(open, ny, nx, fy);
-  k_ft_rows<<<blocks(ny, 64), 64, 0, st.s>>>(fy, ny, nx, g, to_open);
   TRACK_LAUNCH();
+  RACER_TRY(feature_transform(wall, ny, nx, fy, g, to_wall, st.s));
+  RACER_TRY(feature_transform(open, ny, nx, fy, g, to_open, st.s));
   int first[2] = {0, 0};
   RACER_TRY(cudaMemcpyAsync(&first[0], to_wall, sizeof(int), cudaMemcpyDeviceToHost, st.s));
   RACER_TRY(cudaMemcpyAsync(&first[1], to_open, sizeof(int), cudaMemcpyDeviceToHost, st.s));

@@ -2,24 +2,46 @@
 
 1. Nearest cell. racer/sim.mojo:110-114 computes ix = floor((x - x0) / cell
    + 0.5) with a binary32 division and tests 0 <= ix < nx. The CUDA probe
-   (sim.cu, cell_of) multiplies by r = RN(1 / cell) instead; when the
-   fractional parts of both u' = (x - x0) * r + 0.5 lie inside
-   0.5 +- band with band = 0.5 - (max(nx, ny) + 3) * 6 * 2^-24 it uses floor(u')
-   with an integer bounds test, otherwise the division. The claim: on-map
-   status and cell are always the reference's.
+   (sim.cu, cell_of) computes u' = RN(x * r + c) in one fused multiply-add,
+   with r = RN(1 / cell) and c = RN(RN(-x0 * r) + 0.5); when the fractional
+   parts of both u' lie inside 0.5 +- band, band = 0.5 - (5.001 M + 4.001 X +
+   16) * 2^-24 (M = max(nx, ny), X = max(|x0|, |y0|) / cell), it uses
+   floor(u') with an integer bounds test, otherwise the division (whose own
+   shortcut, cell_coord, is replayed too). The claim: on-map status and cell
+   are always the reference's.
 2. Division skip. The march (sim.cu, trace) evaluates fl / descent only when
    fl * RN(1 / descent) <= a * (1 + 2^-20); the claim: whenever it skips,
    RN(fl / descent) >= a, so min(a, fl / descent) = a.
 
 Both are replayed here in numpy binary32 (IEEE round-to-nearest, like the
-GPU built with --fmad=false) on random values and on adversarial ones a few
-ulps either side of every cell boundary.
+GPU built with --fmad=false; the fused multiply-add exactly, through a
+binary64 product and an exact two-sum) on random values and on adversarial
+ones a few ulps either side of every cell boundary and of the band's edge.
 """
 import numpy as np
 import pytest
 
-f32 = np.float32
-BAND_UNIT = f32(6 * 2.0 ** -24)
+f32, f64 = np.float32, np.float64
+
+
+def fma32(a, b, c):
+    """RN32(a * b + c) without intermediate rounding, for binary32 arrays."""
+    p = a.astype(f64) * b.astype(f64)  # exact: 48 significant bits at most
+    s = p + c.astype(f64)
+    bb = s - p
+    err = (p - (s - bb)) + (c.astype(f64) - bb)  # p + c = s + err exactly
+    with np.errstate(all="ignore"):
+        f = s.astype(f32)
+        lo = np.where(f.astype(f64) <= s, f, np.nextafter(f, f32(-np.inf)))
+        hi = np.nextafter(lo, f32(np.inf))
+        tie = s == (lo.astype(f64) + hi.astype(f64)) / 2  # s halfway between two binary32 values
+    # off a halfway point err cannot move s across one; on it, err decides (ties to even if err == 0)
+    return np.where(tie & (err > 0), hi, np.where(tie & (err < 0), lo, f)).astype(f32)
+
+
+def band_delta(v0, cell, nmax):
+    X = np.ceil(abs(float(v0)) / float(cell))
+    return (5.001 * nmax + 4.001 * X + 16.0) * 2.0 ** -24
 
 
 def exact_cell(v, v0, cell, n):
@@ -28,18 +50,31 @@ def exact_cell(v, v0, cell, n):
     return on, np.where(on, f, -1)
 
 
+def division_free_coord(v, v0, cell):
+    """sim.cu cell_coord: the division only within (|u| + 1) * 2^-20 of an integer."""
+    r = f32(1) / cell
+    d = v - v0
+    u = d * r + f32(0.5)
+    fl = np.floor(u)
+    g = u - fl
+    delta = (np.abs(u) + f32(1)) * f32(9.5367431640625e-07)
+    return np.where((g > delta) & (g < f32(1) - delta), fl, np.floor(d / cell + f32(0.5)))
+
+
 def fast_cell(v, v0, cell, n, nmax):
     r = f32(1) / cell
-    band = f32(0.5) - f32(nmax + 3) * BAND_UNIT
-    u = (v - v0) * r + f32(0.5)
+    c = (f32(-v0 * r) + f32(0.5)).astype(f32)
+    band = f32(0.5 - band_delta(v0, cell, nmax) * (1 + 2.0 ** -20))
+    u = fma32(v, np.full_like(v, r), np.full_like(v, c))
     fl = np.floor(u)
     ok = np.abs((u - fl) - f32(0.5)) < band
     with np.errstate(invalid="ignore"):
         i = np.clip(np.nan_to_num(fl, nan=0, posinf=2**31 - 1, neginf=-2**31), -2**31, 2**31 - 1).astype(np.int64)
     on_fast = (i >= 0) & (i < n)
-    on_ex, idx_ex = exact_cell(v, v0, cell, n)
-    on = np.where(ok, on_fast, on_ex)
-    idx = np.where(ok, np.where(on_fast, i.astype(f32), -1), idx_ex)
+    fc = division_free_coord(v, v0, cell)
+    on_slow = (fc >= 0) & (fc < f32(n))
+    on = np.where(ok, on_fast, on_slow)
+    idx = np.where(ok, np.where(on_fast, i.astype(f32), -1), np.where(on_slow, fc, -1))
     return on, idx, ok
 
 
@@ -58,7 +93,7 @@ def test_fast_cell_index_is_exact(cell, n, nmax):
             down = np.nextafter(down, f32(-np.inf))
             adv += [up, down]
         # points whose u' lands just inside and outside the band edge
-        edge = f32(nmax + 3) * BAND_UNIT
+        edge = f32(band_delta(v0, cell, nmax))
         for frac in (edge, -edge):
             target = (ks.astype(np.float64) + frac.astype(np.float64) * np.array([[0.5], [1.0], [1.5], [2.0]]))
             adv += list((v0 + (target - 0.5) * np.float64(cell)).astype(f32))

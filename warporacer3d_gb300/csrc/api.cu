@@ -183,7 +183,16 @@ static int upload_track(const float* track, size_t len, float** d_track, float2*
   t->y0 = track[3];
   t->cell = track[4];
   t->inv_cell = 1.0f / track[4];
-  t->band = 0.5f - (float)((nx > ny ? nx : ny) + 3) * 3.5762786865234375e-07f;  // 3 * 2^-23
+  {
+    // the nearest-cell shortcut (sim.cu, cell_of): u = RN(x * inv_cell + cx) with
+    // cx = RN(RN(-x0 * inv_cell) + 0.5), exact whenever frac(u) lies inside 0.5 +- band
+    volatile float c1 = -t->x0 * t->inv_cell, c2 = -t->y0 * t->inv_cell;  // each product rounded on its own
+    t->cx = c1 + 0.5f;
+    t->cy = c2 + 0.5f;
+    const double X = ceil(std::max(fabs((double)t->x0), fabs((double)t->y0)) / (double)track[4]);
+    const double delta = (5.001 * (nx > ny ? nx : ny) + 4.001 * X + 16.0) * 0x1p-24;
+    t->band = delta < 0.25 ? (float)(0.5 - delta * (1.0 + 0x1p-20)) : 0.0f;  // 0: every lookup divides
+  }
   t->spacing = track[6];
   t->slope = track[8];
   t->nxf = (float)nx;

@@ -42,7 +42,8 @@ struct TrackDev {
   int nx, ny, waypoints, layers;
   float x0, y0, cell, spacing, slope;
   float inv_cell;  // RN(1 / cell), for the division-free cell index
-  float band;      // 0.5 - (max(nx, ny) + 3) * 6 * 2^-24: fractional parts inside +-band need no division
+  float cx, cy;    // RN(RN(-x0 * inv_cell) + 0.5), the same for y0: u = fma(x, inv_cell, cx)
+  float band;      // 0.5 - (5.001 max(nx, ny) + 4.001 max(|x0|, |y0|) / cell + 16) 2^-24: no division inside +-band
   float nxf, nyf;
   long route;
 };

@@ -61,19 +61,20 @@ __device__ __forceinline__ float cell_coord(float v, float v0, float cell, float
 }
 
 // Nearest-cell index (racer/sim.mojo:108-114); false off the map or for
-// non-finite coordinates. One guard band serves the whole grid. With
-// d = RN(v - v0), the reference's u = RN(RN(d / cell) + 0.5) and
-// u' = RN(RN(d * RN(1/cell)) + 0.5): the two quotients differ by at most
-// (3 * 2^-24 + 2^-48) |d / cell| and each + 0.5 rounds by at most
-// 2^-24 |u|, so |u' - u| <= 2^-24 (5 U + 2) where |u'| <= U. Where
-// U <= M + 2 (M = max(nx, ny)) that is below delta = (M + 3) * 6 * 2^-24,
-// even after the fractional part's own rounding (at most 2^-26); farther out
-// both floors are off the map. So when both fractional parts lie more than
-// delta from an integer (|frac - 0.5| < band = 0.5 - delta), the fast floors
-// give the reference's answer (NaN and infinities fail the test and take the
-// exact path).
+// non-finite coordinates. The reference computes u = RN(RN(RN(x - x0) / h)
+// + 0.5) (h = cell) and floors it; the fast path computes u' = RN(x * r + c)
+// in one fused multiply-add, with r = RN(1 / h) and c = RN(RN(-x0 * r) + 0.5)
+// (TrackDev.cx, cy). With e = 2^-24, w = (x - x0) / h + 0.5 exactly,
+// D = |x - x0| / h and X = |x0| / h: |u - w| <= e (2.0001 D + 1.0001 |u|)
+// and |u' - w| <= e (|x| / h + 3.0001 X + 0.5 + 1.0001 |u'|). Where |u'| <=
+// M + 2 (M = max(nx, ny)) that gives |u' - u| <= e (5.0003 M + 4.0001 X +
+// 12.02), so the band delta = e (5.001 M + 4.001 X + 16) also covers the
+// fractional part's own rounding; farther out both floors are off the map
+// (the error is at most 6 e |u'| + e (4 X + 3) there). So when both fractional parts lie within
+// band = 0.5 - delta of one half, the fast floors give the reference's
+// answer; otherwise (NaN and infinities included) the division decides.
 __device__ __forceinline__ bool cell_of(const TrackDev& t, float x, float y, long* idx) {
-  const float ux = (x - t.x0) * t.inv_cell + 0.5f, uy = (y - t.y0) * t.inv_cell + 0.5f;
+  const float ux = __fmaf_rn(x, t.inv_cell, t.cx), uy = __fmaf_rn(y, t.inv_cell, t.cy);
   const float flx = floorf(ux), fly = floorf(uy);
   if (fabsf((ux - flx) - 0.5f) < t.band && fabsf((uy - fly) - 0.5f) < t.band) {
     const int ix = (int)flx, iy = (int)fly;  // saturating conversion: far off the map stays off it

@@ -2,13 +2,12 @@
 
 1. Nearest cell. racer/sim.mojo:110-114 computes ix = floor((x - x0) / cell
    + 0.5) with a binary32 division and tests 0 <= ix < nx. The CUDA probe
-   (sim.cu, cell_of) computes u' = RN(x * r + c) in one fused multiply-add,
-   with r = RN(1 / cell) and c = RN(RN(-x0 * r) + 0.5); when the fractional
-   parts of both u' lie inside 0.5 +- band, band = 0.5 - (5.001 M + 4.001 X +
-   16) * 2^-24 (M = max(nx, ny), X = max(|x0|, |y0|) / cell), it uses
-   floor(u') with an integer bounds test, otherwise the division (whose own
-   shortcut, cell_coord, is replayed too). The claim: on-map status and cell
-   are always the reference's.
+   (sim.cu, cell_of) computes v = RN(x * r + c) in one fused multiply-add,
+   with r = RN(1 / cell) and c = RN(-x0 * r); when both |v - rint(v)| lie
+   below band = 0.5 - (5.001 M + 4.001 X + 16) * 2^-24 (M = max(nx, ny),
+   X = max(|x0|, |y0|) / cell), it uses rint(v) with an integer bounds test,
+   otherwise the division (whose own shortcut, cell_coord, is replayed too).
+   The claim: on-map status and cell are always the reference's.
 2. Division skip. The march (sim.cu, trace) evaluates fl / descent only when
    fl * RN(1 / descent) <= a * (1 + 2^-20); the claim: whenever it skips,
    RN(fl / descent) >= a, so min(a, fl / descent) = a.
@@ -63,11 +62,11 @@ def division_free_coord(v, v0, cell):
 
 def fast_cell(v, v0, cell, n, nmax):
     r = f32(1) / cell
-    c = (f32(-v0 * r) + f32(0.5)).astype(f32)
+    c = f32(-v0 * r)
     band = f32(0.5 - band_delta(v0, cell, nmax) * (1 + 2.0 ** -20))
     u = fma32(v, np.full_like(v, r), np.full_like(v, c))
-    fl = np.floor(u)
-    ok = np.abs((u - fl) - f32(0.5)) < band
+    fl = np.rint(u)
+    ok = np.abs(u - fl) < band
     with np.errstate(invalid="ignore"):
         i = np.clip(np.nan_to_num(fl, nan=0, posinf=2**31 - 1, neginf=-2**31), -2**31, 2**31 - 1).astype(np.int64)
     on_fast = (i >= 0) & (i < n)

@@ -184,11 +184,10 @@ static int upload_track(const float* track, size_t len, float** d_track, float2*
   t->cell = track[4];
   t->inv_cell = 1.0f / track[4];
   {
-    // the nearest-cell shortcut (sim.cu, cell_of): u = RN(x * inv_cell + cx) with
-    // cx = RN(RN(-x0 * inv_cell) + 0.5), exact whenever frac(u) lies inside 0.5 +- band
-    volatile float c1 = -t->x0 * t->inv_cell, c2 = -t->y0 * t->inv_cell;  // each product rounded on its own
-    t->cx = c1 + 0.5f;
-    t->cy = c2 + 0.5f;
+    // the nearest-cell shortcut (sim.cu, cell_of): v = RN(x * inv_cell + cx) with
+    // cx = RN(-x0 * inv_cell); rint(v) is the reference's cell whenever |v - rint(v)| < band
+    t->cx = -t->x0 * t->inv_cell;
+    t->cy = -t->y0 * t->inv_cell;
     const double X = ceil(std::max(fabs((double)t->x0), fabs((double)t->y0)) / (double)track[4]);
     const double delta = (5.001 * (nx > ny ? nx : ny) + 4.001 * X + 16.0) * 0x1p-24;
     t->band = delta < 0.25 ? (float)(0.5 - delta * (1.0 + 0x1p-20)) : 0.0f;  // 0: every lookup divides

@@ -42,7 +42,7 @@ struct TrackDev {
   int nx, ny, waypoints, layers;
   float x0, y0, cell, spacing, slope;
   float inv_cell;  // RN(1 / cell), for the division-free cell index
-  float cx, cy;    // RN(RN(-x0 * inv_cell) + 0.5), the same for y0: u = fma(x, inv_cell, cx)
+  float cx, cy;    // RN(-x0 * inv_cell), RN(-y0 * inv_cell): the cell is rint(fma(x, inv_cell, cx))
   float band;      // 0.5 - (5.001 max(nx, ny) + 4.001 max(|x0|, |y0|) / cell + 16) 2^-24: no division inside +-band
   float nxf, nyf;
   long route;

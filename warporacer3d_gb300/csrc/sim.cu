@@ -62,22 +62,23 @@ __device__ __forceinline__ float cell_coord(float v, float v0, float cell, float
 
 // Nearest-cell index (racer/sim.mojo:108-114); false off the map or for
 // non-finite coordinates. The reference computes u = RN(RN(RN(x - x0) / h)
-// + 0.5) (h = cell) and floors it; the fast path computes u' = RN(x * r + c)
-// in one fused multiply-add, with r = RN(1 / h) and c = RN(RN(-x0 * r) + 0.5)
-// (TrackDev.cx, cy). With e = 2^-24, w = (x - x0) / h + 0.5 exactly,
-// D = |x - x0| / h and X = |x0| / h: |u - w| <= e (2.0001 D + 1.0001 |u|)
-// and |u' - w| <= e (|x| / h + 3.0001 X + 0.5 + 1.0001 |u'|). Where |u'| <=
-// M + 2 (M = max(nx, ny)) that gives |u' - u| <= e (5.0003 M + 4.0001 X +
-// 12.02), so the band delta = e (5.001 M + 4.001 X + 16) also covers the
-// fractional part's own rounding; farther out both floors are off the map
-// (the error is at most 6 e |u'| + e (4 X + 3) there). So when both fractional parts lie within
-// band = 0.5 - delta of one half, the fast floors give the reference's
-// answer; otherwise (NaN and infinities included) the division decides.
+// + 0.5) (h = cell) and takes floor(u); the fast path computes
+// v = RN(x * r + c) in one fused multiply-add, with r = RN(1 / h) and
+// c = RN(-x0 * r) (TrackDev.cx, cy), and takes the nearest integer of v.
+// With e = 2^-24, w = (x - x0) / h exactly, D = |w| and X = |x0| / h:
+// |u - (w + 0.5)| <= e (2.0001 D + 1.0001 |u|) and |v - w| <= e (|x| / h +
+// 2.0001 X + 1.0001 |v|). Where |v| <= M + 2 (M = max(nx, ny)) that gives
+// |u - (v + 0.5)| <= e (5.0003 M + 3.0001 X + 12.02), so with the band delta
+// = e (5.001 M + 4.001 X + 16), which also covers the rounding of v - rint(v),
+// a v farther than delta from every half-integer has floor(u) = rint(v);
+// farther out both are off the map (the error is at most 6 e |v| + e (4 X +
+// 3) there). Inside the band, and for NaN and infinities, the division
+// decides.
 __device__ __forceinline__ bool cell_of(const TrackDev& t, float x, float y, long* idx) {
-  const float ux = __fmaf_rn(x, t.inv_cell, t.cx), uy = __fmaf_rn(y, t.inv_cell, t.cy);
-  const float flx = floorf(ux), fly = floorf(uy);
-  if (fabsf((ux - flx) - 0.5f) < t.band && fabsf((uy - fly) - 0.5f) < t.band) {
-    const int ix = (int)flx, iy = (int)fly;  // saturating conversion: far off the map stays off it
+  const float vx = __fmaf_rn(x, t.inv_cell, t.cx), vy = __fmaf_rn(y, t.inv_cell, t.cy);
+  const float rx = rintf(vx), ry = rintf(vy);
+  if (fabsf(vx - rx) < t.band && fabsf(vy - ry) < t.band) {
+    const int ix = (int)rx, iy = (int)ry;  // saturating conversion: far off the map stays off it
     if ((unsigned)ix >= (unsigned)t.nx || (unsigned)iy >= (unsigned)t.ny) return false;
     *idx = (long)(iy * t.nx + ix);
     return true;

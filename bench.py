@@ -18,6 +18,11 @@ counted from the kernel's own per-beam probe counts; `cpu_baseline` times the
 CPU restatement on this host's cores on a bounded sample of the same
 workload. `--impl reference` times that CPU restatement alone (the reference's
 Mojo/MAX toolchain does not exist on this machine).
+
+Under torchrun (N > 1) every rank runs the headline rollout on its own GPU
+(replicas, max-over-ranks timing); the further sections (FP64 audit,
+surrogate, config 1, batched, training, track compilation, CPU baseline) are
+single-GPU measurements and run at N = 1 only.
 """
 import argparse
 import json
@@ -413,7 +418,12 @@ def main():
         import torch.distributed as dist
         dist.init_process_group("nccl")
     import __graft_entry__
-    __graft_entry__.build()
+    if rank == 0:
+        __graft_entry__.build()  # one rank compiles; the others wait, then load the same files
+    if dist:
+        dist.barrier()
+    if rank != 0:
+        __graft_entry__.build()  # up to date by now: checks timestamps only
     import warporacer3d_gb300 as W
 
     track = W.track(TRACK)
@@ -501,23 +511,27 @@ def main():
                        "policy": "tanh MLP 1086-64-64-3"},
             "beam_steps_per_s": value * BEAMS, "wall_s": wall, "gpu_launches": kernels_per_rollout * args.steps,
             "clocks": clocks.summary(), "e2e": e2e, "roofline": roofline}
-    audit = runner.audit_dynamics(AUDIT_STEPS, False, 10 ** 9)
-    audit["workload"] = f"{TRACK}, {CARS} cars, {AUDIT_STEPS} policy steps after the timed rollouts"
-    audit["method"] = "each binary32 RK4 step re-integrated in FP64 on the GPU from the same state and actions"
-    line["dynamics_fp64_audit"] = audit
-    if not args.no_surrogate:
+    # the single-GPU sections: measured at N = 1 only (at N > 1 every GPU would repeat them while
+    # all N are held, and only rank 0's line is printed)
+    single = world == 1
+    if single:
+        audit = runner.audit_dynamics(AUDIT_STEPS, False, 10 ** 9)
+        audit["workload"] = f"{TRACK}, {CARS} cars, {AUDIT_STEPS} policy steps after the timed rollouts"
+        audit["method"] = "each binary32 RK4 step re-integrated in FP64 on the GPU from the same state and actions"
+        line["dynamics_fp64_audit"] = audit
+    if single and not args.no_surrogate:
         del runner
         steps = args.surrogate_train_steps if args.surrogate_train_steps is not None else SURR_TRAIN_STEPS
         line["surrogate"] = surrogate_section(torch, W, track, stream, flush, steps)
-    if rank == 0 and not args.no_config1:
+    if single and not args.no_config1:
         line["config1"] = config1_section(torch, W, stream)
-    if not args.no_batched:
+    if single and not args.no_batched:
         line["batched"] = batched_section(torch, W, stream, flush)
-    if rank == 0 and not args.no_training:
+    if single and not args.no_training:
         line["training"] = training_section(W, args.training_iterations)
-    if rank == 0 and not args.no_track_compile:
+    if single and not args.no_track_compile:
         line["track_compile"] = track_compile_section()
-    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+    if single and not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline(track)
     if rank == 0:
         print(json.dumps(line), flush=True)

@@ -307,7 +307,7 @@ def training_section(W, iterations):
             runner = W.Runner(track, TRAIN_CARS, beams=TRAIN_BEAMS, seed=seed, policy_seed=seed)
             runner.policy.set_precision(precision)
             state, obs = runner.sim.state.numpy(), runner.sim.obs.numpy()
-            chains, _ = runner.tune_chains(32, 2)  # rollout chains (BF16 only), then back to the start state
+            chains, _ = runner.tune_chains(64, 3)  # rollout chains (BF16 only), then back to the start state
             runner.sim.state.write(state)
             runner.sim.obs.write(obs)
             trainer = W.Trainer(TRAIN_CARS, beams=TRAIN_BEAMS, rollout=TRAIN_ROLLOUT, stream=runner.sim.stream)

@@ -5,7 +5,8 @@
 // Per CTA (one per SM): warp 0 streams the weight k-blocks with TMA through a
 // ring of 32 KB stages (256 weight rows x 64 k) and loads the tile's input
 // block; warp 1 allocates all 512 TMEM columns (two 256-column slots) and
-// issues the MMAs; warps 2-9 are the epilogue. The A operand of every layer
+// issues the MMAs; warps 2-17 are the epilogue, four per TMEM lane quarter
+// (enough warps to hide the accumulator loads and tanh latencies). The A operand of every layer
 // lives in one 128 KB shared buffer (8 k-blocks of 128 rows x 64, K-major,
 // 128B-swizzled): the input block in k-block 0 for layer 1, then each hidden
 // epilogue writes its tanh output there in BF16 as the next layer's A. The
@@ -20,9 +21,9 @@
 // Barriers and their completions per tile (T tiles done before this one):
 //   xfull      1   input block landed (TMA transaction count)
 //   afree      1   every MMA reading the A buffer has completed (after the output layer)
-//   edone      3   a hidden epilogue wrote A and drained TMEM (256 arrivals)
+//   edone      3   a hidden epilogue wrote A and drained TMEM (512 arrivals)
 //   accfull[s] 3 + chunks in slot s: an accumulator slot is complete (MMA commit)
-//   accempty[s] chunks in slot s: the epilogue drained an output chunk (256 arrivals)
+//   accempty[s] chunks in slot s: the epilogue drained an output chunk (512 arrivals)
 // A wait for completion k of a barrier uses parity k & 1; every wait is bounded
 // and a timeout sets *err.
 #pragma once
@@ -37,7 +38,8 @@ constexpr int SF_A_BYTES = SF_KB * 128 * 128;  // 128 rows x 512 BF16
 constexpr int SF_STAGE = 256 * 128;            // 256 weight rows x 64 k (BF16)
 constexpr int SF_STAGES = 3;
 constexpr int SF_SMEM = SF_A_BYTES + SF_STAGES * SF_STAGE + 256 + 1024;  // + barriers, alignment slack
-constexpr int SF_THREADS = 320;
+constexpr int SF_EPI = 512;  // epilogue threads: warps 2-17
+constexpr int SF_THREADS = 64 + SF_EPI;
 
 struct FusedArgs {
   const float* b2;
@@ -160,9 +162,9 @@ __device__ bool sf_mma(uint32_t tmem, uint32_t a0, uint8_t* stages, const SfBars
   return true;
 }
 
-// Epilogue warp (q, h): TMEM lanes 32q .. 32q + 31, column half h.
+// Epilogue warp (q, h, g): TMEM lanes 32q .. 32q + 31, column half h of a slot, column quarter 2h + g.
 __device__ bool sf_epilogue(uint32_t tmem, uint8_t* abuf, const SfBars& b, const FusedArgs& args, int tiles, int nc,
-                            int c0, int c1, int q, int h) {
+                            int c0, int c1, int q, int h, int g) {
   const int lane = threadIdx.x & 31;
   const uint32_t lane_addr = (uint32_t)(q * 32) << 16;
   const int r = q * 32 + lane;  // row of the tile
@@ -177,8 +179,8 @@ __device__ bool sf_epilogue(uint32_t tmem, uint8_t* abuf, const SfBars& b, const
       tc::tc_fence_after();
       const float* bias = layer == 0 ? nullptr : (layer == 1 ? args.b2 : args.b3);
 #pragma unroll 1
-      for (int i = 0; i < 8; ++i) {  // columns 32i .. 32i + 31 of this slot
-        const int col = 256 * h + 32 * i;  // first unit of these 32
+      for (int i = 0; i < 4; ++i) {  // columns 128g + 32i .. + 31 of this slot
+        const int col = 256 * h + 128 * g + 32 * i;  // first unit of these 32
         float bb[32];                      // their biases: 16-byte loads issued before the accumulator read
 #pragma unroll
         for (int q4 = 0; q4 < 8; ++q4) {
@@ -202,13 +204,13 @@ __device__ bool sf_epilogue(uint32_t tmem, uint8_t* abuf, const SfBars& b, const
       tc::mbar_arrive(b.edone);
     }
     float lo = 1.0f;
-    for (int p = 0; p < nc; ++p) {  // output: p-th chunk in slot p & 1, this warp's 128 of its 256 columns
+    for (int p = 0; p < nc; ++p) {  // output: p-th chunk in slot p & 1, this warp's 64 of its 256 columns
       const int s = p & 1, c = (p + rot) % nc;
       if (!sf_wait(&b.accfull[s], ((s ? f1 : f0) + 3 + p / 2) & 1, b.abort)) return false;
       tc::tc_fence_after();
 #pragma unroll 1
-      for (int i = 0; i < 4; ++i) {
-        const int o0 = 256 * c + 128 * h + 32 * i;
+      for (int i = 0; i < 2; ++i) {
+        const int o0 = 256 * c + 128 * h + 64 * g + 32 * i;
         float bb[32];
         if (o0 + 32 <= args.beams) {
 #pragma unroll
@@ -220,7 +222,7 @@ __device__ bool sf_epilogue(uint32_t tmem, uint8_t* abuf, const SfBars& b, const
 #pragma unroll
           for (int j = 0; j < 32; ++j) bb[j] = o0 + j < args.beams ? __ldg(args.b4 + o0 + j) : 0.0f;
         }
-        tc::tmem_ld32_sync(tmem + lane_addr + 256 * s + 128 * h + 32 * i, v);
+        tc::tmem_ld32_sync(tmem + lane_addr + 256 * s + 128 * h + 64 * g + 32 * i, v);
         if (m < args.n) {
 #pragma unroll
           for (int j = 0; j < 32; ++j) {
@@ -274,10 +276,10 @@ __global__ void __launch_bounds__(SF_THREADS, 1)
     }
     tc::mbar_init(b.xfull, 1);
     tc::mbar_init(b.afree, 1);
-    tc::mbar_init(b.edone, 256);
+    tc::mbar_init(b.edone, SF_EPI);
     for (int s = 0; s < 2; ++s) {
       tc::mbar_init(&b.accfull[s], 1);
-      tc::mbar_init(&b.accempty[s], 256);
+      tc::mbar_init(&b.accempty[s], SF_EPI);
     }
     tc::mbar_init(b.mdone, 1);
     *b.abort = 0;
@@ -304,7 +306,8 @@ __global__ void __launch_bounds__(SF_THREADS, 1)
     tc::mma_commit(b.mdone);  // every MMA issued has completed before TMEM is freed
     tc::mbar_wait(b.mdone, 0, 1u << 20);
   } else if (warp >= 2) {
-    ok = sf_epilogue(tmem, abuf, b, args, tiles, nc, c0, c1, warp & 3, (warp - 2) >> 2);
+    const int k = (warp - 2) >> 2;  // 0..3 within the lane quarter warp & 3
+    ok = sf_epilogue(tmem, abuf, b, args, tiles, nc, c0, c1, warp & 3, k >> 1, k & 1);
   }
   tc::tc_fence_before();
   __syncthreads();

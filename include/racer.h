@@ -184,6 +184,10 @@ int racer_trainer_rollout(racer_trainer* trainer, racer_sim* sim, racer_policy* 
                           int iteration, float* mean_reward);
 /* Trainer.update (racer/ppo.mojo:234-257): returns the last minibatch's KL estimate. */
 int racer_trainer_update(racer_trainer* trainer, racer_policy* policy, float* kl);
+/* Updates replay one captured CUDA graph per policy (taken on the update after
+ * the first of a policy's configuration; the same launches and results as the
+ * eager update). enable = 0 runs every update eagerly. */
+int racer_trainer_set_graphs(racer_trainer* trainer, int enable);
 /* Trainer.minibatch (racer/ppo.mojo:259-315) with explicit advantage moments. */
 int racer_trainer_minibatch(racer_trainer* trainer, racer_policy* policy, int m, float adv_mean, float adv_scale);
 

@@ -200,3 +200,30 @@ def test_trainer_rollout_with_chains_matches_one_chain():
     for a, b in zip(out[0][1:], out[1][1:]):
         assert np.array_equal(a, b)
     assert out[0][0] == out[1][0]
+
+
+@pytest.mark.parametrize("precision", ["bf16", "fp32"])
+def test_trainer_update_graph_matches_eager(precision):
+    """Updates replayed from the captured graph (from the third on) give the eager updates' bits: theta,
+    Adam moments and KL over four rollout + update iterations; a policy that changes precision mid-way
+    is re-warmed, not replayed with stale launches."""
+    out = []
+    for graphs in (True, False):
+        sim = W.Sim(W.track("bank"), 1024, 3, beams=108)
+        sim.reset()
+        policy = W.Policy(5, beams=108)
+        policy.set_precision(precision)
+        acts = W.Activations(policy, 1024)
+        trainer = W.Trainer(1024, beams=108, rollout=8)
+        trainer.set_graphs(graphs)
+        kls = []
+        for it in range(5):
+            if it == 3:  # switch precision and back: the captured graph must go stale
+                policy.set_precision("fp32" if precision == "bf16" else "bf16")
+                policy.set_precision(precision)
+            trainer.rollout(sim, policy, acts, it)
+            kls.append(trainer.update(policy))
+        out.append((kls, policy.theta.numpy(), trainer.first.numpy(), trainer.second.numpy()))
+    (ka, ta, fa, sa), (kb, tb, fb, sb) = out
+    assert ka == kb
+    assert np.array_equal(ta, tb) and np.array_equal(fa, fb) and np.array_equal(sa, sb)

@@ -96,6 +96,16 @@ struct racer_trainer {
   racer_acts* acts = nullptr;
   cudaStream_t st = nullptr;
   bool owned = false;
+  // The update as a CUDA graph: captured on the second update of a policy
+  // generation (the first runs eagerly and sets up the policy's workspaces),
+  // replayed after that; Adam's bias corrections of its 16 steps come from
+  // c12_host (pinned), copied inside the graph.
+  float *c12_dev = nullptr, *c12_host = nullptr;
+  cudaGraphExec_t update_exec = nullptr;
+  racer_policy* update_policy = nullptr;
+  int update_generation = -1;
+  bool update_warm = false;
+  bool graphs = true;
 };
 
 extern "C" {
@@ -592,9 +602,16 @@ int racer_trainer_create(int n, int beams, int rollout, void* stream, racer_trai
       (rc = dalloc(&tr->done, R * n)) || (rc = dalloc(&tr->advantage, R * n)) || (rc = dalloc(&tr->x, MINIBATCHES * IN * B)) ||
       (rc = dalloc(&tr->d3, (OUT + 3) * B)) || (rc = dalloc(&tr->d2, (size_t)HA * B)) ||
       (rc = dalloc(&tr->d1, (size_t)HA * B)) || (rc = dalloc(&tr->grad, P)) || (rc = dalloc(&tr->first, P)) ||
-      (rc = dalloc(&tr->second, P)) || (rc = dalloc(&tr->stats, STATS)) || (rc = dalloc(&tr->red, 4096))) {
+      (rc = dalloc(&tr->second, P)) || (rc = dalloc(&tr->stats, STATS)) || (rc = dalloc(&tr->red, 4096)) ||
+      (rc = dalloc(&tr->c12_dev, 2 * EPOCHS * MINIBATCHES))) {
     racer_trainer_destroy(tr);
     return rc;
+  }
+  if (cudaMallocHost((void**)&tr->c12_host, 2 * EPOCHS * MINIBATCHES * sizeof(float)) != cudaSuccess) {
+    set_error("racer_trainer_create: pinned allocation failed");
+    tr->c12_host = nullptr;
+    racer_trainer_destroy(tr);
+    return 2;
   }
   racer_acts* a = new racer_acts();
   a->cols = tr->batch;
@@ -615,9 +632,11 @@ int racer_trainer_create(int n, int beams, int rollout, void* stream, racer_trai
 
 int racer_trainer_destroy(racer_trainer* tr) {
   if (!tr) return 0;
+  if (tr->update_exec) cudaGraphExecDestroy(tr->update_exec);
   for (float* p : {tr->obs, tr->actions, tr->logp, tr->value, tr->reward, tr->done, tr->advantage, tr->x, tr->d3,
-                   tr->d2, tr->d1, tr->grad, tr->first, tr->second, tr->stats, tr->red})
+                   tr->d2, tr->d1, tr->grad, tr->first, tr->second, tr->stats, tr->red, tr->c12_dev})
     cudaFree(p);
+  if (tr->c12_host) cudaFreeHost(tr->c12_host);
   racer_acts_destroy(tr->acts);
   if (tr->owned && tr->st) cudaStreamDestroy(tr->st);
   delete tr;
@@ -735,11 +754,14 @@ int racer_trainer_minibatch(racer_trainer* tr, racer_policy* p, int m, float adv
   return minibatch_on(tr, p, m, 0, adv_mean, adv_scale);
 }
 
-int racer_trainer_update(racer_trainer* tr, racer_policy* p, float* kl) {
-  RACER_ARG(tr && p, "racer_trainer_update: null argument");
-  RACER_ARG(policy_inputs(p) == tr->in_rows, "racer_trainer_update: policy and trainer sizes differ");
+// The launches of one update (racer/ppo.mojo:234-257): advantage moments,
+// the minibatch gather, 4 epochs x 4 minibatches of loss, backward, Adam and
+// weight repacking. Adam's step k reads its bias corrections from c12_dev[2k].
+static int update_body(racer_trainer* tr, racer_policy* p) {
   cudaStream_t st = tr->st;
   const int P = policy_params(p);
+  RACER_TRY(cudaMemcpyAsync(tr->c12_dev, tr->c12_host, 2 * EPOCHS * MINIBATCHES * sizeof(float),
+                            cudaMemcpyHostToDevice, st));
   launch_moments(tr->advantage, (long)tr->rollout * tr->n, tr->stats, tr->red, st);
   // the minibatches' samples are the same in every epoch: gather them once
   launch_gather_all(tr->in_rows, tr->n, tr->rollout, tr->batch, tr->obs, tr->x, st);
@@ -748,19 +770,73 @@ int racer_trainer_update(racer_trainer* tr, racer_policy* p, float* kl) {
     for (int m = 0; m < MINIBATCHES; ++m) {
       int rc = minibatch_on(tr, p, (m + epoch) % MINIBATCHES, 1, 0.0f, 1.0f);
       if (rc) return rc;
-      tr->step += 1;
-      float c1 = 1.0f - powf(0.9f, (float)tr->step), c2 = 1.0f - powf(0.999f, (float)tr->step);
-      launch_adam(P, P - 2, c1, c2, tr->stats, policy_theta(p), tr->grad, tr->first, tr->second, st);
+      launch_adam(P, P - 2, tr->c12_dev + 2 * (epoch * MINIBATCHES + m), tr->stats, policy_theta(p), tr->grad,
+                  tr->first, tr->second, st);
       RACER_LAUNCHED();
       if ((rc = policy_refresh_on(p, st))) return rc;
     }
   }
   launch_rowsum(tr->d3 + (size_t)(OUT + 2) * tr->batch, 1, tr->batch, tr->batch, tr->stats + ST_KL, tr->red, 0, st);
   RACER_LAUNCHED();
+  return 0;
+}
+
+int racer_trainer_update(racer_trainer* tr, racer_policy* p, float* kl) {
+  RACER_ARG(tr && p, "racer_trainer_update: null argument");
+  RACER_ARG(policy_inputs(p) == tr->in_rows, "racer_trainer_update: policy and trainer sizes differ");
+  cudaStream_t st = tr->st;
+  for (int k = 0; k < EPOCHS * MINIBATCHES; ++k) {  // Adam's bias corrections, as the reference computes them
+    const float t = (float)(tr->step + k + 1);
+    tr->c12_host[2 * k] = 1.0f - powf(0.9f, t);
+    tr->c12_host[2 * k + 1] = 1.0f - powf(0.999f, t);
+  }
+  const int generation = policy_generation(p);
+  if (tr->update_policy != p || tr->update_generation != generation || !tr->graphs) {
+    if (tr->update_exec) cudaGraphExecDestroy(tr->update_exec);
+    tr->update_exec = nullptr;
+    tr->update_policy = p;
+    tr->update_generation = generation;
+    tr->update_warm = false;
+  }
+  if (tr->update_exec) {
+    RACER_TRY(cudaGraphLaunch(tr->update_exec, st));
+  } else if (tr->graphs && tr->update_warm) {
+    cudaGraph_t graph = nullptr;
+    RACER_TRY(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
+    const int rc = update_body(tr, p);
+    const cudaError_t end = cudaStreamEndCapture(st, &graph);
+    cudaError_t inst = cudaErrorUnknown;
+    if (!rc && end == cudaSuccess) inst = cudaGraphInstantiate(&tr->update_exec, graph, 0);
+    if (graph) cudaGraphDestroy(graph);
+    if (inst == cudaSuccess) {
+      RACER_TRY(cudaGraphLaunch(tr->update_exec, st));
+    } else {  // nothing ran during the capture: update eagerly, and from now on always
+      tr->update_exec = nullptr;
+      cudaGetLastError();
+      tr->graphs = false;
+      if (int rc2 = update_body(tr, p)) return rc2;
+    }
+  } else {
+    if (int rc = update_body(tr, p)) return rc;
+    // the first update of a policy generation set up its workspaces; the next one is captured
+    tr->update_warm = policy_generation(p) == generation;
+    tr->update_generation = policy_generation(p);
+  }
+  tr->step += EPOCHS * MINIBATCHES;
   float stats[STATS];
   RACER_TRY(cudaMemcpyAsync(stats, tr->stats, sizeof stats, cudaMemcpyDeviceToHost, st));
   RACER_TRY(cudaStreamSynchronize(st));
   if (kl) *kl = stats[ST_KL] / (float)tr->batch;
+  return 0;
+}
+
+int racer_trainer_set_graphs(racer_trainer* tr, int enable) {
+  RACER_ARG(tr, "racer_trainer_set_graphs: null trainer");
+  tr->graphs = enable != 0;
+  if (!tr->graphs && tr->update_exec) {
+    cudaGraphExecDestroy(tr->update_exec);
+    tr->update_exec = nullptr;
+  }
   return 0;
 }
 

@@ -57,7 +57,7 @@ void launch_gather_all(int in, int n, int rollout, int batch, const float* obs, 
 void launch_loss(int n, int batch, int m, const float* actions, const float* logp, const float* value,
                  const float* advantage, const float* o, const float* log_std, const float* adv_moments,
                  int use_moments, float adv_mean, float adv_scale, float* d3, cudaStream_t st);
-void launch_adam(int p, int logstd, float c1, float c2, const float* stats, float* theta, const float* grad,
+void launch_adam(int p, int logstd, const float* c12, const float* stats, float* theta, const float* grad,
                  float* first, float* second, cudaStream_t st);
 // row sums: out[r] = sum_j x[r * ld + j] for r < rows, j < cols (deterministic two-pass)
 void launch_rowsum(const float* x, int rows, int cols, long ld, float* out, float* scratch, int squares,

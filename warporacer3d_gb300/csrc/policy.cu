@@ -22,6 +22,7 @@ struct racer_policy {
   uint8_t* pack = nullptr;   // pre-swizzled BF16 operand images of W0, W1, W2
   int* err = nullptr;        // device error word of the tensor-core kernels
   BackwardWork* work = nullptr;  // BF16 backward workspace for the last batch size
+  int generation = 0;            // changes whenever precision or workspace change (captured graphs go stale)
   cudaStream_t st = nullptr;
   bool owned = false;
 };
@@ -76,9 +77,12 @@ int policy_refresh_on(racer_policy* p, cudaStream_t st) {
 int policy_is_bf16(racer_policy* p) { return p->bf16; }
 
 int policy_set_precision(racer_policy* p, int bf16) {
+  if (p->bf16 != (bf16 ? 1 : 0)) ++p->generation;
   p->bf16 = bf16 ? 1 : 0;
   return 0;
 }
+
+int policy_generation(racer_policy* p) { return p->generation; }
 
 int policy_forward(racer_policy* p, const float* x, int cols, float* h1, float* h2, float* o, int write_hidden,
                    const SampleArgs* sa, cudaStream_t st, int c0, int c1) {
@@ -118,6 +122,7 @@ int policy_backward(racer_policy* p, const float* x, int cols, const float* h1, 
                     float* d2, float* d1, float* grad, cudaStream_t st) {
   if (p->bf16) {
     if (backward_work_cols(p->work) != cols) {
+      ++p->generation;
       backward_work_delete(p->work);
       p->work = nullptr;
       if (int rc = backward_work_new(p->in, cols, &p->work)) return rc;

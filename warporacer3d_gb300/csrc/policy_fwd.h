@@ -28,3 +28,6 @@ int policy_backward(racer_policy* p, const float* x, int cols, const float* h1, 
                     float* d2, float* d1, float* grad, cudaStream_t st);
 // 1: BF16 tensor-core products (default); 0: FP32 CUDA-core products.
 int policy_set_precision(racer_policy* p, int bf16);
+// A counter that changes whenever the precision or the backward workspace
+// changes: a CUDA graph that captured the policy's launches is stale after.
+int policy_generation(racer_policy* p);

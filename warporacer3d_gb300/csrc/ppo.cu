@@ -93,10 +93,13 @@ __global__ void k_loss(int n, int batch, int m, const float* actions, const floa
   d3[(long)(OUT + 2) * batch + b] = (ratio - 1.0f) - logratio;
 }
 
-__global__ void k_adam(int p, int logstd, float c1, float c2, const float* stats, float* theta, const float* grad,
+// c12 = (1 - 0.9^t, 1 - 0.999^t) for this step t, read from device memory so a
+// captured update replays with each step's values.
+__global__ void k_adam(int p, int logstd, const float* c12, const float* stats, float* theta, const float* grad,
                        float* first, float* second) {
   int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= p) return;
+  const float c1 = c12[0], c2 = c12[1];
   float scale = fminf(1.0f, MAX_NORM / (sqrtf(stats[ST_NORM]) + 1e-8f));
   float g = grad[i] * scale;
   float m = 0.9f * first[i] + 0.1f * g;
@@ -188,9 +191,9 @@ void launch_loss(int n, int batch, int m, const float* actions, const float* log
                                               use_moments, adv_mean, adv_scale, d3);
 }
 
-void launch_adam(int p, int logstd, float c1, float c2, const float* stats, float* theta, const float* grad,
+void launch_adam(int p, int logstd, const float* c12, const float* stats, float* theta, const float* grad,
                  float* first, float* second, cudaStream_t st) {
-  k_adam<<<(p + 255) / 256, 256, 0, st>>>(p, logstd, c1, c2, stats, theta, grad, first, second);
+  k_adam<<<(p + 255) / 256, 256, 0, st>>>(p, logstd, c12, stats, theta, grad, first, second);
 }
 
 // scratch must hold rows * 256 doubles (2 * rows * 256 floats).

@@ -311,6 +311,10 @@ class Trainer:
         call("racer_trainer_update", self.handle, policy.handle, ctypes.byref(kl))
         return kl.value
 
+    def set_graphs(self, enable=True):
+        """Replay each update from one captured CUDA graph (default) or launch it eagerly."""
+        call("racer_trainer_set_graphs", self.handle, int(enable))
+
     def minibatch(self, policy, m, adv_mean, adv_scale):
         call("racer_trainer_minibatch", self.handle, policy.handle, m, float(adv_mean), float(adv_scale))
 

@@ -307,6 +307,7 @@ def training_section(W, iterations):
             runner = W.Runner(track, TRAIN_CARS, beams=TRAIN_BEAMS, seed=seed, policy_seed=seed)
             runner.policy.set_precision(precision)
             state, obs = runner.sim.state.numpy(), runner.sim.obs.numpy()
+            shape, _ = runner.sim.autotune(5)  # lidar launch shape (rewrites obs from the same frames)
             chains, _ = runner.tune_chains(64, 3)  # rollout chains (BF16 only), then back to the start state
             runner.sim.state.write(state)
             runner.sim.obs.write(obs)
@@ -318,7 +319,7 @@ def training_section(W, iterations):
                 kls.append(trainer.update(runner.policy))
             dt = time.perf_counter() - t0
             k = max(1, min(20, iterations // 5))
-            runs.append({"seed": seed, "rollout_chains": chains,
+            runs.append({"seed": seed, "rollout_chains": chains, "lidar_shape": shape,
                          "training_transitions_per_s": TRAIN_CARS * TRAIN_ROLLOUT * iterations / dt,
                          "reward_per_step_first": float(np.mean(rewards[:k])),
                          "reward_per_step_last": float(np.mean(rewards[-k:])), "kl_last": float(kls[-1]),

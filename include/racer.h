@@ -78,14 +78,18 @@ int racer_sim_create_segments(int count, const float* const* tracks, const size_
  * (split = 0) or their launch order (split = 1). dynamic (one-track sims and
  * split launches): 1 = a persistent grid per segment whose warps take (car,
  * 32-beam group) units from an atomic counter instead of a fixed block per
- * group of cars (cars_per_block is then unused). Setting a different shape
- * drops the sim's captured rollout graphs. */
+ * group of cars (cars_per_block is then unused). flat (one-track sims and
+ * split launches, not dynamic): 1 = each warp takes the next 32 (car, beam)
+ * pairs in car-major order, across car boundaries, so no lane idles when the
+ * beam count is not a multiple of 32. Setting a different shape drops the
+ * sim's captured rollout graphs. */
 typedef struct {
   int cars_per_block;
   int wide;
   int split;
   int dynamic;
   int order[8];
+  int flat;
 } racer_lidar_shape;
 int racer_sim_set_lidar_shape(racer_sim* sim, const racer_lidar_shape* shape);
 int racer_sim_get_lidar_shape(racer_sim* sim, racer_lidar_shape* shape);

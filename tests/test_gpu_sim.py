@@ -270,7 +270,7 @@ def test_lidar_shapes_and_autotune_keep_results():
     b.reset()
     rng = np.random.default_rng(5)
     shapes = [(2, 0, 0, [3, 1, 0, 2]), (8, 1, 0, None), (4, 1, 1, [2, 3, 1, 0]), (2, 0, 1, None),
-              (2, 0, 1, [1, 0, 2, 3], 1), (2, 1, 1, None, 1), "auto"]
+              (2, 0, 1, [1, 0, 2, 3], 1), (2, 1, 1, None, 1), (4, 0, 1, [3, 2, 1, 0], 0, 1), "auto"]
     for shape in shapes:
         if shape == "auto":
             best, ms = b.autotune(3)
@@ -306,18 +306,20 @@ def test_split_lidar_in_captured_rollouts():
     assert same(runs[0].sim.state.numpy(), runs[1].sim.state.numpy())
 
 
-def test_one_track_lidar_shapes_bit_exact():
-    """Every launch shape of the one-track lidar kernel gives the oracle's ranges."""
+@pytest.mark.parametrize("beams", [1081, 108])
+def test_one_track_lidar_shapes_bit_exact(beams):
+    """Every launch shape of the one-track lidar kernel gives the oracle's ranges, including warps
+    that take (car, beam) pairs across car boundaries (flat; 108 beams = 3.375 warps a car)."""
     track = W.track("bridge")
-    n = 50
-    cpu = O.Sim(track, n, 9, beams=1081)
+    n = 50 if beams == 1081 else 77
+    cpu = O.Sim(track, n, 9, beams=beams)
     cpu.reset()
-    for cars_per_block, dynamic in ((2, 0), (4, 0), (8, 0), (2, 1)):
+    for cars_per_block, dynamic, flat in ((2, 0, 0), (4, 0, 0), (8, 0, 0), (2, 1, 0), (2, 0, 1), (8, 0, 1)):
         for wide in (0, 1):
-            gpu = W.Sim(track, n, 9, beams=1081)
-            gpu.set_lidar_shape(cars_per_block, wide, 0, None, dynamic)
+            gpu = W.Sim(track, n, 9, beams=beams)
+            gpu.set_lidar_shape(cars_per_block, wide, 0, None, dynamic, flat)
             gpu.reset()
-            check_sim(gpu, cpu, f"shape {cars_per_block}/{wide}/{dynamic} ")
+            check_sim(gpu, cpu, f"shape {cars_per_block}/{wide}/{dynamic}/{flat} ")
 
 
 def test_synthetic_occupancy_map_bit_exact():

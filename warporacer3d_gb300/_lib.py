@@ -26,7 +26,7 @@ class SimBuffers(ctypes.Structure):
 
 class LidarShape(ctypes.Structure):
     _fields_ = [("cars_per_block", c_int), ("wide", c_int), ("split", c_int), ("dynamic", c_int),
-                ("order", c_int * 8)]
+                ("order", c_int * 8), ("flat", c_int)]
 
 
 class TrainerBuffers(ctypes.Structure):

@@ -1253,6 +1253,7 @@ static LidarShape from_api(const racer_lidar_shape& in) {
   shape.wide = in.wide;
   shape.split = in.split;
   shape.dynamic = in.dynamic;
+  shape.flat = in.flat;
   for (int j = 0; j < MAX_SEGMENTS; ++j) shape.order[j] = in.order[j];
   return shape;
 }
@@ -1262,6 +1263,7 @@ static void to_api(const racer_sim* s, const LidarShape& shape, racer_lidar_shap
   out->wide = shape.wide;
   out->split = shape.split;
   out->dynamic = shape.dynamic;
+  out->flat = shape.flat;
   int order[MAX_SEGMENTS];
   segment_order(s, shape, order);
   for (int j = 0; j < MAX_SEGMENTS; ++j) out->order[j] = j < s->seg.count ? order[j] : -1;
@@ -1271,7 +1273,7 @@ static bool same_shape(const racer_sim* s, const LidarShape& a, const LidarShape
   int oa[MAX_SEGMENTS], ob[MAX_SEGMENTS];
   segment_order(s, a, oa);
   segment_order(s, b, ob);
-  return a.cars == b.cars && a.wide == b.wide && a.split == b.split && a.dynamic == b.dynamic &&
+  return a.cars == b.cars && a.wide == b.wide && a.split == b.split && a.dynamic == b.dynamic && a.flat == b.flat &&
          std::equal(oa, oa + s->seg.count, ob);
 }
 
@@ -1297,7 +1299,7 @@ int racer_sim_set_lidar_shape(racer_sim* s, const racer_lidar_shape* in) {
   LidarShape shape = from_api(*in);
   RACER_ARG(lidar_shape_ok(shape) && (shape.split == 0 || shape.split == 1) &&
                 (shape.dynamic == 0 || shape.dynamic == 1),
-            "racer_sim_set_lidar_shape: cars per block must be 2, 4 or 8, wide, split and dynamic 0 or 1");
+            "racer_sim_set_lidar_shape: cars per block must be 2, 4 or 8, wide, split, dynamic and flat 0 or 1");
   bool seen[MAX_SEGMENTS] = {};
   for (int j = 0; j < s->seg.count; ++j) {
     RACER_ARG(in->order[j] >= 0 && in->order[j] < s->seg.count && !seen[in->order[j]],
@@ -1343,14 +1345,17 @@ int racer_sim_autotune(racer_sim* s, int reps, racer_lidar_shape* best_out, floa
     for (int cars : {2, 4, 8})
       for (int wide : {0, 1})
         for (int split : {0, 1})
-          for (int sorted : {0, 1}) {
+          for (int sorted : {0, 1})
+            for (int flat : {0, 1}) {
           if (count == 1 && (split || sorted)) continue;
           if (dynamic && (cars != 2 || (count > 1 && !split))) continue;  // per segment; no cars-per-block
+          if (flat && (dynamic || (count > 1 && !split))) continue;       // one-track launches only
           LidarShape shape;
           shape.cars = cars;
           shape.wide = wide;
           shape.split = split;
           shape.dynamic = dynamic;
+          shape.flat = flat;
           for (int j = 0; j < MAX_SEGMENTS; ++j) shape.order[j] = sorted ? heavy[j] : j;
           candidates.push_back(shape);
         }

@@ -69,12 +69,14 @@ struct Segments {
 // segment-table launch; `order` is then the launch order.
 // dynamic = 1 runs each segment's lidar as a persistent grid whose warps take
 // (car, beam group) units from a per-segment counter (counters, zeroed before
-// each launch); it applies to one-track sims and split launches.
+// each launch); it applies to one-track sims and split launches, as does
+// flat = 1 (k_lidar_flat: no idle lanes when beams is not a multiple of 32).
 struct LidarShape {
   int cars = 2;  // measured fastest on every built-in track and the occupancy map
   int wide = 0;  // 1: compiled for 48 resident warps per SM (40 registers) instead of 64 (32)
   int split = 0;
   int dynamic = 0;
+  int flat = 0;  // 1: one-track launches take (car, beam) items 32 at a time across car boundaries
   int order[MAX_SEGMENTS] = {0, 1, 2, 3, 4, 5, 6, 7};
   unsigned* counters = nullptr;  // [MAX_SEGMENTS] device words owned by the sim
   int sms = 152;

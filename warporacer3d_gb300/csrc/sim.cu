@@ -522,6 +522,21 @@ __global__ void __launch_bounds__(CARS * 32, lidar_min_blocks(CARS, WIDE))
   if (car < c1) trace<LAYERS>(t, ray, obs, n, beam_dir, max_iters, iters, car, beam);
 }
 
+// One track with the (car, beam) items of cars [c0, c0 + items / beams) in
+// car-major order, 32 consecutive items per warp: a warp may hold the last
+// beams of one car and the first of the next, so no lane idles at the end of
+// a car's beams when the beam count is not a multiple of 32 (108 beams fill
+// 3.375 warps a car). Each beam is traced exactly as in k_lidar_track.
+template <int LAYERS, int CARS, bool WIDE>
+__global__ void __launch_bounds__(CARS * 32, lidar_min_blocks(CARS, WIDE))
+    k_lidar_flat(TrackDev t, int max_iters, const float4* __restrict__ ray, float* obs, int n, int c0,
+                 unsigned items, int beams, const float2* __restrict__ beam_dir, int* iters) {
+  const unsigned item = (blockIdx.x * CARS + (threadIdx.x >> 5)) * 32u + (threadIdx.x & 31);
+  if (item >= items) return;
+  const unsigned car = item / (unsigned)beams;
+  trace<LAYERS>(t, ray, obs, n, beam_dir, max_iters, iters, c0 + (int)car, (int)(item - car * (unsigned)beams));
+}
+
 // Dynamic variant of k_lidar_track: a persistent grid whose warps take
 // (car, 32-beam group) units from `counter` (zero at launch) one at a time,
 // so no warp holds a block slot waiting for a sibling and the last wave has
@@ -700,7 +715,14 @@ static LidarGrid lidar_grid(const Segments& g, const LidarShape& shape) {
 
 template <int LAYERS, int CARS, bool WIDE>
 static void lidar_track(const TrackDev& t, int max_iters, const float4* ray, float* obs, int n, int c0, int c1,
-                        int beams, const float2* beam_dir, int* iters, cudaStream_t st) {
+                        int beams, const float2* beam_dir, int* iters, cudaStream_t st, bool flat = false) {
+  const long items = (long)(c1 - c0) * beams;
+  if (flat && items > 0 && items < (1L << 31)) {
+    const unsigned blocks = (unsigned)((items + 32 * CARS - 1) / (32 * CARS));
+    k_lidar_flat<LAYERS, CARS, WIDE><<<blocks, CARS * 32, 0, st>>>(t, max_iters, ray, obs, n, c0, (unsigned)items,
+                                                                   beams, beam_dir, iters);
+    return;
+  }
   dim3 grid((c1 - c0 + CARS - 1) / CARS, (beams + 31) / 32);
   if (grid.x == 0) return;
   k_lidar_track<LAYERS, CARS, WIDE, false>
@@ -734,12 +756,13 @@ static void lidar_segment(const Segments& g, int k, const float4* ray, float* ob
       lidar_dynamic<0, WIDE>(t, g.max_iters[k], ray, obs, n, c0, c1, beams, beam_dir, iters, counter, shape.sms, st);
     return;
   }
+  const bool flat = shape.flat == 1;
   if (t.layers == 1)
-    lidar_track<1, CARS, WIDE>(t, g.max_iters[k], ray, obs, n, c0, c1, beams, beam_dir, iters, st);
+    lidar_track<1, CARS, WIDE>(t, g.max_iters[k], ray, obs, n, c0, c1, beams, beam_dir, iters, st, flat);
   else if (t.layers == 2)
-    lidar_track<2, CARS, WIDE>(t, g.max_iters[k], ray, obs, n, c0, c1, beams, beam_dir, iters, st);
+    lidar_track<2, CARS, WIDE>(t, g.max_iters[k], ray, obs, n, c0, c1, beams, beam_dir, iters, st, flat);
   else
-    lidar_track<0, CARS, WIDE>(t, g.max_iters[k], ray, obs, n, c0, c1, beams, beam_dir, iters, st);
+    lidar_track<0, CARS, WIDE>(t, g.max_iters[k], ray, obs, n, c0, c1, beams, beam_dir, iters, st, flat);
 }
 
 template <int CARS, bool WIDE>
@@ -755,7 +778,8 @@ static void lidar_shape(const Segments& g, const LidarShape& shape, const float4
 }
 
 bool lidar_shape_ok(const LidarShape& shape) {
-  return (shape.cars == 2 || shape.cars == 4 || shape.cars == 8) && (shape.wide == 0 || shape.wide == 1);
+  return (shape.cars == 2 || shape.cars == 4 || shape.cars == 8) && (shape.wide == 0 || shape.wide == 1) &&
+         (shape.flat == 0 || shape.flat == 1);
 }
 
 void launch_lidar(const Segments& g, const LidarShape& shape, const float4* ray, float* obs, int n, int beams,
@@ -793,13 +817,14 @@ void launch_lidar_cars(const Segments& g, const LidarShape& shape, int c0, int c
   if (g.count != 1 || c1 <= c0) return;
   const TrackDev& t = g.t[0];
   const bool wide = shape.wide == 1;
+  const bool flat = shape.flat == 1;
 #define RACER_LIDAR_CARS(CARS, WIDE)                                                                         \
   if (t.layers == 1)                                                                                          \
-    lidar_track<1, CARS, WIDE>(t, g.max_iters[0], ray, obs, n, c0, c1, beams, beam_dir, iters, st);         \
+    lidar_track<1, CARS, WIDE>(t, g.max_iters[0], ray, obs, n, c0, c1, beams, beam_dir, iters, st, flat);   \
   else if (t.layers == 2)                                                                                     \
-    lidar_track<2, CARS, WIDE>(t, g.max_iters[0], ray, obs, n, c0, c1, beams, beam_dir, iters, st);         \
+    lidar_track<2, CARS, WIDE>(t, g.max_iters[0], ray, obs, n, c0, c1, beams, beam_dir, iters, st, flat);   \
   else                                                                                                        \
-    lidar_track<0, CARS, WIDE>(t, g.max_iters[0], ray, obs, n, c0, c1, beams, beam_dir, iters, st);
+    lidar_track<0, CARS, WIDE>(t, g.max_iters[0], ray, obs, n, c0, c1, beams, beam_dir, iters, st, flat);
   if (shape.cars == 2) {
     if (wide) { RACER_LIDAR_CARS(2, true) } else { RACER_LIDAR_CARS(2, false) }
   } else if (shape.cars == 8) {

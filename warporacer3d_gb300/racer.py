@@ -163,19 +163,20 @@ class Sim:
         call("racer_sim_snapshot", self.handle, out.ctypes.data_as(ctypes.c_void_p), 1)
         return out
 
-    def set_lidar_shape(self, cars_per_block, wide=0, split=0, order=None, dynamic=0):
+    def set_lidar_shape(self, cars_per_block, wide=0, split=0, order=None, dynamic=0, flat=0):
         """Lidar launch shape: cars per block (2, 4, 8), the 40-register variant (wide), per-segment
-        launches on parallel streams (split), the segments' order (default: index order) and the
-        persistent grid with dynamically assigned (car, beam group) units (dynamic)."""
+        launches on parallel streams (split), the segments' order (default: index order), the
+        persistent grid with dynamically assigned (car, beam group) units (dynamic) and warps taking
+        (car, beam) pairs across car boundaries (flat)."""
         order = list(range(len(self.cars))) if order is None else list(order)
         shape = LidarShape(cars_per_block, wide, split, dynamic,
-                           (ctypes.c_int * 8)(*(order + [-1] * (8 - len(order)))))
+                           (ctypes.c_int * 8)(*(order + [-1] * (8 - len(order)))), flat)
         call("racer_sim_set_lidar_shape", self.handle, ctypes.byref(shape))
 
     @staticmethod
     def _shape(shape):
         return {"cars_per_block": shape.cars_per_block, "wide": shape.wide, "split": shape.split,
-                "dynamic": shape.dynamic, "order": [k for k in shape.order if k >= 0]}
+                "dynamic": shape.dynamic, "order": [k for k in shape.order if k >= 0], "flat": shape.flat}
 
     def lidar_shape(self):
         shape = LidarShape()

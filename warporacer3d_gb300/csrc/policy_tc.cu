@@ -12,7 +12,8 @@
 // are summed in a fixed order and written straight into the theta layout
 // W0 [64, IN] | W1 [64, 65] | W2 [3, 65]. The data gradients are memory-bound
 // (K <= 64): one small kernel per 128 samples fuses them with the tanh
-// derivatives and the BF16 operand copies of the weight-gradient GEMMs.
+// derivatives and the BF16 operand copies of the weight-gradient GEMMs (d1,
+// d2, d3 and the h1, h2 it reads anyway; x is converted on its own).
 #include <cuda_bf16.h>
 
 #include <string>
@@ -66,7 +67,7 @@ __global__ void __launch_bounds__(128, 4)
     k_dgrad_tc(int in, const float* __restrict__ theta, const uint4* __restrict__ w1ts, const float* __restrict__ d3,
                const float* __restrict__ h1, const float* __restrict__ h2, float* __restrict__ d2,
                float* __restrict__ d1, int cols, bf16* __restrict__ d1f, bf16* __restrict__ d2f,
-               bf16* __restrict__ d3f, int ld, int* err) {
+               bf16* __restrict__ d3f, bf16* __restrict__ h1b, bf16* __restrict__ h2b, int ld, int* err) {
   __shared__ __align__(1024) uint8_t A[128 * 128];
   __shared__ __align__(1024) uint8_t B[H * 128];
   __shared__ uint64_t done;
@@ -100,7 +101,10 @@ __global__ void __launch_bounds__(128, 4)
     const float acc = w2[k] * e0 + w2[HA + k] * e1 + w2[2 * HA + k] * e2;
     const float a = hv[k];
     const float v = acc * (1.0f - a * a);
-    if (live) d2[(long)k * cols + j] = v;
+    if (live) {
+      d2[(long)k * cols + j] = v;
+      h2b[(long)k * ld + j] = __float2bfloat16_rn(a);  // the weight-gradient operand of layer 2
+    }
     if (k < H) {
       const bf16 vb = __float2bfloat16_rn(v);
       if (live) d2f[(long)k * ld + j] = vb;
@@ -142,9 +146,11 @@ __global__ void __launch_bounds__(128, 4)
         const float g = acc[k0 + k] * (1.0f - hh[k] * hh[k]);
         d1[(long)(k0 + k) * cols + j] = g;
         d1f[(long)(k0 + k) * ld + j] = __float2bfloat16_rn(g);
+        h1b[(long)(k0 + k) * ld + j] = __float2bfloat16_rn(hh[k]);  // the weight-gradient operand of layer 1
       }
     }
     d1[(long)H * cols + j] = 0.0f;
+    h1b[(long)H * ld + j] = __float2bfloat16_rn(h1[(long)H * cols + j]);
   }
   tc::tc_fence_before();
   __syncthreads();
@@ -264,10 +270,9 @@ int backward_tc(BackwardWork* w, const float* theta, const float* x, const float
   const int in = w->in, cols = w->cols, ld = w->ld;
   const unsigned gx = (unsigned)((cols + 1023) / 1024);
   k_rows_bf16<<<dim3(gx, in), 256, 0, st>>>(x, in, cols, w->xb, ld);
-  k_rows_bf16<<<dim3(gx, HA), 256, 0, st>>>(h1, HA, cols, w->h1b, ld);
-  k_rows_bf16<<<dim3(gx, HA), 256, 0, st>>>(h2, HA, cols, w->h2b, ld);
+  // the BF16 copies of h1 and h2 are written by k_dgrad_tc, which reads them anyway
   k_dgrad_tc<<<(cols + 127) / 128, 128, 0, st>>>(in, theta, reinterpret_cast<const uint4*>(w->w1ts), d3, h1, h2, d2,
-                                                 d1, cols, w->d1f, w->d2f, w->d3f, ld, err);
+                                                 d1, cols, w->d1f, w->d2f, w->d3f, w->h1b, w->h2b, ld, err);
   BW_CHECK(cudaGetLastError());
   int rc;
   if ((rc = wgrad<64>(w, w->txb, w->td1f, in, H, in, grad, in, err, st))) return rc;

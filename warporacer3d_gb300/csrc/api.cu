@@ -23,6 +23,7 @@
 #include "objects.h"
 #include "policy_fwd.h"
 #include "surrogate.h"
+#include "tma.h"
 
 namespace racer_host {
 static thread_local std::string g_error;
@@ -101,6 +102,11 @@ struct racer_trainer {
   // replayed after that; Adam's bias corrections of its 16 steps come from
   // c12_host (pinned), copied inside the graph.
   float *c12_dev = nullptr, *c12_host = nullptr;
+  // BF16 copy of the four minibatches' inputs [4][IN][xld], written by the gather, and its
+  // tensor maps: the BF16 backward's operand for the layer-0 weight gradient
+  void* xb = nullptr;
+  int xld = 0;
+  CUtensorMap xmaps[MINIBATCHES];
   cudaGraphExec_t update_exec = nullptr;
   racer_policy* update_policy = nullptr;
   int update_generation = -1;
@@ -607,6 +613,20 @@ int racer_trainer_create(int n, int beams, int rollout, void* stream, racer_trai
     racer_trainer_destroy(tr);
     return rc;
   }
+  tr->xld = (tr->batch + 7) / 8 * 8;
+  {
+    uint16_t* xb = nullptr;
+    if ((rc = dalloc(&xb, (size_t)MINIBATCHES * IN * tr->xld))) {
+      racer_trainer_destroy(tr);
+      return rc;
+    }
+    tr->xb = xb;
+    for (int m = 0; m < MINIBATCHES; ++m)
+      if ((rc = make_tmap_bf16(&tr->xmaps[m], xb + (size_t)m * IN * tr->xld, IN, tr->xld, tr->xld, 128))) {
+        racer_trainer_destroy(tr);
+        return rc;
+      }
+  }
   if (cudaMallocHost((void**)&tr->c12_host, 2 * EPOCHS * MINIBATCHES * sizeof(float)) != cudaSuccess) {
     set_error("racer_trainer_create: pinned allocation failed");
     tr->c12_host = nullptr;
@@ -637,6 +657,7 @@ int racer_trainer_destroy(racer_trainer* tr) {
                    tr->d2, tr->d1, tr->grad, tr->first, tr->second, tr->stats, tr->red, tr->c12_dev})
     cudaFree(p);
   if (tr->c12_host) cudaFreeHost(tr->c12_host);
+  cudaFree(tr->xb);
   racer_acts_destroy(tr->acts);
   if (tr->owned && tr->st) cudaStreamDestroy(tr->st);
   delete tr;
@@ -738,7 +759,8 @@ static int minibatch_on(racer_trainer* tr, racer_policy* p, int m, int use_momen
   if (rc) return rc;
   launch_loss(tr->n, B, m, tr->actions, tr->logp, tr->value, tr->advantage, tr->acts->o, logstd,
               tr->stats + ST_ADV, use_moments, adv_mean, adv_scale, tr->d3, st);
-  if ((rc = policy_backward(p, x, B, tr->acts->h1, tr->acts->h2, tr->d3, tr->d2, tr->d1, tr->grad, st)))
+  if ((rc = policy_backward(p, x, B, tr->acts->h1, tr->acts->h2, tr->d3, tr->d2, tr->d1, tr->grad, st,
+                            &tr->xmaps[m])))
     return rc;
   launch_rowsum(tr->d3 + (size_t)OUT * B, 2, B, B, tr->grad + P - 2, tr->red, 0, st);
   launch_rowsum(tr->grad, 1, P, P, tr->stats + ST_NORM, tr->red + 2048, 1, st);
@@ -749,7 +771,7 @@ static int minibatch_on(racer_trainer* tr, racer_policy* p, int m, int use_momen
 int racer_trainer_minibatch(racer_trainer* tr, racer_policy* p, int m, float adv_mean, float adv_scale) {
   RACER_ARG(tr && p && m >= 0 && m < MINIBATCHES, "racer_trainer_minibatch: bad argument");
   RACER_ARG(policy_inputs(p) == tr->in_rows, "racer_trainer_minibatch: policy and trainer sizes differ");
-  launch_gather_all(tr->in_rows, tr->n, tr->rollout, tr->batch, tr->obs, tr->x, tr->st);
+  launch_gather_all(tr->in_rows, tr->n, tr->rollout, tr->batch, tr->obs, tr->x, tr->st, tr->xb, tr->xld);
   RACER_LAUNCHED();
   return minibatch_on(tr, p, m, 0, adv_mean, adv_scale);
 }
@@ -764,7 +786,7 @@ static int update_body(racer_trainer* tr, racer_policy* p) {
                             cudaMemcpyHostToDevice, st));
   launch_moments(tr->advantage, (long)tr->rollout * tr->n, tr->stats, tr->red, st);
   // the minibatches' samples are the same in every epoch: gather them once
-  launch_gather_all(tr->in_rows, tr->n, tr->rollout, tr->batch, tr->obs, tr->x, st);
+  launch_gather_all(tr->in_rows, tr->n, tr->rollout, tr->batch, tr->obs, tr->x, st, tr->xb, tr->xld);
   RACER_LAUNCHED();
   for (int epoch = 0; epoch < EPOCHS; ++epoch) {
     for (int m = 0; m < MINIBATCHES; ++m) {

@@ -53,7 +53,8 @@ void launch_gae(int n, int rollout, const float* reward, const float* done, cons
                 const float* last_value, float* advantage, cudaStream_t st);
 void launch_gather(int in, int n, int batch, int m, const float* obs, float* x, cudaStream_t st);
 // x [4][in, batch]: every minibatch's inputs from rollout storage obs [rollout + 1][in, n] in one pass.
-void launch_gather_all(int in, int n, int rollout, int batch, const float* obs, float* x, cudaStream_t st);
+void launch_gather_all(int in, int n, int rollout, int batch, const float* obs, float* x, cudaStream_t st,
+                       void* xb = nullptr, int ldb = 0);  // xb: also the BF16 copy [4][in][ldb]
 void launch_loss(int n, int batch, int m, const float* actions, const float* logp, const float* value,
                  const float* advantage, const float* o, const float* log_std, const float* adv_moments,
                  int use_moments, float adv_mean, float adv_scale, float* d3, cudaStream_t st);

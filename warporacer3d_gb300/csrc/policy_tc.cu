@@ -266,16 +266,17 @@ int backward_refresh(BackwardWork* w, const float* theta, cudaStream_t st) {
 }
 
 int backward_tc(BackwardWork* w, const float* theta, const float* x, const float* h1, const float* h2,
-                const float* d3, float* d2, float* d1, float* grad, int* err, cudaStream_t st) {
+                const float* d3, float* d2, float* d1, float* grad, int* err, cudaStream_t st,
+                const CUtensorMap* xb_map) {
   const int in = w->in, cols = w->cols, ld = w->ld;
   const unsigned gx = (unsigned)((cols + 1023) / 1024);
-  k_rows_bf16<<<dim3(gx, in), 256, 0, st>>>(x, in, cols, w->xb, ld);
+  if (!xb_map) k_rows_bf16<<<dim3(gx, in), 256, 0, st>>>(x, in, cols, w->xb, ld);
   // the BF16 copies of h1 and h2 are written by k_dgrad_tc, which reads them anyway
   k_dgrad_tc<<<(cols + 127) / 128, 128, 0, st>>>(in, theta, reinterpret_cast<const uint4*>(w->w1ts), d3, h1, h2, d2,
                                                  d1, cols, w->d1f, w->d2f, w->d3f, w->h1b, w->h2b, ld, err);
   BW_CHECK(cudaGetLastError());
   int rc;
-  if ((rc = wgrad<64>(w, w->txb, w->td1f, in, H, in, grad, in, err, st))) return rc;
+  if ((rc = wgrad<64>(w, xb_map ? *xb_map : w->txb, w->td1f, in, H, in, grad, in, err, st))) return rc;
   if ((rc = wgrad<64>(w, w->th1b, w->td2f, HA, H, HA, grad + H * in, HA, err, st))) return rc;
   if ((rc = wgrad<16>(w, w->th2b, w->td3f, HA, OUT, HA, grad + H * in + H * HA, HA, err, st))) return rc;
   return 0;

@@ -6,6 +6,8 @@
 // :317-337 (Adam). Built like sim.cu with --fmad=false and rmath.h, so init,
 // GAE and the loss derivatives repeat the CPU restatement's binary32
 // operations; sums use a fixed two-pass tree in double.
+#include <cuda_bf16.h>
+
 #include "common.cuh"
 #include "kernels.h"
 #include "philox.h"
@@ -170,18 +172,23 @@ void launch_gather(int in, int n, int batch, int m, const float* obs, float* x, 
 // All four minibatches at once (racer/ppo.mojo:259-268's sample order
 // s = b * 4 + m): obs[t][r][i] -> x[m][r][b] with s = t * n + i, m = s % 4,
 // b = s / 4, so every rollout row is read once, coalesced.
-__global__ void k_gather_all(int in, int n, int batch, const float* __restrict__ obs, float* __restrict__ x) {
+__global__ void k_gather_all(int in, int n, int batch, const float* __restrict__ obs, float* __restrict__ x,
+                             __nv_bfloat16* __restrict__ xb, int ldb) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
   const int r = blockIdx.y, t = blockIdx.z;
   const long s = (long)t * n + i;
-  x[((s & (MINIBATCHES - 1)) * in + r) * (long)batch + (s >> 2)] = obs[((long)t * in + r) * n + i];
+  const long row = (s & (MINIBATCHES - 1)) * in + r;
+  const float v = obs[((long)t * in + r) * n + i];
+  x[row * batch + (s >> 2)] = v;
+  if (xb) xb[row * ldb + (s >> 2)] = __float2bfloat16_rn(v);  // the weight-gradient operand of layer 0
 }
 
-void launch_gather_all(int in, int n, int rollout, int batch, const float* obs, float* x, cudaStream_t st) {
+void launch_gather_all(int in, int n, int rollout, int batch, const float* obs, float* x, cudaStream_t st, void* xb,
+                       int ldb) {
   static_assert(MINIBATCHES == 4, "the sample split assumes four minibatches");
   dim3 grid((n + 255) / 256, in, rollout);
-  k_gather_all<<<grid, 256, 0, st>>>(in, n, batch, obs, x);
+  k_gather_all<<<grid, 256, 0, st>>>(in, n, batch, obs, x, static_cast<__nv_bfloat16*>(xb), ldb);
 }
 
 void launch_loss(int n, int batch, int m, const float* actions, const float* logp, const float* value,

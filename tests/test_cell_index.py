@@ -11,6 +11,11 @@
 2. Division skip. The march (sim.cu, trace) evaluates fl / descent only when
    fl * RN(1 / descent) <= a * (1 + 2^-20); the claim: whenever it skips,
    RN(fl / descent) >= a, so min(a, fl / descent) = a.
+3. The quotient itself (sim.cu, quotient): from y = RN(1 / b) and
+   q0 = RN(a * y), two residual corrections q <- RN(q + RN(a - b q) y), each a
+   pair of fused multiply-adds, give RN(a / b); the claim is checked on the
+   march's operand ranges, on wide exponents and on quotients a hair from a
+   rounding midpoint.
 
 Both are replayed here in numpy binary32 (IEEE round-to-nearest, like the
 GPU built with --fmad=false; the fused multiply-add exactly, through a
@@ -123,3 +128,34 @@ def test_division_skip_is_exact():
     q = fl / descent
     assert np.all(q[skip] >= a[skip])
     assert skip.any() and (~skip).any()
+
+
+def test_quotient_by_residual_corrections_is_ieee_division():
+    rng = np.random.default_rng(3)
+    bad = total = 0
+    for kind in range(6):
+        n = 500_000
+        if kind in (0, 3):  # the march: floors up to 20 m, descents 1e-4 .. 5
+            a = rng.uniform(0, 20, n).astype(f32)
+            b = (10 ** rng.uniform(-4, 0.7, n)).astype(f32)
+        elif kind == 1:  # wide exponents
+            a = (10 ** rng.uniform(-8, 8, n)).astype(f32)
+            b = (10 ** rng.uniform(-8, 8, n)).astype(f32)
+        elif kind in (2, 4):  # a / b within an ulp's fraction of a rounding midpoint
+            q = (10 ** rng.uniform(-3, 2, n)).astype(f32)
+            mid = (q.astype(f64) + np.nextafter(q, f32(np.inf)).astype(f64)) / 2
+            b = (10 ** rng.uniform(-3, 1, n)).astype(f32)
+            a = (mid * b.astype(f64)).astype(f32)
+        else:  # divisor significands near 2 (the largest reciprocal error)
+            b = ((1.9999 + rng.uniform(0, 1e-4, n)) * 2.0 ** rng.integers(-10, 4, n)).astype(f32)
+            a = rng.uniform(0, 20, n).astype(f32)
+        with np.errstate(all="ignore"):
+            y = f32(1) / b
+            q = a * y
+            for _ in range(2):
+                q = fma32(fma32(-q, b, a), y, q)
+            ref = a / b
+        ok = np.isfinite(ref) & (ref > 0)
+        bad += int(np.sum(q[ok] != ref[ok]))
+        total += int(ok.sum())
+    assert total > 2_900_000 and bad == 0

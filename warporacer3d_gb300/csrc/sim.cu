@@ -612,6 +612,21 @@ __device__ __forceinline__ void trace(const TrackDev& t, const float4* __restric
   if (iters) iters[(long)beam * n + car] = count;
 }
 
+// RN(a / b) from y = RN(1 / b) and q0 = RN(a * y), by two residual
+// corrections (Markstein, IBM J. Res. Dev. 34(1), 1990): r = a - b q is exact
+// in one fused multiply-add when q is within a few ulps of a / b, and
+// RN(q + r y) is then the correctly rounded quotient once q is faithful,
+// which the first correction makes it. For the march's operands (0 <= a,
+// b >= 0, neither subnormal) this is the IEEE quotient; where b = 0 or a
+// value is NaN every path gives NaN or skips, as the division does, and
+// fminf(a, NaN) = a either way. Checked against IEEE division on random and
+// near-midpoint quotients (tests/test_cell_index.py) and by the bit-exact
+// lidar tests.
+__device__ __forceinline__ float quotient(float a, float b, float y, float q0) {
+  const float q1 = __fmaf_rn(__fmaf_rn(-q0, b, a), y, q0);
+  return __fmaf_rn(__fmaf_rn(-q1, b, a), y, q1);
+}
+
 // The march of one beam (racer/sim.mojo:252-266); returns the range.
 template <int LAYERS, bool GUARD>
 __device__ __forceinline__ float march(const TrackDev& t, float ox, float oy, float oz, float dx, float dy, float dz,
@@ -637,7 +652,8 @@ __device__ __forceinline__ float march(const TrackDev& t, float ox, float oy, fl
     // which skips, or NaN (fl == 0), where the quotient is NaN too and fminf
     // returns a: the reference's min(a, fl / 0) either way.
     float step = a;
-    if (!(fl * inv_descent > a * 1.00000095f)) step = fminf(a, fl / descent);
+    const float q0 = fl * inv_descent;
+    if (!(q0 > a * 1.00000095f)) step = fminf(a, quotient(fl, descent, inv_descent, q0));
     if (step < min_step) break;
     last = tt;
     last_floor = fl;

@@ -8,10 +8,11 @@
    X = max(|x0|, |y0|) / cell), it uses rint(v) with an integer bounds test,
    otherwise the division (whose own shortcut, cell_coord, is replayed too).
    The claim: on-map status and cell are always the reference's.
-2. Division skip. The march (sim.cu, trace) evaluates fl / descent only when
-   fl * RN(1 / descent) <= a * (1 + 2^-20); the claim: whenever it skips,
-   RN(fl / descent) >= a, so min(a, fl / descent) = a.
-3. The quotient itself (sim.cu, quotient): from y = RN(1 / b) and
+2. Division skip. The guarded march (sim.cu, march<.., true>: rays with a
+   huge or non-finite origin height or a subnormal descent) evaluates
+   fl / descent only when fl * RN(1 / descent) <= a * (1 + 2^-20); the claim:
+   whenever it skips, RN(fl / descent) >= a, so min(a, fl / descent) = a.
+3. The quotient of the unguarded march (sim.cu, quotient): from y = RN(1 / b) and
    q0 = RN(a * y), two residual corrections q <- RN(q + RN(a - b q) y), each a
    pair of fused multiply-adds, give RN(a / b); the claim is checked on the
    march's operand ranges, on wide exponents and on quotients a hair from a

@@ -605,7 +605,8 @@ __device__ __forceinline__ void trace(const TrackDev& t, const float4* __restric
   int count = 0;
   // every probe height lies within RANGE of the origin's (|dz| <= 1): with
   // |oz| <= 1e20 the probe's height guard cannot fail (NaN takes the guarded loop)
-  const float range = fabsf(oz) <= 1e20f
+  // the unguarded march also needs a descent of 0 or a normal number (its quotient; see march)
+  const float range = fabsf(oz) <= 1e20f && (descent == 0.0f || descent >= 1.17549435e-38f)
                           ? march<LAYERS, false>(t, ox, oy, oz, dx, dy, dz, descent, inv_descent, max_iters, &count)
                           : march<LAYERS, true>(t, ox, oy, oz, dx, dy, dz, descent, inv_descent, max_iters, &count);
   obs[(long)(4 + beam) * n + car] = range / RANGE;
@@ -617,11 +618,10 @@ __device__ __forceinline__ void trace(const TrackDev& t, const float4* __restric
 // in one fused multiply-add when q is within a few ulps of a / b, and
 // RN(q + r y) is then the correctly rounded quotient once q is faithful,
 // which the first correction makes it. For the march's operands (0 <= a,
-// b >= 0, neither subnormal) this is the IEEE quotient; where b = 0 or a
-// value is NaN every path gives NaN or skips, as the division does, and
-// fminf(a, NaN) = a either way. Checked against IEEE division on random and
-// near-midpoint quotients (tests/test_cell_index.py) and by the bit-exact
-// lidar tests.
+// b >= 0, neither subnormal) this is the IEEE quotient whenever that is
+// finite; for b = 0, an overflowing product or a NaN it gives NaN or +inf.
+// Checked against IEEE division on random and near-midpoint quotients
+// (tests/test_cell_index.py) and by the bit-exact lidar tests.
 __device__ __forceinline__ float quotient(float a, float b, float y, float q0) {
   const float q1 = __fmaf_rn(__fmaf_rn(-q0, b, a), y, q0);
   return __fmaf_rn(__fmaf_rn(-q1, b, a), y, q1);
@@ -645,15 +645,21 @@ __device__ __forceinline__ float march(const TrackDev& t, float ox, float oy, fl
     }
     const float a = spot.clearance - cell;
     if (a < min_step) break;  // min(a, fl / descent) <= a < min_step
-    // fl * RN(1/descent) is within (1 + 2^-23) of the exact fl / descent, so
-    // a product above a * (1 + 2^-20) proves the correctly rounded quotient
-    // is >= a and min() returns a: the division is needed only when the
-    // floor term may win. For descent == 0 (fl >= 0 here) the product is +inf,
-    // which skips, or NaN (fl == 0), where the quotient is NaN too and fminf
-    // returns a: the reference's min(a, fl / 0) either way.
-    float step = a;
-    const float q0 = fl * inv_descent;
-    if (!(q0 > a * 1.00000095f)) step = fminf(a, quotient(fl, descent, inv_descent, q0));
+    float step;
+    if (GUARD) {
+      // fl * RN(1/descent) is within (1 + 2^-23) of the exact fl / descent, so
+      // a product above a * (1 + 2^-20) proves the correctly rounded quotient
+      // is >= a and min() returns a: the division is needed only when the
+      // floor term may win.
+      step = a;
+      if (!(fl * inv_descent > a * 1.00000095f)) step = fminf(a, fl / descent);
+    } else {
+      // descent is 0 or normal here: the quotient is RN(fl / descent) whenever
+      // it is finite and below a; otherwise it is >= a or NaN (fl / 0, or a
+      // product that overflowed), and fminf returns a as for the reference's
+      // min(a, inf) or min(a, NaN).
+      step = fminf(a, quotient(fl, descent, inv_descent, fl * inv_descent));
+    }
     if (step < min_step) break;
     last = tt;
     last_floor = fl;

@@ -644,9 +644,9 @@ __device__ __forceinline__ float march(const TrackDev& t, float ox, float oy, fl
       break;
     }
     const float a = spot.clearance - cell;
-    if (a < min_step) break;  // min(a, fl / descent) <= a < min_step
     float step;
     if (GUARD) {
+      if (a < min_step) break;  // min(a, fl / descent) <= a < min_step
       // fl * RN(1/descent) is within (1 + 2^-23) of the exact fl / descent, so
       // a product above a * (1 + 2^-20) proves the correctly rounded quotient
       // is >= a and min() returns a: the division is needed only when the
@@ -657,7 +657,8 @@ __device__ __forceinline__ float march(const TrackDev& t, float ox, float oy, fl
       // descent is 0 or normal here: the quotient is RN(fl / descent) whenever
       // it is finite and below a; otherwise it is >= a or NaN (fl / 0, or a
       // product that overflowed), and fminf returns a as for the reference's
-      // min(a, inf) or min(a, NaN).
+      // min(a, inf) or min(a, NaN). A clearance term below min_step ends the
+      // march through the test below, as the reference's does.
       step = fminf(a, quotient(fl, descent, inv_descent, fl * inv_descent));
     }
     if (step < min_step) break;

@@ -634,6 +634,28 @@ __device__ __forceinline__ float march(const TrackDev& t, float ox, float oy, fl
   const float cell = t.cell, min_step = 0.5f * t.cell;
   float tt = 0.0f, last = 0.0f, last_floor = 0.0f, range = -1.0f;
   int count = 0;
+  if (!GUARD) {
+    // descent is 0 or normal here: the quotient is RN(fl / descent) whenever
+    // it is finite and below the clearance term; otherwise it is >= that term
+    // or NaN (fl / 0, or a product that overflowed), and fminf returns the
+    // clearance term as for the reference's min(a, inf) or min(a, NaN). The
+    // step is computed before the ground test and unused once the ground is
+    // crossed, so one branch ends the march on either condition.
+    float fl = 0.0f;
+    while (tt < RANGE && count < max_iters) {
+      ++count;
+      const float px = ox + tt * dx, py = oy + tt * dy, pz = oz + tt * dz;
+      const Spot spot = probe<LAYERS, false>(t, px, py, pz);
+      fl = (pz - spot.height) - 0.03f;
+      const float step = fminf(spot.clearance - cell, quotient(fl, descent, inv_descent, fl * inv_descent));
+      if (fl < 0.0f || step < min_step) break;
+      last = tt;
+      last_floor = fl;
+      tt += step;
+    }
+    *count_out = count;
+    return fl < 0.0f ? fminf(last + ((tt - last) * last_floor) / (last_floor - fl), RANGE) : fminf(tt, RANGE);
+  }
   while (tt < RANGE && count < max_iters) {
     ++count;
     const float px = ox + tt * dx, py = oy + tt * dy, pz = oz + tt * dz;
@@ -644,23 +666,13 @@ __device__ __forceinline__ float march(const TrackDev& t, float ox, float oy, fl
       break;
     }
     const float a = spot.clearance - cell;
-    float step;
-    if (GUARD) {
-      if (a < min_step) break;  // min(a, fl / descent) <= a < min_step
-      // fl * RN(1/descent) is within (1 + 2^-23) of the exact fl / descent, so
-      // a product above a * (1 + 2^-20) proves the correctly rounded quotient
-      // is >= a and min() returns a: the division is needed only when the
-      // floor term may win.
-      step = a;
-      if (!(fl * inv_descent > a * 1.00000095f)) step = fminf(a, fl / descent);
-    } else {
-      // descent is 0 or normal here: the quotient is RN(fl / descent) whenever
-      // it is finite and below a; otherwise it is >= a or NaN (fl / 0, or a
-      // product that overflowed), and fminf returns a as for the reference's
-      // min(a, inf) or min(a, NaN). A clearance term below min_step ends the
-      // march through the test below, as the reference's does.
-      step = fminf(a, quotient(fl, descent, inv_descent, fl * inv_descent));
-    }
+    if (a < min_step) break;  // min(a, fl / descent) <= a < min_step
+    // fl * RN(1/descent) is within (1 + 2^-23) of the exact fl / descent, so
+    // a product above a * (1 + 2^-20) proves the correctly rounded quotient
+    // is >= a and min() returns a: the division is needed only when the
+    // floor term may win.
+    float step = a;
+    if (!(fl * inv_descent > a * 1.00000095f)) step = fminf(a, fl / descent);
     if (step < min_step) break;
     last = tt;
     last_floor = fl;

@@ -7,8 +7,10 @@
 //
 // This translation unit is compiled with --fmad=false and IEEE division and
 // square root, and every transcendental comes from rmath.h, so each kernel is
-// the same sequence of binary32 operations as the CPU restatement: layer,
-// waypoint and crash outputs, the state and the ranges match it bit for bit.
+// the same sequence of binary32 operations as the CPU restatement (fused
+// multiply-adds appear only as explicit intrinsics where a proof shows the
+// same result): layer, waypoint and crash outputs, the state and the ranges
+// match it bit for bit.
 //
 // Layout in HBM (feature-major, as the reference): state [11, n],
 // actions [2, n], reward [n], done [n], obs [beams + 5, n]. The track array is
@@ -467,10 +469,12 @@ __global__ void k_pose_frames(TrackDev t, const float4* __restrict__ poses, int 
 // A block holds a few warps; each warp marches 32 consecutive beams of one
 // car, so its lanes start at one origin and probe neighbouring cells (L1
 // reuse) and finish after similar numbers of probes. The per-car
-// frame comes from the physics kernel (`ray`). Every floating-point operation
-// of a beam is the reference's, in its order; the nearest-cell index avoids
-// the division where that provably gives the same cell (cell_coord), and
-// floor/descent is skipped where min() cannot select it.
+// frame comes from the physics kernel (`ray`). Every result of a beam is the
+// reference's: its operations are the reference's, in its order, except
+// where another sequence provably gives the same bits: the nearest-cell
+// index (cell_of: one fused multiply-add, the division only near a cell
+// boundary) and floor/descent (quotient: two residual corrections of the
+// reciprocal; the guarded march divides only where min() can select it).
 template <int LAYERS>
 __device__ __forceinline__ void trace(const TrackDev& t, const float4* __restrict__ ray, float* obs, int n,
                                       const float2* __restrict__ beam_dir, int max_iters, int* iters, int car,

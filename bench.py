@@ -64,7 +64,7 @@ def parse():
     ap.add_argument("--track-compile-only", action="store_true", help="print only the track compilation section")
     ap.add_argument("--training-iterations", type=int, default=300)
     ap.add_argument("--surrogate-train-steps", type=int, default=None,
-                    help="surrogate training steps (default 60000; fewer only to profile the rollout)")
+                    help="surrogate training steps (default 80000; fewer only to profile the rollout)")
     return ap.parse_args()
 
 
@@ -182,7 +182,7 @@ def config1_section(torch, W, stream):
             "cpu_sample": cpu["sample"], "gpu_graph_vs_cpu": graph_rate / cpu["value"], "rollout_chains": chains}
 
 
-SURR_CARS, SURR_STEPS, SURR_REPS, SURR_TRAIN_STEPS = 65536, 32, 3, 60000
+SURR_CARS, SURR_STEPS, SURR_REPS, SURR_TRAIN_STEPS = 65536, 32, 3, 80000
 SURR_LR, SURR_HUBER_M = 8e-3, 0.02
 
 

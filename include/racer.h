@@ -265,6 +265,11 @@ int racer_surrogate_set_loss(racer_surrogate* surrogate, float huber_m);
  * kernel (all four layers per tile of 128 cars, activations kept on chip);
  * 0 = four GEMM launches. Both give the same bits. Drops captured rollout graphs. */
 int racer_surrogate_set_fused(racer_surrogate* surrogate, int fused);
+/* Keep the training set's exact labels after their first tracing (enable = 1,
+ * the default; FP32, built by racer_surrogate_set_poses when the set's labels
+ * fit in 32 GB) so later epochs copy instead of tracing again: the same bits.
+ * enable = 0 traces every batch every time (and frees the cache). */
+int racer_surrogate_set_label_cache(racer_surrogate* surrogate, int enable);
 /* Held-out error on `batches` fresh batches drawn with `seed`, surrogate vs exact. */
 int racer_surrogate_evaluate(racer_surrogate* surrogate, int batches, uint64_t seed, float* mae_m, float* rmse_m,
                              float* max_m, float* frac_over_5cm);

@@ -218,3 +218,29 @@ def test_trained_surrogate_rollout_beats_exact_rollout():
           f"fallback {fallback:.3f}")
     assert t_learned < t_exact / 1.5, (t_learned, t_exact)
     assert 0.0 < mae < 0.5 and 0.0 <= fallback < 0.5, (mae, fallback)
+
+
+def test_label_cache_serves_the_traced_labels():
+    """Labels copied back from the training set's label cache (every epoch after the first) are the
+    tracer's own: each batch's labels equal a fresh tracing with the cache switched off, and the
+    held-out evaluation in between neither uses nor replaces the cache."""
+    track = W.track("bridge")
+    sim = W.Sim(track, 8, 0, beams=1081)
+    sur = W.Surrogate(sim, hidden=128, batch=1024, seed=1)
+    sur.set_poses(3 * 1024, seed=2)
+    first, again = [], []
+    for b in range(3):
+        lab = W.DevArray.empty((1081, 1024))
+        sur.gradient(b * 1024, lab)  # traced, then kept
+        first.append(lab.numpy())
+    sur.evaluate(batches=1, seed=77)
+    for b in range(3):
+        lab = W.DevArray.empty((1081, 1024))
+        sur.gradient(b * 1024, lab)  # copied from the cache
+        again.append(lab.numpy())
+    sur.set_label_cache(False)
+    sur.set_poses(3 * 1024, seed=2)
+    for b in range(3):
+        lab = W.DevArray.empty((1081, 1024))
+        sur.gradient(b * 1024, lab)  # traced again, no cache
+        assert np.array_equal(lab.numpy(), first[b]) and np.array_equal(again[b], first[b])

@@ -17,7 +17,10 @@
 //
 // Training poses are uniform over the drivable cells (clearance > 0) of every
 // layer with uniform heading; their labels come from the exact tracer
-// (k_pose_frames + k_lidar) batch by batch, so the labels are never stored.
+// (k_pose_frames + k_lidar) batch by batch. Training walks the pose set in
+// order, epoch after epoch, so each batch's labels are kept after their first
+// tracing (label cache, FP32, up to 32 GB) and copied back in later epochs: the
+// same bits without tracing the same poses again.
 #include <cuda_bf16.h>
 
 #include <cmath>
@@ -402,6 +405,9 @@ struct racer_surrogate {
   int npose = 0;
   float4* ray = nullptr;   // [2, batch]
   float* label = nullptr;  // [4 + beams, batch] (rows 4.. are the exact ranges / RANGE)
+  float* lcache = nullptr;   // [npose / batch][beams][batch] labels of the pose set, when cached
+  std::vector<uint8_t> lcached;  // per batch of the pose set: its labels are in lcache
+  bool use_cache = true;
   float* pred = nullptr;   // [beams, batch]
   float* scratch = nullptr;
   size_t scratch_floats = 0;
@@ -518,12 +524,25 @@ int wgrad(racer_surrogate* s, const CUtensorMap& ta, const CUtensorMap& tb, int 
 }
 
 // Labels and features for batch rows taken from the pose set starting at `first`.
-int prepare(racer_surrogate* s, SurrogateActs* a, long first) {
+// Frames, exact labels and encoded inputs of the batch at pose `first`; with
+// `cached`, the labels come from (or go to) the label cache of the pose set.
+int prepare(racer_surrogate* s, SurrogateActs* a, long first, bool cached = false) {
   racer_sim* sim = s->sim;
   const int B = a->M;
   const float4* poses = s->poses + first;
   launch_pose_frames(sim->t, poses, B, s->ray, s->st);
-  launch_lidar(sim->t, s->ray, s->label, B, sim->beams, sim->beam_dir, nullptr, s->st);
+  const long b = first / B;
+  const size_t block = (size_t)sim->beams * B;
+  float* slot = cached && s->lcache && first % B == 0 ? s->lcache + b * block : nullptr;
+  if (slot && s->lcached[b]) {
+    SURR_CHECK(cudaMemcpyAsync(s->label + 4L * B, slot, block * sizeof(float), cudaMemcpyDeviceToDevice, s->st));
+  } else {
+    launch_lidar(sim->t, s->ray, s->label, B, sim->beams, sim->beam_dir, nullptr, s->st);
+    if (slot) {
+      SURR_CHECK(cudaMemcpyAsync(slot, s->label + 4L * B, block * sizeof(float), cudaMemcpyDeviceToDevice, s->st));
+      s->lcached[b] = 1;
+    }
+  }
   k_features<<<(B + 127) / 128, 128, 0, s->st>>>(s->ray, B, s->nm, a->x, a->xf);
   SURR_CHECK(cudaGetLastError());
   return 0;
@@ -533,7 +552,7 @@ int prepare(racer_surrogate* s, SurrogateActs* a, long first) {
 int gradient(racer_surrogate* s, long first) {
   SurrogateActs* a = &s->train;
   const int H = s->L.H, B = a->M, NP = s->L.npad, beams = s->L.beams;
-  int rc = prepare(s, a, first);
+  int rc = prepare(s, a, first, true);
   if (rc) return rc;
   SURR_CHECK(cudaMemsetAsync(s->grad + s->L.b2, 0, H * sizeof(float), s->st));
   SURR_CHECK(cudaMemsetAsync(s->grad + s->L.b3, 0, H * sizeof(float), s->st));
@@ -654,7 +673,8 @@ int racer_surrogate_destroy(racer_surrogate* s) {
   if (!s) return 0;
   for (void* p : {(void*)s->theta, (void*)s->grad, (void*)s->m1, (void*)s->m2, (void*)s->w1b, (void*)s->w2b,
                   (void*)s->w3b, (void*)s->w4b, (void*)s->w2t, (void*)s->w3t, (void*)s->w4t, (void*)s->cells,
-                  (void*)s->poses, (void*)s->ray, (void*)s->label, (void*)s->pred, (void*)s->scratch, (void*)s->sums,
+                  (void*)s->poses, (void*)s->ray, (void*)s->label, (void*)s->lcache, (void*)s->pred, (void*)s->scratch,
+                  (void*)s->sums,
                   (void*)s->maxbits, (void*)s->over, (void*)s->err})
     cudaFree(p);
   free_acts(&s->train);
@@ -686,8 +706,20 @@ int racer_surrogate_set_poses(racer_surrogate* s, long count, uint64_t seed) {
   }
   cudaFree(s->poses);
   s->poses = nullptr;
+  cudaFree(s->lcache);
+  s->lcache = nullptr;
+  s->lcached.assign(0, 0);
   if (int rc = salloc(&s->poses, (size_t)count)) return rc;
   s->npose = (int)count;
+  const size_t cache_bytes = (size_t)count * s->L.beams * sizeof(float);
+  if (s->use_cache && cache_bytes <= (32ull << 30)) {  // else trace every batch every epoch
+    if (cudaMalloc((void**)&s->lcache, cache_bytes) == cudaSuccess) {
+      s->lcached.assign(count / s->batch, 0);
+    } else {
+      cudaGetLastError();
+      s->lcache = nullptr;
+    }
+  }
   k_sample_poses<<<(unsigned)((count + 255) / 256), 256, 0, s->st>>>(s->cells, s->ncells, (int)count, seed, s->sim->t,
                                                                        s->poses);
   RACER_TRY(cudaGetLastError());
@@ -702,6 +734,19 @@ int racer_surrogate_set_fused(racer_surrogate* s, int fused) {
   s->fused = fused != 0;
   for (auto& kv : s->sim->surrogate_graphs) cudaGraphExecDestroy(kv.second);
   s->sim->surrogate_graphs.clear();
+  return 0;
+}
+
+int racer_surrogate_set_label_cache(racer_surrogate* s, int enable) {
+  if (!s) {
+    racer_host::set_error("racer_surrogate_set_label_cache: null surrogate");
+    return 1;
+  }
+  s->use_cache = enable != 0;
+  RACER_TRY(cudaStreamSynchronize(s->st));
+  cudaFree(s->lcache);  // a later racer_surrogate_set_poses builds it again when enabled
+  s->lcache = nullptr;
+  s->lcached.assign(0, 0);
   return 0;
 }
 
@@ -778,11 +823,20 @@ int racer_surrogate_evaluate(racer_surrogate* s, int batches, uint64_t seed, flo
   }
   float4* keep = s->poses;
   int keep_n = s->npose;
+  float* keep_cache = s->lcache;  // the held-out poses neither use nor replace the training set's labels
+  std::vector<uint8_t> keep_cached;
+  keep_cached.swap(s->lcached);
+  const bool keep_use = s->use_cache;
   s->poses = nullptr;
+  s->lcache = nullptr;
+  s->use_cache = false;
   int rc = racer_surrogate_set_poses(s, (long)batches * s->batch, seed);
+  s->use_cache = keep_use;
   if (rc) {
     s->poses = keep;
     s->npose = keep_n;
+    s->lcache = keep_cache;
+    s->lcached.swap(keep_cached);
     return rc;
   }
   RACER_TRY(cudaMemsetAsync(s->sums + 2, 0, 2 * sizeof(double), s->st));
@@ -800,6 +854,8 @@ int racer_surrogate_evaluate(racer_surrogate* s, int batches, uint64_t seed, flo
   cudaFree(s->poses);
   s->poses = keep;
   s->npose = keep_n;
+  s->lcache = keep_cache;
+  s->lcached.swap(keep_cached);
   if (rc) return rc;
   double sums[2];
   unsigned mx = 0;

@@ -366,6 +366,11 @@ class Surrogate:
         """Rollout inference in one fused kernel (512-wide) or as four GEMMs; the same bits either way."""
         call("racer_surrogate_set_fused", self.handle, int(bool(fused)))
 
+    def set_label_cache(self, enable=True):
+        """Keep the training set's exact labels after their first tracing (the same bits, faster epochs);
+        takes effect from the next set_poses."""
+        call("racer_surrogate_set_label_cache", self.handle, int(bool(enable)))
+
     def set_loss(self, huber_m=0.0):
         """0: squared range error; > 0: Huber loss with that threshold in metres."""
         call("racer_surrogate_set_loss", self.handle, float(huber_m))

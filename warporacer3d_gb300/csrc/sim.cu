@@ -92,6 +92,25 @@ __device__ __forceinline__ bool cell_of(const TrackDev& t, float x, float y, lon
   return true;
 }
 
+// cell_of without the off-map branch: *idx is the cell, or cell 0 off the map,
+// and the result says whether the point is on the map, decided as cell_of
+// decides it.
+__device__ __forceinline__ bool cell_of_any(const TrackDev& t, float x, float y, long* idx) {
+  const float vx = __fmaf_rn(x, t.inv_cell, t.cx), vy = __fmaf_rn(y, t.inv_cell, t.cy);
+  const float rx = rintf(vx), ry = rintf(vy);
+  int ix, iy;
+  if (fabsf(vx - rx) < t.band && fabsf(vy - ry) < t.band) {
+    ix = (int)rx, iy = (int)ry;  // saturating conversion: far off the map stays off it
+  } else {
+    const float fx = cell_coord(x, t.x0, t.cell, t.inv_cell), fy = cell_coord(y, t.y0, t.cell, t.inv_cell);
+    const bool on = fx >= 0.0f && fx < t.nxf && fy >= 0.0f && fy < t.nyf;
+    ix = on ? (int)fx : -1, iy = on ? (int)fy : -1;
+  }
+  const bool on = (unsigned)ix < (unsigned)t.nx && (unsigned)iy < (unsigned)t.ny;
+  *idx = on ? (long)(iy * t.nx + ix) : 0L;
+  return on;
+}
+
 // racer/sim.mojo:116-124. LAYERS = 0 reads the layer count from the track.
 // The first drivable layer is taken only if |height - z| < 1e30 (the initial
 // gap). GUARD = false drops that test where it cannot fail: grid heights are
@@ -129,6 +148,31 @@ __device__ __forceinline__ Spot probe(const TrackDev& t, float x, float y, float
     }
   }
   return best;
+}
+
+// probe<LAYERS, false> for one or two layers with the off-map case selected
+// after an unconditional load (of cell 0 off the map) instead of branched
+// around it: the same Spot, no divergent branch per probe.
+template <int LAYERS>
+__device__ __forceinline__ Spot probe_any(const TrackDev& t, float x, float y, float z) {
+  long idx;
+  const bool on = cell_of_any(t, x, y, &idx);
+  Spot best;
+  if (LAYERS == 2) {
+    const float4 v = __ldg(reinterpret_cast<const float4*>(t.cl) + idx);
+    best = Spot{0, -1.0f, v.y};
+    float gap = 1e30f;
+    if (v.x > 0.0f) {
+      best = Spot{0, v.x, v.y};
+      gap = fabsf(v.y - z);
+    }
+    if (v.z > 0.0f && fabsf(v.w - z) < gap) best = Spot{1, v.z, v.w};
+  } else {
+    const float2 v = __ldg(t.cl + idx);
+    best = Spot{0, -1.0f, v.y};
+    if (v.x > 0.0f) best = Spot{0, v.x, v.y};
+  }
+  return on ? best : Spot{0, -1.0f, -1.0f};  // off the map every grid reads -1
 }
 
 // racer/sim.mojo:126-140: bilinear height and its gradient, in two parts: the
@@ -649,7 +693,7 @@ __device__ __forceinline__ float march(const TrackDev& t, float ox, float oy, fl
     while (tt < RANGE && count < max_iters) {
       ++count;
       const float px = ox + tt * dx, py = oy + tt * dy, pz = oz + tt * dz;
-      const Spot spot = probe<LAYERS, false>(t, px, py, pz);
+      const Spot spot = LAYERS == 1 || LAYERS == 2 ? probe_any<LAYERS>(t, px, py, pz) : probe<LAYERS, false>(t, px, py, pz);
       fl = (pz - spot.height) - 0.03f;
       const float step = fminf(spot.clearance - cell, quotient(fl, descent, inv_descent, fl * inv_descent));
       if (fl < 0.0f || step < min_step) break;

@@ -749,8 +749,9 @@ int racer_trainer_rollout(racer_trainer* tr, racer_sim* s, racer_policy* p, race
 }
 
 // One minibatch on the inputs x[m] gathered beforehand (launch_gather_all).
+// dgrads_f32: also the FP32 data gradients tr->d2, tr->d1 (an update only needs the weight gradients).
 static int minibatch_on(racer_trainer* tr, racer_policy* p, int m, int use_moments, float adv_mean,
-                        float adv_scale) {
+                        float adv_scale, bool dgrads_f32 = true) {
   cudaStream_t st = tr->st;
   const int B = tr->batch, IN = tr->in_rows, P = policy_params(p);
   const float* logstd = policy_theta(p) + P - 2;
@@ -760,7 +761,7 @@ static int minibatch_on(racer_trainer* tr, racer_policy* p, int m, int use_momen
   launch_loss(tr->n, B, m, tr->actions, tr->logp, tr->value, tr->advantage, tr->acts->o, logstd,
               tr->stats + ST_ADV, use_moments, adv_mean, adv_scale, tr->d3, st);
   if ((rc = policy_backward(p, x, B, tr->acts->h1, tr->acts->h2, tr->d3, tr->d2, tr->d1, tr->grad, st,
-                            &tr->xmaps[m])))
+                            &tr->xmaps[m], dgrads_f32)))
     return rc;
   launch_rowsum(tr->d3 + (size_t)OUT * B, 2, B, B, tr->grad + P - 2, tr->red, 0, st);
   launch_rowsum(tr->grad, 1, P, P, tr->stats + ST_NORM, tr->red + 2048, 1, st);
@@ -790,7 +791,7 @@ static int update_body(racer_trainer* tr, racer_policy* p) {
   RACER_LAUNCHED();
   for (int epoch = 0; epoch < EPOCHS; ++epoch) {
     for (int m = 0; m < MINIBATCHES; ++m) {
-      int rc = minibatch_on(tr, p, (m + epoch) % MINIBATCHES, 1, 0.0f, 1.0f);
+      int rc = minibatch_on(tr, p, (m + epoch) % MINIBATCHES, 1, 0.0f, 1.0f, false);
       if (rc) return rc;
       launch_adam(P, P - 2, tr->c12_dev + 2 * (epoch * MINIBATCHES + m), tr->stats, policy_theta(p), tr->grad,
                   tr->first, tr->second, st);

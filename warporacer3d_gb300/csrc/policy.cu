@@ -119,7 +119,7 @@ int policy_status(racer_policy* p, int* code) {
 }
 
 int policy_backward(racer_policy* p, const float* x, int cols, const float* h1, const float* h2, const float* d3,
-                    float* d2, float* d1, float* grad, cudaStream_t st, const CUtensorMap* xb_map) {
+                    float* d2, float* d1, float* grad, cudaStream_t st, const CUtensorMap* xb_map, bool dgrads_f32) {
   if (p->bf16) {
     if (backward_work_cols(p->work) != cols) {
       ++p->generation;
@@ -128,7 +128,7 @@ int policy_backward(racer_policy* p, const float* x, int cols, const float* h1, 
       if (int rc = backward_work_new(p->in, cols, &p->work)) return rc;
       if (int rc = backward_refresh(p->work, p->theta, st)) return rc;
     }
-    return backward_tc(p->work, p->theta, x, h1, h2, d3, d2, d1, grad, p->err, st, xb_map);
+    return backward_tc(p->work, p->theta, x, h1, h2, d3, d2, d1, grad, p->err, st, xb_map, dgrads_f32);
   }
   launch_backward(p->in, p->theta, x, cols, h1, h2, d3, d2, d1, grad, p->scratch, st);
   cudaError_t err = cudaGetLastError();

@@ -25,9 +25,11 @@ int policy_forward(racer_policy* p, const float* x, int cols, float* h1, float* 
 int policy_is_bf16(racer_policy* p);
 // Device-side error word of the tensor-core kernels (0 = none); synchronises.
 int policy_status(racer_policy* p, int* code);
-// xb_map (BF16 path only): x already in BF16 behind a tensor map, see backward_tc.
+// xb_map (BF16 path only): x already in BF16 behind a tensor map; dgrads_f32 = false (BF16 path
+// only): d2 and d1 are not needed in FP32, see backward_tc.
 int policy_backward(racer_policy* p, const float* x, int cols, const float* h1, const float* h2, const float* d3,
-                    float* d2, float* d1, float* grad, cudaStream_t st, const CUtensorMap* xb_map = nullptr);
+                    float* d2, float* d1, float* grad, cudaStream_t st, const CUtensorMap* xb_map = nullptr,
+                    bool dgrads_f32 = true);
 // 1: BF16 tensor-core products (default); 0: FP32 CUDA-core products.
 int policy_set_precision(racer_policy* p, int bf16);
 // A counter that changes whenever the precision or the backward workspace

@@ -67,7 +67,8 @@ __global__ void __launch_bounds__(128, 4)
     k_dgrad_tc(int in, const float* __restrict__ theta, const uint4* __restrict__ w1ts, const float* __restrict__ d3,
                const float* __restrict__ h1, const float* __restrict__ h2, float* __restrict__ d2,
                float* __restrict__ d1, int cols, bf16* __restrict__ d1f, bf16* __restrict__ d2f,
-               bf16* __restrict__ d3f, bf16* __restrict__ h1b, bf16* __restrict__ h2b, int ld, int* err) {
+               bf16* __restrict__ d3f, bf16* __restrict__ h1b, bf16* __restrict__ h2b, int ld, int* err,
+               int write_f32) {
   __shared__ __align__(1024) uint8_t A[128 * 128];
   __shared__ __align__(1024) uint8_t B[H * 128];
   __shared__ uint64_t done;
@@ -102,7 +103,7 @@ __global__ void __launch_bounds__(128, 4)
     const float a = hv[k];
     const float v = acc * (1.0f - a * a);
     if (live) {
-      d2[(long)k * cols + j] = v;
+      if (write_f32) d2[(long)k * cols + j] = v;
       h2b[(long)k * ld + j] = __float2bfloat16_rn(a);  // the weight-gradient operand of layer 2
     }
     if (k < H) {
@@ -144,12 +145,12 @@ __global__ void __launch_bounds__(128, 4)
 #pragma unroll
       for (int k = 0; k < 32; ++k) {
         const float g = acc[k0 + k] * (1.0f - hh[k] * hh[k]);
-        d1[(long)(k0 + k) * cols + j] = g;
+        if (write_f32) d1[(long)(k0 + k) * cols + j] = g;
         d1f[(long)(k0 + k) * ld + j] = __float2bfloat16_rn(g);
         h1b[(long)(k0 + k) * ld + j] = __float2bfloat16_rn(hh[k]);  // the weight-gradient operand of layer 1
       }
     }
-    d1[(long)H * cols + j] = 0.0f;
+    if (write_f32) d1[(long)H * cols + j] = 0.0f;
     h1b[(long)H * ld + j] = __float2bfloat16_rn(h1[(long)H * cols + j]);
   }
   tc::tc_fence_before();
@@ -267,13 +268,14 @@ int backward_refresh(BackwardWork* w, const float* theta, cudaStream_t st) {
 
 int backward_tc(BackwardWork* w, const float* theta, const float* x, const float* h1, const float* h2,
                 const float* d3, float* d2, float* d1, float* grad, int* err, cudaStream_t st,
-                const CUtensorMap* xb_map) {
+                const CUtensorMap* xb_map, bool dgrads_f32) {
   const int in = w->in, cols = w->cols, ld = w->ld;
   const unsigned gx = (unsigned)((cols + 1023) / 1024);
   if (!xb_map) k_rows_bf16<<<dim3(gx, in), 256, 0, st>>>(x, in, cols, w->xb, ld);
   // the BF16 copies of h1 and h2 are written by k_dgrad_tc, which reads them anyway
   k_dgrad_tc<<<(cols + 127) / 128, 128, 0, st>>>(in, theta, reinterpret_cast<const uint4*>(w->w1ts), d3, h1, h2, d2,
-                                                 d1, cols, w->d1f, w->d2f, w->d3f, w->h1b, w->h2b, ld, err);
+                                                 d1, cols, w->d1f, w->d2f, w->d3f, w->h1b, w->h2b, ld, err,
+                                                 dgrads_f32 ? 1 : 0);
   BW_CHECK(cudaGetLastError());
   int rc;
   if ((rc = wgrad<64>(w, xb_map ? *xb_map : w->txb, w->td1f, in, H, in, grad, in, err, st))) return rc;

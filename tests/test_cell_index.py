@@ -12,6 +12,10 @@
    huge or non-finite origin height or a subnormal descent) evaluates
    fl / descent only when fl * RN(1 / descent) <= a * (1 + 2^-20); the claim:
    whenever it skips, RN(fl / descent) >= a, so min(a, fl / descent) = a.
+4. The rounding in the unguarded march's probe (sim.cu, cell_of_any): rint(v)
+   as (v + 1.5 * 2^23) - 1.5 * 2^23 and the cell as the sum's bits less those
+   of 1.5 * 2^23 (unsigned); the claims: exact for |v| < 2^22, and an index of
+   at least 2^22 (off any map) for every larger, infinite or NaN v.
 3. The quotient of the unguarded march (sim.cu, quotient): from y = RN(1 / b) and
    q0 = RN(a * y), two residual corrections q <- RN(q + RN(a - b q) y), each a
    pair of fused multiply-adds, give RN(a / b); the claim is checked on the
@@ -160,3 +164,20 @@ def test_quotient_by_residual_corrections_is_ieee_division():
         bad += int(np.sum(q[ok] != ref[ok]))
         total += int(ok.sum())
     assert total > 2_900_000 and bad == 0
+
+
+def test_magic_rounding_and_off_map_index():
+    rng = np.random.default_rng(11)
+    v = np.concatenate([rng.uniform(-3e6, 3e6, 1_000_000), rng.uniform(-5e7, 5e7, 500_000),
+                        rng.standard_normal(500_000) * 1e3, rng.uniform(-1, 1, 200_000) + 0.5,
+                        np.array([4194303.5, 4194304, -4194304, -4194303.5, 8388608, -8388608, 12582912, -12582912,
+                                  1e30, -1e30, 3.4e38, -3.4e38, np.inf, -np.inf, np.nan])]).astype(f32)
+    magic = f32(12582912.0)
+    with np.errstate(all="ignore"):
+        m = (v + magic).astype(f32)
+        r = (m - magic).astype(f32)
+        ix = (m.view(np.uint32).astype(np.int64) - 0x4B400000) & 0xFFFFFFFF
+    small = np.abs(v) < f32(4194304)
+    assert np.array_equal(r[small], np.rint(v[small]))
+    assert np.array_equal(ix[small], np.rint(v[small]).astype(np.int64) & 0xFFFFFFFF)
+    assert np.all(ix[~small] >= 4194304)

@@ -95,19 +95,26 @@ __device__ __forceinline__ bool cell_of(const TrackDev& t, float x, float y, lon
 // cell_of without the off-map branch: *idx is the cell, or cell 0 off the map,
 // and the result says whether the point is on the map, decided as cell_of
 // decides it.
+// The nearest integer comes from adding and subtracting 1.5 * 2^23 (exactly
+// rint(v) for |v| < 2^22) and the cell from the sum's bits less those of
+// 1.5 * 2^23, in unsigned arithmetic: for |v| >= 2^22, infinities and NaN that
+// is >= 2^22 > nx, so such points are off the map on either path, as they are
+// for the reference. No conversion instruction on the common path.
 __device__ __forceinline__ bool cell_of_any(const TrackDev& t, float x, float y, long* idx) {
+  constexpr float MAGIC = 12582912.0f;  // 1.5 * 2^23
   const float vx = __fmaf_rn(x, t.inv_cell, t.cx), vy = __fmaf_rn(y, t.inv_cell, t.cy);
-  const float rx = rintf(vx), ry = rintf(vy);
-  int ix, iy;
+  const float mx = vx + MAGIC, my = vy + MAGIC;
+  const float rx = mx - MAGIC, ry = my - MAGIC;
+  unsigned ix, iy;
   if (fabsf(vx - rx) < t.band && fabsf(vy - ry) < t.band) {
-    ix = (int)rx, iy = (int)ry;  // saturating conversion: far off the map stays off it
+    ix = (unsigned)__float_as_int(mx) - 0x4B400000u, iy = (unsigned)__float_as_int(my) - 0x4B400000u;
   } else {
     const float fx = cell_coord(x, t.x0, t.cell, t.inv_cell), fy = cell_coord(y, t.y0, t.cell, t.inv_cell);
     const bool on = fx >= 0.0f && fx < t.nxf && fy >= 0.0f && fy < t.nyf;
-    ix = on ? (int)fx : -1, iy = on ? (int)fy : -1;
+    ix = on ? (unsigned)(int)fx : 0xFFFFFFFFu, iy = on ? (unsigned)(int)fy : 0xFFFFFFFFu;
   }
-  const bool on = (unsigned)ix < (unsigned)t.nx && (unsigned)iy < (unsigned)t.ny;
-  *idx = on ? (long)(iy * t.nx + ix) : 0L;
+  const bool on = ix < (unsigned)t.nx && iy < (unsigned)t.ny;
+  *idx = on ? (long)(iy * (unsigned)t.nx + ix) : 0L;
   return on;
 }
 

@@ -12,17 +12,17 @@
    huge or non-finite origin height or a subnormal descent) evaluates
    fl / descent only when fl * RN(1 / descent) <= a * (1 + 2^-20); the claim:
    whenever it skips, RN(fl / descent) >= a, so min(a, fl / descent) = a.
-4. The rounding in the unguarded march's probe (sim.cu, cell_of_any): rint(v)
-   as (v + 1.5 * 2^23) - 1.5 * 2^23 and the cell as the sum's bits less those
-   of 1.5 * 2^23 (unsigned); the claims: exact for |v| < 2^22, and an index of
-   at least 2^22 (off any map) for every larger, infinite or NaN v.
 3. The quotient of the unguarded march (sim.cu, quotient): from y = RN(1 / b) and
    q0 = RN(a * y), two residual corrections q <- RN(q + RN(a - b q) y), each a
    pair of fused multiply-adds, give RN(a / b); the claim is checked on the
    march's operand ranges, on wide exponents and on quotients a hair from a
    rounding midpoint.
+4. The rounding in the unguarded march's probe (sim.cu, cell_of_any): rint(v)
+   as (v + 1.5 * 2^23) - 1.5 * 2^23 and the cell as the sum's bits less those
+   of 1.5 * 2^23 (unsigned); the claims: exact for |v| < 2^22, and an index of
+   at least 2^22 (off any map) for every larger, infinite or NaN v.
 
-Both are replayed here in numpy binary32 (IEEE round-to-nearest, like the
+All are replayed here in numpy binary32 (IEEE round-to-nearest, like the
 GPU built with --fmad=false; the fused multiply-add exactly, through a
 binary64 product and an exact two-sum) on random values and on adversarial
 ones a few ulps either side of every cell boundary and of the band's edge.

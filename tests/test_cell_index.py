@@ -21,6 +21,19 @@
    as (v + 1.5 * 2^23) - 1.5 * 2^23 and the cell as the sum's bits less those
    of 1.5 * 2^23 (unsigned); the claims: exact for |v| < 2^22, and an index of
    at least 2^22 (off any map) for every larger, infinite or NaN v.
+5. The count-free march (sim.cu, march<.., false, false>): where the host
+   sets TrackDev.free_march, the loop tests tt < RANGE alone; the claim: the
+   probe bound max_iters = ceil(RANGE / (0.5 cell)) + 2 can never end the
+   march first there, and the host's test keeps the bound for tiny cells.
+6. The lidar's cells (api.cu, upload_track; sim.cu, lidar_probe): the layer
+   choice folded into a per-cell (c0, h0, c1, h1) gives probe()'s clearance
+   and height for every drivability pattern, NaN clearances, ties and
+   off-map border cells.
+7. The march's cell index along the ray (sim.cu, lidar_cell): v = RN(tt *
+   RN(dx r) + RN(ox r + cx)) in one fused multiply-add instead of the probe
+   point px = RN(ox + RN(tt dx)); the claim: wherever |v - rint(v)| lies
+   inside the wider band 0.5 - (7.001 M + 2.001 X + 3.001 RANGE / cell + 16)
+   * 2^-24, on-map status and cell are the reference's for px.
 
 All are replayed here in numpy binary32 (IEEE round-to-nearest, like the
 GPU built with --fmad=false; the fused multiply-add exactly, through a
@@ -181,3 +194,108 @@ def test_magic_rounding_and_off_map_index():
     assert np.array_equal(r[small], np.rint(v[small]))
     assert np.array_equal(ix[small], np.rint(v[small]).astype(np.int64) & 0xFFFFFFFF)
     assert np.all(ix[~small] >= 4194304)
+
+
+def test_march_reaches_range_before_the_probe_bound():
+    """Every probe the march continues from adds a step >= m = 0.5 cell and RN(tt + step) >=
+    (tt + m)(1 - 2^-24), so after k probes tt >= m k (1 - 2^-24)^k; where that reaches RANGE at
+    k = max_iters (the host's test), `tt < RANGE` ends the loop no later than the bound would."""
+    RANGE = f32(10)
+
+    def free_march(cell):
+        m = f32(0.5) * f32(cell)
+        k = int(np.ceil(RANGE / m)) + 2
+        return m, k, float(m) * k * (1.0 - 2.0 ** -24) ** k >= 10.0 * (1.0 + 1e-9)
+
+    for cell in (0.025, 0.05, 0.0123, 0.1, 0.5, 0.004):
+        m, k, free = free_march(cell)
+        assert free
+        tt, probes = f32(0), 0
+        while tt < RANGE:  # the slowest march: every step exactly m
+            tt = f32(tt + m)
+            probes += 1
+        assert probes < k
+    assert not free_march(1e-4)[2]  # tiny cells keep the counted loop
+
+
+def test_lidar_cells_choose_the_probes_layer():
+    rng = np.random.default_rng(5)
+    n = 400_000
+    vals = np.array([-1.0, 0.0, -0.0, -0.5, np.nan, 1e-30, 0.3, 2.0], f32)
+    c0 = np.where(rng.random(n) < 0.5, rng.choice(vals, n), rng.uniform(0.01, 3, n)).astype(f32)
+    c1 = np.where(rng.random(n) < 0.5, rng.choice(vals, n), rng.uniform(0.01, 3, n)).astype(f32)
+    h0 = rng.uniform(-2, 2, n).astype(f32)
+    h1 = np.where(rng.random(n) < 0.2, h0, rng.uniform(-2, 4, n)).astype(f32)
+    z = np.where(rng.random(n) < 0.1, (h0 + h1) / f32(2), rng.uniform(-3, 5, n)).astype(f32)
+    z[:1000] = rng.uniform(-1e20, 1e20, 1000).astype(f32)
+    # probe<2, false> (sim.cu): layer 0 if drivable, layer 1 if drivable and strictly nearer
+    with np.errstate(invalid="ignore"):
+        d0, d1 = c0 > 0, c1 > 0
+        gap = np.where(d0, np.abs(h0 - z), f32(1e30))
+        take1 = d1 & (np.abs(h1 - z) < gap)
+    ref_c = np.where(take1, c1, np.where(d0, c0, f32(-1)))
+    ref_h = np.where(take1, h1, h0)
+    # the packed cell (upload_track) and lidar_probe's choice
+    both = d0 & d1
+    a = np.where(both | d0, c0, np.where(d1, c1, f32(-1)))
+    b = np.where(both | d0, h0, np.where(d1, h1, h0))
+    c = np.where(both, c1, f32(-1))
+    d = np.where(both, h1, f32(np.nan))
+    with np.errstate(invalid="ignore"):
+        up = np.abs(d - z) < np.abs(b - z)
+    assert np.array_equal(np.where(up, c, a), ref_c, equal_nan=True)
+    assert np.array_equal(np.where(up, d, b), ref_h)
+    # a border cell (-1, -1, -1, NaN) reads as off the map: clearance -1, height -1
+    with np.errstate(invalid="ignore"):
+        assert not (abs(f32(np.nan) - z) < abs(f32(-1) - z)).any()
+
+
+def mband(x0, y0, cell, nmax):
+    X = np.ceil(max(abs(float(x0)), abs(float(y0))) / float(cell))
+    d = (7.001 * nmax + 2.001 * X + 3.001 * 10.0 / float(cell) + 16.0) * 2.0 ** -24
+    return f32(0.5 - d * (1 + 2.0 ** -20))
+
+
+@pytest.mark.parametrize("x0,cell,n,nmax", [(-8.9999361, 0.025, 721, 721), (-5.4998164, 0.025, 441, 721),
+                                            (-51.2, 0.05, 2048, 2048), (3.3, 0.0123, 900, 1400),
+                                            (-7.9985256, 0.025, 641, 641)])
+def test_march_cell_index_along_the_ray_is_exact(x0, cell, n, nmax):
+    x0, cell = f32(x0), f32(cell)
+    rng = np.random.default_rng(n)
+    r = f32(1) / cell
+    c = f32(-x0 * r)
+    band = mband(x0, x0, cell, nmax)
+    span = float(n) * float(cell)
+    m = 300_000
+    ox = rng.uniform(float(x0) - 2, float(x0) + span + 2, m).astype(f32)
+    dx = np.cos(rng.uniform(0, np.pi, m)).astype(f32)
+    dx[:1000] = f32(1)
+    dx[1000:2000] = f32(-1)
+    # tt that puts px on a cell boundary of the reference (px = x0 + (k - 0.5) cell), then its neighbours
+    k = rng.integers(-3, n + 3, m)
+    with np.errstate(all="ignore"):
+        t0 = ((x0.astype(f64) + (k - 0.5) * f64(cell)) - ox.astype(f64)) / dx.astype(f64)
+    t0 = np.where(np.isfinite(t0) & (t0 >= 0) & (t0 < 10), t0, rng.uniform(0, 10, m)).astype(f32)
+    tts, oxs, dxs = [t0], [ox], [dx]
+    up, down = t0.copy(), t0.copy()
+    for _ in range(24):
+        up, down = np.nextafter(up, f32(np.inf)), np.nextafter(down, f32(-np.inf))
+        tts += [up, down]
+        oxs += [ox, ox]
+        dxs += [dx, dx]
+    tts.append(rng.uniform(0, 10, m).astype(f32))
+    oxs.append(ox)
+    dxs.append(dx)
+    tt, ox, dx = (np.concatenate(a).astype(f32) for a in (tts, oxs, dxs))
+    keep = (tt >= 0) & (tt < f32(10))
+    tt, ox, dx = tt[keep], ox[keep], dx[keep]
+    with np.errstate(all="ignore"):
+        px = (ox + (tt * dx).astype(f32)).astype(f32)
+        on_ex, idx_ex = exact_cell(px, x0, cell, n)
+        v = fma32(tt, (dx * r).astype(f32), fma32(ox, np.full_like(ox, r), np.full_like(ox, c)))
+        rv = np.rint(v)
+        ok = np.abs(v - rv) < band
+    on = (rv >= 0) & (rv < n)
+    assert np.array_equal(on[ok], on_ex[ok])
+    assert np.array_equal(rv[ok & on], idx_ex[ok & on])
+    assert (~ok).sum() > 0 and ok[-m:].mean() > 0.99

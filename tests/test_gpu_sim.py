@@ -398,6 +398,50 @@ def test_edge_sizes_bit_exact(n, beams, name):
         check_sim(gpu, cpu, f"step {step} ")
 
 
+@pytest.mark.parametrize("name", ["bank", "bridge"])
+def test_lidar_on_random_drivable_cells_bit_exact(name):
+    """The lidar's per-cell layer choice for one and two layers, on clearance grids with 30% of
+    cells undrivable (-1, 0, -0.5 or NaN) and the rest drawn up to 3 m, so that every combination
+    of drivable layers occurs and long steps carry rays off the map; cars start anywhere on the
+    map and up to 2 m beyond its edges."""
+    base = W.track(name)
+    nx, ny, L = int(base[0]), int(base[1]), int(base[7])
+    x0, y0, cell = float(base[2]), float(base[3]), float(base[4])
+    rng = np.random.default_rng(17 + L)
+    track = base.copy()
+    cells = nx * ny
+    for l in range(L):
+        c = track[12 + 3 * l * cells:12 + (3 * l + 1) * cells]
+        c[:] = rng.uniform(0.02, 3.0, cells).astype(np.float32)
+        bad = rng.random(cells) < 0.3
+        c[bad] = rng.choice(np.array([-1.0, 0.0, -0.5, np.nan], np.float32), int(bad.sum()))
+    n, beams = 512, 1081
+    gpu, cpu = W.Sim(track, n, 3, beams=beams), O.Sim(track, n, 3, beams=beams)
+    gpu.reset()
+    cpu.reset()
+    check_sim(gpu, cpu, "reset ")
+    s = gpu.state.numpy()
+    s[O.X] = rng.uniform(x0 - 2, x0 + nx * cell + 2, n).astype(np.float32)
+    s[O.Y] = rng.uniform(y0 - 2, y0 + ny * cell + 2, n).astype(np.float32)
+    ix = np.clip(np.round((s[O.X] - x0) / cell), 0, nx - 1).astype(np.int64)
+    iy = np.clip(np.round((s[O.Y] - y0) / cell), 0, ny - 1).astype(np.int64)
+    layer = rng.integers(0, L, n)
+    s[O.Z] = track[12 + (3 * layer + 1) * cells + iy * nx + ix] + rng.uniform(-0.2, 1.0, n).astype(np.float32)
+    s[O.HEADING] = rng.uniform(-math.pi, math.pi, n).astype(np.float32)
+    s[O.SPEED] = rng.uniform(0, 2, n).astype(np.float32)
+    gpu.state.write(s)
+    cpu.state[:] = s
+    for step in range(3):
+        act = rng.uniform(-1, 1, (2, n)).astype(np.float32)
+        gpu.actions.write(act)
+        cpu.actions[:] = act
+        gpu.step(gpu.actions, gpu.reward, gpu.done, gpu.obs)
+        cpu.step(cpu.actions, cpu.reward, cpu.done, cpu.obs)
+        check_sim(gpu, cpu, f"step {step} ")
+    ranges = gpu.obs.numpy()[4:]
+    assert (ranges == 1.0).any() and (ranges < 0.1).any()
+
+
 def test_car_trajectory_independent_of_batch_size():
     """Size-independent property at 262144 cars: car i's state depends only on its seed, index and
     actions, so the first 1000 cars of a 262144-car sim equal a 1000-car sim bit for bit."""

@@ -12,6 +12,7 @@
 #include <string.h>
 
 #include <algorithm>
+#include <limits>
 #include <map>
 #include <string>
 #include <tuple>
@@ -179,11 +180,41 @@ static int check_track(const float* d, size_t len) {
 // fills its device view.
 static int upload_track(const float* track, size_t len, float** d_track, float2** d_cl, TrackDev* t) {
   int nx = (int)track[0], ny = (int)track[1], L = (int)track[7];
-  std::vector<float2> cl((size_t)nx * ny * L);
+  const size_t cells = (size_t)nx * ny;
+  // the lidar's cells follow the per-cell repack in the same allocation
+  const size_t lidar = L <= 2 ? (size_t)(nx + 1) * (ny + 1) * L : 0;
+  std::vector<float2> cl(cells * L + lidar);
   for (int l = 0; l < L; ++l) {
     const float* c = track + 12 + (size_t)(3 * l) * nx * ny;
-    const float* h = c + (size_t)nx * ny;
-    for (size_t k = 0; k < (size_t)nx * ny; ++k) cl[k * L + l] = make_float2(c[k], h[k]);
+    const float* h = c + cells;
+    for (size_t k = 0; k < cells; ++k) cl[k * L + l] = make_float2(c[k], h[k]);
+  }
+  // Per cell of the unguarded march's probe (sim.cu, lidar_probe), which
+  // keeps layer 1 only where it is drivable and nearer the ray than layer 0:
+  // (clearance - cell, height) per slot, the clearance of an undrivable
+  // layer (not > 0) read as -1, in binary32 as the march subtracts it. Where
+  // one layer alone is drivable it takes slot 0 and slot 1's height is NaN
+  // (it never compares nearer); where neither is, slot 0 is layer 0. The
+  // border column and row read clearance and height -1, as off the map.
+  if (lidar) {
+    float2* lc = cl.data() + cells * L;
+    const float cell = track[4], nan = std::numeric_limits<float>::quiet_NaN();
+    const float off = -1.0f - cell;
+    auto slot = [&](float2 v) { return make_float2((v.x > 0.0f ? v.x : -1.0f) - cell, v.y); };
+    for (size_t k = 0; k < lidar; ++k) lc[k] = make_float2(off, L == 2 && k % 2 == 1 ? nan : -1.0f);
+    for (int y = 0; y < ny; ++y)
+      for (int x = 0; x < nx; ++x) {
+        const size_t k = (size_t)y * nx + x, q = ((size_t)y * (nx + 1) + x) * L;
+        const float2 v0 = cl[k * L];
+        if (L == 1) {
+          lc[q] = slot(v0);
+          continue;
+        }
+        const float2 v1 = cl[k * L + 1];
+        const bool d0 = v0.x > 0.0f, d1 = v1.x > 0.0f;
+        lc[q] = slot(d0 || !d1 ? v0 : v1);
+        lc[q + 1] = d0 && d1 ? slot(v1) : make_float2(off, nan);
+      }
   }
   if (int rc = dalloc(d_track, len)) return rc;
   if (int rc = dalloc(d_cl, cl.size())) return rc;
@@ -191,6 +222,8 @@ static int upload_track(const float* track, size_t len, float** d_track, float2*
   RACER_TRY(cudaMemcpy(*d_cl, cl.data(), cl.size() * sizeof(float2), cudaMemcpyHostToDevice));
   t->d = *d_track;
   t->cl = *d_cl;
+  t->lc = lidar ? reinterpret_cast<const float*>(*d_cl + cells * L) : nullptr;
+  t->lw = nx + 1;
   t->nx = nx;
   t->ny = ny;
   t->waypoints = (int)track[5];
@@ -207,12 +240,25 @@ static int upload_track(const float* track, size_t len, float** d_track, float2*
     const double X = ceil(std::max(fabs((double)t->x0), fabs((double)t->y0)) / (double)track[4]);
     const double delta = (5.001 * (nx > ny ? nx : ny) + 4.001 * X + 16.0) * 0x1p-24;
     t->band = delta < 0.25 ? (float)(0.5 - delta * (1.0 + 0x1p-20)) : 0.0f;  // 0: every lookup divides
+    // the march's probe takes v = RN(tt * RN(d * inv_cell) + RN(o * inv_cell + cx)) along the ray,
+    // with tt |d| <= RANGE: a wider band (sim.cu, lidar_cell)
+    const double mdelta = (7.001 * (nx > ny ? nx : ny) + 2.001 * X + 3.001 * (double)RANGE / track[4] + 16.0) * 0x1p-24;
+    t->mband = mdelta < 0.25 ? (float)(0.5 - mdelta * (1.0 + 0x1p-20)) : 0.0f;
   }
   t->spacing = track[6];
   t->slope = track[8];
   t->nxf = (float)nx;
   t->nyf = (float)ny;
   t->route = 12 + 3L * L * nx * ny;
+  {
+    // Every probe the march continues from adds a step >= m = 0.5 cell, and
+    // RN(tt + step) >= (tt + m)(1 - 2^-24), so after k probes tt >= m k
+    // (1 - 2^-24)^k. Where that reaches RANGE at k = max_iters the loop's
+    // `tt < RANGE` test always ends it first, and the probe count is not needed.
+    const float m = 0.5f * t->cell;
+    const int k = lidar_max_iters(*t);
+    t->free_march = (double)m * k * pow(1.0 - 0x1p-24, k) >= (double)RANGE * (1.0 + 1e-9) ? 1 : 0;
+  }
   return 0;
 }
 

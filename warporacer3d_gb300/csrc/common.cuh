@@ -46,6 +46,13 @@ struct TrackDev {
   float band;      // 0.5 - (5.001 max(nx, ny) + 4.001 max(|x0|, |y0|) / cell + 16) 2^-24: no division inside +-band
   float nxf, nyf;
   long route;
+  // The lidar's cells for one or two layers (sim.cu, lidar_probe): float2 or
+  // float4 per cell, rows of lw = nx + 1 cells over ny + 1 rows, the last
+  // column and row off-map cells; null for three or more layers.
+  const float* lc;
+  int lw;
+  float mband;     // band of the march's cell index (sim.cu, lidar_cell)
+  int free_march;  // 1: the march provably stops on tt >= RANGE before max_iters probes
 };
 
 // Several tracks in one launch: cars [car0[k], car0[k + 1]) drive on track

@@ -92,30 +92,44 @@ __device__ __forceinline__ bool cell_of(const TrackDev& t, float x, float y, lon
   return true;
 }
 
-// cell_of without the off-map branch: *idx is the cell, or cell 0 off the map,
-// and the result says whether the point is on the map, decided as cell_of
-// decides it.
+// The cell of the march's probe at tt along a ray among the lidar's cells
+// (TrackDev.lc), decided as cell_of decides it for the probe point px =
+// RN(ox + RN(tt dx)), py alike, with every off-map point sent to the border
+// column or row. Fast path: v = RN(tt ax + bx) in one fused multiply-add, with
+// ax = RN(dx r), bx = RN(ox r + cx) held per beam (r = RN(1 / cell), cx =
+// RN(-x0 r)). With e = 2^-24, w = (px - x0) / cell exactly, D = |w|, X =
+// |x0| / cell and T = tt |dx| <= RANGE, the roundings of r, cx, ax, bx and v
+// and those of the product and sum in px give |v - w| <= e (3 D + 3 T / cell
+// + 2 X + |v|) to first order, and the reference's u = RN(RN(RN(px - x0) /
+// cell) + 0.5) has |u - (w + 0.5)| <= e (2.0001 D + 1.0001 |u|). Where |v| <=
+// M + 2 (M = max(nx, ny)) that is |u - (v + 0.5)| <= e (7.0002 M + 3 T / cell
+// + 2 X + 14.6), inside mdelta = e (7.001 M + 2.001 X + 3.001 RANGE / cell +
+// 16) (TrackDev.mband = 0.5 - mdelta): a v farther than mdelta from every
+// half-integer has floor(u) = rint(v), and farther out both are off the map.
+// Inside the band, and for NaN and infinities, the point's own coordinates
+// go through cell_coord.
 // The nearest integer comes from adding and subtracting 1.5 * 2^23 (exactly
 // rint(v) for |v| < 2^22) and the cell from the sum's bits less those of
-// 1.5 * 2^23, in unsigned arithmetic: for |v| >= 2^22, infinities and NaN that
-// is >= 2^22 > nx, so such points are off the map on either path, as they are
-// for the reference. No conversion instruction on the common path.
-__device__ __forceinline__ bool cell_of_any(const TrackDev& t, float x, float y, long* idx) {
+// 1.5 * 2^23, in unsigned arithmetic: for |v| >= 2^22 that is >= 2^22 > nx,
+// so such points are off the map on either path, as they are for the
+// reference. The unsigned column clamped to nx and row to ny then land
+// off-map points on a border cell: no conversion, compare or select on the
+// common path.
+__device__ __forceinline__ unsigned lidar_cell(const TrackDev& t, float vx, float vy, float tt, float ox, float oy,
+                                               float dx, float dy) {
   constexpr float MAGIC = 12582912.0f;  // 1.5 * 2^23
-  const float vx = __fmaf_rn(x, t.inv_cell, t.cx), vy = __fmaf_rn(y, t.inv_cell, t.cy);
   const float mx = vx + MAGIC, my = vy + MAGIC;
   const float rx = mx - MAGIC, ry = my - MAGIC;
   unsigned ix, iy;
-  if (fabsf(vx - rx) < t.band && fabsf(vy - ry) < t.band) {
+  if (fabsf(vx - rx) < t.mband && fabsf(vy - ry) < t.mband) {
     ix = (unsigned)__float_as_int(mx) - 0x4B400000u, iy = (unsigned)__float_as_int(my) - 0x4B400000u;
   } else {
-    const float fx = cell_coord(x, t.x0, t.cell, t.inv_cell), fy = cell_coord(y, t.y0, t.cell, t.inv_cell);
+    const float px = ox + tt * dx, py = oy + tt * dy;
+    const float fx = cell_coord(px, t.x0, t.cell, t.inv_cell), fy = cell_coord(py, t.y0, t.cell, t.inv_cell);
     const bool on = fx >= 0.0f && fx < t.nxf && fy >= 0.0f && fy < t.nyf;
     ix = on ? (unsigned)(int)fx : 0xFFFFFFFFu, iy = on ? (unsigned)(int)fy : 0xFFFFFFFFu;
   }
-  const bool on = ix < (unsigned)t.nx && iy < (unsigned)t.ny;
-  *idx = on ? (long)(iy * (unsigned)t.nx + ix) : 0L;
-  return on;
+  return min(iy, (unsigned)t.ny) * (unsigned)t.lw + min(ix, (unsigned)t.nx);
 }
 
 // racer/sim.mojo:116-124. LAYERS = 0 reads the layer count from the track.
@@ -157,29 +171,25 @@ __device__ __forceinline__ Spot probe(const TrackDev& t, float x, float y, float
   return best;
 }
 
-// probe<LAYERS, false> for one or two layers with the off-map case selected
-// after an unconditional load (of cell 0 off the map) instead of branched
-// around it: the same Spot, no divergent branch per probe.
+// probe<LAYERS, false>'s (clearance - cell, height) for one or two layers at
+// the march's point (lidar_cell's arguments, height z), from the lidar's
+// cells. Per cell they hold (c0 - cell, h0, c1 - cell, h1), the clearance of
+// an undrivable layer as -1; slot 1 holds layer 1 only where both layers are
+// drivable and a NaN height otherwise, which never compares nearer, and a
+// cell where only layer 1 is drivable holds it in slot 0. So layer 1 is taken
+// exactly where probe takes it: where both are drivable and |h1 - z| <
+// |h0 - z|, or where only it is (probe's test |h1 - z| < 1e30 cannot fail
+// with |z| <= 1e20 + 10 and |h1| <= 1e6). The border cells read clearance and
+// height -1, as off the map.
 template <int LAYERS>
-__device__ __forceinline__ Spot probe_any(const TrackDev& t, float x, float y, float z) {
-  long idx;
-  const bool on = cell_of_any(t, x, y, &idx);
-  Spot best;
+__device__ __forceinline__ float2 lidar_probe(const TrackDev& t, float vx, float vy, float tt, float ox, float oy,
+                                              float dx, float dy, float z) {
+  const unsigned idx = lidar_cell(t, vx, vy, tt, ox, oy, dx, dy);
   if (LAYERS == 2) {
-    const float4 v = __ldg(reinterpret_cast<const float4*>(t.cl) + idx);
-    best = Spot{0, -1.0f, v.y};
-    float gap = 1e30f;
-    if (v.x > 0.0f) {
-      best = Spot{0, v.x, v.y};
-      gap = fabsf(v.y - z);
-    }
-    if (v.z > 0.0f && fabsf(v.w - z) < gap) best = Spot{1, v.z, v.w};
-  } else {
-    const float2 v = __ldg(t.cl + idx);
-    best = Spot{0, -1.0f, v.y};
-    if (v.x > 0.0f) best = Spot{0, v.x, v.y};
+    const float4 v = __ldg(reinterpret_cast<const float4*>(t.lc) + idx);
+    return fabsf(v.w - z) < fabsf(v.y - z) ? make_float2(v.z, v.w) : make_float2(v.x, v.y);
   }
-  return on ? best : Spot{0, -1.0f, -1.0f};  // off the map every grid reads -1
+  return __ldg(reinterpret_cast<const float2*>(t.lc) + idx);
 }
 
 // racer/sim.mojo:126-140: bilinear height and its gradient, in two parts: the
@@ -637,7 +647,7 @@ __global__ void __launch_bounds__(CARS * 32, lidar_min_blocks(CARS, WIDE))
   if (car < g.car0[k + 1]) trace_any(g.t[k], ray, obs, n, beam_dir, g.max_iters[k], iters, car, beam);
 }
 
-template <int LAYERS, bool GUARD>
+template <int LAYERS, bool GUARD, bool COUNTED = true>
 __device__ __forceinline__ float march(const TrackDev& t, float ox, float oy, float oz, float dx, float dy, float dz,
                                        float descent, float inv_descent, int max_iters, int* count_out);
 
@@ -661,9 +671,15 @@ __device__ __forceinline__ void trace(const TrackDev& t, const float4* __restric
   // every probe height lies within RANGE of the origin's (|dz| <= 1): with
   // |oz| <= 1e20 the probe's height guard cannot fail (NaN takes the guarded loop)
   // the unguarded march also needs a descent of 0 or a normal number (its quotient; see march)
-  const float range = fabsf(oz) <= 1e20f && (descent == 0.0f || descent >= 1.17549435e-38f)
-                          ? march<LAYERS, false>(t, ox, oy, oz, dx, dy, dz, descent, inv_descent, max_iters, &count)
-                          : march<LAYERS, true>(t, ox, oy, oz, dx, dy, dz, descent, inv_descent, max_iters, &count);
+  // where the probe bound provably never ends the march first (TrackDev.free_march)
+  // and no count is asked for, the loop tests tt < RANGE alone, as the reference does
+  float range;
+  if (!(fabsf(oz) <= 1e20f && (descent == 0.0f || descent >= 1.17549435e-38f)))
+    range = march<LAYERS, true>(t, ox, oy, oz, dx, dy, dz, descent, inv_descent, max_iters, &count);
+  else if (iters || !t.free_march)
+    range = march<LAYERS, false>(t, ox, oy, oz, dx, dy, dz, descent, inv_descent, max_iters, &count);
+  else
+    range = march<LAYERS, false, false>(t, ox, oy, oz, dx, dy, dz, descent, inv_descent, max_iters, &count);
   obs[(long)(4 + beam) * n + car] = range / RANGE;
   if (iters) iters[(long)beam * n + car] = count;
 }
@@ -683,7 +699,7 @@ __device__ __forceinline__ float quotient(float a, float b, float y, float q0) {
 }
 
 // The march of one beam (racer/sim.mojo:252-266); returns the range.
-template <int LAYERS, bool GUARD>
+template <int LAYERS, bool GUARD, bool COUNTED>
 __device__ __forceinline__ float march(const TrackDev& t, float ox, float oy, float oz, float dx, float dy, float dz,
                                        float descent, float inv_descent, int max_iters, int* count_out) {
   const float cell = t.cell, min_step = 0.5f * t.cell;
@@ -696,13 +712,22 @@ __device__ __forceinline__ float march(const TrackDev& t, float ox, float oy, fl
     // clearance term as for the reference's min(a, inf) or min(a, NaN). The
     // step is computed before the ground test and unused once the ground is
     // crossed, so one branch ends the march on either condition.
+    constexpr bool CELLS = LAYERS == 1 || LAYERS == 2;  // the lidar's cells (lidar_probe)
+    const float ax = CELLS ? dx * t.inv_cell : 0.0f, ay = CELLS ? dy * t.inv_cell : 0.0f;
+    const float bx = CELLS ? __fmaf_rn(ox, t.inv_cell, t.cx) : 0.0f, by = CELLS ? __fmaf_rn(oy, t.inv_cell, t.cy) : 0.0f;
     float fl = 0.0f;
-    while (tt < RANGE && count < max_iters) {
-      ++count;
-      const float px = ox + tt * dx, py = oy + tt * dy, pz = oz + tt * dz;
-      const Spot spot = LAYERS == 1 || LAYERS == 2 ? probe_any<LAYERS>(t, px, py, pz) : probe<LAYERS, false>(t, px, py, pz);
-      fl = (pz - spot.height) - 0.03f;
-      const float step = fminf(spot.clearance - cell, quotient(fl, descent, inv_descent, fl * inv_descent));
+    while (tt < RANGE && (!COUNTED || count < max_iters)) {
+      if (COUNTED) ++count;
+      const float pz = oz + tt * dz;
+      float2 spot;  // (clearance - cell, height)
+      if (CELLS) {
+        spot = lidar_probe<LAYERS>(t, __fmaf_rn(tt, ax, bx), __fmaf_rn(tt, ay, by), tt, ox, oy, dx, dy, pz);
+      } else {
+        const Spot s = probe<LAYERS, false>(t, ox + tt * dx, oy + tt * dy, pz);
+        spot = make_float2(s.clearance - cell, s.height);
+      }
+      fl = (pz - spot.y) - 0.03f;
+      const float step = fminf(spot.x, quotient(fl, descent, inv_descent, fl * inv_descent));
       if (fl < 0.0f || step < min_step) break;
       last = tt;
       last_floor = fl;

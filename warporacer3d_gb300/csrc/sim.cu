@@ -715,8 +715,12 @@ __device__ __forceinline__ float march(const TrackDev& t, float ox, float oy, fl
     constexpr bool CELLS = LAYERS == 1 || LAYERS == 2;  // the lidar's cells (lidar_probe)
     const float ax = CELLS ? dx * t.inv_cell : 0.0f, ay = CELLS ? dy * t.inv_cell : 0.0f;
     const float bx = CELLS ? __fmaf_rn(ox, t.inv_cell, t.cx) : 0.0f, by = CELLS ? __fmaf_rn(oy, t.inv_cell, t.cy) : 0.0f;
-    float fl = 0.0f;
-    while (tt < RANGE && (!COUNTED || count < max_iters)) {
+    // The loop enters with tt = 0 < RANGE; one exit test a probe covers the
+    // ground crossed, a step below the minimum and the next probe at or past
+    // RANGE (or past the probe bound), where the reference's loop test would
+    // fail after tt += step.
+    float fl, step, next;
+    for (;;) {
       if (COUNTED) ++count;
       const float pz = oz + tt * dz;
       float2 spot;  // (clearance - cell, height)
@@ -727,14 +731,16 @@ __device__ __forceinline__ float march(const TrackDev& t, float ox, float oy, fl
         spot = make_float2(s.clearance - cell, s.height);
       }
       fl = (pz - spot.y) - 0.03f;
-      const float step = fminf(spot.x, quotient(fl, descent, inv_descent, fl * inv_descent));
-      if (fl < 0.0f || step < min_step) break;
+      step = fminf(spot.x, quotient(fl, descent, inv_descent, fl * inv_descent));
+      next = tt + step;
+      if (fl < 0.0f || step < min_step || !(next < RANGE) || (COUNTED && count >= max_iters)) break;
       last = tt;
       last_floor = fl;
-      tt += step;
+      tt = next;
     }
     *count_out = count;
-    return fl < 0.0f ? fminf(last + ((tt - last) * last_floor) / (last_floor - fl), RANGE) : fminf(tt, RANGE);
+    if (fl < 0.0f) return fminf(last + ((tt - last) * last_floor) / (last_floor - fl), RANGE);
+    return fminf(step < min_step ? tt : next, RANGE);
   }
   while (tt < RANGE && count < max_iters) {
     ++count;

@@ -17,7 +17,7 @@
    pair of fused multiply-adds, give RN(a / b); the claim is checked on the
    march's operand ranges, on wide exponents and on quotients a hair from a
    rounding midpoint.
-4. The rounding in the unguarded march's probe (sim.cu, cell_of_any): rint(v)
+4. The rounding in the unguarded march's probe (sim.cu, lidar_cell): rint(v)
    as (v + 1.5 * 2^23) - 1.5 * 2^23 and the cell as the sum's bits less those
    of 1.5 * 2^23 (unsigned); the claims: exact for |v| < 2^22, and an index of
    at least 2^22 (off any map) for every larger, infinite or NaN v.

@@ -442,6 +442,54 @@ def test_lidar_on_random_drivable_cells_bit_exact(name):
     assert (ranges == 1.0).any() and (ranges < 0.1).any()
 
 
+def three_layer_track():
+    """bridge's two layers plus a third: layer 0 raised 2.5 m with 40% of its cells undrivable."""
+    base = W.track("bridge")
+    nx, ny = int(base[0]), int(base[1])
+    cells = nx * ny
+    grids = base[12:12 + 6 * cells]
+    third = grids[:3 * cells].copy()
+    third[cells:2 * cells] += np.float32(2.5)
+    rng = np.random.default_rng(23)
+    third[:cells][rng.random(cells) < 0.4] = np.float32(-1)
+    head = base[:12].copy()
+    head[7] = 3
+    return np.concatenate([head, grids, third, base[12 + 6 * cells:]]).astype(np.float32)
+
+
+def test_three_layer_track_bit_exact():
+    """The probe of three or more layers (the layer count read from the track), alone and as a
+    segment beside a one-layer track."""
+    track = three_layer_track()
+    n, beams = 96, 1081
+    gpu, cpu = W.Sim(track, n, 6, beams=beams), O.Sim(track, n, 6, beams=beams)
+    gpu.reset()
+    cpu.reset()
+    check_sim(gpu, cpu, "reset ")
+    rng = np.random.default_rng(6)
+    for step in range(5):
+        act = rng.uniform(-1, 1, (2, n)).astype(np.float32)
+        gpu.actions.write(act)
+        cpu.actions[:] = act
+        gpu.step(gpu.actions, gpu.reward, gpu.done, gpu.obs)
+        cpu.step(cpu.actions, cpu.reward, cpu.done, cpu.obs)
+        check_sim(gpu, cpu, f"step {step} ")
+    tracks, cars, seeds = [W.track("bank"), track], [40, 70], [3, 4]
+    seg = W.Sim.segments(tracks, cars, seeds, beams=108)
+    cpus = [O.Sim(t, c, s, beams=108) for t, c, s in zip(tracks, cars, seeds)]
+    seg.reset()
+    for c in cpus:
+        c.reset()
+    for step in range(4):
+        act = rng.uniform(-1, 1, (2, seg.n)).astype(np.float32)
+        seg.actions.write(act)
+        for k, c in enumerate(cpus):
+            c.actions[:] = act[:, seg.car0[k]:seg.car0[k + 1]]
+            c.step(c.actions, c.reward, c.done, c.obs)
+        seg.step(seg.actions, seg.reward, seg.done, seg.obs)
+        check_segments(seg, cpus, f"step {step} ")
+
+
 def test_car_trajectory_independent_of_batch_size():
     """Size-independent property at 262144 cars: car i's state depends only on its seed, index and
     actions, so the first 1000 cars of a 262144-car sim equal a 1000-car sim bit for bit."""

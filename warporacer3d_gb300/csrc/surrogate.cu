@@ -347,17 +347,38 @@ __global__ void k_adam_s(long p, float lr, float c1, float c2, float* th, const 
 // sums[0] += sum |e|, sums[1] += sum e^2, max in bits, count of |e| > 5 cm.
 // FP32 per-thread partial sums (a few thousand terms each; FP64 arithmetic is
 // slow on this GPU), combined in FP64 once per thread.
-__global__ void k_compare(const float* pred, const float* exact, long total, double* sums, unsigned* maxbits,
-                          unsigned long long* over) {
+__device__ __forceinline__ void compare_one(float p, float x, float& a, float& s, float& mx, unsigned& ov) {
+  const float e = fabsf(p - x) * RANGE;
+  a += e;
+  s += e * e;
+  mx = fmaxf(mx, e);
+  ov += e > 0.05f;
+}
+
+// Error statistics of pred against exact (ranges in obs units): sums of |e|
+// and e^2, the largest e and the count over 5 cm. 16-byte loads when both
+// arrays are 16-byte aligned (unrolled, so several loads are in flight).
+__global__ void k_compare(const float* __restrict__ pred, const float* __restrict__ exact, long total, double* sums,
+                          unsigned* maxbits, unsigned long long* over) {
   float a = 0.0f, s = 0.0f, mx = 0.0f;
   unsigned ov = 0;
-  for (long i = (long)blockIdx.x * blockDim.x + threadIdx.x; i < total; i += (long)gridDim.x * blockDim.x) {
-    float e = fabsf(pred[i] - exact[i]) * RANGE;
-    a += e;
-    s += e * e;
-    mx = fmaxf(mx, e);
-    ov += e > 0.05f;
+  const long stride = (long)gridDim.x * blockDim.x, i0 = (long)blockIdx.x * blockDim.x + threadIdx.x;
+  long tail = 0;
+  if ((((uintptr_t)pred | (uintptr_t)exact) & 15) == 0) {
+    const long quads = total / 4;
+    const float4* p4 = reinterpret_cast<const float4*>(pred);
+    const float4* x4 = reinterpret_cast<const float4*>(exact);
+#pragma unroll 4
+    for (long q = i0; q < quads; q += stride) {
+      const float4 p = __ldcs(p4 + q), x = __ldcs(x4 + q);
+      compare_one(p.x, x.x, a, s, mx, ov);
+      compare_one(p.y, x.y, a, s, mx, ov);
+      compare_one(p.z, x.z, a, s, mx, ov);
+      compare_one(p.w, x.w, a, s, mx, ov);
+    }
+    tail = quads * 4;
   }
+  for (long i = tail + i0; i < total; i += stride) compare_one(pred[i], exact[i], a, s, mx, ov);
   a = warp_sum(a);
   s = warp_sum(s);
   for (int o = 16; o > 0; o >>= 1) {
@@ -956,13 +977,14 @@ int surrogate_lidar(racer_surrogate* s, racer_sim* sim, float* obs, bool audit, 
   k_features<<<(n + 127) / 128, 128, 0, st>>>(sim->ray, n, s->nm, a->x, nullptr);
   SURR_CHECK(cudaGetLastError());
   SURR_CHECK(cudaMemsetAsync(s->minr, 0x7f, (size_t)n * sizeof(unsigned), st));
+  // on an audit step the prediction goes to the scratch rows and the exact tracer writes obs
+  float* pred = audit ? s->exact + 4L * n : obs + 4L * n;
   if (s->fused && s->L.H == SF_H) {
     const float* th = s->theta;
-    FusedArgs fa{th + s->L.b2, th + s->L.b3, th + s->L.b4, obs + 4L * n, s->minr, n, beams,
-                 (s->L.npad + 255) / 256, s->err};
+    FusedArgs fa{th + s->L.b2, th + s->L.b3, th + s->L.b4, pred, s->minr, n, beams, (s->L.npad + 255) / 256, s->err};
     SURR_CHECK(surrogate_fused_launch(a->tx, s->tw1, s->tw2, s->tw3, s->tw4, fa, sim->sms, st));
   } else {
-    EpiInfer inf{obs + 4L * n, n, s->theta + s->L.b4, n, beams, s->minr};
+    EpiInfer inf{pred, n, s->theta + s->L.b4, n, beams, s->minr};
     cudaStream_t keep = s->st;
     s->st = st;
     int rc = forward(s, a, false, &inf);
@@ -970,10 +992,8 @@ int surrogate_lidar(racer_surrogate* s, racer_sim* sim, float* obs, bool audit, 
     if (rc) return rc;
   }
   if (audit) {
-    launch_lidar(sim->t, sim->ray, s->exact, n, beams, sim->beam_dir, nullptr, st);
-    k_compare<<<1216, 256, 0, st>>>(obs + 4L * n, s->exact + 4L * n, (long)beams * n, s->rsums, s->rmax, s->rcount);
-    SURR_CHECK(cudaMemcpyAsync(obs + 4L * n, s->exact + 4L * n, (size_t)beams * n * sizeof(float),
-                               cudaMemcpyDeviceToDevice, st));
+    launch_lidar(sim->t, sim->ray, obs, n, beams, sim->beam_dir, nullptr, st);
+    k_compare<<<1216, 256, 0, st>>>(pred, obs + 4L * n, (long)beams * n, s->rsums, s->rmax, s->rcount);
   } else if (fallback > 0.0f) {
     SURR_CHECK(cudaMemsetAsync(s->list_count, 0, sizeof(int), st));
     launch_select_cars(s->minr, n, fallback, s->list, s->list_count, st);

@@ -94,9 +94,10 @@ typedef struct {
 int racer_sim_set_lidar_shape(racer_sim* sim, const racer_lidar_shape* shape);
 int racer_sim_get_lidar_shape(racer_sim* sim, racer_lidar_shape* shape);
 /* Autotuner: times `reps` lidar passes on the sim's current lidar frames for
- * every cars_per_block, wide and (with several segments) split, with the
- * segments in index order and heaviest-first (by probe iterations counted in
- * one pass), keeps the fastest shape and returns it with its mean time in
+ * every cars_per_block, wide, dynamic, flat and (with several segments)
+ * split, with the segments in index order and heaviest-first (by probe
+ * iterations counted in one pass), in two rounds over all shapes; keeps the
+ * shape with the fastest round and returns it with that round's mean time in
  * ms. The lidar only rewrites obs rows from the frames: the sim's state is
  * unchanged. */
 int racer_sim_autotune(racer_sim* sim, int reps, racer_lidar_shape* best, float* best_ms);

@@ -45,6 +45,26 @@ def test_policy_forward(beams, cols):
     assert g.status() == 0
 
 
+def test_policy_forward_staging_paths_agree():
+    """The BF16 forward with its inputs staged by TMA (sample columns 16-byte aligned: 1000
+    columns) and the register-staged forward (1001 columns) give the same bits for the same
+    samples."""
+    beams = 1081
+    g = W.Policy(5, beams=beams)
+    rng = np.random.default_rng(4)
+    x = rng.uniform(-1, 1, (beams + 5, 1001)).astype(np.float32)
+    outs = []
+    for cols in (1000, 1001):
+        xd = W.DevArray.empty((beams + 5, cols))
+        xd.write(np.ascontiguousarray(x[:, :cols]))
+        a = W.Activations(g, cols)
+        g.forward(xd, a)
+        outs.append([getattr(a, name).numpy()[:, :1000] for name in ("h1", "h2", "o")])
+    for p, q in zip(*outs):
+        assert np.array_equal(p, q)
+    assert g.status() == 0
+
+
 @pytest.mark.parametrize("precision", ["bf16", "fp32"])
 def test_gae_bit_exact_and_gradient_and_update(precision):
     """tests/test_mojo.mojo:162-215 on the GPU: GAE, FD gradient (GPU tolerance), KL after one update."""

@@ -24,6 +24,7 @@
 #include "mlp_tc.h"
 #include "sample.cuh"
 #include "tc.cuh"
+#include "tma.h"
 
 namespace racer {
 namespace {
@@ -49,108 +50,17 @@ struct FwdCfg {
   static constexpr int MIN_BLOCKS = GROUPS == 2 ? 2 : 1;
 };
 
-// Grid: one CTA per 128 samples. Warps 0-15 form four producer groups; group
-// g loads k-blocks g, g+4, g+8, ... of X (thread = sample row) and of W0 into
-// stage g, then arrives on full[g]. Warp 16 waits on full[kb % 4], issues the
-// four K=16 MMAs of the block and commits to empty[kb % 4]; after the last
-// block it commits to `done`. Warps 0-3 (TMEM lanes 0-127) then run the
-// epilogues and issue layers 2 and 3.
-template <int GROUPS>
-__global__ void __launch_bounds__(FwdCfg<GROUPS>::THREADS, FwdCfg<GROUPS>::MIN_BLOCKS)
-    k_mlp_fwd(const float* __restrict__ x, int in, int cols, int c0, int c1,
-                                                        const uint4* __restrict__ w0s, int kblocks,
-                                                        const uint4* __restrict__ w1s,
-                                                        const uint4* __restrict__ w2s, float* h1g, float* h2g,
-                                                        float* og, int write_hidden, SampleArgs sa, int* err) {
-  using C = FwdCfg<GROUPS>;
-  constexpr int THREADS = C::THREADS, MMA_WARP = C::MMA_WARP, OFF_A = C::OFF_A, OFF_B = C::OFF_B,
-                OFF_W1 = C::OFF_W1, OFF_W2 = C::OFF_W2, OFF_BAR = C::OFF_BAR;
-  extern __shared__ uint8_t smem_raw[];
-  const uint32_t raw = tc::smem_u32(smem_raw);
-  uint8_t* smem = smem_raw + (((raw + 1023u) & ~1023u) - raw);
-  uint64_t* full = reinterpret_cast<uint64_t*>(smem + OFF_BAR);
-  uint64_t* empty = full + GROUPS;
-  uint64_t* done = empty + GROUPS;
-  uint32_t* tslot = reinterpret_cast<uint32_t*>(done + 1);
-
+// Epilogues of the forward (warps 0-3: TMEM lanes 0-127 = sample rows), once
+// layer 1's accumulator is complete (`done`, phase 0): tanh, H = [h | 1 | 0]
+// as the next layer's A in stages 0-1 (the layer-1 stages, free by then),
+// layers 2 and 3 issued by thread 0, the outputs and the fused sampling.
+__device__ bool fwd_epilogue(uint8_t* smem, int OFF_A, int OFF_W1, int OFF_W2, uint32_t tmem, uint64_t* done, int r,
+                             bool live, int c, int cols, float* h1g, float* h2g, float* og, int write_hidden,
+                             const SampleArgs& sa) {
   const int tid = threadIdx.x, warp = tid >> 5;
-  const int r = tid & (TILE - 1);  // sample row of a producer or epilogue thread
-  const int c = c0 + (int)blockIdx.x * TILE + r;  // column (sample) of the [rows, cols] buffers
-  const bool live = c < c1;
-
-  if (tid == 0) {
-    for (int g = 0; g < GROUPS; ++g) {
-      tc::mbar_init(&full[g], TILE);
-      tc::mbar_init(&empty[g], 1);
-    }
-    tc::mbar_init(done, 1);
-    tc::fence_barrier_init();
-  }
-  if (warp == MMA_WARP) {
-    tc::tmem_alloc(tslot, 64);
-    tc::tmem_relinquish();
-  }
-  {  // W1 (2 x 8 KB) and W2 (2 x 2 KB), resident for the whole tile
-    uint4* w1 = reinterpret_cast<uint4*>(smem + OFF_W1);
-    uint4* w2 = reinterpret_cast<uint4*>(smem + OFF_W2);
-    for (int e = tid; e < 2 * B_BYTES / 16; e += THREADS) w1[e] = __ldg(w1s + e);
-    for (int e = tid; e < 2 * 16 * 128 / 16; e += THREADS) w2[e] = __ldg(w2s + e);
-  }
-  tc::fence_proxy_async_smem();
-  tc::tc_fence_before();
-  __syncthreads();
-  tc::tc_fence_after();
-  const uint32_t tmem = *tslot;
-  const uint32_t id64 = tc::idesc_bf16(TILE, 64), id16 = tc::idesc_bf16(TILE, 16);
   bool ok = true;
-
-  if (warp < MMA_WARP) {
-    // ---- producers: layer-1 operands, one k-block per group in flight ----
-    const int g = warp >> 2;
-    uint8_t* A = smem + OFF_A + g * A_BYTES;
-    uint4* B = reinterpret_cast<uint4*>(smem + OFF_B + g * B_BYTES);
-    for (int j = 0;; ++j) {
-      const int kb = g + GROUPS * j;
-      if (kb >= kblocks) break;
-      float v[64];
-#pragma unroll
-      for (int q = 0; q < 64; ++q) {
-        const int f = kb * 64 + q;
-        v[q] = (live && f < in) ? __ldg(x + (long)f * cols + c) : 0.0f;
-      }
-      uint4 wb[4];
-      const uint4* src = w0s + (long)kb * (B_BYTES / 16);
-#pragma unroll
-      for (int e = 0; e < 4; ++e) wb[e] = __ldg(src + r + e * TILE);
-      if (j >= 1 && !tc::mbar_wait(&empty[g], (j - 1) & 1)) ok = false;
-#pragma unroll
-      for (int q = 0; q < 8; ++q) {
-        uint4 pk = make_uint4(tc::pack_bf16(v[8 * q], v[8 * q + 1]), tc::pack_bf16(v[8 * q + 2], v[8 * q + 3]),
-                              tc::pack_bf16(v[8 * q + 4], v[8 * q + 5]), tc::pack_bf16(v[8 * q + 6], v[8 * q + 7]));
-        *reinterpret_cast<uint4*>(A + r * 128 + ((q ^ (r & 7)) << 4)) = pk;
-      }
-#pragma unroll
-      for (int e = 0; e < 4; ++e) B[r + e * TILE] = wb[e];
-      tc::fence_proxy_async_smem();
-      tc::mbar_arrive(&full[g]);
-    }
-  } else if ((tid & 31) == 0) {
-    // ---- MMA issuer: layer 1 ----
-    for (int kb = 0; kb < kblocks; ++kb) {
-      const int g = kb % GROUPS;
-      if (!tc::mbar_wait(&full[g], (kb / GROUPS) & 1)) ok = false;
-      tc::tc_fence_after();
-      const uint32_t a = tc::smem_u32(smem + OFF_A + g * A_BYTES), b = tc::smem_u32(smem + OFF_B + g * B_BYTES);
-#pragma unroll
-      for (int k = 0; k < 4; ++k)
-        tc::mma_bf16(tmem, tc::sdesc_sw128(a + 32 * k), tc::sdesc_sw128(b + 32 * k), id64, (kb | k) ? 1u : 0u);
-      tc::mma_commit(&empty[g]);
-    }
-    tc::mma_commit(done);
-  }
-
-  if (warp < 4) {
-    // ---- epilogues (TMEM lanes 0-127 = sample rows): layers 2 and 3 ----
+  const uint32_t id64 = tc::idesc_bf16(TILE, 64), id16 = tc::idesc_bf16(TILE, 16);
+  {
     const uint32_t trow = tmem + ((uint32_t)(warp * 32) << 16);
     uint8_t* Hs = smem + OFF_A;
     if (!tc::mbar_wait(done, 0)) ok = false;
@@ -209,9 +119,255 @@ __global__ void __launch_bounds__(FwdCfg<GROUPS>::THREADS, FwdCfg<GROUPS>::MIN_B
       }
     }
   }
+  return ok;
+}
+
+// Grid: one CTA per 128 samples. Warps 0-15 form four producer groups; group
+// g loads k-blocks g, g+4, g+8, ... of X (thread = sample row) and of W0 into
+// stage g, then arrives on full[g]. Warp 16 waits on full[kb % 4], issues the
+// four K=16 MMAs of the block and commits to empty[kb % 4]; after the last
+// block it commits to `done`. Warps 0-3 (TMEM lanes 0-127) then run the
+// epilogues and issue layers 2 and 3.
+template <int GROUPS>
+__global__ void __launch_bounds__(FwdCfg<GROUPS>::THREADS, FwdCfg<GROUPS>::MIN_BLOCKS)
+    k_mlp_fwd(const float* __restrict__ x, int in, int cols, int c0, int c1,
+                                                        const uint4* __restrict__ w0s, int kblocks,
+                                                        const uint4* __restrict__ w1s,
+                                                        const uint4* __restrict__ w2s, float* h1g, float* h2g,
+                                                        float* og, int write_hidden, SampleArgs sa, int* err) {
+  using C = FwdCfg<GROUPS>;
+  constexpr int THREADS = C::THREADS, MMA_WARP = C::MMA_WARP, OFF_A = C::OFF_A, OFF_B = C::OFF_B,
+                OFF_W1 = C::OFF_W1, OFF_W2 = C::OFF_W2, OFF_BAR = C::OFF_BAR;
+  extern __shared__ uint8_t smem_raw[];
+  const uint32_t raw = tc::smem_u32(smem_raw);
+  uint8_t* smem = smem_raw + (((raw + 1023u) & ~1023u) - raw);
+  uint64_t* full = reinterpret_cast<uint64_t*>(smem + OFF_BAR);
+  uint64_t* empty = full + GROUPS;
+  uint64_t* done = empty + GROUPS;
+  uint32_t* tslot = reinterpret_cast<uint32_t*>(done + 1);
+
+  const int tid = threadIdx.x, warp = tid >> 5;
+  const int r = tid & (TILE - 1);  // sample row of a producer or epilogue thread
+  const int c = c0 + (int)blockIdx.x * TILE + r;  // column (sample) of the [rows, cols] buffers
+  const bool live = c < c1;
+
+  if (tid == 0) {
+    for (int g = 0; g < GROUPS; ++g) {
+      tc::mbar_init(&full[g], TILE);
+      tc::mbar_init(&empty[g], 1);
+    }
+    tc::mbar_init(done, 1);
+    tc::fence_barrier_init();
+  }
+  if (warp == MMA_WARP) {
+    tc::tmem_alloc(tslot, 64);
+    tc::tmem_relinquish();
+  }
+  {  // W1 (2 x 8 KB) and W2 (2 x 2 KB), resident for the whole tile
+    uint4* w1 = reinterpret_cast<uint4*>(smem + OFF_W1);
+    uint4* w2 = reinterpret_cast<uint4*>(smem + OFF_W2);
+    for (int e = tid; e < 2 * B_BYTES / 16; e += THREADS) w1[e] = __ldg(w1s + e);
+    for (int e = tid; e < 2 * 16 * 128 / 16; e += THREADS) w2[e] = __ldg(w2s + e);
+  }
+  tc::fence_proxy_async_smem();
+  tc::tc_fence_before();
+  __syncthreads();
+  tc::tc_fence_after();
+  const uint32_t tmem = *tslot;
+  const uint32_t id64 = tc::idesc_bf16(TILE, 64);
+  bool ok = true;
+
+  if (warp < MMA_WARP) {
+    // ---- producers: layer-1 operands, one k-block per group in flight ----
+    const int g = warp >> 2;
+    uint8_t* A = smem + OFF_A + g * A_BYTES;
+    uint4* B = reinterpret_cast<uint4*>(smem + OFF_B + g * B_BYTES);
+    for (int j = 0;; ++j) {
+      const int kb = g + GROUPS * j;
+      if (kb >= kblocks) break;
+      float v[64];
+#pragma unroll
+      for (int q = 0; q < 64; ++q) {
+        const int f = kb * 64 + q;
+        v[q] = (live && f < in) ? __ldg(x + (long)f * cols + c) : 0.0f;
+      }
+      uint4 wb[4];
+      const uint4* src = w0s + (long)kb * (B_BYTES / 16);
+#pragma unroll
+      for (int e = 0; e < 4; ++e) wb[e] = __ldg(src + r + e * TILE);
+      if (j >= 1 && !tc::mbar_wait(&empty[g], (j - 1) & 1)) ok = false;
+#pragma unroll
+      for (int q = 0; q < 8; ++q) {
+        uint4 pk = make_uint4(tc::pack_bf16(v[8 * q], v[8 * q + 1]), tc::pack_bf16(v[8 * q + 2], v[8 * q + 3]),
+                              tc::pack_bf16(v[8 * q + 4], v[8 * q + 5]), tc::pack_bf16(v[8 * q + 6], v[8 * q + 7]));
+        *reinterpret_cast<uint4*>(A + r * 128 + ((q ^ (r & 7)) << 4)) = pk;
+      }
+#pragma unroll
+      for (int e = 0; e < 4; ++e) B[r + e * TILE] = wb[e];
+      tc::fence_proxy_async_smem();
+      tc::mbar_arrive(&full[g]);
+    }
+  } else if ((tid & 31) == 0) {
+    // ---- MMA issuer: layer 1 ----
+    for (int kb = 0; kb < kblocks; ++kb) {
+      const int g = kb % GROUPS;
+      if (!tc::mbar_wait(&full[g], (kb / GROUPS) & 1)) ok = false;
+      tc::tc_fence_after();
+      const uint32_t a = tc::smem_u32(smem + OFF_A + g * A_BYTES), b = tc::smem_u32(smem + OFF_B + g * B_BYTES);
+#pragma unroll
+      for (int k = 0; k < 4; ++k)
+        tc::mma_bf16(tmem, tc::sdesc_sw128(a + 32 * k), tc::sdesc_sw128(b + 32 * k), id64, (kb | k) ? 1u : 0u);
+      tc::mma_commit(&empty[g]);
+    }
+    tc::mma_commit(done);
+  }
+
+  if (warp < 4 && !fwd_epilogue(smem, OFF_A, OFF_W1, OFF_W2, tmem, done, r, live, c, cols, h1g, h2g, og, write_hidden,
+                                  sa))
+    ok = false;
   tc::tc_fence_before();
   __syncthreads();
   if (warp == MMA_WARP) tc::tmem_dealloc(tmem, 64);
+  if (!ok) atomicExch(err, 1);
+}
+
+// Forward with the inputs staged by TMA (wide inputs whose sample columns are
+// 16-byte aligned), so the bytes in flight no longer sit in registers: warp
+// 4's first thread streams each k-block of X as an FP32 box [64 features][128
+// samples] into a ring of XS stages; warps 0-3 (thread = sample row) read
+// their column of the box, arrive on xempty, pack it to BF16 into the swizzled
+// A stage once that stage's previous MMAs completed, with the W0 k-block
+// brought by a bulk copy that thread 0 starts (the stage's extra arrival), and
+// arrive on afull; warp 5's first thread issues the MMAs and commits aempty.
+// Features past `in` and samples past `cols` read zero, as the register
+// path's loads do; samples of a box outside [c0, c1) are never written back.
+// The epilogues are the register path's, so both give the same bits.
+constexpr int XS = 3, XA = 3;
+constexpr int X_BYTES = 64 * TILE * 4;
+struct TmaCfg {
+  static constexpr int THREADS = 6 * 32;
+  static constexpr int OFF_A = 0;  // XA x A; H = [h | 1 | 0] reuses A[0], A[1]
+  static constexpr int OFF_B = OFF_A + XA * A_BYTES;
+  static constexpr int OFF_X = OFF_B + XA * B_BYTES;
+  static constexpr int OFF_W1 = OFF_X + XS * X_BYTES;
+  static constexpr int OFF_W2 = OFF_W1 + 2 * B_BYTES;
+  static constexpr int OFF_BAR = OFF_W2 + 2 * 16 * 128;
+  // + barriers, + alignment slack, + 16 KB so every descriptor-addressed read stays inside the allocation
+  static constexpr int SMEM_BYTES = OFF_BAR + 256 + 1024 + 16384;
+};
+static_assert(TmaCfg::SMEM_BYTES <= 227 * 1024, "one CTA per SM");
+static_assert((2 * XS + 2 * XA + 1) * 8 + 4 <= 256, "barriers and the TMEM slot fit their 256 bytes");
+
+__global__ void __launch_bounds__(TmaCfg::THREADS, 1)
+    k_mlp_fwd_tma(const __grid_constant__ CUtensorMap xmap, int cols, int c0, int c1, const uint4* __restrict__ w0s,
+                  int kblocks, const uint4* __restrict__ w1s, const uint4* __restrict__ w2s, float* h1g, float* h2g,
+                  float* og, int write_hidden, SampleArgs sa, int* err) {
+  using C = TmaCfg;
+  extern __shared__ uint8_t smem_raw[];
+  const uint32_t raw = tc::smem_u32(smem_raw);
+  uint8_t* smem = smem_raw + (((raw + 1023u) & ~1023u) - raw);
+  uint64_t* xfull = reinterpret_cast<uint64_t*>(smem + C::OFF_BAR);
+  uint64_t* xempty = xfull + XS;
+  uint64_t* afull = xempty + XS;
+  uint64_t* aempty = afull + XA;
+  uint64_t* done = aempty + XA;
+  uint32_t* tslot = reinterpret_cast<uint32_t*>(done + 1);
+
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  const int r = tid & (TILE - 1);
+  const int col0 = c0 + (int)blockIdx.x * TILE;
+  const int c = col0 + r;
+  const bool live = c < c1;
+
+  if (tid == 0) {
+    for (int s = 0; s < XS; ++s) {
+      tc::mbar_init(&xfull[s], 1);
+      tc::mbar_init(&xempty[s], TILE);
+    }
+    for (int s = 0; s < XA; ++s) {
+      tc::mbar_init(&afull[s], TILE + 1);
+      tc::mbar_init(&aempty[s], 1);
+    }
+    tc::mbar_init(done, 1);
+    tc::fence_barrier_init();
+  }
+  if (warp == 5) {
+    tc::tmem_alloc(tslot, 64);
+    tc::tmem_relinquish();
+  }
+  {  // W1 (2 x 8 KB) and W2 (2 x 2 KB), resident for the whole tile
+    uint4* w1 = reinterpret_cast<uint4*>(smem + C::OFF_W1);
+    uint4* w2 = reinterpret_cast<uint4*>(smem + C::OFF_W2);
+    for (int e = tid; e < 2 * B_BYTES / 16; e += C::THREADS) w1[e] = __ldg(w1s + e);
+    for (int e = tid; e < 2 * 16 * 128 / 16; e += C::THREADS) w2[e] = __ldg(w2s + e);
+  }
+  tc::fence_proxy_async_smem();
+  tc::tc_fence_before();
+  __syncthreads();
+  tc::tc_fence_after();
+  const uint32_t tmem = *tslot;
+  bool ok = true;
+
+  if (warp == 4) {
+    if (lane == 0) {  // ---- X boxes ----
+      for (int kb = 0; kb < kblocks; ++kb) {
+        const int s = kb % XS, j = kb / XS;
+        if (j >= 1 && !tc::mbar_wait(&xempty[s], (j - 1) & 1)) ok = false;
+        tc::mbar_arrive_expect_tx(&xfull[s], X_BYTES);
+        tc::tma_load_2d(smem + C::OFF_X + s * X_BYTES, &xmap, col0, kb * 64, &xfull[s]);
+      }
+      // no copy may still be landing in shared memory when the CTA exits
+      for (int kb = kblocks > XS ? kblocks - XS : 0; kb < kblocks; ++kb)
+        if (!tc::mbar_wait(&xfull[kb % XS], (kb / XS) & 1)) ok = false;
+    }
+  } else if (warp == 5) {
+    if (lane == 0) {  // ---- MMA issuer: layer 1 ----
+      const uint32_t id64 = tc::idesc_bf16(TILE, 64);
+      for (int kb = 0; kb < kblocks; ++kb) {
+        const int a = kb % XA;
+        if (!tc::mbar_wait(&afull[a], (kb / XA) & 1)) ok = false;
+        tc::tc_fence_after();
+        const uint32_t sa_ = tc::smem_u32(smem + C::OFF_A + a * A_BYTES), sb = tc::smem_u32(smem + C::OFF_B + a * B_BYTES);
+#pragma unroll
+        for (int k = 0; k < 4; ++k)
+          tc::mma_bf16(tmem, tc::sdesc_sw128(sa_ + 32 * k), tc::sdesc_sw128(sb + 32 * k), id64, (kb | k) ? 1u : 0u);
+        tc::mma_commit(&aempty[a]);
+      }
+      tc::mma_commit(done);
+    }
+  } else {
+    // ---- warps 0-3: BF16 operands of layer 1, then the epilogues ----
+    const float* X = reinterpret_cast<const float*>(smem + C::OFF_X);
+    for (int kb = 0; kb < kblocks; ++kb) {
+      const int s = kb % XS, a = kb % XA;
+      if (!tc::mbar_wait(&xfull[s], (kb / XS) & 1)) ok = false;
+      const float* box = X + s * (X_BYTES / 4);
+      float v[64];
+#pragma unroll
+      for (int q = 0; q < 64; ++q) v[q] = box[q * TILE + r];
+      tc::mbar_arrive(&xempty[s]);
+      if (kb >= XA && !tc::mbar_wait(&aempty[a], ((kb / XA) - 1) & 1)) ok = false;
+      uint8_t* A = smem + C::OFF_A + a * A_BYTES;
+      if (r == 0) {  // the stage is free: announce and start the W0 copy
+        tc::mbar_arrive_expect_tx(&afull[a], B_BYTES);
+        tc::bulk_load(smem + C::OFF_B + a * B_BYTES, w0s + (long)kb * (B_BYTES / 16), B_BYTES, &afull[a]);
+      }
+#pragma unroll
+      for (int q = 0; q < 8; ++q) {
+        uint4 pk = make_uint4(tc::pack_bf16(v[8 * q], v[8 * q + 1]), tc::pack_bf16(v[8 * q + 2], v[8 * q + 3]),
+                              tc::pack_bf16(v[8 * q + 4], v[8 * q + 5]), tc::pack_bf16(v[8 * q + 6], v[8 * q + 7]));
+        *reinterpret_cast<uint4*>(A + r * 128 + ((q ^ (r & 7)) << 4)) = pk;
+      }
+      tc::fence_proxy_async_smem();
+      tc::mbar_arrive(&afull[a]);
+    }
+    if (!fwd_epilogue(smem, C::OFF_A, C::OFF_W1, C::OFF_W2, tmem, done, r, live, c, cols, h1g, h2g, og, write_hidden,
+                      sa))
+      ok = false;
+  }
+  tc::tc_fence_before();
+  __syncthreads();
+  if (warp == 5) tc::tmem_dealloc(tmem, 64);
   if (!ok) atomicExch(err, 1);
 }
 
@@ -280,6 +436,21 @@ cudaError_t launch_mlp_fwd(const float* x, int in, int cols, const uint8_t* pack
   const uint4* w1 = reinterpret_cast<const uint4*>(pack + (size_t)kb * 8192);
   const uint4* w2 = reinterpret_cast<const uint4*>(pack + (size_t)kb * 8192 + 2 * 8192);
   if (kb <= 4) return fwd_launch<2>(x, in, cols, c0, c1, kb, w0, w1, w2, h1, h2, o, write_hidden, sa, err, st);
+  // wide inputs: X staged by TMA where its sample columns are 16-byte aligned
+  CUtensorMap xmap;
+  if (c1 > c0 && (cols & 3) == 0 && (c0 & 3) == 0 && (reinterpret_cast<uintptr_t>(x) & 15) == 0 &&
+      make_tmap_f32(&xmap, x, (uint64_t)in, (uint64_t)cols, (uint64_t)cols, TILE, 64) == 0) {
+    static bool configured = false;
+    if (!configured) {
+      cudaError_t e = cudaFuncSetAttribute(k_mlp_fwd_tma, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                           TmaCfg::SMEM_BYTES);
+      if (e != cudaSuccess) return e;
+      configured = true;
+    }
+    k_mlp_fwd_tma<<<(c1 - c0 + TILE - 1) / TILE, TmaCfg::THREADS, TmaCfg::SMEM_BYTES, st>>>(
+        xmap, cols, c0, c1, w0, kb, w1, w2, h1, h2, o, write_hidden, sa, err);
+    return cudaGetLastError();
+  }
   return fwd_launch<4>(x, in, cols, c0, c1, kb, w0, w1, w2, h1, h2, o, write_hidden, sa, err, st);
 }
 

@@ -51,19 +51,19 @@ struct FwdCfg {
 };
 
 // Epilogues of the forward (warps 0-3: TMEM lanes 0-127 = sample rows), once
-// layer 1's accumulator is complete (`done`, phase 0): tanh, H = [h | 1 | 0]
+// layer 1's accumulator is complete (`done`, completion p0): tanh, H = [h | 1 | 0]
 // as the next layer's A in stages 0-1 (the layer-1 stages, free by then),
 // layers 2 and 3 issued by thread 0, the outputs and the fused sampling.
-__device__ bool fwd_epilogue(uint8_t* smem, int OFF_A, int OFF_W1, int OFF_W2, uint32_t tmem, uint64_t* done, int r,
-                             bool live, int c, int cols, float* h1g, float* h2g, float* og, int write_hidden,
-                             const SampleArgs& sa) {
+__device__ bool fwd_epilogue(uint8_t* smem, int OFF_A, int OFF_W1, int OFF_W2, uint32_t tmem, uint64_t* done,
+                             uint32_t p0, int r, bool live, int c, int cols, float* h1g, float* h2g, float* og,
+                             int write_hidden, const SampleArgs& sa) {
   const int tid = threadIdx.x, warp = tid >> 5;
   bool ok = true;
   const uint32_t id64 = tc::idesc_bf16(TILE, 64), id16 = tc::idesc_bf16(TILE, 16);
   {
     const uint32_t trow = tmem + ((uint32_t)(warp * 32) << 16);
     uint8_t* Hs = smem + OFF_A;
-    if (!tc::mbar_wait(done, 0)) ok = false;
+    if (!tc::mbar_wait(done, p0 & 1)) ok = false;
     tc::tc_fence_after();
     float acc[64];
     for (int layer = 0; layer < 2; ++layer) {
@@ -102,7 +102,7 @@ __device__ bool fwd_epilogue(uint8_t* smem, int OFF_A, int OFF_W1, int OFF_W2, u
                          tc::sdesc_sw128(w + kb * wstride + 32 * k), layer == 0 ? id64 : id16, (kb | k) ? 1u : 0u);
         tc::mma_commit(done);
       }
-      if (!tc::mbar_wait(done, (1 + layer) & 1)) ok = false;
+      if (!tc::mbar_wait(done, (p0 + 1 + layer) & 1)) ok = false;
       tc::tc_fence_after();
     }
     float o[4];
@@ -222,8 +222,8 @@ __global__ void __launch_bounds__(FwdCfg<GROUPS>::THREADS, FwdCfg<GROUPS>::MIN_B
     tc::mma_commit(done);
   }
 
-  if (warp < 4 && !fwd_epilogue(smem, OFF_A, OFF_W1, OFF_W2, tmem, done, r, live, c, cols, h1g, h2g, og, write_hidden,
-                                  sa))
+  if (warp < 4 && !fwd_epilogue(smem, OFF_A, OFF_W1, OFF_W2, tmem, done, 0, r, live, c, cols, h1g, h2g, og,
+                                  write_hidden, sa))
     ok = false;
   tc::tc_fence_before();
   __syncthreads();
@@ -242,6 +242,11 @@ __global__ void __launch_bounds__(FwdCfg<GROUPS>::THREADS, FwdCfg<GROUPS>::MIN_B
 // Features past `in` and samples past `cols` read zero, as the register
 // path's loads do; samples of a box outside [c0, c1) are never written back.
 // The epilogues are the register path's, so both give the same bits.
+// PERSIST: CTA b takes tiles b, b + gridDim.x, ...; the rings' stages and
+// parities run on across tiles, so the TMA warp loads the next tile's first
+// boxes while warps 0-3 run this tile's epilogue. Layer 1 of the next tile
+// starts only after those warps packed its first k-block, which follows their
+// last read of this tile's accumulator; `done` completes three times a tile.
 constexpr int XS = 3, XA = 3;
 constexpr int X_BYTES = 64 * TILE * 4;
 struct TmaCfg {
@@ -258,6 +263,7 @@ struct TmaCfg {
 static_assert(TmaCfg::SMEM_BYTES <= 227 * 1024, "one CTA per SM");
 static_assert((2 * XS + 2 * XA + 1) * 8 + 4 <= 256, "barriers and the TMEM slot fit their 256 bytes");
 
+template <bool PERSIST>
 __global__ void __launch_bounds__(TmaCfg::THREADS, 1)
     k_mlp_fwd_tma(const __grid_constant__ CUtensorMap xmap, int cols, int c0, int c1, const uint4* __restrict__ w0s,
                   int kblocks, const uint4* __restrict__ w1s, const uint4* __restrict__ w2s, float* h1g, float* h2g,
@@ -275,9 +281,8 @@ __global__ void __launch_bounds__(TmaCfg::THREADS, 1)
 
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   const int r = tid & (TILE - 1);
-  const int col0 = c0 + (int)blockIdx.x * TILE;
-  const int c = col0 + r;
-  const bool live = c < c1;
+  const int tiles = (c1 - c0 + TILE - 1) / TILE;
+  const int stride = PERSIST ? (int)gridDim.x : tiles;  // one tile per CTA unless persistent
 
   if (tid == 0) {
     for (int s = 0; s < XS; ++s) {
@@ -310,60 +315,71 @@ __global__ void __launch_bounds__(TmaCfg::THREADS, 1)
 
   if (warp == 4) {
     if (lane == 0) {  // ---- X boxes ----
-      for (int kb = 0; kb < kblocks; ++kb) {
-        const int s = kb % XS, j = kb / XS;
-        if (j >= 1 && !tc::mbar_wait(&xempty[s], (j - 1) & 1)) ok = false;
-        tc::mbar_arrive_expect_tx(&xfull[s], X_BYTES);
-        tc::tma_load_2d(smem + C::OFF_X + s * X_BYTES, &xmap, col0, kb * 64, &xfull[s]);
-      }
+      uint32_t it = 0;
+      for (int tile = blockIdx.x; tile < tiles; tile += stride)
+        for (int kb = 0; kb < kblocks; ++kb, ++it) {
+          const uint32_t s = it % XS;
+          if (it >= (uint32_t)XS && !tc::mbar_wait(&xempty[s], ((it / XS) - 1) & 1)) ok = false;
+          tc::mbar_arrive_expect_tx(&xfull[s], X_BYTES);
+          tc::tma_load_2d(smem + C::OFF_X + s * X_BYTES, &xmap, c0 + tile * TILE, kb * 64, &xfull[s]);
+        }
       // no copy may still be landing in shared memory when the CTA exits
-      for (int kb = kblocks > XS ? kblocks - XS : 0; kb < kblocks; ++kb)
-        if (!tc::mbar_wait(&xfull[kb % XS], (kb / XS) & 1)) ok = false;
+      for (uint32_t k = it > (uint32_t)XS ? it - XS : 0; k < it; ++k)
+        if (!tc::mbar_wait(&xfull[k % XS], (k / XS) & 1)) ok = false;
     }
   } else if (warp == 5) {
     if (lane == 0) {  // ---- MMA issuer: layer 1 ----
       const uint32_t id64 = tc::idesc_bf16(TILE, 64);
-      for (int kb = 0; kb < kblocks; ++kb) {
-        const int a = kb % XA;
-        if (!tc::mbar_wait(&afull[a], (kb / XA) & 1)) ok = false;
-        tc::tc_fence_after();
-        const uint32_t sa_ = tc::smem_u32(smem + C::OFF_A + a * A_BYTES), sb = tc::smem_u32(smem + C::OFF_B + a * B_BYTES);
+      uint32_t it = 0;
+      for (int tile = blockIdx.x; tile < tiles; tile += stride) {
+        for (int kb = 0; kb < kblocks; ++kb, ++it) {
+          const uint32_t a = it % XA;
+          if (!tc::mbar_wait(&afull[a], (it / XA) & 1)) ok = false;
+          tc::tc_fence_after();
+          const uint32_t sa_ = tc::smem_u32(smem + C::OFF_A + a * A_BYTES);
+          const uint32_t sb = tc::smem_u32(smem + C::OFF_B + a * B_BYTES);
 #pragma unroll
-        for (int k = 0; k < 4; ++k)
-          tc::mma_bf16(tmem, tc::sdesc_sw128(sa_ + 32 * k), tc::sdesc_sw128(sb + 32 * k), id64, (kb | k) ? 1u : 0u);
-        tc::mma_commit(&aempty[a]);
+          for (int k = 0; k < 4; ++k)
+            tc::mma_bf16(tmem, tc::sdesc_sw128(sa_ + 32 * k), tc::sdesc_sw128(sb + 32 * k), id64, (kb | k) ? 1u : 0u);
+          tc::mma_commit(&aempty[a]);
+        }
+        tc::mma_commit(done);
       }
-      tc::mma_commit(done);
     }
   } else {
     // ---- warps 0-3: BF16 operands of layer 1, then the epilogues ----
     const float* X = reinterpret_cast<const float*>(smem + C::OFF_X);
-    for (int kb = 0; kb < kblocks; ++kb) {
-      const int s = kb % XS, a = kb % XA;
-      if (!tc::mbar_wait(&xfull[s], (kb / XS) & 1)) ok = false;
-      const float* box = X + s * (X_BYTES / 4);
-      float v[64];
+    uint32_t it = 0, t = 0;
+    for (int tile = blockIdx.x; tile < tiles; tile += stride, ++t) {
+      for (int kb = 0; kb < kblocks; ++kb, ++it) {
+        const uint32_t s = it % XS, a = it % XA;
+        if (!tc::mbar_wait(&xfull[s], (it / XS) & 1)) ok = false;
+        const float* box = X + s * (X_BYTES / 4);
+        float v[64];
 #pragma unroll
-      for (int q = 0; q < 64; ++q) v[q] = box[q * TILE + r];
-      tc::mbar_arrive(&xempty[s]);
-      if (kb >= XA && !tc::mbar_wait(&aempty[a], ((kb / XA) - 1) & 1)) ok = false;
-      uint8_t* A = smem + C::OFF_A + a * A_BYTES;
-      if (r == 0) {  // the stage is free: announce and start the W0 copy
-        tc::mbar_arrive_expect_tx(&afull[a], B_BYTES);
-        tc::bulk_load(smem + C::OFF_B + a * B_BYTES, w0s + (long)kb * (B_BYTES / 16), B_BYTES, &afull[a]);
-      }
+        for (int q = 0; q < 64; ++q) v[q] = box[q * TILE + r];
+        tc::mbar_arrive(&xempty[s]);
+        if (it >= (uint32_t)XA && !tc::mbar_wait(&aempty[a], ((it / XA) - 1) & 1)) ok = false;
+        uint8_t* A = smem + C::OFF_A + a * A_BYTES;
+        if (r == 0) {  // the stage is free: announce and start the W0 copy
+          tc::mbar_arrive_expect_tx(&afull[a], B_BYTES);
+          tc::bulk_load(smem + C::OFF_B + a * B_BYTES, w0s + (long)kb * (B_BYTES / 16), B_BYTES, &afull[a]);
+        }
 #pragma unroll
-      for (int q = 0; q < 8; ++q) {
-        uint4 pk = make_uint4(tc::pack_bf16(v[8 * q], v[8 * q + 1]), tc::pack_bf16(v[8 * q + 2], v[8 * q + 3]),
-                              tc::pack_bf16(v[8 * q + 4], v[8 * q + 5]), tc::pack_bf16(v[8 * q + 6], v[8 * q + 7]));
-        *reinterpret_cast<uint4*>(A + r * 128 + ((q ^ (r & 7)) << 4)) = pk;
+        for (int q = 0; q < 8; ++q) {
+          uint4 pk = make_uint4(tc::pack_bf16(v[8 * q], v[8 * q + 1]), tc::pack_bf16(v[8 * q + 2], v[8 * q + 3]),
+                                tc::pack_bf16(v[8 * q + 4], v[8 * q + 5]), tc::pack_bf16(v[8 * q + 6], v[8 * q + 7]));
+          *reinterpret_cast<uint4*>(A + r * 128 + ((q ^ (r & 7)) << 4)) = pk;
+        }
+        tc::fence_proxy_async_smem();
+        if (kb == 0 && t > 0) tc::tc_fence_before();  // after the previous tile's accumulator reads
+        tc::mbar_arrive(&afull[a]);
       }
-      tc::fence_proxy_async_smem();
-      tc::mbar_arrive(&afull[a]);
+      const int c = c0 + tile * TILE + r;
+      if (!fwd_epilogue(smem, C::OFF_A, C::OFF_W1, C::OFF_W2, tmem, done, 3 * t, r, c < c1, c, cols, h1g, h2g, og,
+                        write_hidden, sa))
+        ok = false;
     }
-    if (!fwd_epilogue(smem, C::OFF_A, C::OFF_W1, C::OFF_W2, tmem, done, r, live, c, cols, h1g, h2g, og, write_hidden,
-                      sa))
-      ok = false;
   }
   tc::tc_fence_before();
   __syncthreads();
@@ -442,13 +458,23 @@ cudaError_t launch_mlp_fwd(const float* x, int in, int cols, const uint8_t* pack
       make_tmap_f32(&xmap, x, (uint64_t)in, (uint64_t)cols, (uint64_t)cols, TILE, 64) == 0) {
     static bool configured = false;
     if (!configured) {
-      cudaError_t e = cudaFuncSetAttribute(k_mlp_fwd_tma, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                           TmaCfg::SMEM_BYTES);
-      if (e != cudaSuccess) return e;
+      for (auto* k : {k_mlp_fwd_tma<false>, k_mlp_fwd_tma<true>}) {
+        cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, TmaCfg::SMEM_BYTES);
+        if (e != cudaSuccess) return e;
+      }
       configured = true;
     }
-    k_mlp_fwd_tma<<<(c1 - c0 + TILE - 1) / TILE, TmaCfg::THREADS, TmaCfg::SMEM_BYTES, st>>>(
-        xmap, cols, c0, c1, w0, kb, w1, w2, h1, h2, o, write_hidden, sa, err);
+    int dev = 0, sms = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess)
+      sms = 0;
+    // more tiles than SMs: one persistent CTA per SM, each running ahead into its next tile
+    const int tiles = (c1 - c0 + TILE - 1) / TILE;
+    if (sms > 0 && tiles > sms)
+      k_mlp_fwd_tma<true><<<sms, TmaCfg::THREADS, TmaCfg::SMEM_BYTES, st>>>(xmap, cols, c0, c1, w0, kb, w1, w2, h1, h2,
+                                                                           o, write_hidden, sa, err);
+    else
+      k_mlp_fwd_tma<false><<<tiles, TmaCfg::THREADS, TmaCfg::SMEM_BYTES, st>>>(xmap, cols, c0, c1, w0, kb, w1, w2, h1,
+                                                                             h2, o, write_hidden, sa, err);
     return cudaGetLastError();
   }
   return fwd_launch<4>(x, in, cols, c0, c1, kb, w0, w1, w2, h1, h2, o, write_hidden, sa, err, st);

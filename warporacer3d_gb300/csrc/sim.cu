@@ -533,9 +533,12 @@ __global__ void k_pose_frames(TrackDev t, const float4* __restrict__ poses, int 
 // frame comes from the physics kernel (`ray`). Every result of a beam is the
 // reference's: its operations are the reference's, in its order, except
 // where another sequence provably gives the same bits: the nearest-cell
-// index (cell_of: one fused multiply-add, the division only near a cell
-// boundary) and floor/descent (quotient: two residual corrections of the
-// reciprocal; the guarded march divides only where min() can select it).
+// index (cell_of, and along the ray lidar_cell: one fused multiply-add, the
+// division only near a cell boundary), the probe's layer choice (lidar_probe:
+// folded into the lidar's own cells where it does not depend on the ray),
+// the probe count (dropped where its bound cannot end the march) and
+// floor/descent (quotient: two residual corrections of the reciprocal; the
+// guarded march divides only where min() can select it).
 template <int LAYERS>
 __device__ __forceinline__ void trace(const TrackDev& t, const float4* __restrict__ ray, float* obs, int n,
                                       const float2* __restrict__ beam_dir, int max_iters, int* iters, int car,

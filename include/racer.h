@@ -5,7 +5,7 @@
  * Activations (racer/ppo.mojo:47-138), Trainer (racer/ppo.mojo:141-337),
  * checkpoints (racer/ppo.mojo:341-355) and the benchmark loop's policy step
  * (main.mojo:40-48,82-92). A Mojo host binds these with `external_call`
- * through an `OwnedDLHandle` on libracer.so (INTEGRATION.md shows the shim).
+ * through an `OwnedDLHandle` on libracer.so.
  *
  * Conventions
  *  - Every function returns 0 on success and a nonzero code on failure;
@@ -161,7 +161,8 @@ int racer_policy_backward(racer_policy* policy, const float* x_dev, racer_acts* 
  * The split-K scratch is a 4.75 MiB array inside the
  * library (one per GPU, held until exit); no call allocates or frees. The
  * first call on a device resolves the array's address (make it before any
- * stream capture); calls that overlap on the GPU race on the array. */
+ * stream capture) and keeps it, so do not use it on a device after a
+ * cudaDeviceReset; calls that overlap on the GPU race on the array. */
 int racer_policy_backward_noalloc(int beams, const float* theta_dev, const float* x_dev, int cols,
                                   const float* h1_dev, const float* h2_dev, const float* d3_dev, float* d2_dev,
                                   float* d1_dev, float* grad_dev, void* stream);

@@ -5,9 +5,10 @@ and `pack`, lines 108-125) on a small seeded corridor: the YAML metadata,
 the image file and the centreline-loop extraction (skimage, absent here) are
 supplied by stand-ins, so every other line of that path runs unchanged. The
 output is occupancy_small.npz, which the tests compare with
-warporacer3d_gb300.tracks.occupancy.compile_image on the same inputs.
+the numpy restatement (tests/numpy_tracks.py), the oracle and the GPU
+compiler on the same inputs.
 
-Usage: python tests/golden/make_occupancy_golden.py [reference checkout]
+Usage: python tests/golden/make_occupancy_golden.py <reference checkout>
 """
 import sys
 import tempfile
@@ -60,4 +61,6 @@ def main(reference):
 
 
 if __name__ == "__main__":
-    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
+    if len(sys.argv) != 2:
+        sys.exit("usage: python tests/golden/make_occupancy_golden.py <reference checkout>")
+    main(sys.argv[1])

@@ -6,7 +6,9 @@ unchanged from a checkout of the reference. Its module-level imports of yaml,
 PIL and scikit-image serve only the YAML/occupancy-image path
 (racer/track.py:45-58), so they are replaced by empty stand-in modules here.
 
-Usage: python warporacer3d_gb300/tracks/make_tracks.py /root/reference
+Usage: python tests/golden/make_tracks.py <reference checkout>
+
+The arrays are written to warporacer3d_gb300/tracks/<name>.npz.
 """
 import sys
 import types
@@ -23,7 +25,7 @@ def main(reference):
     sys.path.insert(0, str(reference))
     import racer.track as track
 
-    out = Path(__file__).resolve().parent
+    out = Path(__file__).resolve().parents[2] / "warporacer3d_gb300" / "tracks"
     for name in ("flat", "ramp", "bank", "bridge"):
         array = track.load(name)
         assert array.dtype == np.float32
@@ -32,4 +34,6 @@ def main(reference):
 
 
 if __name__ == "__main__":
-    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
+    if len(sys.argv) != 2:
+        sys.exit("usage: python tests/golden/make_tracks.py <reference checkout>")
+    main(sys.argv[1])

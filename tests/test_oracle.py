@@ -163,6 +163,18 @@ def test_rmath_accuracy():
     assert np.max(np.abs(s - np.sin(xd))) < 4e-7 and np.max(np.abs(c - np.cos(xd))) < 4e-7
     big = np.abs(np.sin(xd)) > 0.1
     assert _ulps(s[big], np.sin(xd[big])).max() <= 4
+    # up to the guard (|x| <= 6426: the three-part pi/2 split is exact for every quadrant there) the
+    # reduction keeps its accuracy; past it sin and cos are NaN rather than silently inexact
+    edge = np.concatenate([rng.uniform(-6426, 6426, 50000), np.float32(6426) - np.arange(64) * np.float32(2 ** -11),
+                           -np.float32(6426) + np.arange(64) * np.float32(2 ** -11)]).astype(np.float32)
+    se, ce = np.zeros_like(edge), np.zeros_like(edge)
+    L.orc_sincos(edge, edge.size, se, ce)
+    ed = edge.astype(np.float64)
+    assert np.max(np.abs(se - np.sin(ed))) < 4e-7 and np.max(np.abs(ce - np.cos(ed))) < 4e-7
+    past = np.array([np.nextafter(np.float32(6426), np.float32(1e9)), -6500.0, 1e5, np.inf, np.nan], np.float32)
+    sp, cp = np.zeros_like(past), np.zeros_like(past)
+    L.orc_sincos(past, past.size, sp, cp)
+    assert np.isnan(sp).all() and np.isnan(cp).all()
     e_in = np.concatenate([rng.uniform(-80, 80, 100000), rng.uniform(-3, 3, 100000)]).astype(np.float32)
     e = np.zeros_like(e_in)
     L.orc_exp(e_in, e_in.size, e)

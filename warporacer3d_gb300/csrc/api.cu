@@ -1274,7 +1274,7 @@ int racer_sim_profile(racer_sim* s, const float* actions, int reps, float* physi
   RACER_TRY(cudaMalloc((void**)&total, sizeof(unsigned long long)));
   RACER_TRY(cudaMemsetAsync(total, 0, sizeof(unsigned long long), st));
   if (int rc = lidar_on(s, s->shape, s->obs, iters, st)) return rc;
-  k_sum_i32<<<152, 256, 0, st>>>(iters, (long)s->beams * s->n, total);
+  k_sum_i32<<<s->sms, 256, 0, st>>>(iters, (long)s->beams * s->n, total);
   RACER_LAUNCHED();
   unsigned long long host_total = 0;
   RACER_TRY(cudaMemcpyAsync(&host_total, total, sizeof host_total, cudaMemcpyDeviceToHost, st));
@@ -1399,7 +1399,7 @@ int racer_sim_autotune(racer_sim* s, int reps, racer_lidar_shape* best_out, floa
   RACER_TRY(cudaMemsetAsync(sums, 0, MAX_SEGMENTS * sizeof(unsigned long long), st));
   if (int rc = lidar_on(s, s->shape, s->obs, iters, st)) return rc;
   for (int k = 0; k < count; ++k)
-    k_sum_cols<<<4 * 152, 256, 0, st>>>(iters, s->n, s->beams, s->seg.car0[k], s->seg.car0[k + 1], sums + k);
+    k_sum_cols<<<4 * s->sms, 256, 0, st>>>(iters, s->n, s->beams, s->seg.car0[k], s->seg.car0[k + 1], sums + k);
   RACER_LAUNCHED();
   unsigned long long host[MAX_SEGMENTS] = {};
   RACER_TRY(cudaMemcpyAsync(host, sums, sizeof host, cudaMemcpyDeviceToHost, st));

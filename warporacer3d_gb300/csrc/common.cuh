@@ -89,6 +89,35 @@ struct LidarShape {
   int sms = 152;
 };
 
+// The current device's SM count, queried once per device (grid sizes of
+// persistent and grid-stride kernels).
+inline int device_sms() {
+  static int cache[64] = {};
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return 148;
+  if (!cache[dev]) {
+    int v = 0;
+    if (cudaDeviceGetAttribute(&v, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || v <= 0) return 148;
+    cache[dev] = v;
+  }
+  return cache[dev];
+}
+
+// Per-device one-time set-up (kernel attributes such as the dynamic shared
+// memory limit belong to each device's context): runs `setup` unless it has
+// already succeeded on the current device, as recorded in `mask`.
+template <typename F>
+cudaError_t once_per_device(unsigned long long* mask, F setup) {
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return e;
+  const unsigned long long bit = dev >= 0 && dev < 64 ? 1ull << dev : 0ull;
+  if (bit && (*mask & bit)) return cudaSuccess;
+  e = setup();
+  if (e == cudaSuccess) *mask |= bit;
+  return e;
+}
+
 }  // namespace racer
 
 // Host-side error state of the C ABI (one message per thread).

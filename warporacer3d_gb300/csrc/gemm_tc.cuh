@@ -160,17 +160,13 @@ __global__ void __launch_bounds__(GemmCfg<BN>::THREADS, 1)
   if (!ok) atomicExch(err, 1);
 }
 
-// Sets the kernel's shared-memory limit once (call before capturing a launch into a graph).
+// Sets the kernel's shared-memory limit once per device (call before capturing a launch into a graph).
 template <int BN, typename Epi>
 cudaError_t gemm_configure() {
-  static bool configured = false;
-  if (!configured) {
-    cudaError_t e =
-        cudaFuncSetAttribute(k_gemm<BN, Epi>, cudaFuncAttributeMaxDynamicSharedMemorySize, GemmCfg<BN>::SMEM);
-    if (e != cudaSuccess) return e;
-    configured = true;
-  }
-  return cudaSuccess;
+  static unsigned long long configured = 0;
+  return once_per_device(&configured, [] {
+    return cudaFuncSetAttribute(k_gemm<BN, Epi>, cudaFuncAttributeMaxDynamicSharedMemorySize, GemmCfg<BN>::SMEM);
+  });
 }
 
 // Launch over an M x N output with K = kblocks * 64 split into `splits` ranges.
@@ -180,12 +176,7 @@ cudaError_t gemm_launch(const CUtensorMap& ta, const CUtensorMap& tb, int M, int
   using C = GemmCfg<BN>;
   cudaError_t ce = gemm_configure<BN, Epi>();
   if (ce != cudaSuccess) return ce;
-  static int sms = 0;
-  if (!sms) {
-    int dev = 0;
-    cudaGetDevice(&dev);
-    if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || sms <= 0) sms = 148;
-  }
+  const int sms = device_sms();
   if (splits < 1) splits = 1;
   const int per = (kblocks + splits - 1) / splits;
   splits = (kblocks + per - 1) / per;

@@ -70,8 +70,13 @@ void launch_sgemm(const float* A, int lda, const float* B, int ldb, float* C, in
                   int squash, cudaStream_t st);
 void launch_backward(int in, const float* theta, const float* x, int cols, const float* h1, const float* h2,
                      const float* d3, float* d2, float* d1, float* grad, float* scratch, cudaStream_t st);
-size_t backward_scratch_floats(int in, int cols);
-// Scratch floats launch_backward actually touches for these sizes (<= backward_scratch_floats).
+// The FP32 weight-gradient GEMMs split K over the batch into at most SPLIT_CTAS / tiles ranges of
+// their 64 x 64 tiles. The plan is the same on every device (two CTAs for each of a GB300's 152
+// SMs), so the partial sums add in the same order everywhere and the scratch has a fixed bound.
+constexpr int SPLIT_CTAS = 2 * 152;
+constexpr size_t BACKWARD_SCRATCH_FLOATS = (size_t)SPLIT_CTAS * 64 * 64;
+size_t backward_scratch_floats(int in, int cols);  // BACKWARD_SCRATCH_FLOATS
+// Scratch floats launch_backward actually touches for these sizes (<= BACKWARD_SCRATCH_FLOATS).
 size_t backward_scratch_needed(int in, int cols);
 
 }  // namespace racer

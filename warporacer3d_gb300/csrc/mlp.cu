@@ -101,7 +101,7 @@ __global__ void k_tanh_mask(float* out, const float* h, long count) {
 
 int splits_for(int K, int tiles) {
   // enough blocks to fill the GPU, at least 512 K per split
-  int want = std::max(1, 2 * 152 / std::max(1, tiles));
+  int want = std::max(1, SPLIT_CTAS / std::max(1, tiles));
   int most = std::max(1, K / 512);
   return std::min(want, most);
 }
@@ -129,11 +129,12 @@ void launch_sgemm(const float* A, int lda, const float* B, int ldb, float* C, in
   sgemm(A, lda, 0, B, ldb, 0, C, ldc, M, N, K, squash, nullptr, st);
 }
 
-// Split-K partials: splits * tiles <= 2 * 152 and every tile is at most 64 x 64.
+// Split-K partials: splits * tiles <= SPLIT_CTAS and every tile is at most 64 x 64.
+static_assert(BM == 64 && BN == 64, "BACKWARD_SCRATCH_FLOATS assumes 64 x 64 tiles");
 size_t backward_scratch_floats(int in, int cols) {
   (void)in;
   (void)cols;
-  return (size_t)2 * 152 * BM * BN;
+  return BACKWARD_SCRATCH_FLOATS;
 }
 
 // Floats of split-K partials one weight-gradient GEMM [M, N] over K uses (0 when unsplit).

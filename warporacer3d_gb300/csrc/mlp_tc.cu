@@ -424,7 +424,7 @@ void launch_pack_weights(const float* theta, int in, uint8_t* pack, cudaStream_t
   auto* w0 = reinterpret_cast<__nv_bfloat16*>(pack);
   auto* w1 = reinterpret_cast<__nv_bfloat16*>(pack + (size_t)kb * 8192);
   auto* w2 = reinterpret_cast<__nv_bfloat16*>(pack + (size_t)kb * 8192 + 2 * 8192);
-  k_pack_weights<<<152, 256, 0, st>>>(theta, in, kb, w0, w1, w2);
+  k_pack_weights<<<device_sms(), 256, 0, st>>>(theta, in, kb, w0, w1, w2);
 }
 
 template <int GROUPS>
@@ -432,12 +432,11 @@ static cudaError_t fwd_launch(const float* x, int in, int cols, int c0, int c1, 
                               const uint4* w1, const uint4* w2, float* h1, float* h2, float* o, int write_hidden,
                               const SampleArgs& sa, int* err, cudaStream_t st) {
   using C = FwdCfg<GROUPS>;
-  static bool configured = false;
-  if (!configured) {
-    cudaError_t e = cudaFuncSetAttribute(k_mlp_fwd<GROUPS>, cudaFuncAttributeMaxDynamicSharedMemorySize, C::SMEM_BYTES);
-    if (e != cudaSuccess) return e;
-    configured = true;
-  }
+  static unsigned long long configured = 0;  // per device
+  cudaError_t e = once_per_device(&configured, [] {
+    return cudaFuncSetAttribute(k_mlp_fwd<GROUPS>, cudaFuncAttributeMaxDynamicSharedMemorySize, C::SMEM_BYTES);
+  });
+  if (e != cudaSuccess) return e;
   if (c1 <= c0) return cudaSuccess;
   k_mlp_fwd<GROUPS><<<(c1 - c0 + TILE - 1) / TILE, C::THREADS, C::SMEM_BYTES, st>>>(x, in, cols, c0, c1, w0, kb, w1, w2,
                                                                                   h1, h2, o, write_hidden, sa, err);
@@ -456,17 +455,16 @@ cudaError_t launch_mlp_fwd(const float* x, int in, int cols, const uint8_t* pack
   CUtensorMap xmap;
   if (c1 > c0 && (cols & 3) == 0 && (c0 & 3) == 0 && (reinterpret_cast<uintptr_t>(x) & 15) == 0 &&
       make_tmap_f32(&xmap, x, (uint64_t)in, (uint64_t)cols, (uint64_t)cols, TILE, 64) == 0) {
-    static bool configured = false;
-    if (!configured) {
+    static unsigned long long configured = 0;  // per device
+    cudaError_t e = once_per_device(&configured, [] {
       for (auto* k : {k_mlp_fwd_tma<false>, k_mlp_fwd_tma<true>}) {
-        cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, TmaCfg::SMEM_BYTES);
-        if (e != cudaSuccess) return e;
+        cudaError_t a = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, TmaCfg::SMEM_BYTES);
+        if (a != cudaSuccess) return a;
       }
-      configured = true;
-    }
-    int dev = 0, sms = 0;
-    if (cudaGetDevice(&dev) != cudaSuccess || cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess)
-      sms = 0;
+      return cudaSuccess;
+    });
+    if (e != cudaSuccess) return e;
+    const int sms = device_sms();
     // more tiles than SMs: one persistent CTA per SM, each running ahead into its next tile
     const int tiles = (c1 - c0 + TILE - 1) / TILE;
     if (sms > 0 && tiles > sms)

@@ -22,6 +22,14 @@
 //  - The first call on each device looks up the array's device address
 //    (cudaGetSymbolAddress) with that device current; make that first call
 //    before any stream capture.
+//  - That address is kept for the life of the process. A cudaDeviceReset
+//    unloads the library's device image, and the array may come back at
+//    another address: do not use this entry point on a device after resetting
+//    it.
+//  - The split plan of the GEMMs (SPLIT_CTAS in kernels.h) is the same for
+//    every size and device and bounds the partials by BACKWARD_SCRATCH_FLOATS,
+//    which the array holds (checked at compile time); the size check in the
+//    entry point restates that bound for the sizes of each call.
 #include <mutex>
 #include <string>
 #include <vector>
@@ -33,6 +41,8 @@
 namespace {
 
 constexpr size_t STATIC_SCRATCH_FLOATS = (size_t)2 * 152 * 64 * 64;
+static_assert(STATIC_SCRATCH_FLOATS >= racer::BACKWARD_SCRATCH_FLOATS,
+              "the static scratch must hold every split-K plan of launch_backward");
 
 static __device__ __align__(256) float g_static_scratch[STATIC_SCRATCH_FLOATS];
 

@@ -66,10 +66,13 @@ RM_HD float cos_kernel(float r2) {
   return 1.0f - (0.5f * r2 - (r2 * r2) * p);
 }
 
-// sin and cos of x together. Inputs with |x| > 1e5 (outside anything the
-// simulator produces) return NaN.
+// sin and cos of x together for |x| <= RM_SINCOS_MAX; larger inputs (outside
+// anything the simulator produces) and NaN return NaN. The bound keeps the
+// quadrant |k| = rint(|x| 2/pi) <= 4092 < 2^12, where k * PIO2_A and
+// k * PIO2_B are exact: beyond it the reduction would lose bits silently.
+#define RM_SINCOS_MAX 6426.0f
 RM_HD void sincosf_(float x, float* s, float* c) {
-  if (!(fabsf(x) <= 1.0e5f)) {
+  if (!(fabsf(x) <= RM_SINCOS_MAX)) {
     *s = *c = x - x + from_bits(0x7fc00000u);
     return;
   }

@@ -318,12 +318,11 @@ __global__ void __launch_bounds__(SF_THREADS, 1)
 cudaError_t surrogate_fused_launch(const CUtensorMap& tx, const CUtensorMap& tw1, const CUtensorMap& tw2,
                                    const CUtensorMap& tw3, const CUtensorMap& tw4, const FusedArgs& args, int sms,
                                    cudaStream_t st) {
-  static bool configured = false;
-  if (!configured) {
-    cudaError_t e = cudaFuncSetAttribute(k_surrogate_fused, cudaFuncAttributeMaxDynamicSharedMemorySize, SF_SMEM);
-    if (e != cudaSuccess) return e;
-    configured = true;
-  }
+  static unsigned long long configured = 0;  // per device
+  cudaError_t e = once_per_device(&configured, [] {
+    return cudaFuncSetAttribute(k_surrogate_fused, cudaFuncAttributeMaxDynamicSharedMemorySize, SF_SMEM);
+  });
+  if (e != cudaSuccess) return e;
   const int tiles = (args.n + 127) / 128;
   k_surrogate_fused<<<tiles < sms ? tiles : sms, SF_THREADS, SF_SMEM, st>>>(tx, tw1, tw2, tw3, tw4, args);
   return cudaGetLastError();

@@ -1,29 +1,29 @@
-"""Occupancy-map tracks: a seeded synthetic corridor and the compiler from a
-free-space image to the packed track array.
+"""Occupancy-map tracks: a seeded synthetic corridor, and the per-waypoint
+helpers the track compiler's host part shares with the reference.
 
 The packed format is the reference's (racer/track.py:14-19): header[12] =
 nx, ny, x0, y0, cell, waypoints, spacing, layers, slope bound, 0, 0, 0; then
 per layer clearance, height and nearest-waypoint grids of ny*nx; then the
 route as (x, y, z, heading) per waypoint.
 
-`compile_image` follows the reference's occupancy-image path
-(racer/track.py:51-58) step for step, and `pack` its packer
-(racer/track.py:108-125), with one substitution: the reference extracts the
-centreline loop with skimage's skeletonize plus a loop search
-(racer/track.py:150-202), which is not available here; the synthetic corridor
-knows its centreline analytically, so that loop is passed in directly (as
-(row, col) pixel coordinates, like the skeleton's).
+`centres`, `arc`, `resample` and `headings` are the reference's numpy
+expressions (racer/track.py:128-147), kept as they are so the compiled arrays
+are the reference's bit for bit (tracks/compile.py). The reference extracts
+an occupancy image's centreline loop with skimage's skeletonize plus a loop
+search (racer/track.py:150-202), which is not available here; the synthetic
+corridor knows its centreline analytically, so that loop is passed to the
+compiler directly (as (row, col) pixel coordinates, like the skeleton's).
 
 `synthetic` builds the 2048 x 2048 px, 0.05 m map of the batched-launch
-workload: a closed corridor whose centreline radius is a seeded, smoothed,
-random function of the polar angle, half-width 0.6-1.0 m, and eight seeded
-1.6 x 1.0 x 0.25 m ramp boxes on the floor.
+workload on the GPU (tracks/compile.py, racer_track_image): a closed
+corridor whose centreline radius is a seeded, smoothed, random function of the
+polar angle, half-width 0.6-1.0 m, and eight seeded 1.6 x 1.0 x 0.25 m ramp
+boxes on the floor.
 """
 from pathlib import Path
 
 import numpy as np
-from scipy.ndimage import distance_transform_edt, gaussian_filter, gaussian_filter1d
-from scipy.signal import savgol_filter
+from scipy.ndimage import gaussian_filter1d
 from scipy.spatial import KDTree
 
 SPACING = 0.15  # metres between waypoints (racer/track.py:32)
@@ -53,40 +53,6 @@ def headings(route):
     """Direction to the next waypoint (racer/track.py:145-147)."""
     d = np.roll(route, -1, 0) - route
     return np.arctan2(d[:, 1], d[:, 0])
-
-
-def pack(clearance, height, waypoint, route, x0, y0, cell, slope, ramps):
-    """Ramps onto the heights, off-road height fill and blur, then the flat
-    float32 array (racer/track.py:108-125). `slope` grows by height / rise
-    per ramp: it bounds the terrain gradient for the lidar march."""
-    ny, nx = clearance.shape[1:]
-    xy = centres((ny, nx), x0, y0, cell)
-    for ramp in ramps:
-        c, s = np.cos(ramp["heading"]), np.sin(ramp["heading"])
-        rx, ry = xy[:, 0] - ramp["center"][0], xy[:, 1] - ramp["center"][1]
-        u = rx * c + ry * s + ramp["length"] / 2
-        v = -rx * s + ry * c
-        rise = ramp.get("rise", ramp["length"] / 2)
-        top = ramp["height"] * np.clip(np.minimum(u, ramp["length"] - u) / rise, 0, 1)
-        height += np.where(abs(v) < ramp["width"] / 2, top, 0).reshape(ny, nx)
-        slope += ramp["height"] / rise
-    for layer in range(len(clearance)):
-        iy, ix = distance_transform_edt(clearance[layer] <= 0, return_indices=True)[1]
-        height[layer] = gaussian_filter(height[layer, iy, ix], 1.5)
-    header = [nx, ny, x0, y0, cell, len(route), arc(route)[-1] / len(route), len(clearance), slope, 0, 0, 0]
-    grids = np.stack([clearance, height, waypoint], 1).ravel()
-    tail = np.column_stack([route, headings(route)]).ravel()
-    return np.concatenate([header, grids, tail]).astype(np.float32)
-
-
-def compile_image(free, loop, x0, y0, cell, ramps=()):
-    """Free-space image (rows south to north) + centreline loop (row, col) ->
-    packed one-layer track (racer/track.py:54-58)."""
-    xy = savgol_filter(loop[:, ::-1] * cell + (x0, y0), 51, 3, axis=0, mode="wrap")
-    route = resample(np.column_stack([xy, 0 * xy[:, 0]]))
-    waypoint = KDTree(route[:, :2]).query(centres(free.shape, x0, y0, cell))[1].reshape(free.shape)
-    clearance = (distance_transform_edt(free) - distance_transform_edt(~free) - 0.5) * cell
-    return pack(clearance[None], np.zeros(free.shape)[None], waypoint[None], route, x0, y0, cell, 0, list(ramps))
 
 
 def _smooth_periodic(rng, count, sigma, knots):
@@ -132,8 +98,10 @@ def corridor(seed=0, size=2048, cell=0.05, radius=30.0, amplitude=10.0, half_wid
 
 def synthetic(seed=0, cache=True):
     """The 2048 x 2048 px, 0.05 m corridor map with 8 ramps as a packed track
-    (about 50 MB), cached under the package's build folder."""
-    path = Path(__file__).resolve().parent.parent / "_build" / f"occupancy_2048_seed{seed}.npy"
+    (about 50 MB), compiled on the GPU and cached under the package's build folder."""
+    from .compile import compile_image
+
+    path = Path(__file__).resolve().parent.parent / "_build" / f"occupancy_2048_seed{seed}_gpu.npy"
     if cache and path.exists():
         return np.load(path)
     free, loop, ramps, x0, y0 = corridor(seed)

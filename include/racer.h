@@ -167,8 +167,18 @@ int racer_policy_backward_noalloc(int beams, const float* theta_dev, const float
                                   const float* h1_dev, const float* h2_dev, const float* d3_dev, float* d2_dev,
                                   float* d1_dev, float* grad_dev, void* stream);
 /* Error word of the policy's tensor-core kernels (0 = none; nonzero when a
- * bounded wait on the tensor core timed out). Synchronises the policy's stream. */
+ * bounded wait on the tensor core timed out), read and cleared. A kernel whose
+ * wait timed out issues no further copy or MMA, lets those it issued complete,
+ * frees its tensor memory and returns; its outputs are then undefined.
+ * Synchronises the policy's stream. */
 int racer_policy_status(racer_policy* policy, int* code);
+/* Test hook for that timeout path (no counterpart in the reference): with
+ * polls > 0 the policy's later BF16 forwards launch their tensor-core kernel
+ * in a mode that issues no TMA copy, bulk copy or MMA, so nothing ever arrives
+ * on the mbarriers it waits on; each wait gives up after `polls` polls and the
+ * kernel returns through its timeout path. polls = 0 (the default) restores
+ * normal launches. Rollout graphs captured meanwhile keep the mode. */
+int racer_policy_wait_test(racer_policy* policy, int polls);
 /* save/load (racer/ppo.mojo:341-355): one float32 .npy holding [iteration, theta]. */
 int racer_policy_save(racer_policy* policy, const char* path, int iteration);
 int racer_policy_load(racer_policy* policy, const char* path, int* iteration);
@@ -335,6 +345,12 @@ int racer_rollout_kernel_count(racer_sim* sim, racer_policy* policy, racer_acts*
  * lidar pass summed over all beams. */
 int racer_sim_profile(racer_sim* sim, const float* actions_dev, int reps, float* physics_ms, float* lidar_ms,
                       int64_t* probe_iterations);
+/* The roofline of random gathers from L2 (no counterpart in the reference):
+ * times `reps` launches in which every thread of 8 CTAs per SM makes random,
+ * independent 16-byte loads (8 in flight) from a zeroed buffer of `bytes` (a
+ * power of two, 4 KB to 256 MB; L2-resident when it fits the L2), as the
+ * lidar gathers its cells, and returns the bytes loaded per second in GB/s. */
+int racer_gather_peak(size_t bytes, int reps, float* gbs);
 
 #ifdef __cplusplus
 }

@@ -247,3 +247,31 @@ def test_trainer_update_graph_matches_eager(precision):
     (ka, ta, fa, sa), (kb, tb, fb, sb) = out
     assert ka == kb
     assert np.array_equal(ta, tb) and np.array_equal(fa, fb) and np.array_equal(sa, sb)
+
+
+@pytest.mark.parametrize("beams,cols", [(1081, 4096), (1081, 65536), (1081, 1001), (108, 1000)])
+def test_forward_timeout_path(beams, cols):
+    """A bounded wait that runs out. In the test mode the forward's tensor-core kernel issues no copy
+    and no MMA, so nothing arrives on its mbarriers: every wait gives up after 2048 polls, the kernel
+    drains, frees its tensor memory and returns, and the policy's error word says so. The next
+    normal forward gives the oracle's outputs and leaves the word at 0. Covered: the TMA-staged
+    kernel (aligned columns, one tile per CTA and persistent) and the register-staged one."""
+    g, c = W.Policy(9, beams=beams), O.Policy(9, beams=beams)
+    rng = np.random.default_rng(cols)
+    x = rng.uniform(-1, 1, (beams + 5, cols)).astype(np.float32)
+    x[-1] = 1
+    xd = W.DevArray.empty(x.shape)
+    xd.write(x)
+    ga, ca = W.Activations(g, cols), O.Activations(cols)
+    assert g.status() == 0
+    g.wait_test(2048)
+    g.forward(xd, ga)
+    assert g.status() != 0, "the timed-out wait is reported"
+    assert g.status() == 0, "the status word is read and cleared"
+    g.wait_test(0)
+    g.forward(xd, ga)
+    c.forward(x, ca)
+    for name in ("h1", "h2", "o"):
+        a, b = getattr(ga, name).numpy(), getattr(ca, name)
+        assert np.all(np.abs(a - b) <= FWD_ATOL + FWD_RTOL * np.abs(b)), (name, np.abs(a - b).max())
+    assert g.status() == 0

@@ -527,3 +527,11 @@ def test_eight_segments_bit_exact():
             c.step(c.actions, c.reward, c.done, c.obs)
         gpu.step(gpu.actions, gpu.reward, gpu.done, gpu.obs)
         check_segments(gpu, cpus, f"step {step} ")
+
+
+def test_gather_peak_is_plausible():
+    """The L2 random-gather roofline: far above zero, and an L2-resident buffer gathers faster than
+    one eight times the L2's size, whose loads must come from HBM."""
+    l2 = W.gather_peak(8 << 20, 10)
+    hbm = W.gather_peak(256 << 20, 5)
+    assert 500 < hbm < l2 < 100000, (l2, hbm)

@@ -83,3 +83,11 @@ def test_segment_arguments_checked_on_host(lib):
         W.Sim.segments([track, track], [4, 0], [1, 2])
     with pytest.raises(ValueError):
         W.Sim.segments([track, track], [4], [1, 2])
+
+
+def test_gather_peak_arguments_checked_on_host(lib):
+    gbs = ctypes.c_float()
+    for size in (1000, 2048, 3 << 20, 1 << 29):
+        assert lib.racer_gather_peak(size, 3, ctypes.byref(gbs)) == 1
+        assert b"power of two" in lib.racer_last_error()
+    assert lib.racer_gather_peak(1 << 20, 0, ctypes.byref(gbs)) == 1

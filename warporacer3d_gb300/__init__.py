@@ -11,7 +11,7 @@ import numpy as np
 
 from ._lib import RacerError, load_library  # noqa: F401
 from .racer import (CRASH, STATE, TIMEOUT, Activations, DevArray, Policy, Runner, Sim, Surrogate, Trainer,  # noqa: F401
-                    load, save)
+                    gather_peak, load, save)
 
 TRACKS = Path(__file__).resolve().parent / "tracks"
 

@@ -69,6 +69,7 @@ SIGNATURES = {
     "racer_policy_backward_noalloc": [c_int, c_void_p, c_void_p, c_int, c_void_p, c_void_p, c_void_p, c_void_p,
                                       c_void_p, c_void_p, c_void_p],
     "racer_policy_status": [c_void_p, P(c_int)],
+    "racer_policy_wait_test": [c_void_p, c_int],
     "racer_policy_save": [c_void_p, ctypes.c_char_p, c_int],
     "racer_policy_load": [c_void_p, ctypes.c_char_p, P(c_int)],
     "racer_trainer_create": [c_int, c_int, c_int, c_void_p, P(c_void_p)],
@@ -101,6 +102,7 @@ SIGNATURES = {
                         c_void_p, c_void_p],
     "racer_rollout_kernel_count":[c_void_p, c_void_p, c_void_p, c_void_p, c_int, c_int, P(c_int64)],
     "racer_sim_profile": [c_void_p, c_void_p, c_int, P(c_float), P(c_float), P(c_int64)],
+    "racer_gather_peak": [c_size_t, c_int, P(c_float)],
     "racer_trainer_set_graphs": [c_void_p, c_int],
     "racer_track_ribbon": [P(ctypes.c_double)] * 4 + [c_int] + [ctypes.c_double] * 5 + [c_int, c_int,
                                                                                        P(ctypes.c_double), c_int,

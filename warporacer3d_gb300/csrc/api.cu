@@ -546,6 +546,12 @@ int racer_policy_status(racer_policy* p, int* code) {
   return policy_status(p, code);
 }
 
+int racer_policy_wait_test(racer_policy* p, int polls) {
+  RACER_ARG(p && polls >= 0, "racer_policy_wait_test: null policy or negative poll count");
+  policy_set_stall(p, (uint32_t)polls);
+  return 0;
+}
+
 int racer_policy_forward(racer_policy* p, const float* x, racer_acts* a) {
   RACER_ARG(p && x && a, "racer_policy_forward: null argument");
   return forward_on(p, x, a, policy_stream(p));
@@ -1293,6 +1299,61 @@ int racer_sim_profile(racer_sim* s, const float* actions, int reps, float* physi
   if (physics_ms) *physics_ms = (float)(phys / reps);
   if (lidar_ms) *lidar_ms = (float)(lid / reps);
   if (probe_iterations) *probe_iterations = (int64_t)host_total;
+  return 0;
+}
+
+// Random 16-byte gathers from an L2-resident buffer: every thread walks its
+// own linear congruential sequence of float4 indices (8 loads in flight),
+// the way the lidar's probes gather its cells, and folds what it read into
+// one value so no load is dead code.
+__global__ void k_gather_peak(const float4* __restrict__ buf, unsigned mask, int rounds, unsigned seed,
+                              float* sink) {
+  unsigned h[8];
+  const unsigned t = blockIdx.x * blockDim.x + threadIdx.x;
+#pragma unroll
+  for (int u = 0; u < 8; ++u) h[u] = (t * 8u + u) * 2654435761u ^ seed;
+  float acc = 0.0f;
+  for (int k = 0; k < rounds; ++k) {
+#pragma unroll
+    for (int u = 0; u < 8; ++u) {
+      h[u] = h[u] * 1664525u + 1013904223u;
+      const float4 v = __ldg(buf + ((h[u] >> 8) & mask));
+      acc += (v.x + v.y) + (v.z + v.w);
+    }
+  }
+  if (acc == -1.0f) sink[t] = acc;  // never true for the nonnegative buffer
+}
+
+int racer_gather_peak(size_t bytes, int reps, float* gbs) {
+  RACER_ARG(gbs && reps >= 1 && bytes >= 4096 && (bytes & (bytes - 1)) == 0 && bytes <= (1ull << 28),
+            "racer_gather_peak: bytes must be a power of two from 4 KB to 256 MB, reps >= 1");
+  float4* buf = nullptr;
+  float* sink = nullptr;
+  cudaStream_t st = nullptr;
+  RACER_TRY(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking));
+  RACER_TRY(cudaMalloc((void**)&buf, bytes));
+  RACER_TRY(cudaMalloc((void**)&sink, sizeof(float) * 4));
+  RACER_TRY(cudaMemsetAsync(buf, 0, bytes, st));
+  const int sms = device_sms(), blocks = sms * 8, threads = 256, rounds = 64;
+  const unsigned mask = (unsigned)(bytes / sizeof(float4)) - 1u;
+  cudaEvent_t a, b;
+  RACER_TRY(cudaEventCreate(&a));
+  RACER_TRY(cudaEventCreate(&b));
+  for (int w = 0; w < 3; ++w) k_gather_peak<<<blocks, threads, 0, st>>>(buf, mask, rounds, 17u + w, sink);
+  RACER_TRY(cudaEventRecord(a, st));
+  for (int r = 0; r < reps; ++r) k_gather_peak<<<blocks, threads, 0, st>>>(buf, mask, rounds, 101u + r, sink);
+  RACER_TRY(cudaEventRecord(b, st));
+  RACER_TRY(cudaEventSynchronize(b));
+  RACER_LAUNCHED();
+  float ms = 0.0f;
+  RACER_TRY(cudaEventElapsedTime(&ms, a, b));
+  const double loaded = (double)blocks * threads * rounds * 8 * sizeof(float4) * reps;
+  *gbs = (float)(loaded / (ms / 1000.0) / 1e9);
+  cudaEventDestroy(a);
+  cudaEventDestroy(b);
+  cudaFree(buf);
+  cudaFree(sink);
+  cudaStreamDestroy(st);
   return 0;
 }
 

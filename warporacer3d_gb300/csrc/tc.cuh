@@ -62,10 +62,30 @@ __device__ __forceinline__ void bulk_load(void* dst, const void* src, uint32_t b
 __device__ __forceinline__ void named_sync(int id, int count) {
   asm volatile("bar.sync %0, %1;" ::"r"(id), "r"(count) : "memory");
 }
+// Polls of a bounded wait in normal operation (each try_wait may also suspend
+// the thread for a system-dependent time).
+constexpr uint32_t WAIT_LIMIT = 1u << 24;
+
 // Bounded wait: false if the phase did not complete within `limit` polls.
-__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity, uint32_t limit = (1u << 24)) {
+__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity, uint32_t limit = WAIT_LIMIT) {
   for (uint32_t i = 0; i < limit; ++i)
     if (mbar_try_wait(bar, parity)) return true;
+  return false;
+}
+
+// Bounded wait of a CTA that shares an abort word in shared memory: a wait
+// that runs out of polls sets *abort, and every wait of the CTA that sees it
+// set returns false at once. A kernel stops issuing copies and MMAs once
+// *abort is set, so after one timeout no thread sits out the limit again on a
+// phase that can no longer complete; the kernel then drains what it had
+// issued (mbar_wait, not this) and returns with its error word set.
+__device__ __forceinline__ bool mbar_wait_abort(uint64_t* bar, uint32_t parity, volatile int* abort,
+                                                uint32_t limit = WAIT_LIMIT) {
+  for (uint32_t i = 0; i < limit; ++i) {
+    if (mbar_try_wait(bar, parity)) return true;
+    if (*abort) return false;
+  }
+  *abort = 1;
   return false;
 }
 

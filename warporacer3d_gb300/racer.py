@@ -231,10 +231,16 @@ class Policy:
         call("racer_policy_set_precision", self.handle, int(precision == "bf16"))
 
     def status(self):
-        """Error word of the tensor-core kernels (0 = none)."""
+        """Error word of the tensor-core kernels (0 = none), read and cleared."""
         code = ctypes.c_int()
         call("racer_policy_status", self.handle, ctypes.byref(code))
         return code.value
+
+    def wait_test(self, polls):
+        """Timeout test mode of the BF16 forward's tensor-core kernel: with polls > 0 it issues no copy
+        and no MMA, so its waits (each `polls` polls long) run out and it returns through its timeout
+        path; 0 restores normal launches."""
+        call("racer_policy_wait_test", self.handle, int(polls))
 
     def forward(self, x, acts):
         call("racer_policy_forward", self.handle, x.c, acts.handle)
@@ -391,6 +397,14 @@ class Surrogate:
         out = [ctypes.c_float() for _ in range(4)]
         call("racer_surrogate_evaluate", self.handle, batches, seed, *[ctypes.byref(o) for o in out])
         return tuple(o.value for o in out)
+
+
+def gather_peak(bytes_=8 << 20, reps=20):
+    """GB/s of random 16-byte gathers from an L2-resident buffer of `bytes_` (racer_gather_peak):
+    the roofline of the lidar's probes."""
+    gbs = ctypes.c_float()
+    call("racer_gather_peak", int(bytes_), int(reps), ctypes.byref(gbs))
+    return gbs.value
 
 
 def save(policy, path, iteration):

@@ -172,12 +172,12 @@ int racer_policy_backward_noalloc(int beams, const float* theta_dev, const float
  * frees its tensor memory and returns; its outputs are then undefined.
  * Synchronises the policy's stream. */
 int racer_policy_status(racer_policy* policy, int* code);
-/* Test hook for that timeout path (no counterpart in the reference): with
- * polls > 0 the policy's later BF16 forwards launch their tensor-core kernel
- * in a mode that issues no TMA copy, bulk copy or MMA, so nothing ever arrives
- * on the mbarriers it waits on; each wait gives up after `polls` polls and the
- * kernel returns through its timeout path. polls = 0 (the default) restores
- * normal launches. Rollout graphs captured meanwhile keep the mode. */
+/* Test of the timeout mechanism (no counterpart in the reference): launches,
+ * on the policy's stream, a one-CTA tensor-core kernel that holds tensor
+ * memory and waits on an mbarrier nothing will ever arrive on, issuing no
+ * copy, MMA or tensor-memory load. Its bounded wait gives up after `polls`
+ * (>= 1) polls, it records the timeout in the policy's error word (read by
+ * racer_policy_status), frees its tensor memory and returns. */
 int racer_policy_wait_test(racer_policy* policy, int polls);
 /* save/load (racer/ppo.mojo:341-355): one float32 .npy holding [iteration, theta]. */
 int racer_policy_save(racer_policy* policy, const char* path, int iteration);

@@ -249,13 +249,14 @@ def test_trainer_update_graph_matches_eager(precision):
     assert np.array_equal(ta, tb) and np.array_equal(fa, fb) and np.array_equal(sa, sb)
 
 
-@pytest.mark.parametrize("beams,cols", [(1081, 4096), (1081, 65536), (1081, 1001), (108, 1000)])
-def test_forward_timeout_path(beams, cols):
-    """A bounded wait that runs out. In the test mode the forward's tensor-core kernel issues no copy
-    and no MMA, so nothing arrives on its mbarriers: every wait gives up after 2048 polls, the kernel
-    drains, frees its tensor memory and returns, and the policy's error word says so. The next
-    normal forward gives the oracle's outputs and leaves the word at 0. Covered: the TMA-staged
-    kernel (aligned columns, one tile per CTA and persistent) and the register-staged one."""
+@pytest.mark.parametrize("beams,cols", [(1081, 4096), (108, 1000)])
+def test_bounded_wait_timeout_is_reported(beams, cols):
+    """A bounded wait that runs out (tests/test_mojo.mojo has no counterpart; main.mojo:61-62 is the
+    reference's error surface for a failed step). The probe is a tensor-core kernel holding tensor
+    memory whose threads wait on an mbarrier that nothing arrives on; after 2048 polls the wait gives
+    up, the kernel records the timeout in the policy's error word, frees its tensor memory and
+    returns, so the context stays usable: the status reads nonzero once (it is cleared on read), and
+    the next forward on the same stream gives the oracle's outputs with the word at 0."""
     g, c = W.Policy(9, beams=beams), O.Policy(9, beams=beams)
     rng = np.random.default_rng(cols)
     x = rng.uniform(-1, 1, (beams + 5, cols)).astype(np.float32)
@@ -265,13 +266,13 @@ def test_forward_timeout_path(beams, cols):
     ga, ca = W.Activations(g, cols), O.Activations(cols)
     assert g.status() == 0
     g.wait_test(2048)
-    g.forward(xd, ga)
-    assert g.status() != 0, "the timed-out wait is reported"
+    assert g.status() == 2, "the timed-out wait is reported"
     assert g.status() == 0, "the status word is read and cleared"
-    g.wait_test(0)
     g.forward(xd, ga)
     c.forward(x, ca)
     for name in ("h1", "h2", "o"):
         a, b = getattr(ga, name).numpy(), getattr(ca, name)
         assert np.all(np.abs(a - b) <= FWD_ATOL + FWD_RTOL * np.abs(b)), (name, np.abs(a - b).max())
     assert g.status() == 0
+    with pytest.raises(W.RacerError, match="poll count"):
+        g.wait_test(0)

@@ -547,9 +547,8 @@ int racer_policy_status(racer_policy* p, int* code) {
 }
 
 int racer_policy_wait_test(racer_policy* p, int polls) {
-  RACER_ARG(p && polls >= 0, "racer_policy_wait_test: null policy or negative poll count");
-  policy_set_stall(p, (uint32_t)polls);
-  return 0;
+  RACER_ARG(p && polls >= 1, "racer_policy_wait_test: null policy or a poll count below 1");
+  return policy_wait_probe(p, (uint32_t)polls);
 }
 
 int racer_policy_forward(racer_policy* p, const float* x, racer_acts* a) {

@@ -48,18 +48,21 @@ struct FwdCfg {
   // + barriers, + alignment slack, + 16 KB so every descriptor-addressed read stays inside the allocation
   static constexpr int SMEM_BYTES = OFF_BAR + 128 + 1024 + 16384;
   static constexpr int MIN_BLOCKS = GROUPS == 2 ? 2 : 1;
+  static_assert((2 * GROUPS + 3) * 8 + 8 <= 128, "barriers, the TMEM slot and the abort word fit their 128 bytes");
 };
 
 // Epilogues of the forward (warps 0-3: TMEM lanes 0-127 = sample rows), once
 // layer 1's accumulator is complete (`done`, completion p0): tanh, H = [h | 1 | 0]
 // as the next layer's A in stages 0-1 (the layer-1 stages, free by then),
 // layers 2 and 3 issued by thread 0, the outputs and the fused sampling.
-// After a timed-out wait (*abort set) thread 0 issues no more MMAs and the
-// waits return at once; the results are then undefined and the error word set.
+// After a timed-out wait (*abort set) thread 0 issues no more MMAs, the
+// waits return at once and no warp reads the accumulator (which no MMA may
+// have written); the results are then undefined and the error word set.
+// *issued records whether this thread issued an MMA (the drain commits only then).
 __device__ bool fwd_epilogue(uint8_t* smem, int OFF_A, int OFF_W1, int OFF_W2, uint32_t tmem, uint64_t* done,
                              uint32_t p0, int r, bool live, int c, int cols, float* h1g, float* h2g, float* og,
                              int write_hidden, const SampleArgs& sa, volatile int* abort, uint32_t limit,
-                             bool issue) {
+                             bool* issued) {
   const int tid = threadIdx.x, warp = tid >> 5;
   bool ok = true;
   const uint32_t id64 = tc::idesc_bf16(TILE, 64), id16 = tc::idesc_bf16(TILE, 16);
@@ -67,12 +70,18 @@ __device__ bool fwd_epilogue(uint8_t* smem, int OFF_A, int OFF_W1, int OFF_W2, u
     const uint32_t trow = tmem + ((uint32_t)(warp * 32) << 16);
     uint8_t* Hs = smem + OFF_A;
     if (!tc::mbar_wait_abort(done, p0 & 1, abort, limit)) ok = false;
+    __syncwarp();  // the TMEM loads are warp-collective
     tc::tc_fence_after();
     float acc[64];
     for (int layer = 0; layer < 2; ++layer) {
+      if (!__any_sync(0xffffffffu, *abort != 0)) {  // warp-uniform: the loads are warp-collective
 #pragma unroll
-      for (int q = 0; q < 4; ++q) tc::tmem_ld16(trow + 16 * q, acc + 16 * q);
-      tc::tmem_wait_ld();
+        for (int q = 0; q < 4; ++q) tc::tmem_ld16(trow + 16 * q, acc + 16 * q);
+        tc::tmem_wait_ld();
+      } else {
+#pragma unroll
+        for (int q = 0; q < 64; ++q) acc[q] = 0.0f;
+      }
 #pragma unroll
       for (int q = 0; q < 64; ++q) acc[q] = tc::tanh_fast(acc[q]);
 #pragma unroll
@@ -92,7 +101,8 @@ __device__ bool fwd_epilogue(uint8_t* smem, int OFF_A, int OFF_W1, int OFF_W2, u
       tc::fence_proxy_async_smem();
       tc::tc_fence_before();
       tc::named_sync(1, TILE);
-      if (tid == 0 && issue && !*abort) {
+      if (tid == 0 && !*abort) {
+        *issued = true;
         tc::tc_fence_after();
         const uint32_t h = tc::smem_u32(Hs);
         const uint32_t w = tc::smem_u32(smem + (layer == 0 ? OFF_W1 : OFF_W2));
@@ -106,11 +116,14 @@ __device__ bool fwd_epilogue(uint8_t* smem, int OFF_A, int OFF_W1, int OFF_W2, u
         tc::mma_commit(done);
       }
       if (!tc::mbar_wait_abort(done, (p0 + 1 + layer) & 1, abort, limit)) ok = false;
+      __syncwarp();
       tc::tc_fence_after();
     }
-    float o[4];
-    tc::tmem_ld4(trow, o);
-    tc::tmem_wait_ld();
+    float o[4] = {0.0f, 0.0f, 0.0f, 0.0f};
+    if (!__any_sync(0xffffffffu, *abort != 0)) {
+      tc::tmem_ld4(trow, o);
+      tc::tmem_wait_ld();
+    }
     if (live) {
       og[c] = o[0];
       og[(long)cols + c] = o[1];
@@ -137,8 +150,7 @@ __global__ void __launch_bounds__(FwdCfg<GROUPS>::THREADS, FwdCfg<GROUPS>::MIN_B
                                                         const uint4* __restrict__ w0s, int kblocks,
                                                         const uint4* __restrict__ w1s,
                                                         const uint4* __restrict__ w2s, float* h1g, float* h2g,
-                                                        float* og, int write_hidden, SampleArgs sa, int* err,
-                                                        uint32_t stall) {
+                                                        float* og, int write_hidden, SampleArgs sa, int* err) {
   using C = FwdCfg<GROUPS>;
   constexpr int THREADS = C::THREADS, MMA_WARP = C::MMA_WARP, OFF_A = C::OFF_A, OFF_B = C::OFF_B,
                 OFF_W1 = C::OFF_W1, OFF_W2 = C::OFF_W2, OFF_BAR = C::OFF_BAR;
@@ -148,12 +160,10 @@ __global__ void __launch_bounds__(FwdCfg<GROUPS>::THREADS, FwdCfg<GROUPS>::MIN_B
   uint64_t* full = reinterpret_cast<uint64_t*>(smem + OFF_BAR);
   uint64_t* empty = full + GROUPS;
   uint64_t* done = empty + GROUPS;
-  uint64_t* drain = done + 1;  // the MMA issuers' final commits after a timeout
-  uint32_t* tslot = reinterpret_cast<uint32_t*>(drain + 1);
-  volatile int* abort = reinterpret_cast<volatile int*>(tslot + 1);
-  // stall > 0: test mode, no MMA is issued (nothing arrives on `done` or `empty`)
-  // and every wait gives up after `stall` polls
-  const uint32_t limit = stall ? stall : tc::WAIT_LIMIT;
+  uint64_t* drain = done + 1;  // [2]: thread 0's and the MMA lane's final commits after a timeout
+  uint32_t* tslot = reinterpret_cast<uint32_t*>(drain + 2);
+  volatile int* abort = reinterpret_cast<volatile int*>(tslot + 1);  // set by a timed-out wait
+  constexpr uint32_t limit = tc::WAIT_LIMIT;
 
   const int tid = threadIdx.x, warp = tid >> 5;
   const int r = tid & (TILE - 1);  // sample row of a producer or epilogue thread
@@ -166,7 +176,8 @@ __global__ void __launch_bounds__(FwdCfg<GROUPS>::THREADS, FwdCfg<GROUPS>::MIN_B
       tc::mbar_init(&empty[g], 1);
     }
     tc::mbar_init(done, 1);
-    tc::mbar_init(drain, 2);
+    tc::mbar_init(&drain[0], 1);
+    tc::mbar_init(&drain[1], 1);
     *abort = 0;
     tc::fence_barrier_init();
   }
@@ -187,6 +198,7 @@ __global__ void __launch_bounds__(FwdCfg<GROUPS>::THREADS, FwdCfg<GROUPS>::MIN_B
   const uint32_t tmem = *tslot;
   const uint32_t id64 = tc::idesc_bf16(TILE, 64);
   bool ok = true;
+  bool issued = false;  // this thread issued an MMA
 
   if (warp < MMA_WARP) {
     // ---- producers: layer-1 operands, one k-block per group in flight ----
@@ -223,7 +235,8 @@ __global__ void __launch_bounds__(FwdCfg<GROUPS>::THREADS, FwdCfg<GROUPS>::MIN_B
     for (int kb = 0; kb < kblocks; ++kb) {
       const int g = kb % GROUPS;
       if (!tc::mbar_wait_abort(&full[g], (kb / GROUPS) & 1, abort, limit)) ok = false;
-      if (stall || *abort) continue;  // issue nothing after a timeout
+      if (*abort) continue;  // issue nothing after a timeout
+      issued = true;
       tc::tc_fence_after();
       const uint32_t a = tc::smem_u32(smem + OFF_A + g * A_BYTES), b = tc::smem_u32(smem + OFF_B + g * B_BYTES);
 #pragma unroll
@@ -231,22 +244,24 @@ __global__ void __launch_bounds__(FwdCfg<GROUPS>::THREADS, FwdCfg<GROUPS>::MIN_B
         tc::mma_bf16(tmem, tc::sdesc_sw128(a + 32 * k), tc::sdesc_sw128(b + 32 * k), id64, (kb | k) ? 1u : 0u);
       tc::mma_commit(&empty[g]);
     }
-    if (!stall && !*abort) tc::mma_commit(done);
+    if (!*abort) tc::mma_commit(done);
   }
 
   if (warp < 4 && !fwd_epilogue(smem, OFF_A, OFF_W1, OFF_W2, tmem, done, 0, r, live, c, cols, h1g, h2g, og,
-                                  write_hidden, sa, abort, limit, !stall))
+                                  write_hidden, sa, abort, limit, &issued))
     ok = false;
   tc::tc_fence_before();
   __syncthreads();
   if (*abort) {  // the MMAs issued before the timeout complete before the TMEM is freed
-    if (tid == 0 || tid == MMA_WARP * 32) {
-      tc::mma_commit(drain);
-      if (!tc::mbar_wait(drain, 0, tc::WAIT_LIMIT)) ok = false;
+    if (issued) {  // thread 0 and the MMA warp's lane 0, if they issued any, each on its own barrier
+      uint64_t* mine = &drain[tid == 0 ? 0 : 1];
+      tc::mma_commit(mine);
+      if (!tc::mbar_wait(mine, 0, tc::WAIT_LIMIT)) ok = false;
     }
     tc::tc_fence_before();
     __syncthreads();
   }
+  __syncwarp();
   if (warp == MMA_WARP) tc::tmem_dealloc(tmem, 64);
   if (!ok) atomicExch(err, 1);
 }
@@ -281,13 +296,13 @@ struct TmaCfg {
   static constexpr int SMEM_BYTES = OFF_BAR + 256 + 1024 + 16384;
 };
 static_assert(TmaCfg::SMEM_BYTES <= 227 * 1024, "one CTA per SM");
-static_assert((2 * XS + 2 * XA + 2) * 8 + 8 <= 256, "barriers, the TMEM slot and the abort word fit their 256 bytes");
+static_assert((2 * XS + 2 * XA + 3) * 8 + 8 <= 256, "barriers, the TMEM slot and the abort word fit their 256 bytes");
 
 template <bool PERSIST>
 __global__ void __launch_bounds__(TmaCfg::THREADS, 1)
     k_mlp_fwd_tma(const __grid_constant__ CUtensorMap xmap, int cols, int c0, int c1, const uint4* __restrict__ w0s,
                   int kblocks, const uint4* __restrict__ w1s, const uint4* __restrict__ w2s, float* h1g, float* h2g,
-                  float* og, int write_hidden, SampleArgs sa, int* err, uint32_t stall) {
+                  float* og, int write_hidden, SampleArgs sa, int* err) {
   using C = TmaCfg;
   extern __shared__ uint8_t smem_raw[];
   const uint32_t raw = tc::smem_u32(smem_raw);
@@ -297,12 +312,10 @@ __global__ void __launch_bounds__(TmaCfg::THREADS, 1)
   uint64_t* afull = xempty + XS;
   uint64_t* aempty = afull + XA;
   uint64_t* done = aempty + XA;
-  uint64_t* drain = done + 1;  // the MMA issuers' final commits after a timeout
-  uint32_t* tslot = reinterpret_cast<uint32_t*>(drain + 1);
-  volatile int* abort = reinterpret_cast<volatile int*>(tslot + 1);
-  // stall > 0: test mode, no TMA copy, bulk copy or MMA is issued (nothing
-  // arrives on any barrier) and every wait gives up after `stall` polls
-  const uint32_t limit = stall ? stall : tc::WAIT_LIMIT;
+  uint64_t* drain = done + 1;  // [2]: thread 0's and the MMA lane's final commits after a timeout
+  uint32_t* tslot = reinterpret_cast<uint32_t*>(drain + 2);
+  volatile int* abort = reinterpret_cast<volatile int*>(tslot + 1);  // set by a timed-out wait
+  constexpr uint32_t limit = tc::WAIT_LIMIT;
 
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   const int r = tid & (TILE - 1);
@@ -319,7 +332,8 @@ __global__ void __launch_bounds__(TmaCfg::THREADS, 1)
       tc::mbar_init(&aempty[s], 1);
     }
     tc::mbar_init(done, 1);
-    tc::mbar_init(drain, 2);
+    tc::mbar_init(&drain[0], 1);
+    tc::mbar_init(&drain[1], 1);
     *abort = 0;
     tc::fence_barrier_init();
   }
@@ -339,12 +353,13 @@ __global__ void __launch_bounds__(TmaCfg::THREADS, 1)
   tc::tc_fence_after();
   const uint32_t tmem = *tslot;
   bool ok = true;
+  bool issued = false;   // this thread issued an MMA
   uint32_t w0_last = 0;  // thread 0: W0 copies issued (the stage of copy k is k % XA)
 
   if (warp == 4) {
     if (lane == 0) {  // ---- X boxes ----
       uint32_t it = 0;  // boxes issued
-      for (int tile = blockIdx.x; tile < tiles && !stall; tile += stride) {
+      for (int tile = blockIdx.x; tile < tiles; tile += stride) {
         for (int kb = 0; kb < kblocks; ++kb) {
           const uint32_t s = it % XS;
           if (it >= (uint32_t)XS && !tc::mbar_wait_abort(&xempty[s], ((it / XS) - 1) & 1, abort, limit)) ok = false;
@@ -369,7 +384,8 @@ __global__ void __launch_bounds__(TmaCfg::THREADS, 1)
         for (int kb = 0; kb < kblocks; ++kb, ++it) {
           const uint32_t a = it % XA;
           if (!tc::mbar_wait_abort(&afull[a], (it / XA) & 1, abort, limit)) ok = false;
-          if (stall || *abort) continue;  // issue nothing after a timeout
+          if (*abort) continue;  // issue nothing after a timeout
+          issued = true;
           tc::tc_fence_after();
           const uint32_t sa_ = tc::smem_u32(smem + C::OFF_A + a * A_BYTES);
           const uint32_t sb = tc::smem_u32(smem + C::OFF_B + a * B_BYTES);
@@ -378,7 +394,7 @@ __global__ void __launch_bounds__(TmaCfg::THREADS, 1)
             tc::mma_bf16(tmem, tc::sdesc_sw128(sa_ + 32 * k), tc::sdesc_sw128(sb + 32 * k), id64, (kb | k) ? 1u : 0u);
           tc::mma_commit(&aempty[a]);
         }
-        if (!stall && !*abort) tc::mma_commit(done);
+        if (!*abort) tc::mma_commit(done);
       }
     }
   } else {
@@ -396,7 +412,7 @@ __global__ void __launch_bounds__(TmaCfg::THREADS, 1)
         tc::mbar_arrive(&xempty[s]);
         if (it >= (uint32_t)XA && !tc::mbar_wait_abort(&aempty[a], ((it / XA) - 1) & 1, abort, limit)) ok = false;
         uint8_t* A = smem + C::OFF_A + a * A_BYTES;
-        if (r == 0 && !stall && !*abort) {  // the stage is free: announce and start the W0 copy
+        if (r == 0 && !*abort) {  // the stage is free: announce and start the W0 copy
           tc::mbar_arrive_expect_tx(&afull[a], B_BYTES);
           tc::bulk_load(smem + C::OFF_B + a * B_BYTES, w0s + (long)kb * (B_BYTES / 16), B_BYTES, &afull[a]);
           w0_last = it + 1;
@@ -413,7 +429,7 @@ __global__ void __launch_bounds__(TmaCfg::THREADS, 1)
       }
       const int c = c0 + tile * TILE + r;
       if (!fwd_epilogue(smem, C::OFF_A, C::OFF_W1, C::OFF_W2, tmem, done, 3 * t, r, c < c1, c, cols, h1g, h2g, og,
-                        write_hidden, sa, abort, limit, !stall))
+                        write_hidden, sa, abort, limit, &issued))
         ok = false;
     }
   }
@@ -426,13 +442,15 @@ __global__ void __launch_bounds__(TmaCfg::THREADS, 1)
     if (tid == 0)
       for (uint32_t k = w0_last > (uint32_t)XA ? w0_last - XA : 0; k < w0_last; ++k)
         if (!tc::mbar_wait(&afull[k % XA], (k / XA) & 1, tc::WAIT_LIMIT)) ok = false;
-    if (tid == 0 || tid == 5 * 32) {
-      tc::mma_commit(drain);
-      if (!tc::mbar_wait(drain, 0, tc::WAIT_LIMIT)) ok = false;
+    if (issued) {  // thread 0 and the MMA warp's lane 0, if they issued any, each on its own barrier
+      uint64_t* mine = &drain[tid == 0 ? 0 : 1];
+      tc::mma_commit(mine);
+      if (!tc::mbar_wait(mine, 0, tc::WAIT_LIMIT)) ok = false;
     }
     tc::tc_fence_before();
     __syncthreads();
   }
+  __syncwarp();
   if (warp == 5) tc::tmem_dealloc(tmem, 64);
   if (!ok) atomicExch(err, 1);
 }
@@ -462,7 +480,42 @@ __global__ void k_pack_weights(const float* __restrict__ theta, int in, int kblo
   }
 }
 
+// Timeout probe: a tensor-core kernel (it holds tensor memory) whose every
+// thread waits on an mbarrier that nothing will ever arrive on, `polls` polls
+// at most (or until another thread's wait ran out). It issues no copy, no MMA
+// and no tensor-memory load; the timed-out wait sets *err, the tensor memory
+// is freed and the kernel returns, as in the forward kernels' timeout path.
+__global__ void __launch_bounds__(128, 1) k_wait_probe(int* err, uint32_t polls) {
+  __shared__ __align__(8) uint64_t bar;
+  __shared__ uint32_t slot;
+  __shared__ int abort;
+  const int tid = threadIdx.x;
+  if (tid == 0) {
+    tc::mbar_init(&bar, 1);
+    abort = 0;
+    tc::fence_barrier_init();
+  }
+  if (tid < 32) {
+    tc::tmem_alloc(&slot, 32);
+    tc::tmem_relinquish();
+  }
+  tc::tc_fence_before();
+  __syncthreads();
+  tc::tc_fence_after();
+  const uint32_t tmem = slot;
+  const bool ok = tc::mbar_wait_abort(&bar, 0, &abort, polls);
+  tc::tc_fence_before();
+  __syncthreads();
+  if (tid < 32) tc::tmem_dealloc(tmem, 32);
+  if (!ok) atomicExch(err, 2);
+}
+
 }  // namespace
+
+cudaError_t launch_wait_probe(int* err, uint32_t polls, cudaStream_t st) {
+  k_wait_probe<<<1, 128, 0, st>>>(err, polls);
+  return cudaGetLastError();
+}
 
 size_t mlp_pack_bytes(int in) {
   int kb = (in + 63) / 64;
@@ -480,7 +533,7 @@ void launch_pack_weights(const float* theta, int in, uint8_t* pack, cudaStream_t
 template <int GROUPS>
 static cudaError_t fwd_launch(const float* x, int in, int cols, int c0, int c1, int kb, const uint4* w0,
                               const uint4* w1, const uint4* w2, float* h1, float* h2, float* o, int write_hidden,
-                              const SampleArgs& sa, int* err, cudaStream_t st, uint32_t stall) {
+                              const SampleArgs& sa, int* err, cudaStream_t st) {
   using C = FwdCfg<GROUPS>;
   static unsigned long long configured = 0;  // per device
   cudaError_t e = once_per_device(&configured, [] {
@@ -489,20 +542,18 @@ static cudaError_t fwd_launch(const float* x, int in, int cols, int c0, int c1, 
   if (e != cudaSuccess) return e;
   if (c1 <= c0) return cudaSuccess;
   k_mlp_fwd<GROUPS><<<(c1 - c0 + TILE - 1) / TILE, C::THREADS, C::SMEM_BYTES, st>>>(x, in, cols, c0, c1, w0, kb, w1, w2,
-                                                                                  h1, h2, o, write_hidden, sa, err,
-                                                                                  stall);
+                                                                                  h1, h2, o, write_hidden, sa, err);
   return cudaGetLastError();
 }
 
 cudaError_t launch_mlp_fwd(const float* x, int in, int cols, const uint8_t* pack, float* h1, float* h2, float* o,
-                           int write_hidden, const SampleArgs& sa, int* err, cudaStream_t st, int c0, int c1,
-                           uint32_t stall) {
+                           int write_hidden, const SampleArgs& sa, int* err, cudaStream_t st, int c0, int c1) {
   if (c1 < 0) c1 = cols;
   int kb = (in + 63) / 64;
   const uint4* w0 = reinterpret_cast<const uint4*>(pack);
   const uint4* w1 = reinterpret_cast<const uint4*>(pack + (size_t)kb * 8192);
   const uint4* w2 = reinterpret_cast<const uint4*>(pack + (size_t)kb * 8192 + 2 * 8192);
-  if (kb <= 4) return fwd_launch<2>(x, in, cols, c0, c1, kb, w0, w1, w2, h1, h2, o, write_hidden, sa, err, st, stall);
+  if (kb <= 4) return fwd_launch<2>(x, in, cols, c0, c1, kb, w0, w1, w2, h1, h2, o, write_hidden, sa, err, st);
   // wide inputs: X staged by TMA where its sample columns are 16-byte aligned
   CUtensorMap xmap;
   if (c1 > c0 && (cols & 3) == 0 && (c0 & 3) == 0 && (reinterpret_cast<uintptr_t>(x) & 15) == 0 &&
@@ -521,13 +572,13 @@ cudaError_t launch_mlp_fwd(const float* x, int in, int cols, const uint8_t* pack
     const int tiles = (c1 - c0 + TILE - 1) / TILE;
     if (sms > 0 && tiles > sms)
       k_mlp_fwd_tma<true><<<sms, TmaCfg::THREADS, TmaCfg::SMEM_BYTES, st>>>(xmap, cols, c0, c1, w0, kb, w1, w2, h1, h2,
-                                                                           o, write_hidden, sa, err, stall);
+                                                                           o, write_hidden, sa, err);
     else
       k_mlp_fwd_tma<false><<<tiles, TmaCfg::THREADS, TmaCfg::SMEM_BYTES, st>>>(xmap, cols, c0, c1, w0, kb, w1, w2, h1,
-                                                                             h2, o, write_hidden, sa, err, stall);
+                                                                             h2, o, write_hidden, sa, err);
     return cudaGetLastError();
   }
-  return fwd_launch<4>(x, in, cols, c0, c1, kb, w0, w1, w2, h1, h2, o, write_hidden, sa, err, st, stall);
+  return fwd_launch<4>(x, in, cols, c0, c1, kb, w0, w1, w2, h1, h2, o, write_hidden, sa, err, st);
 }
 
 }  // namespace racer

@@ -23,7 +23,6 @@ struct racer_policy {
   int* err = nullptr;        // device error word of the tensor-core kernels
   BackwardWork* work = nullptr;  // BF16 backward workspace for the last batch size
   int generation = 0;            // changes whenever precision or workspace change (captured graphs go stale)
-  uint32_t stall = 0;            // > 0: the forward's timeout test mode (racer_policy_wait_test)
   cudaStream_t st = nullptr;
   bool owned = false;
 };
@@ -91,8 +90,7 @@ int policy_forward(racer_policy* p, const float* x, int cols, float* h1, float* 
   if (c1 < 0) c1 = cols;
   if (p->bf16) {
     SampleArgs none;
-    err = launch_mlp_fwd(x, p->in, cols, p->pack, h1, h2, o, write_hidden, sa ? *sa : none, p->err, st, c0, c1,
-                         p->stall);
+    err = launch_mlp_fwd(x, p->in, cols, p->pack, h1, h2, o, write_hidden, sa ? *sa : none, p->err, st, c0, c1);
   } else {
     if (c0 != 0 || c1 != cols) {
       racer_host::set_error("policy forward: column ranges need the BF16 path");
@@ -121,7 +119,14 @@ int policy_status(racer_policy* p, int* code) {
   return 0;
 }
 
-void policy_set_stall(racer_policy* p, uint32_t polls) { p->stall = polls; }
+int policy_wait_probe(racer_policy* p, uint32_t polls) {
+  cudaError_t err = launch_wait_probe(p->err, polls, p->st);
+  if (err != cudaSuccess) {
+    racer_host::set_error(std::string("timeout probe: ") + cudaGetErrorString(err));
+    return 2;
+  }
+  return 0;
+}
 
 int policy_backward(racer_policy* p, const float* x, int cols, const float* h1, const float* h2, const float* d3,
                     float* d2, float* d1, float* grad, cudaStream_t st, const CUtensorMap* xb_map, bool dgrads_f32) {

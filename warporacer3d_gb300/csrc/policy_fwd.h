@@ -25,8 +25,8 @@ int policy_forward(racer_policy* p, const float* x, int cols, float* h1, float* 
 int policy_is_bf16(racer_policy* p);
 // Device-side error word of the tensor-core kernels (0 = none), read and cleared; synchronises.
 int policy_status(racer_policy* p, int* code);
-// polls > 0: the forward's tensor-core kernels run in their timeout test mode (launch_mlp_fwd's stall).
-void policy_set_stall(racer_policy* p, uint32_t polls);
+// The timeout probe on the policy's stream, reporting into the policy's error word.
+int policy_wait_probe(racer_policy* p, uint32_t polls);
 // xb_map (BF16 path only): x already in BF16 behind a tensor map; dgrads_f32 = false (BF16 path
 // only): d2 and d1 are not needed in FP32, see backward_tc.
 int policy_backward(racer_policy* p, const float* x, int cols, const float* h1, const float* h2, const float* d3,

@@ -237,9 +237,9 @@ class Policy:
         return code.value
 
     def wait_test(self, polls):
-        """Timeout test mode of the BF16 forward's tensor-core kernel: with polls > 0 it issues no copy
-        and no MMA, so its waits (each `polls` polls long) run out and it returns through its timeout
-        path; 0 restores normal launches."""
+        """Launch the timeout probe: a tensor-core kernel whose bounded wait (`polls` polls) on an
+        mbarrier that nothing arrives on runs out; it records the timeout in the error word (status),
+        frees its tensor memory and returns."""
         call("racer_policy_wait_test", self.handle, int(polls))
 
     def forward(self, x, acts):

@@ -121,12 +121,7 @@ __device__ __forceinline__ unsigned lidar_cell(const TrackDev& t, float vx, floa
   const float mx = vx + MAGIC, my = vy + MAGIC;
   const float rx = mx - MAGIC, ry = my - MAGIC;
   unsigned ix, iy;
-  // One compare for both coordinates. fmaxf drops a NaN operand, so a NaN v
-  // (a NaN or infinite origin or direction) can pass with the other
-  // coordinate; its index from the bits is then >= 2^22 and lands, clamped, on
-  // a border cell, which reads off the map as the division path and the
-  // reference do.
-  if (fmaxf(fabsf(vx - rx), fabsf(vy - ry)) < t.mband) {
+  if (fabsf(vx - rx) < t.mband && fabsf(vy - ry) < t.mband) {
     ix = (unsigned)__float_as_int(mx) - 0x4B400000u, iy = (unsigned)__float_as_int(my) - 0x4B400000u;
   } else {
     const float px = ox + tt * dx, py = oy + tt * dy;
@@ -658,9 +653,6 @@ __global__ void __launch_bounds__(CARS * 32, lidar_min_blocks(CARS, WIDE))
 template <int LAYERS, bool GUARD, bool COUNTED = true>
 __device__ __forceinline__ float march(const TrackDev& t, float ox, float oy, float oz, float dx, float dy, float dz,
                                        float descent, float inv_descent, int max_iters, int* count_out);
-template <int LAYERS>
-__device__ __forceinline__ float march_sloped(const TrackDev& t, float ox, float oy, float oz, float dx, float dy,
-                                              float dz, float descent, float inv_descent);
 
 template <int LAYERS>
 __device__ __forceinline__ void trace(const TrackDev& t, const float4* __restrict__ ray, float* obs, int n,
@@ -685,10 +677,7 @@ __device__ __forceinline__ void trace(const TrackDev& t, const float4* __restric
   // where the probe bound provably never ends the march first (TrackDev.free_march)
   // and no count is asked for, the loop tests tt < RANGE alone, as the reference does
   float range;
-  constexpr bool CELLS = LAYERS == 1 || LAYERS == 2;
-  if (CELLS && !iters && t.free_march && fabsf(oz) <= 1e20f && descent >= 1e-10f)
-    range = march_sloped<LAYERS>(t, ox, oy, oz, dx, dy, dz, descent, inv_descent);
-  else if (!(fabsf(oz) <= 1e20f && (descent == 0.0f || descent >= 1.17549435e-38f)))
+  if (!(fabsf(oz) <= 1e20f && (descent == 0.0f || descent >= 1.17549435e-38f)))
     range = march<LAYERS, true>(t, ox, oy, oz, dx, dy, dz, descent, inv_descent, max_iters, &count);
   else if (iters || !t.free_march)
     range = march<LAYERS, false>(t, ox, oy, oz, dx, dy, dz, descent, inv_descent, max_iters, &count);
@@ -780,49 +769,6 @@ __device__ __forceinline__ float march(const TrackDev& t, float ox, float oy, fl
   }
   *count_out = count;
   return range < 0.0f ? fminf(tt, RANGE) : range;
-}
-
-// The uncounted march on the lidar's cells (march<LAYERS, false, false>'s
-// results) for rays whose descent is at least 1e-10, every ray on a sloped
-// track. There the quotient floor / descent is finite (|floor| < 1e21), so
-// where the ray has crossed the ground (floor < 0) it is negative (or -0) and
-// step = min(clearance - cell, quotient) is below the minimum step: the test
-// step < min_step covers the ground crossing, and one exit test of two
-// compares ends the march where the reference's loop ends it. The loop is
-// unrolled by two, each copy keeping the previous probe's position and floor
-// for the interpolation.
-template <int LAYERS>
-__device__ __forceinline__ float march_sloped(const TrackDev& t, float ox, float oy, float oz, float dx, float dy,
-                                              float dz, float descent, float inv_descent) {
-  const float min_step = 0.5f * t.cell;
-  const float ax = dx * t.inv_cell, ay = dy * t.inv_cell;
-  const float bx = __fmaf_rn(ox, t.inv_cell, t.cx), by = __fmaf_rn(oy, t.inv_cell, t.cy);
-  // one probe at `at`: the floor below the ray there, the step and the next probe's position
-  auto probe_at = [&](float at, float& fl, float& step, float& next) {
-    const float pz = oz + at * dz;
-    const float2 spot =
-        lidar_probe<LAYERS>(t, __fmaf_rn(at, ax, bx), __fmaf_rn(at, ay, by), at, ox, oy, dx, dy, pz);
-    fl = (pz - spot.y) - 0.03f;
-    step = fminf(spot.x, quotient(fl, descent, inv_descent, fl * inv_descent));
-    next = at + step;
-  };
-  // the range of a march that stopped at `at` (the previous probe at `prev` with floor `prev_floor`)
-  auto finish = [&](float at, float prev, float prev_floor, float fl, float step, float next) {
-    if (fl < 0.0f) return fminf(prev + ((at - prev) * prev_floor) / (prev_floor - fl), RANGE);
-    return fminf(step < min_step ? at : next, RANGE);
-  };
-  float tt = 0.0f, last = 0.0f, last_floor = 0.0f;
-  for (;;) {
-    float fl0, step0, next0;
-    probe_at(tt, fl0, step0, next0);
-    if (!(step0 >= min_step && next0 < RANGE)) return finish(tt, last, last_floor, fl0, step0, next0);
-    float fl1, step1, next1;
-    probe_at(next0, fl1, step1, next1);
-    if (!(step1 >= min_step && next1 < RANGE)) return finish(next0, tt, fl0, fl1, step1, next1);
-    last = next0;
-    last_floor = fl1;
-    tt = next1;
-  }
 }
 
 // racer/sim.mojo:323-348. step = *step_base (if given) + step_add.

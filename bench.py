@@ -219,9 +219,10 @@ SURR_CARS, SURR_STEPS, SURR_REPS, SURR_TRAIN_STEPS = 65536, 32, 3, 80000
 SURR_LR, SURR_HUBER_M = 8e-3, 0.02
 
 
-def surrogate_section(torch, W, track, stream, flush, train_steps=SURR_TRAIN_STEPS):
+def surrogate_section(torch, W, track, stream, flush, train_steps=SURR_TRAIN_STEPS, keep=None):
     """Learned lidar on bridge at 65536 cars: exact FP32 rollout vs BF16 surrogate rollout
     (audit every 16th step, exact fallback under 0.5 m), both device-timed like `value`."""
+    keep = {} if keep is None else keep
     exact = W.Runner(track, SURR_CARS, beams=BEAMS, seed=7, stream=stream)
     learned = W.Runner(track, SURR_CARS, beams=BEAMS, seed=7, stream=stream)
     sur = W.Surrogate(learned.sim, hidden=512, batch=8192, seed=1)
@@ -251,6 +252,7 @@ def surrogate_section(torch, W, track, stream, flush, train_steps=SURR_TRAIN_STE
     exact_rate = timed(lambda t0: exact.rollout(SURR_STEPS, False, t0))
     learned_rate = timed(lambda t0: learned.rollout_surrogate(sur, SURR_STEPS, False, t0, 16, 0.5))
     mae, rmse, mx, over, fallback = sur.rollout_stats()
+    keep["surrogate"] = sur  # trained once, reused by the training section
     return {"workload": f"{TRACK}, {SURR_CARS} cars, {BEAMS} beams, {SURR_STEPS}-step rollouts",
             "exact_fp32_env_steps_per_s": exact_rate, "surrogate_bf16_env_steps_per_s": learned_rate,
             "speedup": learned_rate / exact_rate, "audit_every": 16, "fallback_m": 0.5,
@@ -261,6 +263,55 @@ def surrogate_section(torch, W, track, stream, flush, train_steps=SURR_TRAIN_STE
             "training": f"{train_steps} Adam steps x 8192 poses from 2^22 drawn over drivable cells, exact-tracer "
                         f"labels, Huber loss ({SURR_HUBER_M} m), lr {SURR_LR} cosine-decayed, {train_s:.1f} s",
             "target_mae_m": 0.02}
+
+
+SURR_TRAIN_SEEDS, SURR_TRAIN_ROLLOUT = (42, 43, 44), 32
+
+
+def surrogate_training_section(W, track, sur, iterations):
+    """PPO with the learned lidar (config 4: used in 65536-car PPO rollouts): bridge, 65536 cars x
+    32-step rollouts at 1081 beams, `iterations` iterations of rollout + GAE + update per run, three
+    seeds with exact observations and the same three with the surrogate's (audit every 16th step of
+    training, exact fallback under 0.5 m; racer/ppo.mojo:187-337 per iteration, main.mojo:54-68 loop).
+    The reward comes from the exact physics either way, so the mean reward per step of the last
+    iterations compares the policies the two kinds of observation trained."""
+    out = {"workload": f"{TRACK}, {SURR_CARS} cars x {SURR_TRAIN_ROLLOUT}-step rollouts, {BEAMS} beams, "
+                       f"{iterations} iterations, seeds {list(SURR_TRAIN_SEEDS)}; surrogate: audit every 16th "
+                       "step, fallback under 0.5 m"}
+    for mode in ("exact", "surrogate"):
+        runs = []
+        if mode == "surrogate":
+            sur.rollout_stats(reset=True)
+        for seed in SURR_TRAIN_SEEDS:
+            runner = W.Runner(track, SURR_CARS, beams=BEAMS, seed=seed, policy_seed=seed)
+            trainer = W.Trainer(SURR_CARS, beams=BEAMS, rollout=SURR_TRAIN_ROLLOUT, stream=runner.sim.stream)
+            if mode == "surrogate":
+                sur.bind(runner.sim)
+                trainer.set_surrogate(sur, audit_every=16, fallback_m=0.5)
+            rewards, kls = [], []
+            t0 = time.perf_counter()
+            for it in range(iterations):
+                rewards.append(trainer.rollout(runner.sim, runner.policy, runner.acts, it))
+                kls.append(trainer.update(runner.policy))
+            dt = time.perf_counter() - t0
+            k = max(1, min(20, iterations // 5))
+            runs.append({"seed": seed, "training_transitions_per_s": SURR_CARS * SURR_TRAIN_ROLLOUT * iterations / dt,
+                         "reward_per_step_first": float(np.mean(rewards[:k])),
+                         "reward_per_step_last": float(np.mean(rewards[-k:])), "kl_last": float(kls[-1]),
+                         "finite": bool(np.isfinite(rewards).all() and np.isfinite(kls).all()), "seconds": dt})
+            trainer.set_surrogate(None)
+            del trainer, runner
+        out[mode] = {"training_transitions_per_s": float(np.mean([r["training_transitions_per_s"] for r in runs])),
+                     "reward_per_step_last_mean": float(np.mean([r["reward_per_step_last"] for r in runs])),
+                     "reward_per_step_last_spread": float(np.ptp([r["reward_per_step_last"] for r in runs])),
+                     "runs": runs}
+        if mode == "surrogate":
+            mae, rmse, mx, over, fallback = sur.rollout_stats()
+            out[mode].update({"audited_mae_m": mae, "audited_frac_over_5cm": over, "fallback_frac": fallback})
+    last_s, last_e = out["surrogate"]["reward_per_step_last_mean"], out["exact"]["reward_per_step_last_mean"]
+    out["return_ratio_surrogate_vs_exact"] = last_s / last_e if last_e else None
+    out["speedup"] = out["surrogate"]["training_transitions_per_s"] / out["exact"]["training_transitions_per_s"]
+    return out
 
 
 BATCH_TRACKS = ("flat", "ramp", "bank", "bridge", "occupancy")
@@ -471,7 +522,12 @@ def main():
         return
     if args.surrogate_only:
         steps = args.surrogate_train_steps if args.surrogate_train_steps is not None else SURR_TRAIN_STEPS
-        print(json.dumps({"surrogate": surrogate_section(torch, W, track, stream, flush, steps)}), flush=True)
+        kept = {}
+        out = {"surrogate": surrogate_section(torch, W, track, stream, flush, steps, kept)}
+        if not args.no_training:
+            out["surrogate_training"] = surrogate_training_section(W, track, kept["surrogate"],
+                                                                   args.training_iterations)
+        print(json.dumps(out), flush=True)
         return
     runner = W.Runner(track, CARS, beams=BEAMS, seed=replica_seed(42, rank), policy_seed=42, stream=stream)
     chains, _ = runner.tune_chains(50, 3)  # rollout graph as 1-4 independent chains over car ranges
@@ -569,7 +625,13 @@ def main():
     if single and not args.no_surrogate:
         del runner
         steps = args.surrogate_train_steps if args.surrogate_train_steps is not None else SURR_TRAIN_STEPS
-        line["surrogate"] = surrogate_section(torch, W, track, stream, flush, steps)
+        kept = {}
+        line["surrogate"] = surrogate_section(torch, W, track, stream, flush, steps, kept)
+        if not args.no_training:
+            line["surrogate_training"] = surrogate_training_section(W, track, kept["surrogate"],
+                                                                    args.training_iterations)
+            line["surrogate_training_return_ratio"] = line["surrogate_training"]["return_ratio_surrogate_vs_exact"]
+        del kept
         sur = line["surrogate"]  # the metric's second half, at the top level of the line
         line["surrogate_env_steps_per_s"] = sur["surrogate_bf16_env_steps_per_s"]
         line["surrogate_speedup"] = sur["speedup"]

@@ -185,6 +185,7 @@ int racer_policy_load(racer_policy* policy, const char* path, int* iteration);
 
 /* ---- Trainer: racer/ppo.mojo:141-337 (rollout length is a parameter) ---- */
 typedef struct racer_trainer racer_trainer;
+typedef struct racer_surrogate racer_surrogate; /* the learned lidar, declared with its functions below */
 typedef struct {
   float *obs, *actions, *logp, *value, *reward, *done, *advantage; /* rollout storage */
   float *x, *d3, *d2, *d1, *grad, *first, *second, *stats;         /* minibatch scratch (x: [4][IN, batch], the
@@ -198,6 +199,15 @@ int racer_trainer_get_buffers(racer_trainer* trainer, racer_trainer_buffers* out
 /* Trainer.rollout (racer/ppo.mojo:187-232): returns the mean reward per step. */
 int racer_trainer_rollout(racer_trainer* trainer, racer_sim* sim, racer_policy* policy, racer_acts* acts,
                           int iteration, float* mean_reward);
+/* Rollouts of racer_trainer_rollout with the learned lidar (no counterpart in
+ * the reference, whose Trainer.rollout traces every step, racer/ppo.mojo:187-232):
+ * after each physics step the lidar rows of the rollout storage come from
+ * `surrogate` (bound to the rollout's sim), every `audit_every`-th step of
+ * training (iteration * rollout + t, 0 = never) is traced exactly for all cars
+ * and its error accumulated (racer_surrogate_rollout_stats), and on the other
+ * steps each car whose smallest predicted range is below `fallback_m` metres is
+ * traced exactly. surrogate = NULL restores exact tracing. */
+int racer_trainer_set_surrogate(racer_trainer* trainer, racer_surrogate* surrogate, int audit_every, float fallback_m);
 /* Trainer.update (racer/ppo.mojo:234-257): returns the last minibatch's KL estimate. */
 int racer_trainer_update(racer_trainer* trainer, racer_policy* policy, float* kl);
 /* Updates replay one captured CUDA graph per policy (taken on the update after
@@ -247,7 +257,6 @@ int racer_runner_audit_dynamics(racer_sim* sim, racer_policy* policy, racer_acts
 
 /* ---- learned lidar surrogate (no counterpart in the reference; replaces
  * racer/sim.mojo:238-266's tracing during rollouts, audited by it) ---- */
-typedef struct racer_surrogate racer_surrogate;
 /* MLP from the lidar frame (origin x, y, z; sin/cos heading; layer one-hot;
  * constant 1; fixed Fourier features of x, y, z and heading: 64 inputs)
  * through three tanh layers of `hidden` (128, 256 or 512) to the sim's
@@ -273,6 +282,10 @@ int racer_surrogate_train(racer_surrogate* surrogate, int steps, float lr, float
 /* Training loss: huber_m = 0 (the default) is the squared range error; > 0 the
  * Huber loss with that threshold in metres (gradient clamped beyond it). */
 int racer_surrogate_set_loss(racer_surrogate* surrogate, float huber_m);
+/* Use the surrogate with another sim on the same track array (same header,
+ * length and beam count), for example a trained surrogate driving training
+ * runs of several seeds; drops the old sim's learned-lidar rollout graphs. */
+int racer_surrogate_bind(racer_surrogate* surrogate, racer_sim* sim);
 /* Rollout inference of a 512-wide surrogate: 1 (the default) = one fused
  * kernel (all four layers per tile of 128 cars, activations kept on chip);
  * 0 = four GEMM launches. Both give the same bits. Drops captured rollout graphs. */

@@ -244,3 +244,74 @@ def test_label_cache_serves_the_traced_labels():
         lab = W.DevArray.empty((1081, 1024))
         sur.gradient(b * 1024, lab)  # traced again, no cache
         assert np.array_equal(lab.numpy(), first[b]) and np.array_equal(again[b], first[b])
+
+
+def test_training_with_surrogate_audited_every_step_equals_exact_training():
+    """Trainer.rollout (racer/ppo.mojo:187-232) with the learned lidar audited on every step: the
+    exact tracer rewrites every car's ranges in rollout storage, so two iterations of rollout and
+    update equal exact training bit for bit (storage, advantages, parameters)."""
+    track = W.track("bridge")
+    n, beams, R = 512, 1081, 8
+    runs = [W.Runner(track, n, beams=beams, seed=3, policy_seed=5) for _ in range(2)]
+    trainers = [W.Trainer(n, beams=beams, rollout=R, stream=r.sim.stream) for r in runs]
+    sur = W.Surrogate(runs[1].sim, hidden=512, batch=1024, seed=1)
+    trainers[1].set_surrogate(sur, audit_every=1, fallback_m=0.5)
+    for it in range(2):
+        rewards = [t.rollout(r.sim, r.policy, r.acts, it) for t, r in zip(trainers, runs)]
+        assert rewards[0] == rewards[1]
+        for name in ("obs", "actions", "reward", "done", "value", "advantage"):
+            assert np.array_equal(getattr(trainers[0], name).numpy(), getattr(trainers[1], name).numpy()), name
+        kls = [t.update(r.policy) for t, r in zip(trainers, runs)]
+        assert kls[0] == kls[1]
+        assert np.array_equal(runs[0].policy.theta.numpy(), runs[1].policy.theta.numpy())
+    mae, rmse, mx, over, fb = sur.rollout_stats()
+    assert mae > 0 and rmse >= mae and fb == 0.0  # every step audited: no fallback steps
+
+
+def test_training_with_surrogate_audits_and_fallback():
+    """Surrogate rollouts in training with an audit every 4th step and the 0.5 m fallback: finite
+    rewards, the audited error and fallback fraction accumulate, and the audited steps' ranges in
+    rollout storage are the exact tracer's."""
+    track = W.track("bridge")
+    n, beams, R = 1024, 1081, 8
+    run = W.Runner(track, n, beams=beams, seed=5)
+    ref = W.Runner(track, n, beams=beams, seed=5)
+    sur = W.Surrogate(run.sim, hidden=512, batch=1024, seed=2)
+    sur.set_poses(1 << 14, seed=3)
+    sur.train(200, lr=2e-3)
+    trainer = W.Trainer(n, beams=beams, rollout=R, stream=run.sim.stream)
+    trainer.set_surrogate(sur, audit_every=4, fallback_m=0.5)
+    sur.rollout_stats(reset=True)
+    reward = trainer.rollout(run.sim, run.policy, run.acts, 0)
+    assert np.isfinite(reward)
+    mae, rmse, mx, over, fb = sur.rollout_stats()
+    assert 0 < mae < 5 and rmse >= mae and 0 <= fb <= 1
+    # steps 0 and 4 were audited: storage rows t + 1 = 1, 5 hold the exact ranges of the frames the
+    # physics wrote; retrace those frames with an exact sim stepped on the same actions
+    obs = trainer.obs.numpy()
+    actions = trainer.actions.numpy()
+    ref_obs = []
+    for t in range(R):
+        ref.sim.actions.write(actions[t])
+        ref.sim.step(ref.sim.actions, ref.sim.reward, ref.sim.done, ref.sim.obs)
+        ref_obs.append(ref.sim.obs.numpy())
+    for t in (0, 4):
+        assert np.array_equal(obs[t + 1], ref_obs[t]), t
+    assert np.isfinite(trainer.update(run.policy))
+
+
+def test_surrogate_binds_to_sims_of_the_same_track_only():
+    track = W.track("bridge")
+    a = W.Runner(track, 256, beams=1081, seed=1)
+    b = W.Runner(track, 384, beams=1081, seed=2)
+    sur = W.Surrogate(a.sim, hidden=128, batch=1024, seed=1)
+    a.rollout_surrogate(sur, 2, audit_every=1)
+    sur.bind(b.sim)
+    b.rollout_surrogate(sur, 2, audit_every=1)  # inference buffers re-sized for 384 cars
+    exact = W.Runner(track, 384, beams=1081, seed=2)
+    exact.rollout(2)
+    assert np.array_equal(b.sim.obs.numpy(), exact.sim.obs.numpy())
+    with pytest.raises(W.RacerError, match="differs"):
+        sur.bind(W.Sim(W.track("bank"), 16, 1, beams=1081))
+    with pytest.raises(W.RacerError, match="differs"):
+        sur.bind(W.Sim(track, 16, 1, beams=108))

@@ -104,6 +104,8 @@ SIGNATURES = {
     "racer_sim_profile": [c_void_p, c_void_p, c_int, P(c_float), P(c_float), P(c_int64)],
     "racer_gather_peak": [c_size_t, c_int, P(c_float)],
     "racer_trainer_set_graphs": [c_void_p, c_int],
+    "racer_trainer_set_surrogate": [c_void_p, c_void_p, c_int, c_float],
+    "racer_surrogate_bind": [c_void_p, c_void_p],
     "racer_track_ribbon": [P(ctypes.c_double)] * 4 + [c_int] + [ctypes.c_double] * 5 + [c_int, c_int,
                                                                                        P(ctypes.c_double), c_int,
                                                                                        P(c_float), c_int64, P(c_int)],

@@ -113,6 +113,10 @@ struct racer_trainer {
   int update_generation = -1;
   bool update_warm = false;
   bool graphs = true;
+  // rollouts with the learned lidar (racer_trainer_set_surrogate)
+  racer_surrogate* sur = nullptr;
+  int audit_every = 16;
+  float fallback = 0.05f;  // obs units (range / RANGE)
 };
 
 extern "C" {
@@ -745,9 +749,12 @@ int racer_trainer_rollout(racer_trainer* tr, racer_sim* s, racer_policy* p, race
   cudaStream_t st = tr->st;
   const size_t n = tr->n, IN = tr->in_rows, R = tr->rollout;
   const float* logstd = policy_theta(p) + policy_params(p) - 2;
+  if (tr->sur)
+    if (int rc = surrogate_prepare(tr->sur, s)) return rc;
   RACER_TRY(cudaMemcpyAsync(tr->obs, s->obs, IN * n * sizeof(float), cudaMemcpyDeviceToDevice, st));
   // with rollout chains (racer_sim_set_chains), each car range steps on its own stream
-  const int chains = s->chains > 1 && s->seg.count == 1 && policy_is_bf16(p) ? s->chains : 1;
+  const int chains = !tr->sur && s->chains > 1 && s->seg.count == 1 && policy_is_bf16(p) ? s->chains : 1;
+  int audits = 0;
   int bound[9];
   for (int c = 0; c <= chains; ++c) bound[c] = c == chains ? (int)n : std::min((int)n, (int)((long)n * c / chains / 128 * 128));
   if (chains > 1) {
@@ -762,6 +769,19 @@ int racer_trainer_rollout(racer_trainer* tr, racer_sim* s, racer_policy* p, race
     sa.logp = tr->logp + t * n;
     sa.value = tr->value + t * n;
     sa.step_add = (int64_t)iteration * (int64_t)R + (int64_t)t;
+    if (tr->sur) {  // physics, then the learned lidar (audited every audit_every-th step of training)
+      int rc = forward_on(p, tr->obs + t * IN * n, a, st, &sa, 0);
+      if (rc) return rc;
+      float* obs_next = tr->obs + (t + 1) * IN * n;
+      launch_advance(s->seg, s->state, tr->actions + t * 2 * n, tr->reward + t * n, tr->done + t * n, obs_next,
+                     (int)n, s->beams, s->ray, st);
+      RACER_LAUNCHED();
+      const int64_t global = (int64_t)iteration * (int64_t)R + (int64_t)t;
+      const bool audit = tr->audit_every > 0 && global % tr->audit_every == 0;
+      audits += audit;
+      if ((rc = surrogate_lidar(tr->sur, s, obs_next, audit, tr->fallback, st))) return rc;
+      continue;
+    }
     if (chains == 1) {
       int rc = forward_on(p, tr->obs + t * IN * n, a, st, &sa, 0);
       if (rc) return rc;
@@ -795,7 +815,16 @@ int racer_trainer_rollout(racer_trainer* tr, racer_sim* s, racer_policy* p, race
   float stats[STATS];
   RACER_TRY(cudaMemcpyAsync(stats, tr->stats, sizeof stats, cudaMemcpyDeviceToHost, st));
   RACER_TRY(cudaStreamSynchronize(st));
+  if (tr->sur) surrogate_account(tr->sur, s, (int)R, audits);
   if (mean_reward) *mean_reward = stats[ST_REWARD] / (float)(R * n);
+  return 0;
+}
+
+int racer_trainer_set_surrogate(racer_trainer* tr, racer_surrogate* sur, int audit_every, float fallback_m) {
+  RACER_ARG(tr && audit_every >= 0 && fallback_m >= 0.0f, "racer_trainer_set_surrogate: bad argument");
+  tr->sur = sur;
+  tr->audit_every = audit_every;
+  tr->fallback = fallback_m / RANGE;
   return 0;
 }
 

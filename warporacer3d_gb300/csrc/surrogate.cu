@@ -747,6 +747,39 @@ int racer_surrogate_set_poses(racer_surrogate* s, long count, uint64_t seed) {
   return 0;
 }
 
+// Use the surrogate with another sim of the same track (a trained surrogate
+// serving several sims, one after the other): the track's header, array
+// length and beam count must match the sim it was built for.
+int racer_surrogate_bind(racer_surrogate* s, racer_sim* sim) {
+  using racer_host::set_error;
+  if (!s || !sim) {
+    set_error("racer_surrogate_bind: null argument");
+    return 1;
+  }
+  if (sim == s->sim) return 0;
+  const TrackDev &a = s->sim->t, &b = sim->t;
+  if (sim->seg.count != 1 || sim->beams != s->L.beams || sim->track_len != s->sim->track_len || a.nx != b.nx ||
+      a.ny != b.ny || a.layers != b.layers || a.x0 != b.x0 || a.y0 != b.y0 || a.cell != b.cell ||
+      a.waypoints != b.waypoints) {
+    set_error("racer_surrogate_bind: the sim's track or beam count differs from the surrogate's");
+    return 1;
+  }
+  RACER_TRY(cudaStreamSynchronize(s->st));
+  // the old sim's learned-lidar graphs read this surrogate's inference buffers
+  for (auto& kv : s->sim->surrogate_graphs) cudaGraphExecDestroy(kv.second);
+  s->sim->surrogate_graphs.clear();
+  if (s->infer.M && s->infer.M != sim->n) {  // inference buffers are sized for the cars
+    free_acts(&s->infer);
+    s->infer = SurrogateActs();
+    for (void* p : {(void*)s->minr, (void*)s->list, (void*)s->list_count, (void*)s->list_units, (void*)s->exact})
+      cudaFree(p);
+    s->minr = nullptr, s->list = nullptr, s->list_count = nullptr, s->list_units = nullptr, s->exact = nullptr;
+  }
+  s->sim = sim;
+  s->st = sim->st;
+  return 0;
+}
+
 int racer_surrogate_set_fused(racer_surrogate* s, int fused) {
   if (!s) {
     racer_host::set_error("racer_surrogate_set_fused: null surrogate");
@@ -953,8 +986,9 @@ int surrogate_prepare(racer_surrogate* s, racer_sim* sim) {
   SURR_CHECK((gemm_configure<256, EpiInfer>()));
   if ((rc = make_acts(s, &s->infer, n, false)) || (rc = salloc(&s->minr, (size_t)n)) ||
       (rc = salloc(&s->list, (size_t)n)) || (rc = salloc(&s->list_count, 1)) || (rc = salloc(&s->list_units, 1)) ||
-      (rc = salloc(&s->exact, (size_t)(4 + sim->beams) * n)) || (rc = salloc(&s->rsums, 2)) ||
-      (rc = salloc(&s->rmax, 1)) || (rc = salloc(&s->rcount, 2)))
+      (rc = salloc(&s->exact, (size_t)(4 + sim->beams) * n)))
+    return rc;
+  if (!s->rsums && ((rc = salloc(&s->rsums, 2)) || (rc = salloc(&s->rmax, 1)) || (rc = salloc(&s->rcount, 2))))
     return rc;
   return 0;
 }

@@ -322,6 +322,13 @@ class Trainer:
         """Replay each update from one captured CUDA graph (default) or launch it eagerly."""
         call("racer_trainer_set_graphs", self.handle, int(enable))
 
+    def set_surrogate(self, surrogate, audit_every=16, fallback_m=0.5):
+        """Rollouts with the learned lidar (audit every `audit_every`-th step of training, exact fallback
+        for cars with a predicted range under `fallback_m`); None restores exact tracing."""
+        self._surrogate = surrogate  # the trainer uses it until it is replaced
+        call("racer_trainer_set_surrogate", self.handle, surrogate.handle if surrogate else None, int(audit_every),
+             float(fallback_m))
+
     def minibatch(self, policy, m, adv_mean, adv_scale):
         call("racer_trainer_minibatch", self.handle, policy.handle, m, float(adv_mean), float(adv_scale))
 
@@ -357,6 +364,11 @@ class Surrogate:
 
     def set_poses(self, count, seed=1):
         call("racer_surrogate_set_poses", self.handle, count, seed)
+
+    def bind(self, sim):
+        """Serve another sim on the same track array (same header, length and beam count)."""
+        call("racer_surrogate_bind", self.handle, sim.handle)
+        self.sim = sim
 
     def poses(self):
         p, count = ctypes.c_void_p(), ctypes.c_long()

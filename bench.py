@@ -259,7 +259,7 @@ def surrogate_section(torch, W, track, stream, flush, train_steps=SURR_TRAIN_STE
             "audited_mae_m": mae, "audited_rmse_m": rmse, "audited_max_m": mx, "audited_frac_over_5cm": over,
             "fallback_frac": fallback,
             "heldout_mae_m": heldout[0], "heldout_rmse_m": heldout[1], "heldout_frac_over_5cm": heldout[3],
-            "surrogate": "128 encoded inputs -> 3 x 512 tanh -> 1081, BF16 tcgen05, FP32 Adam",
+            "surrogate": "64 encoded inputs -> 3 x 512 tanh -> 1081, BF16 tcgen05, FP32 Adam",
             "training": f"{train_steps} Adam steps x 8192 poses from 2^22 drawn over drivable cells, exact-tracer "
                         f"labels, Huber loss ({SURR_HUBER_M} m), lr {SURR_LR} cosine-decayed, {train_s:.1f} s",
             "target_mae_m": 0.02}

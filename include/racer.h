@@ -258,14 +258,13 @@ int racer_runner_audit_dynamics(racer_sim* sim, racer_policy* policy, racer_acts
 /* ---- learned lidar surrogate (no counterpart in the reference; replaces
  * racer/sim.mojo:238-266's tracing during rollouts, audited by it) ---- */
 /* MLP from the lidar frame (origin x, y, z; sin/cos heading; layer one-hot;
- * constant 1; fixed Fourier features of x, y, z and heading harmonics up to
- * 35: 128 inputs)
+ * constant 1; fixed Fourier features of x, y, z and heading: 64 inputs)
  * through three tanh layers of `hidden` (128, 256 or 512) to the sim's
  * `beams` ranges / 10 m, for the sim's track (at most two layers).
  * `batch` (a multiple of 128) is the training batch; `seed` the init. */
 int racer_surrogate_create(racer_sim* sim, int hidden, int batch, uint64_t seed, racer_surrogate** out);
 int racer_surrogate_destroy(racer_surrogate* surrogate);
-/* FP32 master parameters W1 [H,128] | W2 [H,H] | b2 [H] | W3 [H,H] | b3 [H] |
+/* FP32 master parameters W1 [H,64] | W2 [H,H] | b2 [H] | W3 [H,H] | b3 [H] |
  * W4 [beams,H] | b4 [beams], and their last gradient (device pointers). */
 int racer_surrogate_params(racer_surrogate* surrogate, float** theta_dev, float** grad_dev, long* count, int* hidden);
 /* Training set: `count` poses (a multiple of the batch), uniform over the

@@ -3,9 +3,9 @@
 //
 // Network (one hidden width H, default 512):
 //   inputs  f = encode(x', y', z, sin h, cos h, layer): the frame itself, a
-//           constant 1 and fixed Fourier features (k_features), 128 values;
+//           constant 1 and fixed Fourier features (k_features), 64 values;
 //           (x, y, z) is the lidar origin, x', y' scaled to [-1, 1] over the map
-//   h1 = tanh(W1 f)            W1 [H, 128] (the constant input is its bias)
+//   h1 = tanh(W1 f)            W1 [H, 64] (the constant input is its bias)
 //   h2 = tanh(W2 h1 + b2)      W2 [H, H]
 //   h3 = tanh(W3 h2 + b3)      W3 [H, H]
 //   y  = W4 h3 + b4            W4 [beams, H]; y = range / RANGE per beam
@@ -42,7 +42,7 @@ using bf16 = __nv_bfloat16;
 namespace racer {
 namespace {
 
-constexpr int NIN = 128;  // encoded inputs (see k_features)
+constexpr int NIN = 64;  // encoded inputs (see k_features)
 
 struct Norm {
   float xc, inv_xs, yc, inv_ys;
@@ -208,17 +208,14 @@ struct EpiInfer {
   }
 };
 
-// ray frames [2, count] -> encoded inputs, sample-major x [count, 128] and feature-major xf [128, count]:
-//   0..7     x', y', z, sin h, cos h, [layer 0], [layer 1], 1
-//   8..51    sin/cos(2^k pi x'), sin/cos(2^k pi y') for k = 0..10  (Fourier features,
-//            Tancik et al. 2020: a plain MLP on raw coordinates fits the
-//            high-frequency range field far too slowly)
-//   52..55   sin/cos(pi z), sin/cos(2 pi z)
-//   56..123  sin/cos(j h) for j = 2..35: beam b's range is the world-frame
-//            range field at angle h + azimuth_b, so a change of heading shifts
-//            the whole profile across the outputs; harmonics up to 35 (a 10 degree
-//            period) let the network form those shifts
-//   124..127 0
+// ray frames [2, count] -> encoded inputs, sample-major x [count, 64] and feature-major xf [64, count]:
+//   0..7    x', y', z, sin h, cos h, [layer 0], [layer 1], 1
+//   8..47   sin/cos(2^k pi x'), sin/cos(2^k pi y') for k = 0..9  (Fourier features,
+//           Tancik et al. 2020: a plain MLP on raw coordinates fits the
+//           high-frequency range field far too slowly)
+//   48..55  sin/cos(j h) for j = 2..5
+//   56..59  sin/cos(pi z), sin/cos(2 pi z)
+//   60..63  0
 __device__ __forceinline__ void encode(float xn, float yn, float z, float sh, float ch, float layer, float* f) {
   f[0] = xn;
   f[1] = yn;
@@ -228,29 +225,19 @@ __device__ __forceinline__ void encode(float xn, float yn, float z, float sh, fl
   f[5] = layer == 0.0f ? 1.0f : 0.0f;
   f[6] = layer == 1.0f ? 1.0f : 0.0f;
   f[7] = 1.0f;
-  // octave k + 1 from octave k by the double-angle formulas, heading harmonic j
-  // from j - 1 by one rotation: the features are rounded to BF16 (8 bits), far
-  // coarser than the recurrences' accumulated error (about 2^-13 after ten doublings)
-  float sx, cx, sy, cy;
-  sincospif(xn, &sx, &cx);
-  sincospif(yn, &sy, &cy);
+  float scale = 1.0f;
 #pragma unroll
-  for (int k = 0; k < 11; ++k) {
-    f[8 + 4 * k] = sx, f[9 + 4 * k] = cx, f[10 + 4 * k] = sy, f[11 + 4 * k] = cy;
-    const float sx2 = 2.0f * sx * cx, cx2 = (cx - sx) * (cx + sx);
-    const float sy2 = 2.0f * sy * cy, cy2 = (cy - sy) * (cy + sy);
-    sx = sx2, cx = cx2, sy = sy2, cy = cy2;
+  for (int k = 0; k < 10; ++k) {
+    sincospif(scale * xn, &f[8 + 4 * k], &f[9 + 4 * k]);
+    sincospif(scale * yn, &f[10 + 4 * k], &f[11 + 4 * k]);
+    scale *= 2.0f;
   }
-  sincospif(z, &f[52], &f[53]);
-  sincospif(2.0f * z, &f[54], &f[55]);
-  float sj = sh, cj = ch;  // sin, cos of j h, from the frame's exact sin h and cos h
+  const float h = atan2f(sh, ch);
 #pragma unroll
-  for (int j = 2; j <= 35; ++j) {
-    const float s2 = sj * ch + cj * sh, c2 = cj * ch - sj * sh;
-    sj = s2, cj = c2;
-    f[56 + 2 * (j - 2)] = sj, f[57 + 2 * (j - 2)] = cj;
-  }
-  f[124] = f[125] = f[126] = f[127] = 0.0f;
+  for (int j = 2; j <= 5; ++j) sincosf((float)j * h, &f[48 + 2 * (j - 2)], &f[49 + 2 * (j - 2)]);
+  sincospif(z, &f[56], &f[57]);
+  sincospif(2.0f * z, &f[58], &f[59]);
+  f[60] = f[61] = f[62] = f[63] = 0.0f;
 }
 
 __global__ void k_features(const float4* __restrict__ ray, int count, Norm nm, bf16* x, bf16* xf) {
@@ -526,7 +513,7 @@ int forward(racer_surrogate* s, SurrogateActs* a, bool training, const EpiInfer*
   const int H = s->L.H, M = a->M;
   const float* th = s->theta;
   cudaStream_t st = s->st;
-  SURR_CHECK(gemm_launch<256>(a->tx, s->tw1, M, H, NIN / 64, 1, EpiTanhOut{a->h1s, H, training ? a->h1f : nullptr, M, nullptr, M, H},
+  SURR_CHECK(gemm_launch<256>(a->tx, s->tw1, M, H, 1, 1, EpiTanhOut{a->h1s, H, training ? a->h1f : nullptr, M, nullptr, M, H},
                               s->err, st));
   SURR_CHECK(gemm_launch<256>(a->th1, s->tw2, M, H, H / 64, 1,
                               EpiTanhOut{a->h2s, H, training ? a->h2f : nullptr, M, th + s->L.b2, M, H}, s->err, st));
@@ -1026,7 +1013,6 @@ int surrogate_lidar(racer_surrogate* s, racer_sim* sim, float* obs, bool audit, 
   SURR_CHECK(cudaMemsetAsync(s->minr, 0x7f, (size_t)n * sizeof(unsigned), st));
   // on an audit step the prediction goes to the scratch rows and the exact tracer writes obs
   float* pred = audit ? s->exact + 4L * n : obs + 4L * n;
-  static_assert(SF_KB1 * 64 == NIN, "the fused kernel's input block is the encoded input");
   if (s->fused && s->L.H == SF_H) {
     const float* th = s->theta;
     FusedArgs fa{th + s->L.b2, th + s->L.b3, th + s->L.b4, pred, s->minr, n, beams, (s->L.npad + 255) / 256, s->err};

@@ -4,11 +4,11 @@
 //
 // Per CTA (one per SM): warp 0 streams the weight k-blocks with TMA through a
 // ring of 32 KB stages (256 weight rows x 64 k) and loads the tile's input
-// block (two k-blocks of 64 features); warp 1 allocates all 512 TMEM columns (two 256-column slots) and
+// block; warp 1 allocates all 512 TMEM columns (two 256-column slots) and
 // issues the MMAs; warps 2-17 are the epilogue, four per TMEM lane quarter
 // (enough warps to hide the accumulator loads and tanh latencies). The A operand of every layer
 // lives in one 128 KB shared buffer (8 k-blocks of 128 rows x 64, K-major,
-// 128B-swizzled): the input block in k-blocks 0-1 for layer 1, then each hidden
+// 128B-swizzled): the input block in k-block 0 for layer 1, then each hidden
 // epilogue writes its tanh output there in BF16 as the next layer's A. The
 // output layer runs in 256-column chunks alternating between the two TMEM
 // slots, so the epilogue of one chunk (clamp, obs rows, per-car minimum)
@@ -34,15 +34,9 @@ namespace {
 
 constexpr int SF_H = 512;                      // hidden width
 constexpr int SF_KB = SF_H / 64;               // k-blocks of a hidden activation
-constexpr int SF_KB1 = 2;                      // k-blocks of the encoded input (128 features)
-constexpr int SF_E1 = 2 * SF_KB1;              // weight stages of layer 1 (two 256-row halves a k-block)
 constexpr int SF_A_BYTES = SF_KB * 128 * 128;  // 128 rows x 512 BF16
 constexpr int SF_STAGE = 256 * 128;            // 256 weight rows x 64 k (BF16)
 constexpr int SF_STAGES = 3;
-// The producer issues the tile's input block after this many of its weight
-// stages: the MMA thread waits for the input before it consumes any stage of
-// the tile, so the producer may run at most SF_STAGES - 1 stages ahead first.
-constexpr int SF_XAT = SF_E1 < SF_STAGES - 1 ? SF_E1 : SF_STAGES - 1;
 constexpr int SF_SMEM = SF_A_BYTES + SF_STAGES * SF_STAGE + 256 + 1024;  // + barriers, alignment slack
 constexpr int SF_EPI = 512;  // epilogue threads: warps 2-17
 constexpr int SF_THREADS = 64 + SF_EPI;
@@ -78,24 +72,24 @@ __device__ bool sf_producer(const CUtensorMap* tx, const CUtensorMap* tw1, const
                             const SfBars& b, int tiles, int nc, uint32_t* issued, uint32_t* xloads) {
   uint32_t it = 0, local = 0;
   for (int tile = blockIdx.x; tile < tiles; tile += gridDim.x, ++local) {
-    for (int e = 0; e < SF_E1 + 4 * SF_KB + nc * SF_KB; ++e) {
-      if (e == SF_XAT) {  // the input block, once the previous tile's output layer no longer reads A
+    for (int e = 0; e < 2 + 4 * SF_KB + nc * SF_KB; ++e) {
+      if (e == 2) {  // the input block, once the previous tile's output layer no longer reads A
         if (local > 0 && !sf_wait(b.afree, (local - 1) & 1, b.abort)) return false;
-        tc::mbar_arrive_expect_tx(b.xfull, SF_KB1 * 128 * 128);
-        for (int k = 0; k < SF_KB1; ++k) tc::tma_load_2d(abuf + k * 16384, tx, 64 * k, tile * 128, b.xfull);
+        tc::mbar_arrive_expect_tx(b.xfull, 128 * 128);
+        tc::tma_load_2d(abuf, tx, 0, tile * 128, b.xfull);
         *xloads = local + 1;
       }
       const CUtensorMap* map;
       int row, kb;
-      if (e < SF_E1) {  // k-block, then half
-        map = tw1, row = 256 * (e & 1), kb = e >> 1;
-      } else if (e < SF_E1 + 4 * SF_KB) {
-        const int f = e - SF_E1;  // layer (f / (2 KB)), then k-block, then half
+      if (e < 2) {
+        map = tw1, row = 256 * e, kb = 0;
+      } else if (e < 2 + 4 * SF_KB) {
+        const int f = e - 2;  // layer (f / (2 KB)), then k-block, then half
         map = f < 2 * SF_KB ? tw2 : tw3;
         kb = (f % (2 * SF_KB)) / 2;
         row = 256 * (f & 1);
       } else {
-        const int f = e - SF_E1 - 4 * SF_KB;  // chunk position, then k-block
+        const int f = e - 2 - 4 * SF_KB;  // chunk position, then k-block
         map = tw4, row = 256 * ((f / SF_KB + blockIdx.x % nc) % nc), kb = f % SF_KB;
       }
       const uint32_t s = it % SF_STAGES;
@@ -120,13 +114,13 @@ __device__ bool sf_mma(uint32_t tmem, uint32_t a0, uint8_t* stages, const SfBars
     }
     if (!sf_wait(b.xfull, local & 1, b.abort)) return false;
     tc::tc_fence_after();
-    for (int e = 0; e < SF_E1 + 4 * SF_KB + nc * SF_KB; ++e) {
+    for (int e = 0; e < 2 + 4 * SF_KB + nc * SF_KB; ++e) {
       uint32_t d, a;
       bool first;
-      if (e < SF_E1) {
-        d = tmem + 256 * (e & 1), a = a0 + (e >> 1) * 16384, first = (e >> 1) == 0;
-      } else if (e < SF_E1 + 4 * SF_KB) {
-        const int f = e - SF_E1;
+      if (e < 2) {
+        d = tmem + 256 * e, a = a0, first = true;
+      } else if (e < 2 + 4 * SF_KB) {
+        const int f = e - 2;
         if (f % (2 * SF_KB) == 0) {  // a new hidden layer: its A written and TMEM drained
           if (!sf_wait(b.edone, (local * 3 + f / (2 * SF_KB)) & 1, b.abort)) return false;
           tc::tc_fence_after();
@@ -134,7 +128,7 @@ __device__ bool sf_mma(uint32_t tmem, uint32_t a0, uint8_t* stages, const SfBars
         const int kb = (f % (2 * SF_KB)) / 2;
         d = tmem + 256 * (f & 1), a = a0 + kb * 16384, first = kb == 0;
       } else {
-        const int f = e - SF_E1 - 4 * SF_KB, c = f / SF_KB, kb = f % SF_KB, sl = c & 1;
+        const int f = e - 2 - 4 * SF_KB, c = f / SF_KB, kb = f % SF_KB, sl = c & 1;
         if (f == 0) {  // the last hidden layer's activations are in A
           if (!sf_wait(b.edone, (local * 3 + 2) & 1, b.abort)) return false;
           tc::tc_fence_after();
@@ -156,11 +150,11 @@ __device__ bool sf_mma(uint32_t tmem, uint32_t a0, uint8_t* stages, const SfBars
       tc::mma_commit(&b.empty[s]);
       ++it;
       // accumulators complete: after layer 1, after each hidden layer, after each output chunk
-      if (e == SF_E1 - 1 || (e >= SF_E1 && e < SF_E1 + 4 * SF_KB && (e - SF_E1) % (2 * SF_KB) == 2 * SF_KB - 1)) {
+      if (e == 1 || (e >= 2 && e < 2 + 4 * SF_KB && (e - 2) % (2 * SF_KB) == 2 * SF_KB - 1)) {
         tc::mma_commit(&b.accfull[0]);
         tc::mma_commit(&b.accfull[1]);
-      } else if (e >= SF_E1 + 4 * SF_KB && (e - SF_E1 - 4 * SF_KB) % SF_KB == SF_KB - 1) {
-        tc::mma_commit(&b.accfull[((e - SF_E1 - 4 * SF_KB) / SF_KB) & 1]);
+      } else if (e >= 2 + 4 * SF_KB && (e - 2 - 4 * SF_KB) % SF_KB == SF_KB - 1) {
+        tc::mma_commit(&b.accfull[((e - 2 - 4 * SF_KB) / SF_KB) & 1]);
       }
     }
     tc::mma_commit(b.afree);

@@ -353,7 +353,7 @@ class Surrogate:
             self.handle = None
 
     def layout(self):
-        H, beams, n = self.hidden, self.sim.beams, 128
+        H, beams, n = self.hidden, self.sim.beams, 64
         sizes = [("W1", (H, n)), ("W2", (H, H)), ("b2", (H,)), ("W3", (H, H)), ("b3", (H,)), ("W4", (beams, H)),
                  ("b4", (beams,))]
         out, off = {}, 0

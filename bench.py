@@ -217,6 +217,7 @@ def fp32_policy_section(torch, W, track, stream, flush, runner):
 
 SURR_CARS, SURR_STEPS, SURR_REPS, SURR_TRAIN_STEPS = 65536, 32, 3, 80000
 SURR_LR, SURR_HUBER_M = 8e-3, 0.02
+SPOT_STRIDE, SPOT_TOL_M = 64, 0.25
 
 
 def surrogate_section(torch, W, track, stream, flush, train_steps=SURR_TRAIN_STEPS, keep=None):
@@ -251,13 +252,24 @@ def surrogate_section(torch, W, track, stream, flush, train_steps=SURR_TRAIN_STE
 
     exact_rate = timed(lambda t0: exact.rollout(SURR_STEPS, False, t0))
     learned_rate = timed(lambda t0: learned.rollout_surrogate(sur, SURR_STEPS, False, t0, 16, 0.5))
-    mae, rmse, mx, over, fallback = sur.rollout_stats()
+    mae, rmse, mx, over, fallback = sur.rollout_stats(reset=True)
+    # the same rules plus the spot check between audits (every 64th beam, rotating, 0.25 m)
+    sur.set_spot_check(SPOT_STRIDE, SPOT_TOL_M)
+    spot_rate = timed(lambda t0: learned.rollout_surrogate(sur, SURR_STEPS, False, t0, 16, 0.5))
+    spot_stats = sur.rollout_stats(reset=True)
+    sur.set_spot_check(0, SPOT_TOL_M)
     keep["surrogate"] = sur  # trained once, reused by the training section
     return {"workload": f"{TRACK}, {SURR_CARS} cars, {BEAMS} beams, {SURR_STEPS}-step rollouts",
             "exact_fp32_env_steps_per_s": exact_rate, "surrogate_bf16_env_steps_per_s": learned_rate,
             "speedup": learned_rate / exact_rate, "audit_every": 16, "fallback_m": 0.5,
             "audited_mae_m": mae, "audited_rmse_m": rmse, "audited_max_m": mx, "audited_frac_over_5cm": over,
             "fallback_frac": fallback,
+            "spot_check": {"stride": SPOT_STRIDE, "tolerance_m": SPOT_TOL_M, "env_steps_per_s": spot_rate,
+                           "speedup": spot_rate / exact_rate, "audited_mae_m": spot_stats[0],
+                           "audited_max_m": spot_stats[2], "fallback_frac": spot_stats[4],
+                           "rule": "between audits every 64th beam of every car (offset rotating with the step) is "
+                                   "traced exactly; a car with one off by more than the tolerance, too long or too "
+                                   "short, takes the exact tracer"},
             "heldout_mae_m": heldout[0], "heldout_rmse_m": heldout[1], "heldout_frac_over_5cm": heldout[3],
             "surrogate": "64 encoded inputs -> 3 x 512 tanh -> 1081, BF16 tcgen05, FP32 Adam",
             "training": f"{train_steps} Adam steps x 8192 poses from 2^22 drawn over drivable cells, exact-tracer "
@@ -357,7 +369,11 @@ def batched_section(torch, W, stream, flush):
     for r in separate:
         r.rollout(BATCH_STEPS, False, 0)
     separate_rate, separate_ms = timed(lambda t0: [r.rollout(BATCH_STEPS, False, t0) for r in separate])
-    per_track_lidar = {name: r.profile_sim(3)[1] for name, r in zip(BATCH_TRACKS, separate)}
+    per_track_lidar, per_track_probes = {}, {}
+    for name, r, cars in zip(BATCH_TRACKS, separate, BATCH_CARS):
+        _, lid_ms, probes_k = r.profile_sim(3)
+        per_track_lidar[name] = lid_ms
+        per_track_probes[name] = probes_k / (cars * BEAMS)
     return {"workload": ", ".join(f"{n} {c}" for n, c in zip(BATCH_TRACKS, BATCH_CARS)) +
                         f" cars ({total} in all), {BEAMS} beams, {BATCH_STEPS}-step rollouts from one CUDA graph",
             "batched_env_steps_per_s": batched_rate, "batched_ms_per_env_step": batched_ms,
@@ -368,7 +384,9 @@ def batched_section(torch, W, stream, flush):
             "lidar_shape_autotuned": dict(tuned, order=[BATCH_TRACKS[k] for k in tuned["order"]], ms=tuned_ms),
             "batched_physics_ms": phys_ms, "batched_lidar_ms": lidar_ms,
             "probes_per_beam": probes / (total * BEAMS), "kernels_per_rollout": launches,
-            "separate_lidar_ms": per_track_lidar}
+            "separate_lidar_ms": per_track_lidar, "separate_probes_per_beam": per_track_probes,
+            "dominant_segment": max(per_track_lidar, key=per_track_lidar.get),
+            "dominant_share": max(per_track_lidar.values()) / sum(per_track_lidar.values())}
 
 
 TRAIN_TRACK, TRAIN_CARS, TRAIN_ROLLOUT, TRAIN_BEAMS = "bank", 16384, 64, 108

@@ -299,6 +299,13 @@ int racer_surrogate_set_label_cache(racer_surrogate* surrogate, int enable);
 int racer_surrogate_evaluate(racer_surrogate* surrogate, int batches, uint64_t seed, float* mae_m, float* rmse_m,
                              float* max_m, float* frac_over_5cm);
 
+/* Spot check between audits (no counterpart in the reference; off, stride 0,
+ * by default): on every non-audit step of a learned-lidar rollout, beams
+ * (step % stride) + k * stride of every car are traced exactly and compared
+ * with the prediction; a car with one off by more than tolerance_m metres
+ * (too long, a missed wall, as well as too short) falls back to the exact
+ * tracer for all its beams, like a car under the fallback threshold. */
+int racer_surrogate_set_spot_check(racer_surrogate* surrogate, int stride, float tolerance_m);
 /* `steps` Runner steps from one CUDA graph with the lidar rows of the
  * observations predicted by `surrogate` (built for this sim): every
  * `audit_every`-th step (0 = never) is traced exactly for all cars and the

@@ -315,3 +315,45 @@ def test_surrogate_binds_to_sims_of_the_same_track_only():
         sur.bind(W.Sim(W.track("bank"), 16, 1, beams=1081))
     with pytest.raises(W.RacerError, match="differs"):
         sur.bind(W.Sim(track, 16, 1, beams=108))
+
+
+def test_spot_check_sends_every_mismatching_car_to_the_exact_tracer():
+    """The spot check between audits. With every beam checked at a tolerance of 1 um every car of an
+    untrained surrogate mismatches, so the rollout is the exact one; with every beam checked at 0.25 m
+    no car keeps a range more than 0.25 m from the exact tracer's, while without the check (and no
+    fallback threshold) some cars do, including ranges predicted too long."""
+    track = W.track("bridge")
+    n, beams = 1024, 1081
+    exact = W.Runner(track, n, beams=beams, seed=4)
+    exact.rollout(3, False, 0)
+    run = W.Runner(track, n, beams=beams, seed=4)
+    sur = W.Surrogate(run.sim, hidden=512, batch=1024, seed=1)
+    sur.set_spot_check(1, 1e-6)
+    run.rollout_surrogate(sur, 3, False, 0, audit_every=0, fallback_m=0.0)
+    run.synchronize()
+    for name in ("state", "obs", "reward", "done", "actions"):
+        assert np.array_equal(getattr(exact.sim, name).numpy(), getattr(run.sim, name).numpy()), name
+    assert sur.rollout_stats()[4] == 1.0
+
+    ref = W.Runner(track, n, beams=beams, seed=6)
+    ref.rollout(1, False, 0)  # one step: the actions come from the (exact) reset observations
+    want = ref.sim.obs.numpy()[4:4 + beams] * 10
+    trained = W.Runner(track, n, beams=beams, seed=6)
+    sur2 = W.Surrogate(trained.sim, hidden=512, batch=1024, seed=2)
+    sur2.set_poses(1 << 14, seed=3)
+    sur2.train(300, lr=2e-3)
+    state0, obs0 = trained.sim.state.numpy(), trained.sim.obs.numpy()
+    errs, long_miss = {}, {}
+    for stride in (0, 1):
+        sur2.set_spot_check(stride, 0.25)
+        trained.sim.state.write(state0)  # both runs start from the same reset
+        trained.sim.obs.write(obs0)
+        trained.rollout_surrogate(sur2, 1, False, 0, audit_every=0, fallback_m=0.0)
+        trained.synchronize()
+        got = trained.sim.obs.numpy()[4:4 + beams] * 10
+        errs[stride] = np.abs(got - want).max(axis=0)  # per car
+        long_miss[stride] = int(((got - want) > 0.25 * 1.0001).sum())  # predicted beyond the exact range
+    assert (errs[0] > 0.25 * 1.0001).any() and long_miss[0] > 0 and long_miss[1] == 0
+    assert (errs[1] <= 0.25 * 1.0001).all()
+    with pytest.raises(W.RacerError, match="stride"):
+        sur2.set_spot_check(-1, 0.25)

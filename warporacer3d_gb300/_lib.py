@@ -87,6 +87,7 @@ SIGNATURES = {
     "racer_surrogate_create": [c_void_p, c_int, c_int, c_uint64, P(c_void_p)],
     "racer_surrogate_destroy": [c_void_p],
     "racer_surrogate_set_loss": [c_void_p, c_float],
+    "racer_surrogate_set_spot_check": [c_void_p, c_int, c_float],
     "racer_surrogate_set_fused": [c_void_p, c_int],
     "racer_surrogate_set_label_cache": [c_void_p, c_int],
     "racer_surrogate_params": [c_void_p, P(c_void_p), P(c_void_p), P(ctypes.c_long), P(c_int)],

@@ -779,7 +779,7 @@ int racer_trainer_rollout(racer_trainer* tr, racer_sim* s, racer_policy* p, race
       const int64_t global = (int64_t)iteration * (int64_t)R + (int64_t)t;
       const bool audit = tr->audit_every > 0 && global % tr->audit_every == 0;
       audits += audit;
-      if ((rc = surrogate_lidar(tr->sur, s, obs_next, audit, tr->fallback, st))) return rc;
+      if ((rc = surrogate_lidar(tr->sur, s, obs_next, audit, tr->fallback, st, nullptr, global))) return rc;
       continue;
     }
     if (chains == 1) {
@@ -985,7 +985,7 @@ static int runner_step_on(racer_sim* s, racer_policy* p, racer_acts* a, float* s
   if (!sur) return sim_step_on(s, s->actions, s->reward, s->done, s->obs, nullptr, st, eval);
   launch_advance(s->seg, s->state, s->actions, s->reward, s->done, s->obs, s->n, s->beams, s->ray, st);
   RACER_LAUNCHED();
-  return surrogate_lidar(sur, s, s->obs, audit, fallback, st);
+  return surrogate_lidar(sur, s, s->obs, audit, fallback, st, base, add);
 }
 
 int racer_rollout_surrogate(racer_sim* s, racer_policy* p, racer_acts* a, float* scratch, racer_surrogate* sur,

@@ -33,6 +33,12 @@ void launch_lidar_list(const TrackDev& t, const float4* ray, float* obs, int n, 
                        const int* list, const int* list_count, int list_max, unsigned* counter, int sms,
                        cudaStream_t st);
 bool lidar_shape_ok(const LidarShape& shape);
+// Spot check: beams (step % stride) + k stride of every car traced exactly and compared with the
+// predicted rows pred [beams, n]; cars off by more than tol (range / RANGE units) get minr = 0.
+// step = *step_base (if given, read on the device) + step_add.
+void launch_lidar_spot(const TrackDev& t, const float4* ray, const float* pred, int n, int beams,
+                       const float2* beam_dir, int stride, const int64_t* step_base, int64_t step_add, float tol,
+                       unsigned* minr, cudaStream_t st);
 // Cars whose smallest predicted range (ordered uint bits of a nonnegative float) is below threshold.
 void launch_select_cars(const unsigned* minr, int n, float threshold, int* list, int* count, cudaStream_t st);
 int lidar_max_iters(const TrackDev& t);

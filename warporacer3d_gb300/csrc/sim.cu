@@ -654,10 +654,26 @@ template <int LAYERS, bool GUARD, bool COUNTED = true>
 __device__ __forceinline__ float march(const TrackDev& t, float ox, float oy, float oz, float dx, float dy, float dz,
                                        float descent, float inv_descent, int max_iters, int* count_out);
 
+// The range of one beam (racer/sim.mojo:240-266); `count` gets its probes.
+template <int LAYERS>
+__device__ __forceinline__ float beam_range(const TrackDev& t, const float4* __restrict__ ray, int n,
+                                            const float2* __restrict__ beam_dir, int max_iters, bool counted,
+                                            int car, int beam, int* count_out);
+
 template <int LAYERS>
 __device__ __forceinline__ void trace(const TrackDev& t, const float4* __restrict__ ray, float* obs, int n,
                                       const float2* __restrict__ beam_dir, int max_iters, int* iters, int car,
                                       int beam) {
+  int count = 0;
+  const float range = beam_range<LAYERS>(t, ray, n, beam_dir, max_iters, iters != nullptr, car, beam, &count);
+  obs[(long)(4 + beam) * n + car] = range / RANGE;
+  if (iters) iters[(long)beam * n + car] = count;
+}
+
+template <int LAYERS>
+__device__ __forceinline__ float beam_range(const TrackDev& t, const float4* __restrict__ ray, int n,
+                                            const float2* __restrict__ beam_dir, int max_iters, bool counted,
+                                            int car, int beam, int* count_out) {
   const float4 r0 = __ldg(ray + car), r1 = __ldg(ray + n + car);  // (ox, oy, oz, cos h), (sin h, along, across)
   const float2 az = __ldg(beam_dir + beam);                        // (cos azimuth, sin azimuth)
   float dx = az.x * r0.w + az.y * -r1.x;
@@ -679,12 +695,12 @@ __device__ __forceinline__ void trace(const TrackDev& t, const float4* __restric
   float range;
   if (!(fabsf(oz) <= 1e20f && (descent == 0.0f || descent >= 1.17549435e-38f)))
     range = march<LAYERS, true>(t, ox, oy, oz, dx, dy, dz, descent, inv_descent, max_iters, &count);
-  else if (iters || !t.free_march)
+  else if (counted || !t.free_march)
     range = march<LAYERS, false>(t, ox, oy, oz, dx, dy, dz, descent, inv_descent, max_iters, &count);
   else
     range = march<LAYERS, false, false>(t, ox, oy, oz, dx, dy, dz, descent, inv_descent, max_iters, &count);
-  obs[(long)(4 + beam) * n + car] = range / RANGE;
-  if (iters) iters[(long)beam * n + car] = count;
+  *count_out = count;
+  return range;
 }
 
 // RN(a / b) from y = RN(1 / b) and q0 = RN(a * y), by two residual
@@ -984,9 +1000,51 @@ void launch_lidar_list(const TrackDev& t, const float4* ray, float* obs, int n, 
                                                                      nullptr, counter, list, list_count);
 }
 
+// Spot check of a learned prediction: beams offset, offset + stride, ... of
+// every car traced exactly (beam_range, the reference's range) and compared
+// with the predicted obs rows pred [beams, n] (range / RANGE); a car with a
+// beam off by more than tol (obs units) gets minr = 0, which puts it on the
+// exact-fallback list (k_select_cars). One thread per (car, checked beam).
+// The offset is (*step_base + step_add) % stride, so it moves on with the
+// step in replays of a captured rollout.
+template <int LAYERS>
+__global__ void k_lidar_spot(TrackDev t, int max_iters, const float4* __restrict__ ray, const float* __restrict__ pred,
+                             int n, int beams, const float2* __restrict__ beam_dir, int stride,
+                             const int64_t* step_base, int64_t step_add, int per_car, float tol, unsigned* minr) {
+  const long item = (long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (item >= (long)n * per_car) return;
+  const int64_t step = (step_base ? *step_base : 0) + step_add;
+  const int offset = (int)(((step % stride) + stride) % stride);
+  const int car = (int)(item / per_car), beam = offset + (int)(item % per_car) * stride;
+  if (beam >= beams) return;
+  int count = 0;
+  const float range = beam_range<LAYERS>(t, ray, n, beam_dir, max_iters, false, car, beam, &count);
+  if (!(fabsf(range / RANGE - __ldg(pred + (long)beam * n + car)) <= tol)) atomicMin(minr + car, 0u);
+}
+
 __global__ void k_select_cars(const unsigned* minr, int n, unsigned threshold_bits, int* list, int* count) {
   int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i < n && minr[i] < threshold_bits) list[atomicAdd(count, 1)] = i;
+}
+
+void launch_lidar_spot(const TrackDev& t, const float4* ray, const float* pred, int n, int beams,
+                       const float2* beam_dir, int stride, const int64_t* step_base, int64_t step_add, float tol,
+                       unsigned* minr, cudaStream_t st) {
+  if (stride < 1 || n < 1) return;
+  const int per_car = (beams + stride - 1) / stride;  // the most any offset checks
+  const long items = (long)n * per_car;
+  const unsigned blocks = (unsigned)((items + 127) / 128);
+  const int mi = lidar_max_iters(t);
+#define RACER_SPOT(L)                                                                                            \
+  k_lidar_spot<L><<<blocks, 128, 0, st>>>(t, mi, ray, pred, n, beams, beam_dir, stride, step_base, step_add, per_car, \
+                                          tol, minr)
+  if (t.layers == 1)
+    RACER_SPOT(1);
+  else if (t.layers == 2)
+    RACER_SPOT(2);
+  else
+    RACER_SPOT(0);
+#undef RACER_SPOT
 }
 
 void launch_select_cars(const unsigned* minr, int n, float threshold, int* list, int* count, cudaStream_t st) {

@@ -449,6 +449,10 @@ struct racer_surrogate {
   unsigned* rmax = nullptr;
   unsigned long long* rcount = nullptr;  // [0] beams over 5 cm, [1] fallback cars
   double audited_beams = 0, car_steps = 0;
+  // spot check between audits (racer_surrogate_set_spot_check): every spot_stride-th beam traced
+  // exactly, cars off by more than spot_tol (range / RANGE units) fall back to the exact tracer
+  int spot_stride = 0;
+  float spot_tol = 0.025f;
 };
 
 namespace {
@@ -804,6 +808,18 @@ int racer_surrogate_set_label_cache(racer_surrogate* s, int enable) {
   return 0;
 }
 
+int racer_surrogate_set_spot_check(racer_surrogate* s, int stride, float tolerance_m) {
+  if (!s || stride < 0 || !(tolerance_m > 0.0f)) {
+    racer_host::set_error("racer_surrogate_set_spot_check: stride must be >= 0 and the tolerance positive");
+    return 1;
+  }
+  s->spot_stride = stride;
+  s->spot_tol = tolerance_m / RANGE;
+  for (auto& kv : s->sim->surrogate_graphs) cudaGraphExecDestroy(kv.second);
+  s->sim->surrogate_graphs.clear();
+  return 0;
+}
+
 int racer_surrogate_set_loss(racer_surrogate* s, float huber_m) {
   if (!s || !(huber_m >= 0.0f)) {
     racer_host::set_error("racer_surrogate_set_loss: null surrogate or negative threshold");
@@ -1005,7 +1021,8 @@ __global__ void k_count_fallback(const int* count, unsigned long long* total) {
 // surrogate's prediction, replaced by the exact tracer for every car on an
 // audit step (with the error accumulated), else for the cars whose smallest
 // predicted range is below `fallback` (obs units, range / RANGE).
-int surrogate_lidar(racer_surrogate* s, racer_sim* sim, float* obs, bool audit, float fallback, cudaStream_t st) {
+int surrogate_lidar(racer_surrogate* s, racer_sim* sim, float* obs, bool audit, float fallback, cudaStream_t st,
+                    const int64_t* step_base, int64_t step_add) {
   const int n = sim->n, beams = sim->beams;
   SurrogateActs* a = &s->infer;
   k_features<<<(n + 127) / 128, 128, 0, st>>>(sim->ray, n, s->nm, a->x, nullptr);
@@ -1028,9 +1045,13 @@ int surrogate_lidar(racer_surrogate* s, racer_sim* sim, float* obs, bool audit, 
   if (audit) {
     launch_lidar(sim->t, sim->ray, obs, n, beams, sim->beam_dir, nullptr, st);
     k_compare<<<1216, 256, 0, st>>>(pred, obs + 4L * n, (long)beams * n, s->rsums, s->rmax, s->rcount);
-  } else if (fallback > 0.0f) {
+  } else if (fallback > 0.0f || s->spot_stride > 0) {
+    if (s->spot_stride > 0)  // a checked beam off by more than the tolerance marks its car (minr = 0)
+      launch_lidar_spot(sim->t, sim->ray, pred, n, beams, sim->beam_dir, s->spot_stride, step_base, step_add,
+                        s->spot_tol, s->minr, st);
     SURR_CHECK(cudaMemsetAsync(s->list_count, 0, sizeof(int), st));
-    launch_select_cars(s->minr, n, fallback, s->list, s->list_count, st);
+    // the threshold stays above 0 so that marked cars are always selected
+    launch_select_cars(s->minr, n, fallback > 0.0f ? fallback : 1e-30f, s->list, s->list_count, st);
     launch_lidar_list(sim->t, sim->ray, obs, n, beams, sim->beam_dir, s->list, s->list_count, n, s->list_units,
                       sim->sms, st);
     k_count_fallback<<<1, 32, 0, st>>>(s->list_count, s->rcount + 1);

@@ -389,6 +389,11 @@ class Surrogate:
         takes effect from the next set_poses."""
         call("racer_surrogate_set_label_cache", self.handle, int(bool(enable)))
 
+    def set_spot_check(self, stride=64, tolerance_m=0.25):
+        """Between audits, trace every `stride`-th beam (offset rotating with the step) exactly and send
+        cars with a beam off by more than `tolerance_m` to the exact tracer; stride 0 turns it off."""
+        call("racer_surrogate_set_spot_check", self.handle, int(stride), float(tolerance_m))
+
     def set_loss(self, huber_m=0.0):
         """0: squared range error; > 0: Huber loss with that threshold in metres."""
         call("racer_surrogate_set_loss", self.handle, float(huber_m))

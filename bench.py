@@ -217,7 +217,7 @@ def fp32_policy_section(torch, W, track, stream, flush, runner):
 
 SURR_CARS, SURR_STEPS, SURR_REPS, SURR_TRAIN_STEPS = 65536, 32, 3, 80000
 SURR_LR, SURR_HUBER_M = 8e-3, 0.02
-SPOT_STRIDE, SPOT_TOL_M = 64, 0.25
+SPOT_STRIDE, SPOT_TOL_M = 64, 1.0
 
 
 def surrogate_section(torch, W, track, stream, flush, train_steps=SURR_TRAIN_STEPS, keep=None):

@@ -108,6 +108,15 @@ int racer_sim_autotune(racer_sim* sim, int reps, racer_lidar_shape* best, float*
  * one-chain rollout's. Applies to one-track sims with a BF16 policy; drops
  * captured graphs. */
 int racer_sim_set_chains(racer_sim* sim, int chains);
+/* Rollout graphs (racer_rollout) as one launch of the fused persistent kernel
+ * (enable = 1; one-track sims with a BF16 policy, else ignored): each CTA owns
+ * a slice of at most 128 cars for all steps and runs, step after step, the
+ * policy forward on the tensor cores with the sampling, the physics and the
+ * lidar of its cars, the observations never leaving the SM's L2 slice between
+ * phases. Every result is the chained graph's (racer/sim.mojo:307-321,
+ * main.mojo:40-48 per step). 0 (the default) = kernels per step. Drops
+ * captured graphs. */
+int racer_sim_set_fused_rollout(racer_sim* sim, int enable);
 int racer_sim_destroy(racer_sim* sim);
 int racer_sim_get_buffers(racer_sim* sim, racer_sim_buffers* out);
 /* Sim.reset (racer/sim.mojo:291-305): spawn every car, then a step at rest. */
@@ -227,9 +236,11 @@ int racer_runner_step(racer_sim* sim, racer_policy* policy, racer_acts* acts, fl
  * offsets are step0, step0 + 1, ... */
 int racer_rollout(racer_sim* sim, racer_policy* policy, racer_acts* acts, float* scratch_dev, int steps,
                   int deterministic, int64_t step0);
-/* Autotuner for the chain count: times `reps` rollouts of `steps` stochastic
- * Runner steps for 1 to 4 chains (after one warm-up rollout each; the sim
- * state advances), keeps the fastest and returns it with its env-steps/s. */
+/* Autotuner for the rollout graph: times `reps` rollouts of `steps` stochastic
+ * Runner steps for 1 to 4 chains and (one-track sims, BF16 policy) the fused
+ * persistent kernel (after one warm-up rollout each; the sim state advances),
+ * keeps the fastest and returns it with its env-steps/s; best_chains = 0
+ * means the fused kernel won. */
 int racer_runner_tune_chains(racer_sim* sim, racer_policy* policy, racer_acts* acts, float* scratch_dev, int steps,
                              int reps, int* best_chains, float* best_rate);
 /* Runner.evaluate (main.mojo:70-80): `steps` deterministic Runner steps

@@ -535,3 +535,39 @@ def test_gather_peak_is_plausible():
     l2 = W.gather_peak(8 << 20, 10)
     hbm = W.gather_peak(256 << 20, 5)
     assert 500 < hbm < l2 < 100000, (l2, hbm)
+
+
+@pytest.mark.parametrize("name,n,beams", [("bridge", 40, 1081), ("bridge", 4096, 1081), ("ramp", 1024, 108),
+                                          ("flat", 700, 108), ("bank", 333, 2)])
+def test_fused_rollout_equals_chained_graph(name, n, beams):
+    """The fused persistent rollout kernel (forward + sampling, physics and lidar of a slice of cars
+    per CTA, all steps in one launch) gives the chained graph's bits: state, observations, actions,
+    rewards, done flags and the policy outputs, over 12 steps; car counts that fill a CTA's slice
+    unevenly, one car per CTA, the minimum beam count."""
+    track = W.track(name)
+    chained = W.Runner(track, n, beams=beams, seed=13, policy_seed=5)
+    fused = W.Runner(track, n, beams=beams, seed=13, policy_seed=5)
+    fused.sim.set_fused_rollout(True)
+    assert fused.rollout_kernel_count(12) == 2  # one launch of the fused kernel, plus the step offset
+    for runner in (chained, fused):
+        runner.rollout(12, False, 40)
+        runner.rollout(12, False, 52)  # a replay of the captured graph from the state reached
+        runner.synchronize()
+    for arr in ("state", "obs", "actions", "reward", "done"):
+        assert same(getattr(chained.sim, arr).numpy(), getattr(fused.sim, arr).numpy()), arr
+    assert same(chained.acts.o.numpy(), fused.acts.o.numpy())
+    assert same(chained.scratch.numpy(), fused.scratch.numpy())
+    assert fused.policy.status() == 0
+
+
+def test_fused_rollout_on_three_layers_and_deterministic():
+    """Three layers (the probe reads the layer count from the track) and deterministic actions."""
+    track = three_layer_track()
+    chained = W.Runner(track, 200, beams=1081, seed=2, policy_seed=3)
+    fused = W.Runner(track, 200, beams=1081, seed=2, policy_seed=3)
+    fused.sim.set_fused_rollout(True)
+    for runner in (chained, fused):
+        runner.rollout(6, True, 0)
+        runner.synchronize()
+    for arr in ("state", "obs", "actions"):
+        assert same(getattr(chained.sim, arr).numpy(), getattr(fused.sim, arr).numpy()), arr

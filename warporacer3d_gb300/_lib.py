@@ -49,6 +49,7 @@ SIGNATURES = {
     "racer_sim_get_lidar_shape": [c_void_p, P(LidarShape)],
     "racer_sim_autotune": [c_void_p, c_int, P(LidarShape), P(c_float)],
     "racer_sim_set_chains": [c_void_p, c_int],
+    "racer_sim_set_fused_rollout": [c_void_p, c_int],
     "racer_runner_tune_chains": [c_void_p, c_void_p, c_void_p, c_void_p, c_int, c_int, P(c_int), P(c_float)],
     "racer_sim_destroy": [c_void_p],
     "racer_sim_get_buffers": [c_void_p, P(SimBuffers)],

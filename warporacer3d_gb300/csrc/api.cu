@@ -1179,7 +1179,25 @@ static int rollout_graph(racer_sim* s, racer_policy* p, racer_acts* a, float* sc
     RACER_TRY(cudaStreamBeginCapture(s->st, cudaStreamCaptureModeThreadLocal));
     int rc = 0;
     const int chains = s->chains > 1 && s->seg.count == 1 && policy_is_bf16(p) ? s->chains : 1;
-    if (chains == 1) {
+    if (s->fused && s->seg.count == 1 && policy_is_bf16(p)) {
+      // the whole rollout as one launch of the fused persistent kernel
+      SampleArgs sa;
+      sa.seed = s->seed;
+      sa.log_std = policy_theta(p) + policy_params(p) - 2;
+      sa.actions = s->actions;
+      sa.logp = scratch;
+      sa.value = scratch + s->n;
+      sa.deterministic = det;
+      sa.step_base = s->step_base;
+      sa.step_add = 0;
+      const cudaError_t e = launch_rollout_fused(s->seg, s->state, s->actions, s->reward, s->done, s->obs, s->n,
+                                                 s->beams, s->ray, s->beam_dir, steps, policy_pack(p), a->o, sa,
+                                                 policy_err(p), s->sms, s->st);
+      if (e != cudaSuccess) {
+        set_error(std::string("fused rollout: ") + cudaGetErrorString(e));
+        rc = 2;
+      }
+    } else if (chains == 1) {
       for (int k = 0; k < steps && !rc; ++k) rc = runner_step_on(s, p, a, scratch, det, s->step_base, k, s->st);
     } else {
       // independent chains over car ranges (multiples of 128, the forward's tile), forked from and joined
@@ -1246,10 +1264,14 @@ int racer_runner_tune_chains(racer_sim* s, racer_policy* p, racer_acts* a, float
   RACER_TRY(cudaEventCreate(&t1));
   int best = 1;
   float rate = 0.0f;
-  const int max_chains = s->seg.count == 1 && policy_is_bf16(p) ? 4 : 1;
+  const bool eligible = s->seg.count == 1 && policy_is_bf16(p);
+  const int max_chains = eligible ? 4 : 1;
   int64_t step0 = 0;
-  for (int chains = 1; chains <= max_chains; ++chains) {
-    if (int rc = racer_sim_set_chains(s, chains)) return rc;
+  // candidates: 1 .. max_chains chains of kernels, then (eligible sims) the fused persistent kernel, as 0
+  for (int cand = 1; cand <= max_chains + (eligible ? 1 : 0); ++cand) {
+    const int chains = cand <= max_chains ? cand : 0;
+    if (int rc = racer_sim_set_fused_rollout(s, chains == 0)) return rc;
+    if (int rc = racer_sim_set_chains(s, chains == 0 ? 1 : chains)) return rc;
     if (int rc = racer_rollout(s, p, a, scratch, steps, 0, step0)) return rc;  // capture and warm up
     step0 += steps;
     RACER_TRY(cudaEventRecord(t0, s->st));
@@ -1264,7 +1286,8 @@ int racer_runner_tune_chains(racer_sim* s, racer_policy* p, racer_acts* a, float
   }
   cudaEventDestroy(t0);
   cudaEventDestroy(t1);
-  if (int rc = racer_sim_set_chains(s, best)) return rc;
+  if (int rc = racer_sim_set_fused_rollout(s, best == 0)) return rc;
+  if (int rc = racer_sim_set_chains(s, best == 0 ? 1 : best)) return rc;
   if (best_chains) *best_chains = best;
   if (best_rate) *best_rate = rate;
   return 0;
@@ -1449,6 +1472,14 @@ int racer_sim_set_chains(racer_sim* s, int chains) {
   }
   if (chains != s->chains) drop_graphs(s);
   s->chains = chains;
+  return 0;
+}
+
+int racer_sim_set_fused_rollout(racer_sim* s, int enable) {
+  RACER_ARG(s, "racer_sim_set_fused_rollout: null sim");
+  RACER_TRY(cudaStreamSynchronize(s->st));
+  if ((enable != 0) != (s->fused != 0)) drop_graphs(s);
+  s->fused = enable != 0;
   return 0;
 }
 

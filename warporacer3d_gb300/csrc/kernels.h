@@ -4,6 +4,7 @@
 #include <stdint.h>
 
 #include "common.cuh"
+#include "mlp_tc.h"
 
 namespace racer {
 
@@ -39,6 +40,14 @@ bool lidar_shape_ok(const LidarShape& shape);
 void launch_lidar_spot(const TrackDev& t, const float4* ray, const float* pred, int n, int beams,
                        const float2* beam_dir, int stride, const int64_t* step_base, int64_t step_add, float tol,
                        unsigned* minr, cudaStream_t st);
+// The fused persistent rollout (sim.cu, k_rollout_fused): `steps` Runner steps of a one-track
+// sim in one launch, each CTA owning cars_per_cta cars for all of them; pack = the policy's BF16
+// weight images (mlp_tc.cu), og [3, n] its outputs, sa the sampling (step_add = the first step).
+int rollout_fused_cars_per_cta(int n, int sms);
+cudaError_t launch_rollout_fused(const Segments& g, float* state, float* actions, float* reward, float* done,
+                                 float* obs, int n, int beams, float4* ray, const float2* beam_dir, int steps,
+                                 const uint8_t* pack, float* og, const SampleArgs& sa, int* err, int sms,
+                                 cudaStream_t st);
 // Cars whose smallest predicted range (ordered uint bits of a nonnegative float) is below threshold.
 void launch_select_cars(const unsigned* minr, int n, float threshold, int* list, int* count, cudaStream_t st);
 int lidar_max_iters(const TrackDev& t);

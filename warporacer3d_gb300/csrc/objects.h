@@ -31,6 +31,8 @@ struct racer_sim {
   unsigned* counters = nullptr;  // [MAX_SEGMENTS] unit counters of the dynamic lidar
   // rollouts as independent chains over car ranges (parallel branches of the graph)
   int chains = 1;
+  // 1: rollout graphs are one launch of the fused persistent kernel (racer_sim_set_fused_rollout)
+  int fused = 0;
   std::vector<cudaStream_t> chain_st;
   std::vector<cudaEvent_t> chain_join;
   cudaEvent_t chain_fork = nullptr;

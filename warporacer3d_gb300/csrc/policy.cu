@@ -75,6 +75,8 @@ int policy_refresh_on(racer_policy* p, cudaStream_t st) {
 }
 
 int policy_is_bf16(racer_policy* p) { return p->bf16; }
+const uint8_t* policy_pack(racer_policy* p) { return p->pack; }
+int* policy_err(racer_policy* p) { return p->err; }
 
 int policy_set_precision(racer_policy* p, int bf16) {
   if (p->bf16 != (bf16 ? 1 : 0)) ++p->generation;

@@ -23,6 +23,9 @@ int policy_forward(racer_policy* p, const float* x, int cols, float* h1, float* 
                    const racer::SampleArgs* sa, cudaStream_t st, int c0 = 0, int c1 = -1);
 // 1 if the policy computes in BF16 on the tensor cores.
 int policy_is_bf16(racer_policy* p);
+// The BF16 weight images of the tensor-core forward and its error word (the fused rollout kernel).
+const uint8_t* policy_pack(racer_policy* p);
+int* policy_err(racer_policy* p);
 // Device-side error word of the tensor-core kernels (0 = none), read and cleared; synchronises.
 int policy_status(racer_policy* p, int* code);
 // The timeout probe on the policy's stream, reporting into the policy's error word.

@@ -20,6 +20,7 @@
 #include <string.h>
 
 #include "common.cuh"
+#include "fwd_tc.cuh"
 #include "kernels.h"
 #include "philox.h"
 #include "rmath.h"
@@ -539,8 +540,8 @@ __global__ void k_pose_frames(TrackDev t, const float4* __restrict__ poses, int 
 // the probe count (dropped where its bound cannot end the march) and
 // floor/descent (quotient: two residual corrections of the reciprocal; the
 // guarded march divides only where min() can select it).
-template <int LAYERS>
-__device__ __forceinline__ void trace(const TrackDev& t, const float4* __restrict__ ray, float* obs, int n,
+template <int LAYERS, bool NC = true>
+__device__ __forceinline__ void trace(const TrackDev& t, const float4* ray, float* obs, int n,
                                       const float2* __restrict__ beam_dir, int max_iters, int* iters, int car,
                                       int beam);
 
@@ -655,26 +656,30 @@ __device__ __forceinline__ float march(const TrackDev& t, float ox, float oy, fl
                                        float descent, float inv_descent, int max_iters, int* count_out);
 
 // The range of one beam (racer/sim.mojo:240-266); `count` gets its probes.
-template <int LAYERS>
-__device__ __forceinline__ float beam_range(const TrackDev& t, const float4* __restrict__ ray, int n,
+// NC: the ray frames are read-only for the whole launch (the read-only data
+// path); the fused rollout, which rewrites them every step, loads them
+// through L2 instead, where the block's own writes before a barrier are seen.
+template <int LAYERS, bool NC = true>
+__device__ __forceinline__ float beam_range(const TrackDev& t, const float4* ray, int n,
                                             const float2* __restrict__ beam_dir, int max_iters, bool counted,
                                             int car, int beam, int* count_out);
 
-template <int LAYERS>
-__device__ __forceinline__ void trace(const TrackDev& t, const float4* __restrict__ ray, float* obs, int n,
+template <int LAYERS, bool NC>
+__device__ __forceinline__ void trace(const TrackDev& t, const float4* ray, float* obs, int n,
                                       const float2* __restrict__ beam_dir, int max_iters, int* iters, int car,
                                       int beam) {
   int count = 0;
-  const float range = beam_range<LAYERS>(t, ray, n, beam_dir, max_iters, iters != nullptr, car, beam, &count);
+  const float range = beam_range<LAYERS, NC>(t, ray, n, beam_dir, max_iters, iters != nullptr, car, beam, &count);
   obs[(long)(4 + beam) * n + car] = range / RANGE;
   if (iters) iters[(long)beam * n + car] = count;
 }
 
-template <int LAYERS>
-__device__ __forceinline__ float beam_range(const TrackDev& t, const float4* __restrict__ ray, int n,
+template <int LAYERS, bool NC>
+__device__ __forceinline__ float beam_range(const TrackDev& t, const float4* ray, int n,
                                             const float2* __restrict__ beam_dir, int max_iters, bool counted,
                                             int car, int beam, int* count_out) {
-  const float4 r0 = __ldg(ray + car), r1 = __ldg(ray + n + car);  // (ox, oy, oz, cos h), (sin h, along, across)
+  // (ox, oy, oz, cos h), (sin h, along, across)
+  const float4 r0 = NC ? __ldg(ray + car) : __ldcg(ray + car), r1 = NC ? __ldg(ray + n + car) : __ldcg(ray + n + car);
   const float2 az = __ldg(beam_dir + beam);                        // (cos azimuth, sin azimuth)
   float dx = az.x * r0.w + az.y * -r1.x;
   float dy = az.x * r1.x + az.y * r0.w;
@@ -1022,6 +1027,186 @@ __global__ void k_lidar_spot(TrackDev t, int max_iters, const float4* __restrict
   if (!(fabsf(range / RANGE - __ldg(pred + (long)beam * n + car)) <= tol)) atomicMin(minr + car, 0u);
 }
 
+// ---- the fused persistent rollout: policy forward, sampling, physics and lidar ----
+//
+// One CTA owns cars [c0, c1) (at most 128) for all `steps` Runner steps
+// (main.mojo:40-48), whose phases run one after the other, separated by block
+// barriers: the BF16 policy forward on tcgen05 with the fused sampling, the
+// physics of each car (one thread each), the lidar (a warp marches 32 beams of
+// one car at a time). Cars never interact, so no grid-wide synchronisation is
+// needed, and every result is the chained graph's: the same device functions
+// (advance_car, trace) and the same forward (k-blocks, MMAs, epilogue) as
+// mlp_tc.cu's register-staged kernel. Two CTAs share an SM, so one's forward or
+// physics, latency-bound, runs beside the other's lidar.
+// Data the kernel rewrites every step (obs, the ray frames, actions) is read
+// with coherent loads (never the read-only path); the block's barrier orders
+// its writes before the next phase's reads.
+struct FusedRolloutCfg {
+  static constexpr int GROUPS = 2;              // forward producer groups of four warps, one stage each
+  static constexpr int MMA_WARP = GROUPS * 4;  // warp 8: layer 1's MMAs
+  static constexpr int THREADS = 16 * 32;       // every warp marches beams
+  static constexpr int OFF_A = 0;               // GROUPS x A; H = [h | 1 | 0] reuses A[0], A[1]
+  static constexpr int OFF_B = OFF_A + GROUPS * A_BYTES;
+  static constexpr int OFF_W1 = OFF_B + GROUPS * B_BYTES;
+  static constexpr int OFF_W2 = OFF_W1 + 2 * B_BYTES;
+  static constexpr int OFF_BAR = OFF_W2 + 2 * 16 * 128;
+  // + barriers, + alignment slack, + 16 KB so every descriptor-addressed read stays inside the allocation
+  static constexpr int SMEM_BYTES = OFF_BAR + 128 + 1024 + 16384;
+  static_assert((2 * GROUPS + 3) * 8 + 8 <= 128, "barriers, the TMEM slot and the abort word fit their 128 bytes");
+};
+static_assert(2 * FusedRolloutCfg::SMEM_BYTES <= 227 * 1024, "two CTAs per SM");
+
+template <int LAYERS>
+__global__ void __launch_bounds__(FusedRolloutCfg::THREADS, 2)
+    k_rollout_fused(const __grid_constant__ Segments g, float* s, float* act, float* reward, float* done_rows,
+                    float* obs, int n, int beams, float4* ray, const float2* __restrict__ beam_dir, int cars_per_cta,
+                    int steps, const uint4* __restrict__ w0s, int kblocks, const uint4* __restrict__ w1s,
+                    const uint4* __restrict__ w2s, float* og, SampleArgs sa, int* err) {
+  using C = FusedRolloutCfg;
+  constexpr int GROUPS = C::GROUPS, MMA_WARP = C::MMA_WARP;
+  extern __shared__ uint8_t smem_raw[];
+  const uint32_t raw = tc::smem_u32(smem_raw);
+  uint8_t* smem = smem_raw + (((raw + 1023u) & ~1023u) - raw);
+  uint64_t* full = reinterpret_cast<uint64_t*>(smem + C::OFF_BAR);
+  uint64_t* empty = full + GROUPS;
+  uint64_t* done = empty + GROUPS;
+  uint64_t* drain = done + 1;  // [2]: thread 0's and the MMA lane's final commits after a timeout
+  uint32_t* tslot = reinterpret_cast<uint32_t*>(drain + 2);
+  volatile int* abort = reinterpret_cast<volatile int*>(tslot + 1);  // set by a timed-out wait
+  constexpr uint32_t limit = tc::WAIT_LIMIT;
+
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  const int r = tid & (TILE - 1);  // sample row of a producer or epilogue thread
+  const int c0 = (int)blockIdx.x * cars_per_cta, c1 = min(n, c0 + cars_per_cta);
+  const int in = beams + 5;
+  const TrackDev& t = g.t[0];
+
+  if (tid == 0) {
+    for (int q = 0; q < GROUPS; ++q) {
+      tc::mbar_init(&full[q], TILE);
+      tc::mbar_init(&empty[q], 1);
+    }
+    tc::mbar_init(done, 1);
+    tc::mbar_init(&drain[0], 1);
+    tc::mbar_init(&drain[1], 1);
+    *abort = 0;
+    tc::fence_barrier_init();
+  }
+  if (warp == MMA_WARP) {
+    tc::tmem_alloc(tslot, 64);
+    tc::tmem_relinquish();
+  }
+  {  // W1 (2 x 8 KB) and W2 (2 x 2 KB), resident for the whole rollout
+    uint4* w1 = reinterpret_cast<uint4*>(smem + C::OFF_W1);
+    uint4* w2 = reinterpret_cast<uint4*>(smem + C::OFF_W2);
+    for (int e = tid; e < 2 * B_BYTES / 16; e += C::THREADS) w1[e] = __ldg(w1s + e);
+    for (int e = tid; e < 2 * 16 * 128 / 16; e += C::THREADS) w2[e] = __ldg(w2s + e);
+  }
+  tc::fence_proxy_async_smem();
+  tc::tc_fence_before();
+  __syncthreads();
+  tc::tc_fence_after();
+  const uint32_t tmem = *tslot;
+  const uint32_t id64 = tc::idesc_bf16(TILE, 64);
+  bool ok = true;
+  bool issued = false;  // this thread issued an MMA
+  const int beam_groups = (beams + 31) >> 5;
+
+  for (int step = 0; step < steps; ++step) {
+    // ---- policy forward on the cars' observations, with the sampling in the epilogue ----
+    const int c = c0 + r;
+    const bool live = c < c1;
+    if (warp < MMA_WARP) {
+      const int q = warp >> 2;                               // producer group: k-blocks q, q + GROUPS, ...
+      const uint32_t uses = (kblocks - q + GROUPS - 1) / GROUPS;  // uses of its stage in a step
+      uint8_t* A = smem + C::OFF_A + q * A_BYTES;
+      uint4* B = reinterpret_cast<uint4*>(smem + C::OFF_B + q * B_BYTES);
+      for (int j = 0;; ++j) {
+        const int kb = q + GROUPS * j;
+        if (kb >= kblocks) break;
+        const uint32_t use = (uint32_t)step * uses + (uint32_t)j;
+        uint4 wb[4];
+        const uint4* src = w0s + (long)kb * (B_BYTES / 16);
+#pragma unroll
+        for (int e = 0; e < 4; ++e) wb[e] = __ldg(src + r + e * TILE);
+        if (use >= 1 && !tc::mbar_wait_abort(&empty[q], (use - 1) & 1, abort, limit)) ok = false;
+        // the k-block's 64 inputs of this row in four chunks of 16 (the same BF16 operand as mlp_tc.cu's
+        // producers write; fewer live registers)
+#pragma unroll 1
+        for (int h = 0; h < 4; ++h) {
+          float v[16];
+#pragma unroll
+          for (int f = 0; f < 16; ++f) {
+            const int row = kb * 64 + 16 * h + f;
+            v[f] = (live && row < in) ? __ldcg(obs + (long)row * n + c) : 0.0f;
+          }
+#pragma unroll
+          for (int f = 0; f < 2; ++f) {
+            const int chunk = 2 * h + f;
+            const uint4 pk = make_uint4(tc::pack_bf16(v[8 * f], v[8 * f + 1]), tc::pack_bf16(v[8 * f + 2], v[8 * f + 3]),
+                                        tc::pack_bf16(v[8 * f + 4], v[8 * f + 5]),
+                                        tc::pack_bf16(v[8 * f + 6], v[8 * f + 7]));
+            *reinterpret_cast<uint4*>(A + r * 128 + ((chunk ^ (r & 7)) << 4)) = pk;
+          }
+        }
+#pragma unroll
+        for (int e = 0; e < 4; ++e) B[r + e * TILE] = wb[e];
+        tc::fence_proxy_async_smem();
+        tc::mbar_arrive(&full[q]);
+      }
+    } else if (warp == MMA_WARP && lane == 0) {
+      for (int kb = 0; kb < kblocks; ++kb) {
+        const int q = kb % GROUPS;
+        const uint32_t uses = (kblocks - q + GROUPS - 1) / GROUPS;
+        const uint32_t use = (uint32_t)step * uses + (uint32_t)(kb / GROUPS);
+        if (!tc::mbar_wait_abort(&full[q], use & 1, abort, limit)) ok = false;
+        if (*abort) continue;  // issue nothing after a timeout
+        issued = true;
+        tc::tc_fence_after();
+        const uint32_t a = tc::smem_u32(smem + C::OFF_A + q * A_BYTES), b = tc::smem_u32(smem + C::OFF_B + q * B_BYTES);
+#pragma unroll
+        for (int k = 0; k < 4; ++k)
+          tc::mma_bf16(tmem, tc::sdesc_sw128(a + 32 * k), tc::sdesc_sw128(b + 32 * k), id64, (kb | k) ? 1u : 0u);
+        tc::mma_commit(&empty[q]);
+      }
+      if (!*abort) tc::mma_commit(done);
+    }
+    if (warp < 4) {
+      SampleArgs sk = sa;
+      sk.step_add = sa.step_add + step;
+      if (!fwd_epilogue(smem, C::OFF_A, C::OFF_W1, C::OFF_W2, tmem, done, 3u * (uint32_t)step, r, live, c, n, nullptr,
+                        nullptr, og, 0, sk, abort, limit, &issued))
+        ok = false;
+    }
+    tc::tc_fence_before();
+    __syncthreads();  // the actions of this step are written
+    // ---- physics: one thread per car ----
+    for (int i = c0 + tid; i < c1; i += C::THREADS)
+      advance_car<LAYERS>(t, s, act, reward, done_rows, obs, n, beams, g.seed[0], ray, i, i);
+    __syncthreads();  // frames and obs rows 0-3 written
+    // ---- lidar: (car, 32-beam group) units over the warps ----
+    const int units = (c1 - c0) * beam_groups;
+    for (int u = warp; u < units; u += C::THREADS / 32) {
+      const int car = c0 + u / beam_groups, beam = (u % beam_groups) * 32 + lane;
+      if (beam < beams) trace<LAYERS, false>(t, ray, obs, n, beam_dir, g.max_iters[0], nullptr, car, beam);
+    }
+    tc::tc_fence_before();
+    __syncthreads();  // obs complete before the next step's forward reads it
+  }
+  if (*abort) {  // the MMAs issued before a timeout complete before the TMEM is freed
+    if (issued) {
+      uint64_t* mine = &drain[tid == 0 ? 0 : 1];
+      tc::mma_commit(mine);
+      if (!tc::mbar_wait(mine, 0, tc::WAIT_LIMIT)) ok = false;
+    }
+    tc::tc_fence_before();
+    __syncthreads();
+  }
+  __syncwarp();
+  if (warp == MMA_WARP) tc::tmem_dealloc(tmem, 64);
+  if (!ok) atomicExch(err, 1);
+}
+
 __global__ void k_select_cars(const unsigned* minr, int n, unsigned threshold_bits, int* list, int* count) {
   int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i < n && minr[i] < threshold_bits) list[atomicAdd(count, 1)] = i;
@@ -1045,6 +1230,48 @@ void launch_lidar_spot(const TrackDev& t, const float4* ray, const float* pred, 
   else
     RACER_SPOT(0);
 #undef RACER_SPOT
+}
+
+// The fused rollout's cars per CTA: two CTAs per SM over all cars, at most 128
+// (one MMA tile); at least 1.
+int rollout_fused_cars_per_cta(int n, int sms) {
+  const int ctas = 2 * (sms > 0 ? sms : 1);
+  const int per = (n + ctas - 1) / ctas;
+  return per < 1 ? 1 : (per > TILE ? TILE : per);
+}
+
+cudaError_t launch_rollout_fused(const Segments& g, float* state, float* actions, float* reward, float* done,
+                                 float* obs, int n, int beams, float4* ray, const float2* beam_dir, int steps,
+                                 const uint8_t* pack, float* og, const SampleArgs& sa, int* err, int sms,
+                                 cudaStream_t st) {
+  static unsigned long long configured = 0;  // per device
+  cudaError_t e = once_per_device(&configured, [] {
+    for (auto* k : {k_rollout_fused<0>, k_rollout_fused<1>, k_rollout_fused<2>}) {
+      cudaError_t a = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, FusedRolloutCfg::SMEM_BYTES);
+      if (a != cudaSuccess) return a;
+    }
+    return cudaSuccess;
+  });
+  if (e != cudaSuccess) return e;
+  if (g.count != 1 || n < 1 || steps < 1) return cudaErrorInvalidValue;
+  const int kb = (beams + 5 + 63) / 64;
+  const uint4* w0 = reinterpret_cast<const uint4*>(pack);
+  const uint4* w1 = reinterpret_cast<const uint4*>(pack + (size_t)kb * 8192);
+  const uint4* w2 = reinterpret_cast<const uint4*>(pack + (size_t)kb * 8192 + 2 * 8192);
+  const int per = rollout_fused_cars_per_cta(n, sms);
+  const unsigned blocks = (unsigned)((n + per - 1) / per);
+  const int layers = g.t[0].layers;
+#define RACER_FUSED(L)                                                                                              \
+  k_rollout_fused<L><<<blocks, FusedRolloutCfg::THREADS, FusedRolloutCfg::SMEM_BYTES, st>>>(                        \
+      g, state, actions, reward, done, obs, n, beams, ray, beam_dir, per, steps, w0, kb, w1, w2, og, sa, err)
+  if (layers == 1)
+    RACER_FUSED(1);
+  else if (layers == 2)
+    RACER_FUSED(2);
+  else
+    RACER_FUSED(0);
+#undef RACER_FUSED
+  return cudaGetLastError();
 }
 
 void launch_select_cars(const unsigned* minr, int n, float threshold, int* list, int* count, cudaStream_t st) {

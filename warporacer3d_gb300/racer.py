@@ -183,6 +183,11 @@ class Sim:
         call("racer_sim_get_lidar_shape", self.handle, ctypes.byref(shape))
         return self._shape(shape)
 
+    def set_fused_rollout(self, enable=True):
+        """Rollout graphs as one launch of the fused persistent kernel (forward, sampling, physics and
+        lidar per step inside it; the same results)."""
+        call("racer_sim_set_fused_rollout", self.handle, int(bool(enable)))
+
     def set_chains(self, chains):
         """Rollout graphs as `chains` independent chains over car ranges (the same results)."""
         call("racer_sim_set_chains", self.handle, int(chains))

@@ -215,6 +215,34 @@ def fp32_policy_section(torch, W, track, stream, flush, runner):
             "policy_precision": "f32 (CUDA cores)", "rollout_chains": 1}
 
 
+def fused_rollout_section(torch, W, track, stream, flush, runner):
+    """The headline workload as one launch of the fused persistent kernel per rollout (each CTA owns
+    a slice of cars for all 1000 steps: forward + sampling on tcgen05, physics, lidar), device-timed
+    like `value`, beside the chained graph the autotuner chose; both give the same bits."""
+    state, obs = runner.sim.state.numpy(), runner.sim.obs.numpy()
+    fused = W.Runner(track, CARS, beams=BEAMS, seed=42, policy_seed=42, stream=stream)
+    fused.sim.set_fused_rollout(True)
+    fused.sim.state.write(state)
+    fused.sim.obs.write(obs)
+    fused.rollout(HORIZON_STEPS, False, 0)  # capture and warm up
+    torch.cuda.synchronize()
+    ms = 0.0
+    reps = 2
+    for k in range(reps):
+        with torch.cuda.stream(stream):
+            flush.zero_()
+            a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            a.record(stream)
+            fused.rollout(HORIZON_STEPS, False, (k + 1) * HORIZON_STEPS)
+            b.record(stream)
+        torch.cuda.synchronize()
+        ms += a.elapsed_time(b)
+    return {"workload": f"{TRACK}, {CARS} cars, {BEAMS} beams, {HORIZON_STEPS}-env-step rollouts",
+            "env_steps_per_s": CARS * HORIZON_STEPS * reps / (ms / 1000.0),
+            "ms_per_env_step": ms / (reps * HORIZON_STEPS), "kernels_per_rollout": fused.rollout_kernel_count(HORIZON_STEPS),
+            "cars_per_cta": -(-CARS // (2 * 152)), "status": fused.policy.status()}
+
+
 SURR_CARS, SURR_STEPS, SURR_REPS, SURR_TRAIN_STEPS = 65536, 32, 3, 80000
 SURR_LR, SURR_HUBER_M = 8e-3, 0.02
 SPOT_STRIDE, SPOT_TOL_M = 64, 1.0
@@ -627,6 +655,9 @@ def main():
                        "env_steps_per_bench_step": HORIZON_STEPS, "l2": "flushed between timed steps (256 MB write)",
                        "parallelism": f"replicas x{world} (cars independent, no collective)",
                        "rollout_chains": chains,
+                       "rollout_kernel": "fused persistent kernel" if chains == 0 else
+                                         f"chained graph of per-step kernels, {chains} chain(s) (autotuned against "
+                                         "the fused persistent kernel, timed in `fused_rollout`)",
                        "policy": "tanh MLP 1086-64-64-3"},
             "beam_steps_per_s": value * BEAMS, "wall_s": wall, "gpu_launches": kernels_per_rollout * args.steps,
             "clocks": clocks.summary(), "e2e": e2e, "roofline": roofline}
@@ -635,6 +666,7 @@ def main():
     single = world == 1
     if single:
         line["fp32_policy"] = fp32_policy_section(torch, W, track, stream, flush, runner)
+        line["fused_rollout"] = fused_rollout_section(torch, W, track, stream, flush, runner)
     if single:
         audit = runner.audit_dynamics(AUDIT_STEPS, False, 10 ** 9)
         audit["workload"] = f"{TRACK}, {CARS} cars, {AUDIT_STEPS} policy steps after the timed rollouts"

@@ -576,7 +576,9 @@ def main():
         print(json.dumps(out), flush=True)
         return
     runner = W.Runner(track, CARS, beams=BEAMS, seed=replica_seed(42, rank), policy_seed=42, stream=stream)
-    chains, _ = runner.tune_chains(50, 3)  # rollout graph as 1-4 independent chains over car ranges
+    runner.rollout(50, False, 0)  # cars leave their spawn poses
+    lidar_shape, _ = runner.sim.autotune(5)  # lidar launch shape (rewrites obs from the same frames)
+    chains, _ = runner.tune_chains(50, 3)  # rollout graph: independent chains over car ranges, or the fused kernel
     kernels_per_rollout = runner.rollout_kernel_count(HORIZON_STEPS)
 
     def barrier():
@@ -654,7 +656,7 @@ def main():
                        "policy_precision": "bf16 operands, f32 accumulation (tcgen05); f32 master weights",
                        "env_steps_per_bench_step": HORIZON_STEPS, "l2": "flushed between timed steps (256 MB write)",
                        "parallelism": f"replicas x{world} (cars independent, no collective)",
-                       "rollout_chains": chains,
+                       "rollout_chains": chains, "lidar_shape": lidar_shape,
                        "rollout_kernel": "fused persistent kernel" if chains == 0 else
                                          f"chained graph of per-step kernels, {chains} chain(s) (autotuned against "
                                          "the fused persistent kernel, timed in `fused_rollout`)",

@@ -237,7 +237,7 @@ int racer_runner_step(racer_sim* sim, racer_policy* policy, racer_acts* acts, fl
 int racer_rollout(racer_sim* sim, racer_policy* policy, racer_acts* acts, float* scratch_dev, int steps,
                   int deterministic, int64_t step0);
 /* Autotuner for the rollout graph: times `reps` rollouts of `steps` stochastic
- * Runner steps for 1 to 4 chains and (one-track sims, BF16 policy) the fused
+ * Runner steps for 1, 2, 3, 4, 6 and 8 chains and (one-track sims, BF16 policy) the fused
  * persistent kernel (after one warm-up rollout each; the sim state advances),
  * keeps the fastest and returns it with its env-steps/s; best_chains = 0
  * means the fused kernel won. */

@@ -1265,11 +1265,11 @@ int racer_runner_tune_chains(racer_sim* s, racer_policy* p, racer_acts* a, float
   int best = 1;
   float rate = 0.0f;
   const bool eligible = s->seg.count == 1 && policy_is_bf16(p);
-  const int max_chains = eligible ? 4 : 1;
   int64_t step0 = 0;
-  // candidates: 1 .. max_chains chains of kernels, then (eligible sims) the fused persistent kernel, as 0
-  for (int cand = 1; cand <= max_chains + (eligible ? 1 : 0); ++cand) {
-    const int chains = cand <= max_chains ? cand : 0;
+  // candidates: 1, 2, 3, 4, 6, 8 chains of kernels (one without a BF16 one-track policy), then (eligible
+  // sims) the fused persistent kernel, as 0
+  std::vector<int> cands = eligible ? std::vector<int>{1, 2, 3, 4, 6, 8, 0} : std::vector<int>{1};
+  for (const int chains : cands) {
     if (int rc = racer_sim_set_fused_rollout(s, chains == 0)) return rc;
     if (int rc = racer_sim_set_chains(s, chains == 0 ? 1 : chains)) return rc;
     if (int rc = racer_rollout(s, p, a, scratch, steps, 0, step0)) return rc;  // capture and warm up

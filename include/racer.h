@@ -101,7 +101,7 @@ int racer_sim_get_lidar_shape(racer_sim* sim, racer_lidar_shape* shape);
  * ms. The lidar only rewrites obs rows from the frames: the sim's state is
  * unchanged. */
 int racer_sim_autotune(racer_sim* sim, int reps, racer_lidar_shape* best, float* best_ms);
-/* Rollout graphs (racer_rollout) as `chains` (1..8) independent chains of
+/* Rollout graphs (racer_rollout) as `chains` (1..16) independent chains of
  * Runner steps over consecutive car ranges (multiples of 128), forked from and
  * joined into the sim's stream, so one chain's policy forward and physics run
  * beside another chain's lidar. Cars never interact, so every result is the
@@ -237,7 +237,7 @@ int racer_runner_step(racer_sim* sim, racer_policy* policy, racer_acts* acts, fl
 int racer_rollout(racer_sim* sim, racer_policy* policy, racer_acts* acts, float* scratch_dev, int steps,
                   int deterministic, int64_t step0);
 /* Autotuner for the rollout graph: times `reps` rollouts of `steps` stochastic
- * Runner steps for 1, 2, 3, 4, 6 and 8 chains and (one-track sims, BF16 policy) the fused
+ * Runner steps for 1, 2, 3, 4, 6, 8, 12 and 16 chains and (one-track sims, BF16 policy) the fused
  * persistent kernel (after one warm-up rollout each; the sim state advances),
  * keeps the fastest and returns it with its env-steps/s; best_chains = 0
  * means the fused kernel won. */

@@ -75,13 +75,14 @@ def test_config2_bridge_4096_cars_1081_beams_bit_exact():
     drive(gpu, cpu, 8, 2)
 
 
-def test_config2_chained_rollout_graph_equals_step_loop():
-    """The benchmark's rollout (one CUDA graph, four chains over car ranges) gives the bits of the
-    reference's host loop of Runner steps, at 4096 cars and 1081 beams."""
+@pytest.mark.parametrize("chains", [4, 8, 16])
+def test_config2_chained_rollout_graph_equals_step_loop(chains):
+    """The benchmark's rollout (one CUDA graph of independent chains over car ranges) gives the bits of
+    the reference's host loop of Runner steps, at 4096 cars and 1081 beams."""
     track = W.track("bridge")
     graph = W.Runner(track, 4096, beams=1081, seed=42, policy_seed=42)
     loop = W.Runner(track, 4096, beams=1081, seed=42, policy_seed=42)
-    graph.sim.set_chains(4)
+    graph.sim.set_chains(chains)
     graph.rollout(10, False, 100)
     for t in range(10):
         loop.step(False, 100 + t)

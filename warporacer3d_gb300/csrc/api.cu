@@ -755,7 +755,7 @@ int racer_trainer_rollout(racer_trainer* tr, racer_sim* s, racer_policy* p, race
   // with rollout chains (racer_sim_set_chains), each car range steps on its own stream
   const int chains = !tr->sur && s->chains > 1 && s->seg.count == 1 && policy_is_bf16(p) ? s->chains : 1;
   int audits = 0;
-  int bound[9];
+  int bound[MAX_CHAINS + 1];
   for (int c = 0; c <= chains; ++c) bound[c] = c == chains ? (int)n : std::min((int)n, (int)((long)n * c / chains / 128 * 128));
   if (chains > 1) {
     RACER_TRY(cudaEventRecord(s->chain_fork, st));
@@ -1203,7 +1203,7 @@ static int rollout_graph(racer_sim* s, racer_policy* p, racer_acts* a, float* sc
       // independent chains over car ranges (multiples of 128, the forward's tile), forked from and joined
       // into the sim's stream: parallel branches, so one chain's latency-bound kernels run beside
       // another's lidar
-      int bound[9];
+      int bound[MAX_CHAINS + 1];
       for (int c = 0; c <= chains; ++c) bound[c] = c == chains ? s->n : std::min(s->n, (int)((long)s->n * c / chains / 128 * 128));
       cudaError_t e = cudaEventRecord(s->chain_fork, s->st);
       for (int c = 1; c < chains && e == cudaSuccess; ++c) e = cudaStreamWaitEvent(s->chain_st[c - 1], s->chain_fork, 0);
@@ -1266,9 +1266,9 @@ int racer_runner_tune_chains(racer_sim* s, racer_policy* p, racer_acts* a, float
   float rate = 0.0f;
   const bool eligible = s->seg.count == 1 && policy_is_bf16(p);
   int64_t step0 = 0;
-  // candidates: 1, 2, 3, 4, 6, 8 chains of kernels (one without a BF16 one-track policy), then (eligible
+  // candidates: 1 to 16 chains of kernels (one without a BF16 one-track policy), then (eligible
   // sims) the fused persistent kernel, as 0
-  std::vector<int> cands = eligible ? std::vector<int>{1, 2, 3, 4, 6, 8, 0} : std::vector<int>{1};
+  std::vector<int> cands = eligible ? std::vector<int>{1, 2, 3, 4, 6, 8, 12, 16, 0} : std::vector<int>{1};
   for (const int chains : cands) {
     if (int rc = racer_sim_set_fused_rollout(s, chains == 0)) return rc;
     if (int rc = racer_sim_set_chains(s, chains == 0 ? 1 : chains)) return rc;
@@ -1459,7 +1459,7 @@ static bool same_shape(const racer_sim* s, const LidarShape& a, const LidarShape
 }
 
 int racer_sim_set_chains(racer_sim* s, int chains) {
-  RACER_ARG(s && chains >= 1 && chains <= 8, "racer_sim_set_chains: 1 to 8 chains");
+  RACER_ARG(s && chains >= 1 && chains <= MAX_CHAINS, "racer_sim_set_chains: 1 to 16 chains");
   RACER_TRY(cudaStreamSynchronize(s->st));
   if (!s->chain_fork) RACER_TRY(cudaEventCreateWithFlags(&s->chain_fork, cudaEventDisableTiming));
   while ((int)s->chain_st.size() < chains - 1) {

@@ -60,6 +60,8 @@ struct TrackDev {
 // counters, so segment k evolves exactly as a sim of that track alone.
 // Passed by value as a kernel parameter (about 0.8 KB).
 constexpr int MAX_SEGMENTS = 8;
+// Rollout graphs as at most this many independent chains over car ranges (racer_sim_set_chains).
+constexpr int MAX_CHAINS = 16;
 struct Segments {
   int count;
   int car0[MAX_SEGMENTS + 1];

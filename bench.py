@@ -21,7 +21,7 @@ Mojo/MAX toolchain does not exist on this machine).
 
 Under torchrun (N > 1) every rank runs the headline rollout on its own GPU
 (replicas, max-over-ranks timing); the further sections (FP64 audit,
-surrogate, config 1, batched, training, track compilation, CPU baseline) are
+surrogate, the reference's CPU-runnable benchmark, batched, training, track compilation, CPU baseline) are
 single-GPU measurements and run at N = 1 only.
 """
 import argparse
@@ -189,7 +189,7 @@ FP32_STEPS, FP32_REPS = 200, 3
 
 
 def fp32_policy_section(torch, W, track, stream, flush, runner):
-    """The headline workload with every product in FP32 (config 2 as stated: all float32): the
+    """The headline workload with every product in FP32 (the simulator and the policy all float32): the
     policy forward on the CUDA cores instead of BF16 tensor cores, rollouts of FP32_STEPS env steps
     from one graph (one chain: the chained graph needs the BF16 forward), device-timed like `value`."""
     state, obs = runner.sim.state.numpy(), runner.sim.obs.numpy()
@@ -309,7 +309,7 @@ SURR_TRAIN_SEEDS, SURR_TRAIN_ROLLOUT = (42, 43, 44), 32
 
 
 def surrogate_training_section(W, track, sur, iterations):
-    """PPO with the learned lidar (config 4: used in 65536-car PPO rollouts): bridge, 65536 cars x
+    """PPO with the learned lidar driving 65536-car PPO rollouts: bridge, 65536 cars x
     32-step rollouts at 1081 beams, `iterations` iterations of rollout + GAE + update per run, three
     seeds with exact observations and the same three with the surrogate's (audit every 16th step of
     training, exact fallback under 0.5 m; racer/ppo.mojo:187-337 per iteration, main.mojo:54-68 loop).

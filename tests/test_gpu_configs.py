@@ -1,12 +1,12 @@
-"""Parity at the benchmark configurations' own sizes.
+"""Parity at the benchmark workloads' own sizes.
 
 The other GPU tests check every kernel on small batches; these run the
 shapes the benchmark measures, where different launch paths are taken:
 
-- config 1 (the reference's CPU-runnable benchmark, `racer benchmark ramp cpu
-  1024 1000`): ramp, 1024 cars, 108 beams, sim seed 0;
-- config 2: bridge, 4096 cars, 1081 beams, and its rollout graph of four
-  chains over car ranges;
+- the reference's CPU-runnable benchmark (`racer benchmark ramp cpu 1024
+  1000`): ramp, 1024 cars, 108 beams, sim seed 0;
+- the headline workload: bridge, 4096 cars, 1081 beams, and its rollout graph
+  of independent chains over car ranges;
 - the policy forward at 65536 and 119,808 samples (the learned-lidar rollout
   and the uneven five-track batch), where the tiles of 128 samples outnumber
   the SMs and the persistent, TMA-staged forward runs;
@@ -55,7 +55,7 @@ def drive(gpu, cpu, steps, seed):
         check_sim(gpu, cpu, f"step {step}: ")
 
 
-def test_config1_ramp_1024_cars_seed0_bit_exact():
+def test_ramp_1024_cars_108_beams_seed0_bit_exact():
     """ramp, 1024 cars, 108 beams, sim seed 0: reset and 12 steps."""
     track = W.track("ramp")
     gpu, cpu = W.Sim(track, 1024, 0, beams=108), O.Sim(track, 1024, 0, beams=108)
@@ -65,7 +65,7 @@ def test_config1_ramp_1024_cars_seed0_bit_exact():
     drive(gpu, cpu, 12, 1)
 
 
-def test_config2_bridge_4096_cars_1081_beams_bit_exact():
+def test_bridge_4096_cars_1081_beams_bit_exact():
     """bridge, 4096 cars, 1081 beams: reset and 8 steps."""
     track = W.track("bridge")
     gpu, cpu = W.Sim(track, 4096, 42, beams=1081), O.Sim(track, 4096, 42, beams=1081)
@@ -76,7 +76,7 @@ def test_config2_bridge_4096_cars_1081_beams_bit_exact():
 
 
 @pytest.mark.parametrize("chains", [4, 8, 16])
-def test_config2_chained_rollout_graph_equals_step_loop(chains):
+def test_bridge_4096_chained_rollout_graph_equals_step_loop(chains):
     """The benchmark's rollout (one CUDA graph of independent chains over car ranges) gives the bits of
     the reference's host loop of Runner steps, at 4096 cars and 1081 beams."""
     track = W.track("bridge")

@@ -278,6 +278,7 @@ def surrogate_section(torch, W, track, stream, flush, train_steps=SURR_TRAIN_STE
             ms += a.elapsed_time(b)
         return SURR_CARS * SURR_STEPS * SURR_REPS / (ms / 1000.0)
 
+    exact_chains, _ = exact.tune_chains(SURR_STEPS, 2)  # the exact baseline in its fastest rollout form
     exact_rate = timed(lambda t0: exact.rollout(SURR_STEPS, False, t0))
     learned_rate = timed(lambda t0: learned.rollout_surrogate(sur, SURR_STEPS, False, t0, 16, 0.5))
     mae, rmse, mx, over, fallback = sur.rollout_stats(reset=True)
@@ -288,7 +289,8 @@ def surrogate_section(torch, W, track, stream, flush, train_steps=SURR_TRAIN_STE
     sur.set_spot_check(0, SPOT_TOL_M)
     keep["surrogate"] = sur  # trained once, reused by the training section
     return {"workload": f"{TRACK}, {SURR_CARS} cars, {BEAMS} beams, {SURR_STEPS}-step rollouts",
-            "exact_fp32_env_steps_per_s": exact_rate, "surrogate_bf16_env_steps_per_s": learned_rate,
+            "exact_fp32_env_steps_per_s": exact_rate, "exact_rollout_chains": exact_chains,
+            "surrogate_bf16_env_steps_per_s": learned_rate,
             "speedup": learned_rate / exact_rate, "audit_every": 16, "fallback_m": 0.5,
             "audited_mae_m": mae, "audited_rmse_m": rmse, "audited_max_m": mx, "audited_frac_over_5cm": over,
             "fallback_frac": fallback,

@@ -538,12 +538,13 @@ def test_gather_peak_is_plausible():
 
 
 @pytest.mark.parametrize("name,n,beams", [("bridge", 40, 1081), ("bridge", 4096, 1081), ("ramp", 1024, 108),
-                                          ("flat", 700, 108), ("bank", 333, 2)])
+                                          ("flat", 700, 108), ("bank", 333, 2), ("bridge", 65536, 1081)])
 def test_fused_rollout_equals_chained_graph(name, n, beams):
     """The fused persistent rollout kernel (forward + sampling, physics and lidar of a slice of cars
     per CTA, all steps in one launch) gives the chained graph's bits: state, observations, actions,
     rewards, done flags and the policy outputs, over 12 steps; car counts that fill a CTA's slice
-    unevenly, one car per CTA, the minimum beam count."""
+    unevenly, one car per CTA, the minimum beam count, and more CTAs than fit on the GPU at once
+    (65536 cars: 512 CTAs of 128)."""
     track = W.track(name)
     chained = W.Runner(track, n, beams=beams, seed=13, policy_seed=5)
     fused = W.Runner(track, n, beams=beams, seed=13, policy_seed=5)

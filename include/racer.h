@@ -274,10 +274,34 @@ int racer_runner_audit_dynamics(racer_sim* sim, racer_policy* policy, racer_acts
  * `beams` ranges / 10 m, for the sim's track (at most two layers).
  * `batch` (a multiple of 128) is the training batch; `seed` the init. */
 int racer_surrogate_create(racer_sim* sim, int hidden, int batch, uint64_t seed, racer_surrogate** out);
+/* frame 0: as racer_surrogate_create (one output per beam, the car frame).
+ * frame 1: the world frame: the network predicts the range profile at
+ * K = 4 (beams - 1) / 3 fixed world angles (the beam spacing; beams - 1 must
+ * be a multiple of 12) and beam b of a car reads the sample at its heading's
+ * offset plus b, so the rotation by the heading is exact rather than learned;
+ * the inputs are trainable feature grids per layer at the origin (five
+ * resolutions, eight features each), fixed Fourier features of x and y and
+ * the sub-sample phase of the heading. */
+int racer_surrogate_create_frame(racer_sim* sim, int hidden, int batch, uint64_t seed, int frame,
+                                 racer_surrogate** out);
 int racer_surrogate_destroy(racer_surrogate* surrogate);
 /* FP32 master parameters W1 [H,64] | W2 [H,H] | b2 [H] | W3 [H,H] | b3 [H] |
- * W4 [beams,H] | b4 [beams], and their last gradient (device pointers). */
+ * W4 [nout,H] | b4 [nout] (nout = beams, or K in the world frame) | (world
+ * frame, from the next multiple of 8) the feature grids, level by level
+ * [layers][gy][gx][8], and their last gradient (device pointers). */
 int racer_surrogate_params(racer_surrogate* surrogate, float** theta_dev, float** grad_dev, long* count, int* hidden);
+/* The world frame's feature-grid geometry: per level (5) the vertex counts
+ * gx, gy, the spacing in metres and the offset of the level's block in the
+ * parameters (null pointers are skipped); fails for a car-frame surrogate. */
+int racer_surrogate_grid(racer_surrogate* surrogate, int* gx, int* gy, float* spacing_m, long* offset);
+/* The encoded inputs (host, [batch, 64], the BF16 values as float) and, in the
+ * world frame, each sample's first world sample k0 (host, [batch]) of the
+ * batch of the last racer_surrogate_gradient call. */
+int racer_surrogate_batch_inputs(racer_surrogate* surrogate, float* inputs, int* k0);
+/* The surrogate's predictions (ranges / 10 m, clamped to [0, 1]) for that
+ * batch into pred_dev [beams, batch], through the rollouts' layered inference
+ * path (in the world frame: FP16 profiles, then the gather by heading). */
+int racer_surrogate_batch_predict(racer_surrogate* surrogate, float* pred_dev);
 /* Training set: `count` poses (a multiple of the batch), uniform over the
  * drivable cells of every layer, heading uniform in (-pi, pi). */
 int racer_surrogate_set_poses(racer_surrogate* surrogate, long count, uint64_t seed);

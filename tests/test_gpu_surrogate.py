@@ -4,7 +4,11 @@
   are bit-identical to the CPU oracle's scan of the same car.
 - Gradient: the GPU backward (tcgen05 GEMMs, BF16 operands, FP32
   accumulation) matches a float64 numpy backprop of the same network with the
-  same BF16 roundings, within 2e-2 relative (Frobenius) per parameter block.
+  same BF16 roundings, within 2e-2 relative (Frobenius) per parameter block,
+  in the car frame and in the world frame (its feature grids included).
+- World frame: the inputs and the heading offsets match a float64
+  recomputation, and inference reads each beam from the world profile at the
+  heading's offset.
 - Training: a few hundred Adam steps cut the held-out error against the exact
   tracer substantially.
 - Gain: a briefly trained surrogate, with its audits and per-car fallback to
@@ -115,14 +119,144 @@ def test_gradient_matches_float64_backprop():
         assert rel < 2e-2, (k, rel)
 
 
+FOV = 4.71238898
+
+
+def world_setup(hidden=128, B=256, steps=20):
+    """A briefly trained world-frame surrogate on bridge at 1081 beams and the gradient of its batch 0."""
+    track = W.track("bridge")
+    beams = 1081
+    sim = W.Sim(track, 8, 0, beams=beams)
+    sur = W.Surrogate(sim, hidden=hidden, batch=B, seed=3, frame="world")
+    sur.set_poses(4 * B, seed=9)
+    sur.train(steps, lr=3e-3)  # grids and weights away from their initial values
+    labels = W.DevArray.empty((beams, B))
+    sur.gradient(0, labels)
+    return track, sim, sur, labels.numpy().T.astype(np.float64)
+
+
+def grid_corners(sur, track, ox, oy):
+    """Per level: cell (iu, iv) and fractions (fu, fv) of the bilinear lookup, in float64."""
+    gx, gy, sp, offs = sur.grid()
+    x0, y0 = float(track[2]), float(track[3])
+    out = []
+    for l in range(W.Surrogate.GRID_LEVELS):
+        u = np.clip((ox.astype(np.float64) - x0) / sp[l], 0, gx[l] - 2)
+        v = np.clip((oy.astype(np.float64) - y0) / sp[l], 0, gy[l] - 2)
+        iu = np.minimum(np.floor(u).astype(int), gx[l] - 3)
+        iv = np.minimum(np.floor(v).astype(int), gy[l] - 3)
+        out.append((iu, iv, u - iu, v - iv))
+    return out
+
+
+def world_forward(sur, P, X):
+    Wb = {k: bf16(P[k]) for k in ("W1", "W2", "W3", "W4")}
+    h1 = bf16(np.tanh(X @ Wb["W1"].T))
+    h2 = bf16(np.tanh(h1 @ Wb["W2"].T + P["b2"]))
+    h3 = bf16(np.tanh(h2 @ Wb["W3"].T + P["b3"]))
+    return Wb, h1, h2, h3, h3 @ Wb["W4"].T + P["b4"]
+
+
+def test_world_frame_inputs_and_gradient_match_float64():
+    """The world frame's encoded inputs (feature grids at the lidar origin, Fourier features, heading
+    phase) match a float64 recomputation within BF16 rounding, its first world samples the heading's
+    offset, and the GPU gradient (world loss read through each sample's offset, the GEMM chain, the
+    input gradient scattered onto the grids) matches a float64 backprop with the same BF16 roundings
+    within 2e-2 relative (Frobenius) per block."""
+    track, sim, sur, T = world_setup()
+    B, beams, K = sur.batch, sim.beams, sur.nout
+    X, k0 = sur.batch_inputs()
+    theta, grad = sur.theta.numpy(), sur.grad.numpy()
+    lay = sur.layout()
+    P = {k: theta[o:o + int(np.prod(s))].reshape(s).astype(np.float64) for k, (o, s) in lay.items()}
+    poses = sur.poses().numpy()[:B]
+    fr = rest_frames(track, poses)
+    ox, oy, oz, sh, ch = fr[:, 3], fr[:, 4], fr[:, 5], fr[:, 6], fr[:, 7]
+    layer = poses[:, 3].astype(int)
+    # first world sample and phase
+    u = np.mod((np.arctan2(sh.astype(np.float64), ch.astype(np.float64)) - FOV / 2) * K / (2 * np.pi), K)
+    clear = np.abs(u - np.round(u)) > 1e-3
+    assert clear.sum() > 0.9 * B
+    assert np.array_equal(k0[clear], np.floor(u[clear]).astype(int) % K)
+    # inputs
+    corners = grid_corners(sur, track, ox, oy)
+    ref = np.zeros((B, 64))
+    for l, (iu, iv, fu, fv) in enumerate(corners):
+        G = P[f"G{l}"]
+        ref[:, 8 * l:8 * l + 8] = (G[layer, iv, iu] * ((1 - fu) * (1 - fv))[:, None] +
+                                   G[layer, iv, iu + 1] * (fu * (1 - fv))[:, None] +
+                                   G[layer, iv + 1, iu] * ((1 - fu) * fv)[:, None] +
+                                   G[layer, iv + 1, iu + 1] * (fu * fv)[:, None])
+    nx, ny, x0, y0, cell = track[0], track[1], track[2], track[3], track[4]
+    hx, hy = np.float32(0.5) * np.float32(nx - 1) * cell, np.float32(0.5) * np.float32(ny - 1) * cell
+    xn = ((ox - (x0 + hx)) * (np.float32(1) / hx)).astype(np.float64)
+    yn = ((oy - (y0 + hy)) * (np.float32(1) / hy)).astype(np.float64)
+    ref[:, 40:46] = np.stack([xn, yn, oz, layer == 0, layer == 1, np.ones(B)], 1)
+    for k in range(4):
+        a, b = np.pi * 2.0 ** k * xn, np.pi * 2.0 ** k * yn
+        ref[:, 46 + 4 * k:50 + 4 * k] = np.stack([np.sin(a), np.cos(a), np.sin(b), np.cos(b)], 1)
+    ref[:, 62], ref[:, 63] = np.sin(2 * np.pi * (u - np.floor(u))), np.cos(2 * np.pi * (u - np.floor(u)))
+    err = np.abs(X - ref)
+    assert np.all(err[clear] <= 2e-3 + 8e-3 * np.abs(ref[clear])), err[clear].max()
+    # backprop
+    Wb, h1, h2, h3, y = world_forward(sur, P, X.astype(np.float64))
+    idx = (k0[:, None] + np.arange(beams)) % K
+    G4 = np.zeros((B, K))
+    np.put_along_axis(G4, idx, 2.0 / (B * beams) * (np.take_along_axis(y, idx, 1) - T), 1)
+    g4 = bf16(G4)
+    g3 = bf16((g4 @ Wb["W4"]) * (1 - h3 * h3))
+    g2 = bf16((g3 @ Wb["W3"]) * (1 - h2 * h2))
+    g1 = bf16((g2 @ Wb["W2"]) * (1 - h1 * h1))
+    refg = {"W4": g4.T @ h3, "b4": G4.sum(0), "W3": g3.T @ h2, "b3": g3.sum(0), "W2": g2.T @ h1, "b2": g2.sum(0),
+            "W1": g1.T @ X.astype(np.float64)}
+    dX = g1 @ Wb["W1"]
+    for l, (iu, iv, fu, fv) in enumerate(corners):
+        Gg = np.zeros(P[f"G{l}"].shape)
+        d = dX[:, 8 * l:8 * l + 8]
+        for di, dj, w in ((0, 0, (1 - fu) * (1 - fv)), (1, 0, fu * (1 - fv)), (0, 1, (1 - fu) * fv), (1, 1, fu * fv)):
+            np.add.at(Gg, (layer, iv + dj, iu + di), w[:, None] * d)
+        refg[f"G{l}"] = Gg
+    for k, r in refg.items():
+        o, s = lay[k]
+        g = grad[o:o + int(np.prod(s))].reshape(s)
+        rel = np.linalg.norm(g - r) / np.linalg.norm(r)
+        assert rel < 2e-2, (k, rel)
+
+
+def test_world_frame_prediction_is_the_profile_read_at_the_heading():
+    """Inference in the world frame (FP16 world profiles, then the gather by heading): beam b of a
+    sample is its clamped world sample (k0 + b) mod K, against a float64 forward of the same inputs."""
+    track, sim, sur, T = world_setup()
+    B, beams, K = sur.batch, sim.beams, sur.nout
+    X, k0 = sur.batch_inputs()
+    pred = W.DevArray.empty((beams, B))
+    sur.batch_predict(pred)
+    got = pred.numpy().T
+    theta = sur.theta.numpy()
+    P = {k: theta[o:o + int(np.prod(s))].reshape(s).astype(np.float64) for k, (o, s) in sur.layout().items()}
+    y = world_forward(sur, P, X.astype(np.float64))[-1]
+    want = np.clip(y, 0, 1).astype(np.float16).astype(np.float64)
+    want = np.take_along_axis(want, (k0[:, None] + np.arange(beams)) % K, 1)
+    assert np.all((got >= 0) & (got <= 1))
+    assert np.abs(got - want).max() < 2e-3
+
+
+def test_world_frame_needs_the_beam_spacing_to_divide_the_circle():
+    sim = W.Sim(W.track("bridge"), 8, 0, beams=108)
+    with pytest.raises(W.RacerError, match="multiple of 12"):
+        W.Surrogate(sim, hidden=128, batch=256, seed=1, frame="world")
+    W.Surrogate(W.Sim(W.track("bridge"), 8, 0, beams=109), hidden=128, batch=256, seed=1, frame="world")
+
+
+@pytest.mark.parametrize("frame", ["car", "world"])
 @pytest.mark.parametrize("audit_every,fallback_m", [(1, 0.5), (0, 100.0)])
-def test_fully_exact_surrogate_rollout_equals_exact_rollout(audit_every, fallback_m):
+def test_fully_exact_surrogate_rollout_equals_exact_rollout(audit_every, fallback_m, frame):
     """Audit on every step, or a fallback threshold every car crosses: the rollout is the exact one."""
     track = W.track("bridge")
     n = 512
     exact = W.Runner(track, n, beams=1081, seed=3)
     sur_run = W.Runner(track, n, beams=1081, seed=3)
-    sur = W.Surrogate(sur_run.sim, hidden=128, batch=1024, seed=1)
+    sur = W.Surrogate(sur_run.sim, hidden=128, batch=1024, seed=1, frame=frame)
     exact.rollout(6, False, 40)
     sur_run.rollout_surrogate(sur, 6, False, 40, audit_every=audit_every, fallback_m=fallback_m)
     sur_run.synchronize()
@@ -149,10 +283,11 @@ def test_surrogate_rollout_stats_and_fallback():
     assert sur.rollout_stats()[0] == 0.0  # reset
 
 
-def test_training_reduces_heldout_error():
+@pytest.mark.parametrize("frame", ["car", "world"])
+def test_training_reduces_heldout_error(frame):
     track = W.track("bridge")
     sim = W.Sim(track, 8, 0, beams=1081)
-    sur = W.Surrogate(sim, hidden=256, batch=1024, seed=1)
+    sur = W.Surrogate(sim, hidden=256, batch=1024, seed=1, frame=frame)
     sur.set_poses(1 << 16, seed=2)
     before = sur.evaluate(batches=2, seed=77)
     mse, mae = sur.train(300, lr=1e-3)
@@ -161,17 +296,18 @@ def test_training_reduces_heldout_error():
     assert after[0] < 0.7 * before[0], (before, after)
 
 
+@pytest.mark.parametrize("frame", ["car", "world"])
 @pytest.mark.parametrize("cars", [300, 128 * 160 + 37])
-def test_fused_inference_equals_layered_gemms(cars):
+def test_fused_inference_equals_layered_gemms(cars, frame):
     """The fused 512-wide inference kernel (activations kept on chip, output in TMEM chunks) gives the
     same bits as the four GEMM launches: obs, the fallback cars picked from the per-car minimum
     ranges, state. 128 * 160 + 37 cars is more tiles than SMs, so CTAs run several tiles. One
     trained surrogate serves both (training sums bias gradients with atomics), and the sim's state
     and observations are restored between the two rollouts."""
     run = W.Runner(W.track("bridge"), cars, beams=1081, seed=5)
-    sur = W.Surrogate(run.sim, hidden=512, batch=1024, seed=2)
+    sur = W.Surrogate(run.sim, hidden=512, batch=1024, seed=2, frame=frame)
     sur.set_poses(1 << 14, seed=4)
-    sur.train(30, lr=2e-3)
+    sur.train(30 if frame == "car" else 400, lr=2e-3)  # until some cars' smallest prediction passes 0.5 m
     state0, obs0 = run.sim.state.numpy(), run.sim.obs.numpy()
     out = []
     for fused in (True, False):

@@ -86,6 +86,10 @@ SIGNATURES = {
     "racer_runner_audit_dynamics": [c_void_p, c_void_p, c_void_p, c_void_p, c_int, c_int, c_int64,
                                     P(ctypes.c_double)],
     "racer_surrogate_create": [c_void_p, c_int, c_int, c_uint64, P(c_void_p)],
+    "racer_surrogate_create_frame": [c_void_p, c_int, c_int, c_uint64, c_int, P(c_void_p)],
+    "racer_surrogate_grid": [c_void_p, P(c_int), P(c_int), P(c_float), P(ctypes.c_long)],
+    "racer_surrogate_batch_inputs": [c_void_p, P(c_float), P(c_int)],
+    "racer_surrogate_batch_predict": [c_void_p, c_void_p],
     "racer_surrogate_destroy": [c_void_p],
     "racer_surrogate_set_loss": [c_void_p, c_float],
     "racer_surrogate_set_spot_check": [c_void_p, c_int, c_float],

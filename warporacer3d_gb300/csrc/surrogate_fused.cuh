@@ -27,10 +27,64 @@
 // A wait for completion k of a barrier uses parity k & 1; every wait is bounded
 // and a timeout sets *err.
 #pragma once
+#include <cuda_fp16.h>
+
+#include "common.cuh"
 #include "tc.cuh"
 
 namespace racer {
 namespace {
+
+// World sample read by beam 0 of a car with heading (sin h, cos h), and the
+// phase (fractional part) of its angle: u = (h - FOV / 2) K / (2 pi) mod K.
+__device__ __forceinline__ int world_phase(float sh, float ch, int K, float* phase) {
+  float u = (atan2f(sh, ch) - 0.5f * FOV) * ((float)K / TWO_PI_F);
+  if (u < 0.0f) u += (float)K;        // u > -K before
+  if (!(u < (float)K)) u = 0.0f;     // rounded up to K, or a NaN heading
+  const int k = (int)u;
+  *phase = u - (float)k;
+  return k;
+}
+
+// World frame, inference: 16 world samples o0 .. o0 + 15 of one car (o0 a
+// multiple of 16, K of 16), saturated to [0, 1], rounded to FP16 into row
+// (16-byte aligned), and the smallest of those inside the car's field of view
+// (beam (o - k0) mod K < beams), taken before the rounding and rounded once
+// (rounding is monotonic, so that is the smallest rounded value). A group
+// with no sample in the field of view is not stored (nothing reads it). The
+// fused kernel and the layered epilogue both use it.
+__device__ __forceinline__ float world_store16(const float* v, const float* bias, int o0, int K, int k0, int beams,
+                                               __half* row, float lo) {
+  if (o0 >= K) return lo;
+  int b0 = o0 - k0;  // beam of sample o0 (mod K)
+  if (b0 < 0) b0 += K;
+  if (b0 >= beams && b0 + 15 < K) return lo;  // wholly outside the field of view
+  float y[16];
+#pragma unroll
+  for (int j = 0; j < 16; ++j) y[j] = __saturatef(v[j] + bias[j]);
+  uint32_t w[8];
+#pragma unroll
+  for (int j = 0; j < 8; ++j) {
+    const __half2 t = __floats2half2_rn(y[2 * j], y[2 * j + 1]);
+    w[j] = *reinterpret_cast<const uint32_t*>(&t);
+  }
+  uint4* dst = reinterpret_cast<uint4*>(row + o0);
+  dst[0] = make_uint4(w[0], w[1], w[2], w[3]);
+  dst[1] = make_uint4(w[4], w[5], w[6], w[7]);
+  float mn = 1.0f;
+  if (b0 + 15 < beams) {  // wholly inside
+#pragma unroll
+    for (int j = 0; j < 16; ++j) mn = fminf(mn, y[j]);
+  } else {
+#pragma unroll
+    for (int j = 0; j < 16; ++j) {
+      int b = b0 + j;
+      if (b >= K) b -= K;
+      if (b < beams) mn = fminf(mn, y[j]);
+    }
+  }
+  return fminf(lo, __half2float(__float2half_rn(mn)));
+}
 
 constexpr int SF_H = 512;                      // hidden width
 constexpr int SF_KB = SF_H / 64;               // k-blocks of a hidden activation
@@ -45,10 +99,15 @@ struct FusedArgs {
   const float* b2;
   const float* b3;
   const float* b4;
-  float* out;  // obs + 4 n: out[o * n + car]
+  float* out;  // obs + 4 n: out[o * n + car] (car frame)
   unsigned* minr;
   int n, beams, chunks;  // chunks = ceil(npad / 256)
   int* err;
+  // world frame (wout not null): world profiles wout[car * ldw + o] (FP16), K world samples;
+  // the ray frames [2, n] give each car's field of view
+  __half* wout;
+  int ldw, K;
+  const float4* ray;
 };
 
 struct SfBars {
@@ -204,6 +263,12 @@ __device__ bool sf_epilogue(uint32_t tmem, uint8_t* abuf, const SfBars& b, const
       tc::mbar_arrive(b.edone);
     }
     float lo = 1.0f;
+    const int nout = args.wout ? args.K : args.beams;  // outputs: world samples or beams
+    int k0 = 0;  // world frame: the world sample of the car's beam 0
+    if (args.wout && m < args.n) {
+      float ph;
+      k0 = world_phase(args.ray[args.n + m].x, args.ray[m].w, args.K, &ph);
+    }
     for (int p = 0; p < nc; ++p) {  // output: p-th chunk in slot p & 1, this warp's 64 of its 256 columns
       const int s = p & 1, c = (p + rot) % nc;
       if (!sf_wait(&b.accfull[s], ((s ? f1 : f0) + 3 + p / 2) & 1, b.abort)) return false;
@@ -212,7 +277,7 @@ __device__ bool sf_epilogue(uint32_t tmem, uint8_t* abuf, const SfBars& b, const
       for (int i = 0; i < 2; ++i) {
         const int o0 = 256 * c + 128 * h + 64 * g + 32 * i;
         float bb[32];
-        if (o0 + 32 <= args.beams) {
+        if (o0 + 32 <= nout) {
 #pragma unroll
           for (int q4 = 0; q4 < 8; ++q4) {
             const float4 t4 = __ldg(reinterpret_cast<const float4*>(args.b4 + o0) + q4);
@@ -220,10 +285,16 @@ __device__ bool sf_epilogue(uint32_t tmem, uint8_t* abuf, const SfBars& b, const
           }
         } else {
 #pragma unroll
-          for (int j = 0; j < 32; ++j) bb[j] = o0 + j < args.beams ? __ldg(args.b4 + o0 + j) : 0.0f;
+          for (int j = 0; j < 32; ++j) bb[j] = o0 + j < nout ? __ldg(args.b4 + o0 + j) : 0.0f;
         }
         tc::tmem_ld32_sync(tmem + lane_addr + 256 * s + 128 * h + 64 * g + 32 * i, v);
-        if (m < args.n) {
+        if (args.wout) {
+          if (m < args.n && o0 < args.ldw) {  // o0 is a multiple of 32, ldw of 64
+            __half* row = args.wout + (long)m * args.ldw;
+            lo = world_store16(v, bb, o0, args.K, k0, args.beams, row, lo);
+            lo = world_store16(v + 16, bb + 16, o0 + 16, args.K, k0, args.beams, row, lo);
+          }
+        } else if (m < args.n) {
 #pragma unroll
           for (int j = 0; j < 32; ++j) {
             const int o = o0 + j;

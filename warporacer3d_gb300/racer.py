@@ -339,14 +339,24 @@ class Trainer:
 
 
 class Surrogate:
-    """Learned lidar for one sim's track: lidar frame -> all beam ranges (BF16 MLP on tcgen05)."""
+    """Learned lidar for one sim's track: lidar frame -> all beam ranges (BF16 MLP on tcgen05).
 
-    def __init__(self, sim, hidden=512, batch=8192, seed=0):
+    frame="car": one output per beam from fixed Fourier features of the frame. frame="world": the
+    range profile at fixed world angles (the beam spacing), read at each car's heading offset, from
+    trainable feature grids of the origin (beams - 1 must be a multiple of 12)."""
+
+    GRID_LEVELS, GRID_F = 5, 8
+
+    def __init__(self, sim, hidden=512, batch=8192, seed=0, frame="car"):
+        if frame not in ("car", "world"):
+            raise ValueError("frame must be 'car' or 'world'")
         self.sim = sim
         h = ctypes.c_void_p()
-        call("racer_surrogate_create", sim.handle, hidden, batch, seed, ctypes.byref(h))
+        call("racer_surrogate_create_frame", sim.handle, hidden, batch, seed, int(frame == "world"),
+             ctypes.byref(h))
         self.handle = h
-        self.batch, self.hidden = batch, hidden
+        self.batch, self.hidden, self.frame = batch, hidden, frame
+        self.nout = 4 * (sim.beams - 1) // 3 if frame == "world" else sim.beams
         th, gr, count = ctypes.c_void_p(), ctypes.c_void_p(), ctypes.c_long()
         call("racer_surrogate_params", h, ctypes.byref(th), ctypes.byref(gr), ctypes.byref(count), None)
         self.theta = DevArray(th.value, (count.value,), owner=self, stream=sim.stream)
@@ -358,14 +368,42 @@ class Surrogate:
             self.handle = None
 
     def layout(self):
-        H, beams, n = self.hidden, self.sim.beams, 64
-        sizes = [("W1", (H, n)), ("W2", (H, H)), ("b2", (H,)), ("W3", (H, H)), ("b3", (H,)), ("W4", (beams, H)),
-                 ("b4", (beams,))]
+        """{name: (offset, shape)} of the parameter blocks; the world frame adds the grids G0..G4,
+        each [layers, gy, gx, 8]."""
+        H, K, n = self.hidden, self.nout, 64
+        sizes = [("W1", (H, n)), ("W2", (H, H)), ("b2", (H,)), ("W3", (H, H)), ("b3", (H,)), ("W4", (K, H)),
+                 ("b4", (K,))]
         out, off = {}, 0
         for name, shape in sizes:
             out[name] = (off, shape)
             off += int(np.prod(shape))
+        if self.frame == "world":
+            gx, gy, sp, offs = self.grid()
+            layers = (offs[1] - offs[0]) // (gx[0] * gy[0] * self.GRID_F)
+            for l in range(self.GRID_LEVELS):
+                out[f"G{l}"] = (int(offs[l]), (layers, int(gy[l]), int(gx[l]), self.GRID_F))
         return out
+
+    def grid(self):
+        """World frame: per level the vertex counts gx, gy, the spacing (m) and the parameter offset."""
+        L = self.GRID_LEVELS
+        gx, gy, sp, off = (ctypes.c_int * L)(), (ctypes.c_int * L)(), (ctypes.c_float * L)(), (ctypes.c_long * L)()
+        call("racer_surrogate_grid", self.handle, gx, gy, sp, off)
+        return list(gx), list(gy), list(sp), list(off)
+
+    def batch_inputs(self):
+        """Encoded inputs [batch, 64] of the last gradient() batch and (world frame) each sample's k0."""
+        x = np.zeros((self.batch, 64), np.float32)
+        k0 = np.zeros(self.batch, np.int32)
+        fp, ip = ctypes.POINTER(ctypes.c_float), ctypes.POINTER(ctypes.c_int)
+        call("racer_surrogate_batch_inputs", self.handle, x.ctypes.data_as(fp),
+             k0.ctypes.data_as(ip) if self.frame == "world" else None)
+        return x, (k0 if self.frame == "world" else None)
+
+    def batch_predict(self, pred):
+        """Predictions [beams, batch] (DevArray) for the last gradient() batch, through the layered
+        inference path."""
+        call("racer_surrogate_batch_predict", self.handle, pred.c)
 
     def set_poses(self, count, seed=1):
         call("racer_surrogate_set_poses", self.handle, count, seed)

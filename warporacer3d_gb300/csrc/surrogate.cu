@@ -503,8 +503,6 @@ __global__ void k_grid_grad(const float4* __restrict__ ray, int B, GridGeom gg, 
 // elements are the only ones read; the rest of a piece may hold anything
 // (world_store16 skips groups outside every window). Small blocks (35 KB of
 // shared memory at 1081 beams) let several per SM overlap loads and stores.
-// Cars with minr below skip_bits (the exact fallback's cars, traced at the
-// same time on another stream) are left alone.
 constexpr int WR_CARS = 16, WR_THREADS = 256;
 // Words (2 halves) per staged row: the window plus a partial piece at each end,
 // rounded to an odd count so that rows start in different banks.
@@ -512,16 +510,15 @@ __host__ __device__ constexpr int world_rotate_words(int beams) { return (((beam
 
 __global__ void __launch_bounds__(WR_THREADS) k_world_rotate(const __half* __restrict__ wout, int ldw,
                                                              const float4* __restrict__ ray, int n, int beams, int K,
-                                                             float* pred, long ldp, const unsigned* __restrict__ minr,
-                                                             unsigned skip_bits) {
+                                                             float* pred, long ldp) {
   extern __shared__ __align__(16) uint8_t wr_smem[];
   uint32_t* rows = reinterpret_cast<uint32_t*>(wr_smem);
   __shared__ int k0s[WR_CARS];
   const int words = world_rotate_words(beams), m0 = blockIdx.x * WR_CARS;
   if (threadIdx.x < WR_CARS) {
-    int k0 = -1;  // -1: nothing to write for this car
+    int k0 = -1;  // -1: no car
     const int m = m0 + threadIdx.x;
-    if (m < n && !(minr && minr[m] < skip_bits)) {
+    if (m < n) {
       float ph;
       k0 = world_phase(ray[n + m].x, ray[m].w, K, &ph);
     }
@@ -745,9 +742,6 @@ struct racer_surrogate {
   float* dx = nullptr;
   __half* wbatch = nullptr;
   __half* wout = nullptr;
-  // world frame rollouts: the exact tracer's second stream and its fork/join events
-  cudaStream_t side = nullptr;
-  cudaEvent_t fork_ev = nullptr, join_ev = nullptr;
   int2* cells = nullptr;
   int ncells = 0;
   float4* poses = nullptr;
@@ -868,10 +862,9 @@ int world_profiles(racer_surrogate* s, SurrogateActs* a, const float4* ray, __ha
   return 0;
 }
 
-// Beam rows pred [beams, ldp] of M cars from their world profiles (k_world_rotate);
-// cars with minr below skip_bits are not written.
+// Beam rows pred [beams, ldp] of M cars from their world profiles (k_world_rotate).
 int world_rotate(racer_surrogate* s, const __half* wout, const float4* ray, int M, float* pred, long ldp,
-                 cudaStream_t st, const unsigned* minr = nullptr, unsigned skip_bits = 0) {
+                 cudaStream_t st) {
   if (s->L.beams > 1537) {
     racer_host::set_error("surrogate: the world frame serves at most 1537 beams");
     return 1;
@@ -879,7 +872,7 @@ int world_rotate(racer_surrogate* s, const __half* wout, const float4* ray, int 
   SURR_CHECK(world_rotate_configure());
   const int smem = WR_CARS * world_rotate_words(s->L.beams) * 4;
   k_world_rotate<<<(M + WR_CARS - 1) / WR_CARS, WR_THREADS, smem, st>>>(wout, s->L.npad, ray, M, s->L.beams,
-                                                                        s->L.nout, pred, ldp, minr, skip_bits);
+                                                                        s->L.nout, pred, ldp);
   SURR_CHECK(cudaGetLastError());
   return 0;
 }
@@ -1120,9 +1113,6 @@ int racer_surrogate_destroy(racer_surrogate* s) {
   if (!s) return 0;
   for (void* p : {(void*)s->w1t, (void*)s->wy, (void*)s->dx, (void*)s->wbatch, (void*)s->wout})
     cudaFree(p);
-  if (s->fork_ev) cudaEventDestroy(s->fork_ev);
-  if (s->join_ev) cudaEventDestroy(s->join_ev);
-  if (s->side) cudaStreamDestroy(s->side);
   for (void* p : {(void*)s->theta, (void*)s->grad, (void*)s->m1, (void*)s->m2, (void*)s->w1b, (void*)s->w2b,
                   (void*)s->w3b, (void*)s->w4b, (void*)s->w2t, (void*)s->w3t, (void*)s->w4t, (void*)s->cells,
                   (void*)s->poses, (void*)s->ray, (void*)s->label, (void*)s->lcache, (void*)s->pred, (void*)s->scratch,
@@ -1506,11 +1496,6 @@ int surrogate_prepare(racer_surrogate* s, racer_sim* sim) {
   if (s->L.world) {
     SURR_CHECK(world_rotate_configure());  // before any capture
     if ((rc = salloc(&s->wout, (size_t)n * s->L.npad))) return rc;
-    if (!s->side) {
-      SURR_CHECK(cudaStreamCreateWithFlags(&s->side, cudaStreamNonBlocking));
-      SURR_CHECK(cudaEventCreateWithFlags(&s->fork_ev, cudaEventDisableTiming));
-      SURR_CHECK(cudaEventCreateWithFlags(&s->join_ev, cudaEventDisableTiming));
-    }
   }
   if ((rc = make_acts(s, &s->infer, n, false)) || (rc = salloc(&s->minr, (size_t)n)) ||
       (rc = salloc(&s->list, (size_t)n)) || (rc = salloc(&s->list_count, 1)) || (rc = salloc(&s->list_units, 1)) ||
@@ -1560,39 +1545,24 @@ int surrogate_lidar(racer_surrogate* s, racer_sim* sim, float* obs, bool audit, 
     s->st = keep;
     if (rc) return rc;
   }
-  // The exact tracer for the audit or the fallback cars. In the world frame it
-  // runs on a second stream while the gather writes the predicted rows (other
-  // rows: the audit's scratch rows, or the cars not falling back); with the
-  // spot check, which reads the predicted rows, everything stays in order.
-  const bool exact_work = audit || fallback > 0.0f || s->spot_stride > 0;
-  const bool overlap = world && exact_work && (audit || s->spot_stride == 0);
-  cudaStream_t xs = st;
-  if (overlap) {
-    SURR_CHECK(cudaEventRecord(s->fork_ev, st));
-    SURR_CHECK(cudaStreamWaitEvent(s->side, s->fork_ev, 0));
-    xs = s->side;
-  }
-  if (world && !overlap)
+  // The predicted rows first (the spot check reads them), then the exact
+  // tracer for the audit or the fallback cars. (Tracing the fallback cars on a
+  // second stream beside the world frame's gather measured slower than this
+  // order: the two kernels contend for the SMs.)
+  if (world)
     if (int rc = world_rotate(s, s->wout, sim->ray, n, pred, n, st)) return rc;
   if (audit) {
-    launch_lidar(sim->t, sim->ray, obs, n, beams, sim->beam_dir, nullptr, xs);
-  } else if (exact_work) {
+    launch_lidar(sim->t, sim->ray, obs, n, beams, sim->beam_dir, nullptr, st);
+  } else if (fallback > 0.0f || s->spot_stride > 0) {
     if (s->spot_stride > 0)  // a checked beam off by more than the tolerance marks its car (minr = 0)
       launch_lidar_spot(sim->t, sim->ray, pred, n, beams, sim->beam_dir, s->spot_stride, step_base, step_add,
-                        s->spot_tol, s->minr, xs);
-    SURR_CHECK(cudaMemsetAsync(s->list_count, 0, sizeof(int), xs));
+                        s->spot_tol, s->minr, st);
+    SURR_CHECK(cudaMemsetAsync(s->list_count, 0, sizeof(int), st));
     // the threshold stays above 0 so that marked cars are always selected
-    launch_select_cars(s->minr, n, fallback > 0.0f ? fallback : 1e-30f, s->list, s->list_count, xs);
+    launch_select_cars(s->minr, n, fallback > 0.0f ? fallback : 1e-30f, s->list, s->list_count, st);
     launch_lidar_list(sim->t, sim->ray, obs, n, beams, sim->beam_dir, s->list, s->list_count, n, s->list_units,
-                      sim->sms, xs);
-    k_count_fallback<<<1, 32, 0, xs>>>(s->list_count, s->rcount + 1);
-  }
-  if (overlap) {
-    unsigned skip = 0;  // the fallback cars' rows belong to the exact tracer
-    if (!audit) memcpy(&skip, &fallback, sizeof skip);
-    if (int rc = world_rotate(s, s->wout, sim->ray, n, pred, n, st, s->minr, skip)) return rc;
-    SURR_CHECK(cudaEventRecord(s->join_ev, s->side));
-    SURR_CHECK(cudaStreamWaitEvent(st, s->join_ev, 0));
+                      sim->sms, st);
+    k_count_fallback<<<1, 32, 0, st>>>(s->list_count, s->rcount + 1);
   }
   if (audit) k_compare<<<1216, 256, 0, st>>>(pred, obs + 4L * n, (long)beams * n, s->rsums, s->rmax, s->rcount);
   SURR_CHECK(cudaGetLastError());

@@ -246,7 +246,7 @@ def fused_rollout_section(torch, W, track, stream, flush, runner):
 
 
 SURR_CARS, SURR_STEPS, SURR_REPS, SURR_TRAIN_STEPS = 65536, 32, 3, 80000
-SURR_LR = {"world": 3e-3, "car": 8e-3}
+SURR_LR = {"world": 2e-3, "car": 8e-3}
 SURR_HUBER_M = 0.02
 SPOT_STRIDE, SPOT_TOL_M = 64, 1.0
 SURR_NETWORK = {

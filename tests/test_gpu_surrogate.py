@@ -323,7 +323,8 @@ def test_fused_inference_equals_layered_gemms(cars, frame):
     assert 0.0 < fb_f < 1.0
 
 
-def test_trained_surrogate_rollout_beats_exact_rollout():
+@pytest.mark.parametrize("frame", ["car", "world"])
+def test_trained_surrogate_rollout_beats_exact_rollout(frame):
     """What the learned part gains over the method without it: after 3000 Adam steps on 2^18
     traced poses, the surrogate rollout (every 16th step traced exactly for all cars, and each car
     whose smallest predicted range is under 0.5 m traced exactly) of 16384 cars at 1081 beams takes
@@ -333,10 +334,10 @@ def test_trained_surrogate_rollout_beats_exact_rollout():
     cars, steps = 16384, 32
     exact = W.Runner(track, cars, beams=1081, seed=7)
     learned = W.Runner(track, cars, beams=1081, seed=7)
-    sur = W.Surrogate(learned.sim, hidden=512, batch=8192, seed=1)
+    sur = W.Surrogate(learned.sim, hidden=512, batch=8192, seed=1, frame=frame)
     sur.set_poses(1 << 18, seed=2)
     sur.set_loss(0.02)
-    sur.train(3000, lr=8e-3)
+    sur.train(3000, lr=8e-3 if frame == "car" else 2e-3)
 
     def wall(runner, roll):
         roll(0)  # capture and warm up the graph

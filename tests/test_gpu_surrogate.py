@@ -241,6 +241,29 @@ def test_world_frame_prediction_is_the_profile_read_at_the_heading():
     assert np.abs(got - want).max() < 2e-3
 
 
+def test_world_frame_on_a_one_layer_track():
+    """bank (one layer): one grid layer, the same training and inference paths; training cuts the
+    held-out error and a surrogate rollout with audits on every step is the exact rollout."""
+    track = W.track("bank")
+    sim = W.Sim(track, 8, 0, beams=1081)
+    sur = W.Surrogate(sim, hidden=128, batch=1024, seed=1, frame="world")
+    lay = sur.layout()
+    assert all(lay[f"G{l}"][1][0] == 1 for l in range(W.Surrogate.GRID_LEVELS))
+    sur.set_poses(1 << 14, seed=2)
+    before = sur.evaluate(batches=2, seed=77)
+    sur.train(300, lr=2e-3)
+    after = sur.evaluate(batches=2, seed=77)
+    assert after[0] < 0.7 * before[0], (before, after)
+    exact = W.Runner(track, 256, beams=1081, seed=4)
+    run = W.Runner(track, 256, beams=1081, seed=4)
+    sur.bind(run.sim)
+    exact.rollout(3, False, 0)
+    run.rollout_surrogate(sur, 3, False, 0, audit_every=1, fallback_m=0.5)
+    run.synchronize()
+    for name in ("state", "obs", "reward", "done", "actions"):
+        assert np.array_equal(getattr(exact.sim, name).numpy(), getattr(run.sim, name).numpy()), name
+
+
 def test_world_frame_needs_the_beam_spacing_to_divide_the_circle():
     sim = W.Sim(W.track("bridge"), 8, 0, beams=108)
     with pytest.raises(W.RacerError, match="multiple of 12"):

@@ -12,7 +12,8 @@
    huge or non-finite origin height or a subnormal descent) evaluates
    fl / descent only when fl * RN(1 / descent) <= a * (1 + 2^-20); the claim:
    whenever it skips, RN(fl / descent) >= a, so min(a, fl / descent) = a.
-3. The quotient of the unguarded march (sim.cu, quotient): from y = RN(1 / b) and
+3. The quotient of the unguarded march (sim.cu, quotient; also the ray's
+   normalisation, div_by, and the obs value range / 10, range_obs): from y = RN(1 / b) and
    q0 = RN(a * y), two residual corrections q <- RN(q + RN(a - b q) y), each a
    pair of fused multiply-adds, give RN(a / b); the claim is checked on the
    march's operand ranges, on wide exponents and on quotients a hair from a
@@ -177,6 +178,46 @@ def test_quotient_by_residual_corrections_is_ieee_division():
         bad += int(np.sum(q[ok] != ref[ok]))
         total += int(ok.sum())
     assert total > 2_900_000 and bad == 0
+
+
+def test_ray_normalisation_by_residual_corrections_is_ieee_division():
+    """sim.cu div_by: the ray's components (either sign, zeros of either sign, magnitudes down to
+    1e-20) over norms from 0.9 to 4, against IEEE division, signs of zero included."""
+    rng = np.random.default_rng(11)
+    n = 1_000_000
+    a = (rng.choice([-1, 1], n) * 10 ** rng.uniform(-20, 0.3, n)).astype(f32)
+    a[:1000] = f32(0)
+    a[1000:2000] = f32(-0.0)
+    b = rng.uniform(0.9, 4.0, n).astype(f32)
+    with np.errstate(all="ignore"):
+        y = f32(1) / b
+        q = a * y
+        for _ in range(2):
+            q = fma32(fma32(-q, b, a), y, q)
+        q = np.where(a == 0, a, q)
+        ref = a / b
+    assert np.array_equal(q, ref) and np.array_equal(np.signbit(q), np.signbit(ref))
+
+
+def test_range_over_ten_by_residual_corrections_is_ieee_division():
+    """sim.cu range_obs: RN(range / 10) as quotient(range, 10, 0.1f, range * 0.1f) for ranges from
+    2^-60 up. With a fixed divisor every step of the corrections scales exactly with the dividend's
+    power of two while no intermediate is subnormal (true from 2^-60), so one binade checked at every
+    binary32 value covers every binade; the ranges' own [8, 10] and the lowest binade are checked too."""
+    def corrected(a):
+        with np.errstate(all="ignore"):
+            ten, y = np.full_like(a, f32(10)), np.full_like(a, f32(0.1))
+            q = a * y
+            for _ in range(2):
+                q = fma32(fma32(-q, ten, a), y, q)
+        return q
+    binades = [np.arange(0x3F800000, 0x40000000, dtype=np.uint32),  # [1, 2): every value
+               np.arange(0x41000000, 0x41200001, dtype=np.uint32),  # [8, 10]
+               np.arange(0x21800000, 0x21800000 + (1 << 20), dtype=np.uint32)]  # from 2^-60
+    for bits in binades:
+        for chunk in np.array_split(bits, 8):
+            a = chunk.view(f32)
+            assert np.array_equal(corrected(a), a / f32(10))
 
 
 def test_magic_rounding_and_off_map_index():

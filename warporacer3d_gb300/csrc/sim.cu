@@ -664,13 +664,29 @@ __device__ __forceinline__ float beam_range(const TrackDev& t, const float4* ray
                                             const float2* __restrict__ beam_dir, int max_iters, bool counted,
                                             int car, int beam, int* count_out);
 
+__device__ __forceinline__ float quotient(float a, float b, float y, float q0);
+
+// RN(a / b) for b normal and a zero or normal of either sign, from y = RN(1 / b):
+// the quotient's residual corrections (a sign-symmetric computation), with a
+// zero returned as itself so that -0 / b stays -0.
+__device__ __forceinline__ float div_by(float a, float b, float y) { return a == 0.0f ? a : quotient(a, b, y, a * y); }
+
+// range / RANGE for a range in [0, RANGE] (the march's result): below 2^-60
+// the IEEE division; above, the corrections with RN(1 / 10) = 0.1f, whose
+// steps scale with the dividend's exponent there (no subnormal intermediate),
+// so one binade checked exhaustively (tests/test_cell_index.py) covers them all.
+__device__ __forceinline__ float range_obs(float range) {
+  static_assert(RANGE == 10.0f, "range_obs divides by 10");
+  return range < 8.67361738e-19f ? range / RANGE : quotient(range, RANGE, 0.1f, range * 0.1f);
+}
+
 template <int LAYERS, bool NC>
 __device__ __forceinline__ void trace(const TrackDev& t, const float4* ray, float* obs, int n,
                                       const float2* __restrict__ beam_dir, int max_iters, int* iters, int car,
                                       int beam) {
   int count = 0;
   const float range = beam_range<LAYERS, NC>(t, ray, n, beam_dir, max_iters, iters != nullptr, car, beam, &count);
-  obs[(long)(4 + beam) * n + car] = range / RANGE;
+  obs[(long)(4 + beam) * n + car] = range_obs(range);
   if (iters) iters[(long)beam * n + car] = count;
 }
 
@@ -685,9 +701,19 @@ __device__ __forceinline__ float beam_range(const TrackDev& t, const float4* ray
   float dy = az.x * r1.x + az.y * r0.w;
   float dz = az.x * r1.y + az.y * r1.z;
   const float norm = sqrtf((dx * dx + dz * dz) + (dy * dy + 0.0f));
-  dx = dx / norm;
-  dy = dy / norm;
-  dz = dz / norm;
+  // the reference's three divisions by norm, a normal number (at least about
+  // 1: the heading rotation keeps dx^2 + dy^2 near 1) unless the frame holds a
+  // NaN or an infinity, which take the IEEE divisions
+  if (norm <= 3.40282347e38f) {
+    const float rnorm = 1.0f / norm;
+    dx = div_by(dx, norm, rnorm);
+    dy = div_by(dy, norm, rnorm);
+    dz = div_by(dz, norm, rnorm);
+  } else {
+    dx = dx / norm;
+    dy = dy / norm;
+    dz = dz / norm;
+  }
   const float ox = r0.x, oy = r0.y, oz = r0.z;
   const float descent = (1.5f * t.slope) * sqrtf(dx * dx + dy * dy) + fmaxf(-dz, 0.0f);
   const float inv_descent = 1.0f / descent;

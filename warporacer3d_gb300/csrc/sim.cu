@@ -172,9 +172,10 @@ __device__ __forceinline__ Spot probe(const TrackDev& t, float x, float y, float
   return best;
 }
 
-// probe<LAYERS, false>'s (clearance - cell, height) for one or two layers at
-// the march's point (lidar_cell's arguments, height z), from the lidar's
-// cells. Per cell they hold (c0 - cell, h0, c1 - cell, h1), the clearance of
+// probe<LAYERS, false>'s (clearance - cell, height - z) for one or two layers
+// at the march's point (lidar_cell's arguments, height z), from the lidar's
+// cells: RN(height - z), the negation of the reference's RN(z - height), which
+// the layer choice computes anyway. Per cell they hold (c0 - cell, h0, c1 - cell, h1), the clearance of
 // an undrivable layer as -1; slot 1 holds layer 1 only where both layers are
 // drivable and a NaN height otherwise, which never compares nearer, and a
 // cell where only layer 1 is drivable holds it in slot 0. So layer 1 is taken
@@ -188,9 +189,11 @@ __device__ __forceinline__ float2 lidar_probe(const TrackDev& t, float vx, float
   const unsigned idx = lidar_cell(t, vx, vy, tt, ox, oy, dx, dy);
   if (LAYERS == 2) {
     const float4 v = __ldg(reinterpret_cast<const float4*>(t.lc) + idx);
-    return fabsf(v.w - z) < fabsf(v.y - z) ? make_float2(v.z, v.w) : make_float2(v.x, v.y);
+    const float d0 = v.y - z, d1 = v.w - z;
+    return fabsf(d1) < fabsf(d0) ? make_float2(v.z, d1) : make_float2(v.x, d0);
   }
-  return __ldg(reinterpret_cast<const float2*>(t.lc) + idx);
+  const float2 v = __ldg(reinterpret_cast<const float2*>(t.lc) + idx);
+  return make_float2(v.x, v.y - z);
 }
 
 // racer/sim.mojo:126-140: bilinear height and its gradient, in two parts: the
@@ -773,14 +776,14 @@ __device__ __forceinline__ float march(const TrackDev& t, float ox, float oy, fl
     for (;;) {
       if (COUNTED) ++count;
       const float pz = oz + tt * dz;
-      float2 spot;  // (clearance - cell, height)
+      float2 spot;  // (clearance - cell, height - pz)
       if (CELLS) {
         spot = lidar_probe<LAYERS>(t, __fmaf_rn(tt, ax, bx), __fmaf_rn(tt, ay, by), tt, ox, oy, dx, dy, pz);
       } else {
         const Spot s = probe<LAYERS, false>(t, ox + tt * dx, oy + tt * dy, pz);
-        spot = make_float2(s.clearance - cell, s.height);
+        spot = make_float2(s.clearance - cell, s.height - pz);
       }
-      fl = (pz - spot.y) - 0.03f;
+      fl = -spot.y - 0.03f;  // the reference's (pz - height) - 0.03: RN(pz - h) = -RN(h - pz)
       step = fminf(spot.x, quotient(fl, descent, inv_descent, fl * inv_descent));
       next = tt + step;
       if (fl < 0.0f || step < min_step || !(next < RANGE) || (COUNTED && count >= max_iters)) break;

@@ -250,7 +250,7 @@ struct EpiInfer {
 #pragma unroll
     for (int j = 0; j < 16; ++j) {
       if (n + j < N) {
-        float y = fminf(fmaxf(v[j] + bias[n + j], 0.0f), 1.0f);
+        const float y = __saturatef(v[j] + bias[n + j]);  // as the fused kernel: [0, 1], NaN to 0
         out[(long)(n + j) * ldo + m] = y;
         lo = fminf(lo, y);
       }

@@ -299,7 +299,7 @@ __device__ bool sf_epilogue(uint32_t tmem, uint8_t* abuf, const SfBars& b, const
           for (int j = 0; j < 32; ++j) {
             const int o = o0 + j;
             if (o < args.beams) {
-              const float y = fminf(fmaxf(v[j] + bb[j], 0.0f), 1.0f);
+              const float y = __saturatef(v[j] + bb[j]);  // as EpiInfer: [0, 1], NaN to 0
               args.out[(long)o * args.n + m] = y;
               lo = fminf(lo, y);
             }

@@ -11,8 +11,9 @@
 // 128B-swizzled): the input block in k-block 0 for layer 1, then each hidden
 // epilogue writes its tanh output there in BF16 as the next layer's A. The
 // output layer runs in 256-column chunks alternating between the two TMEM
-// slots, so the epilogue of one chunk (clamp, obs rows, per-car minimum)
-// overlaps the MMAs of the next; each CTA starts at a different chunk so the
+// slots, so the epilogue of one chunk (clamp, then the obs rows in the car
+// frame or the FP16 world-profile rows in the world frame, and the per-car
+// minimum) overlaps the MMAs of the next; each CTA starts at a different chunk so the
 // SMs do not all read the same weight lines at once. The MMAs, their k order
 // and the BF16 rounding of
 // the activations are those of the layer-by-layer GEMMs, so the two paths give

@@ -59,7 +59,7 @@ def parse():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-surrogate", action="store_true")
     ap.add_argument("--surrogate-only", action="store_true", help="print only the surrogate section")
-    ap.add_argument("--surrogate-frame", default="world", choices=["world", "car"],
+    ap.add_argument("--surrogate-frame", default="world", choices=["world", "car", "car_grid"],
                     help="output frame of the surrogate in --surrogate-only runs")
     ap.add_argument("--no-training", action="store_true")
     ap.add_argument("--no-batched", action="store_true")
@@ -246,7 +246,7 @@ def fused_rollout_section(torch, W, track, stream, flush, runner):
 
 
 SURR_CARS, SURR_STEPS, SURR_REPS, SURR_TRAIN_STEPS = 65536, 32, 3, 80000
-SURR_LR = {"world": 2e-3, "car": 8e-3}
+SURR_LR = {"world": 2e-3, "car": 8e-3, "car_grid": 3e-3}
 SURR_HUBER_M = 0.02
 SPOT_STRIDE, SPOT_TOL_M = 64, 1.0
 SURR_NETWORK = {
@@ -254,7 +254,9 @@ SURR_NETWORK = {
              "heading phase) -> 3 x 512 tanh -> 1440 world samples, each beam read at its heading's offset; "
              "BF16 tcgen05, FP32 Adam",
     "car": "64 encoded inputs (fixed Fourier features of the frame) -> 3 x 512 tanh -> 1081 beams, BF16 "
-           "tcgen05, FP32 Adam"}
+           "tcgen05, FP32 Adam",
+    "car_grid": "64 inputs (feature grids of the origin: 5 resolutions x 8 features; the frame; heading "
+                "harmonics; 8 fixed Fourier features) -> 3 x 512 tanh -> 1081 beams, BF16 tcgen05, FP32 Adam"}
 
 
 def surrogate_section(torch, W, track, stream, flush, train_steps=SURR_TRAIN_STEPS, keep=None, frame="world",
@@ -696,7 +698,7 @@ def main():
         del runner
         steps = args.surrogate_train_steps if args.surrogate_train_steps is not None else SURR_TRAIN_STEPS
         kept = {}
-        line["surrogate_car_frame"] = surrogate_section(torch, W, track, stream, flush, steps, kept, "car",
+        line["surrogate_car_frame"] = surrogate_section(torch, W, track, stream, flush, steps, kept, "car_grid",
                                                         spot=False)
         line["surrogate"] = surrogate_section(torch, W, track, stream, flush, steps, kept, "world")
         if not args.no_training:

@@ -281,18 +281,20 @@ int racer_surrogate_create(racer_sim* sim, int hidden, int batch, uint64_t seed,
  * offset plus b, so the rotation by the heading is exact rather than learned;
  * the inputs are trainable feature grids per layer at the origin (five
  * resolutions, eight features each), fixed Fourier features of x and y and
- * the sub-sample phase of the heading. */
+ * the sub-sample phase of the heading.
+ * frame 2: the car frame's outputs (one per beam) from the same feature grids
+ * beside the frame, heading harmonics and two Fourier octaves. */
 int racer_surrogate_create_frame(racer_sim* sim, int hidden, int batch, uint64_t seed, int frame,
                                  racer_surrogate** out);
 int racer_surrogate_destroy(racer_surrogate* surrogate);
 /* FP32 master parameters W1 [H,64] | W2 [H,H] | b2 [H] | W3 [H,H] | b3 [H] |
  * W4 [nout,H] | b4 [nout] (nout = beams, or K in the world frame) | (world
- * frame, from the next multiple of 8) the feature grids, level by level
+ * frame and frame 2, from the next multiple of 8) the feature grids, level by level
  * [layers][gy][gx][8], and their last gradient (device pointers). */
 int racer_surrogate_params(racer_surrogate* surrogate, float** theta_dev, float** grad_dev, long* count, int* hidden);
-/* The world frame's feature-grid geometry: per level (5) the vertex counts
- * gx, gy, the spacing in metres and the offset of the level's block in the
- * parameters (null pointers are skipped); fails for a car-frame surrogate. */
+/* The feature-grid geometry (frames 1 and 2): per level (5) the vertex
+ * counts gx, gy, the spacing in metres and the offset of the level's block in
+ * the parameters (null pointers are skipped); fails without feature grids. */
 int racer_surrogate_grid(racer_surrogate* surrogate, int* gx, int* gy, float* spacing_m, long* offset);
 /* The encoded inputs (host, [batch, 64], the BF16 values as float) and, in the
  * world frame, each sample's first world sample k0 (host, [batch]) of the

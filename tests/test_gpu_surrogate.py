@@ -122,12 +122,13 @@ def test_gradient_matches_float64_backprop():
 FOV = 4.71238898
 
 
-def world_setup(hidden=128, B=256, steps=20):
-    """A briefly trained world-frame surrogate on bridge at 1081 beams and the gradient of its batch 0."""
+def world_setup(hidden=128, B=256, steps=20, frame="world"):
+    """A briefly trained grid surrogate (world frame, or car frame with grids) on bridge at 1081 beams
+    and the gradient of its batch 0."""
     track = W.track("bridge")
     beams = 1081
     sim = W.Sim(track, 8, 0, beams=beams)
-    sur = W.Surrogate(sim, hidden=hidden, batch=B, seed=3, frame="world")
+    sur = W.Surrogate(sim, hidden=hidden, batch=B, seed=3, frame=frame)
     sur.set_poses(4 * B, seed=9)
     sur.train(steps, lr=3e-3)  # grids and weights away from their initial values
     labels = W.DevArray.empty((beams, B))
@@ -223,6 +224,74 @@ def test_world_frame_inputs_and_gradient_match_float64():
         assert rel < 2e-2, (k, rel)
 
 
+def grid_inputs(sur, track, P, fr, layer):
+    """float64 feature-grid inputs [B, 40] at the lidar origins."""
+    ref = np.zeros((len(layer), 40))
+    for l, (iu, iv, fu, fv) in enumerate(grid_corners(sur, track, fr[:, 3], fr[:, 4])):
+        G = P[f"G{l}"]
+        ref[:, 8 * l:8 * l + 8] = (G[layer, iv, iu] * ((1 - fu) * (1 - fv))[:, None] +
+                                   G[layer, iv, iu + 1] * (fu * (1 - fv))[:, None] +
+                                   G[layer, iv + 1, iu] * ((1 - fu) * fv)[:, None] +
+                                   G[layer, iv + 1, iu + 1] * (fu * fv)[:, None])
+    return ref
+
+
+def grid_gradient(sur, track, P, fr, layer, dX):
+    out = {}
+    for l, (iu, iv, fu, fv) in enumerate(grid_corners(sur, track, fr[:, 3], fr[:, 4])):
+        Gg = np.zeros(P[f"G{l}"].shape)
+        d = dX[:, 8 * l:8 * l + 8]
+        for di, dj, w in ((0, 0, (1 - fu) * (1 - fv)), (1, 0, fu * (1 - fv)), (0, 1, (1 - fu) * fv), (1, 1, fu * fv)):
+            np.add.at(Gg, (layer, iv + dj, iu + di), w[:, None] * d)
+        out[f"G{l}"] = Gg
+    return out
+
+
+def test_car_frame_with_grids_inputs_and_gradient_match_float64():
+    """Frame 2 (car-frame outputs, feature-grid inputs): the inputs against a float64 recomputation
+    within BF16 rounding, and the gradient, grids included, against a float64 backprop with the same
+    BF16 roundings within 2e-2 relative (Frobenius) per block."""
+    track, sim, sur, T = world_setup(frame="car_grid")
+    B, beams = sur.batch, sim.beams
+    X, _ = sur.batch_inputs()
+    theta, grad = sur.theta.numpy(), sur.grad.numpy()
+    lay = sur.layout()
+    P = {k: theta[o:o + int(np.prod(s))].reshape(s).astype(np.float64) for k, (o, s) in lay.items()}
+    poses = sur.poses().numpy()[:B]
+    fr = rest_frames(track, poses)
+    layer = poses[:, 3].astype(int)
+    ref = np.zeros((B, 64))
+    ref[:, :40] = grid_inputs(sur, track, P, fr, layer)
+    nx, ny, x0, y0, cell = track[0], track[1], track[2], track[3], track[4]
+    hx, hy = np.float32(0.5) * np.float32(nx - 1) * cell, np.float32(0.5) * np.float32(ny - 1) * cell
+    xn = ((fr[:, 3] - (x0 + hx)) * (np.float32(1) / hx)).astype(np.float64)
+    yn = ((fr[:, 4] - (y0 + hy)) * (np.float32(1) / hy)).astype(np.float64)
+    sh, ch = fr[:, 6].astype(np.float64), fr[:, 7].astype(np.float64)
+    ref[:, 40:48] = np.stack([xn, yn, fr[:, 5], sh, ch, layer == 0, layer == 1, np.ones(B)], 1)
+    h = np.arctan2(sh, ch)
+    for j in range(2, 6):
+        ref[:, 48 + 2 * (j - 2)], ref[:, 49 + 2 * (j - 2)] = np.sin(j * h), np.cos(j * h)
+    for k, sc in enumerate((np.pi, 2 * np.pi)):
+        ref[:, 56 + 4 * k:60 + 4 * k] = np.stack([np.sin(sc * xn), np.cos(sc * xn), np.sin(sc * yn),
+                                                  np.cos(sc * yn)], 1)
+    err = np.abs(X - ref)
+    assert np.all(err <= 2e-3 + 8e-3 * np.abs(ref)), err.max()
+    Wb, h1, h2, h3, y = world_forward(sur, P, X.astype(np.float64))
+    G4 = 2.0 / (B * beams) * (y - T)
+    g4 = bf16(G4)
+    g3 = bf16((g4 @ Wb["W4"]) * (1 - h3 * h3))
+    g2 = bf16((g3 @ Wb["W3"]) * (1 - h2 * h2))
+    g1 = bf16((g2 @ Wb["W2"]) * (1 - h1 * h1))
+    refg = {"W4": g4.T @ h3, "b4": G4.sum(0), "W3": g3.T @ h2, "b3": g3.sum(0), "W2": g2.T @ h1, "b2": g2.sum(0),
+            "W1": g1.T @ X.astype(np.float64)}
+    refg.update(grid_gradient(sur, track, P, fr, layer, g1 @ Wb["W1"]))
+    for k, r in refg.items():
+        o, s = lay[k]
+        g = grad[o:o + int(np.prod(s))].reshape(s)
+        rel = np.linalg.norm(g - r) / np.linalg.norm(r)
+        assert rel < 2e-2, (k, rel)
+
+
 def test_world_frame_prediction_is_the_profile_read_at_the_heading():
     """Inference in the world frame (FP16 world profiles, then the gather by heading): beam b of a
     sample is its clamped world sample (k0 + b) mod K, against a float64 forward of the same inputs."""
@@ -271,7 +340,7 @@ def test_world_frame_needs_the_beam_spacing_to_divide_the_circle():
     W.Surrogate(W.Sim(W.track("bridge"), 8, 0, beams=109), hidden=128, batch=256, seed=1, frame="world")
 
 
-@pytest.mark.parametrize("frame", ["car", "world"])
+@pytest.mark.parametrize("frame", ["car", "world", "car_grid"])
 @pytest.mark.parametrize("audit_every,fallback_m", [(1, 0.5), (0, 100.0)])
 def test_fully_exact_surrogate_rollout_equals_exact_rollout(audit_every, fallback_m, frame):
     """Audit on every step, or a fallback threshold every car crosses: the rollout is the exact one."""
@@ -306,7 +375,7 @@ def test_surrogate_rollout_stats_and_fallback():
     assert sur.rollout_stats()[0] == 0.0  # reset
 
 
-@pytest.mark.parametrize("frame", ["car", "world"])
+@pytest.mark.parametrize("frame", ["car", "world", "car_grid"])
 def test_training_reduces_heldout_error(frame):
     track = W.track("bridge")
     sim = W.Sim(track, 8, 0, beams=1081)
@@ -319,7 +388,7 @@ def test_training_reduces_heldout_error(frame):
     assert after[0] < 0.7 * before[0], (before, after)
 
 
-@pytest.mark.parametrize("frame", ["car", "world"])
+@pytest.mark.parametrize("frame", ["car", "world", "car_grid"])
 @pytest.mark.parametrize("cars", [300, 128 * 160 + 37])
 def test_fused_inference_equals_layered_gemms(cars, frame):
     """The fused 512-wide inference kernel (activations kept on chip, output in TMEM chunks) gives the

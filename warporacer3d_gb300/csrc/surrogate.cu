@@ -28,6 +28,12 @@
 //   y  = W4 h3 + b4            W4 [K, H]: the world profile
 // Training backpropagates into the grids through dL/df = W1^T dL/dh1 (one
 // more GEMM) and a bilinear scatter; the grids take Adam at a higher rate.
+//
+// Car frame with feature grids (frame 2): the car frame's outputs (one per
+// beam) from the same feature grids at the origin beside the frame itself,
+// heading harmonics up to 5 and two Fourier octaves of x and y
+// (k_features_cargrid); trained and served like the car frame, the grids
+// like the world frame's.
 // Inference writes the clamped world profile as FP16 rows per car and a
 // gather kernel turns them into the beam rows of obs.
 //
@@ -352,22 +358,13 @@ __global__ void k_features(const float4* __restrict__ ray, int count, Norm nm, b
     for (int k = 0; k < NIN; ++k) xf[(long)k * count + i] = __float2bfloat16_rn(f[k]);
 }
 
-// World frame: ray frames [2, count] -> encoded inputs (see the top of this file):
-//   0..39   the feature grids of the origin's layer at (x, y), level by level
-//   40..45  x', y', z, [layer 0], [layer 1], 1
-//   46..61  sin/cos(2^k pi x'), sin/cos(2^k pi y') for k = 0..3
-//   62, 63  sin/cos(2 pi phase)
-__global__ void k_features_world(const float4* __restrict__ ray, int count, Norm nm, GridGeom gg,
-                                 const float* __restrict__ grid, int K, bf16* x, bf16* xf) {
-  int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= count) return;
-  const float4 r0 = ray[i], r1 = ray[count + i];
-  const int layer = r1.w == 1.0f ? 1 : 0;
-  float f[NIN];
+// The feature grids of `layer` at (ox, oy), level by level, into f[0 .. 39].
+__device__ __forceinline__ void grid_features(const GridGeom& gg, const float* __restrict__ grid, float ox, float oy,
+                                              int layer, float* f) {
 #pragma unroll
   for (int l = 0; l < GRID_LEVELS; ++l) {
     float fu, fv;
-    const long c = grid_cell(gg, l, r0.x, r0.y, layer, &fu, &fv);
+    const long c = grid_cell(gg, l, ox, oy, layer, &fu, &fv);
     const long dy = (long)gg.gx[l] * GRID_F;
     const float w00 = (1.0f - fu) * (1.0f - fv), w10 = fu * (1.0f - fv), w01 = (1.0f - fu) * fv, w11 = fu * fv;
 #pragma unroll
@@ -383,6 +380,64 @@ __global__ void k_features_world(const float4* __restrict__ ray, int count, Norm
       o[3] = w00 * a.w + w10 * b.w + w01 * d.w + w11 * e.w;
     }
   }
+}
+
+__device__ __forceinline__ void store_inputs(const float* f, int i, int count, bf16* x, bf16* xf) {
+  uint4* row = reinterpret_cast<uint4*>(x + (long)i * NIN);
+#pragma unroll
+  for (int q = 0; q < NIN / 8; ++q)
+    row[q] = make_uint4(tc::pack_bf16(f[8 * q], f[8 * q + 1]), tc::pack_bf16(f[8 * q + 2], f[8 * q + 3]),
+                        tc::pack_bf16(f[8 * q + 4], f[8 * q + 5]), tc::pack_bf16(f[8 * q + 6], f[8 * q + 7]));
+  if (xf)
+#pragma unroll
+    for (int k = 0; k < NIN; ++k) xf[(long)k * count + i] = __float2bfloat16_rn(f[k]);
+}
+
+// Car frame with feature grids (frame 2): ray frames [2, count] -> encoded inputs:
+//   0..39   the feature grids of the origin's layer at (x, y), level by level
+//   40..47  x', y', z, sin h, cos h, [layer 0], [layer 1], 1
+//   48..55  sin/cos(j h) for j = 2..5
+//   56..63  sin/cos(2^k pi x'), sin/cos(2^k pi y') for k = 0, 1
+__global__ void k_features_cargrid(const float4* __restrict__ ray, int count, Norm nm, GridGeom gg,
+                                   const float* __restrict__ grid, bf16* x, bf16* xf) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= count) return;
+  const float4 r0 = ray[i], r1 = ray[count + i];
+  const int layer = r1.w == 1.0f ? 1 : 0;
+  float f[NIN];
+  grid_features(gg, grid, r0.x, r0.y, layer, f);
+  const float xn = (r0.x - nm.xc) * nm.inv_xs, yn = (r0.y - nm.yc) * nm.inv_ys;
+  f[40] = xn;
+  f[41] = yn;
+  f[42] = r0.z;
+  f[43] = r1.x;
+  f[44] = r0.w;
+  f[45] = layer == 0 ? 1.0f : 0.0f;
+  f[46] = layer == 1 ? 1.0f : 0.0f;
+  f[47] = 1.0f;
+  const float h = atan2f(r1.x, r0.w);
+#pragma unroll
+  for (int j = 2; j <= 5; ++j) sincosf((float)j * h, &f[48 + 2 * (j - 2)], &f[49 + 2 * (j - 2)]);
+  sincospif(xn, &f[56], &f[57]);
+  sincospif(yn, &f[58], &f[59]);
+  sincospif(2.0f * xn, &f[60], &f[61]);
+  sincospif(2.0f * yn, &f[62], &f[63]);
+  store_inputs(f, i, count, x, xf);
+}
+
+// World frame: ray frames [2, count] -> encoded inputs (see the top of this file):
+//   0..39   the feature grids of the origin's layer at (x, y), level by level
+//   40..45  x', y', z, [layer 0], [layer 1], 1
+//   46..61  sin/cos(2^k pi x'), sin/cos(2^k pi y') for k = 0..3
+//   62, 63  sin/cos(2 pi phase)
+__global__ void k_features_world(const float4* __restrict__ ray, int count, Norm nm, GridGeom gg,
+                                 const float* __restrict__ grid, int K, bf16* x, bf16* xf) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= count) return;
+  const float4 r0 = ray[i], r1 = ray[count + i];
+  const int layer = r1.w == 1.0f ? 1 : 0;
+  float f[NIN];
+  grid_features(gg, grid, r0.x, r0.y, layer, f);
   const float xn = (r0.x - nm.xc) * nm.inv_xs, yn = (r0.y - nm.yc) * nm.inv_ys;
   f[40] = xn;
   f[41] = yn;
@@ -400,14 +455,7 @@ __global__ void k_features_world(const float4* __restrict__ ray, int count, Norm
   float phase;
   world_phase(r1.x, r0.w, K, &phase);
   sincospif(2.0f * phase, &f[62], &f[63]);
-  uint4* row = reinterpret_cast<uint4*>(x + (long)i * NIN);
-#pragma unroll
-  for (int q = 0; q < NIN / 8; ++q)
-    row[q] = make_uint4(tc::pack_bf16(f[8 * q], f[8 * q + 1]), tc::pack_bf16(f[8 * q + 2], f[8 * q + 3]),
-                        tc::pack_bf16(f[8 * q + 4], f[8 * q + 5]), tc::pack_bf16(f[8 * q + 6], f[8 * q + 7]));
-  if (xf)
-#pragma unroll
-    for (int k = 0; k < NIN; ++k) xf[(long)k * count + i] = __float2bfloat16_rn(f[k]);
+  store_inputs(f, i, count, x, xf);
 }
 
 // World frame, training loss: one thread per sample m and 64 world samples
@@ -590,6 +638,7 @@ __global__ void k_reduce_splits(const float* P, int splits, long mn, int N, int 
 struct Layout {
   int H, beams, npad;  // npad: nout rounded up to 64
   int world;           // 0: car frame (nout = beams), 1: world frame (nout = K world samples)
+  int grid;            // 1: the first 40 inputs are the trainable feature grids (world frame, frame 2)
   int nout;
   long w1, w2, b2, w3, b3, w4, b4, g, total;
 };
@@ -903,6 +952,8 @@ int featurise(racer_surrogate* s, const float4* ray, int count, bf16* x, bf16* x
   if (s->L.world)
     k_features_world<<<(count + 127) / 128, 128, 0, st>>>(ray, count, s->nm, s->gg, s->theta + s->L.g, s->L.nout, x,
                                                           xf);
+  else if (s->L.grid)
+    k_features_cargrid<<<(count + 127) / 128, 128, 0, st>>>(ray, count, s->nm, s->gg, s->theta + s->L.g, x, xf);
   else
     k_features<<<(count + 127) / 128, 128, 0, st>>>(ray, count, s->nm, x, xf);
   SURR_CHECK(cudaGetLastError());
@@ -943,7 +994,7 @@ int gradient(racer_surrogate* s, long first) {
   const int nout = s->L.nout;
   SURR_CHECK(cudaMemsetAsync(s->grad + s->L.b4, 0, nout * sizeof(float), s->st));
   SURR_CHECK(cudaMemsetAsync(s->sums, 0, 2 * sizeof(double), s->st));
-  if (s->L.world)
+  if (s->L.grid)
     SURR_CHECK(cudaMemsetAsync(s->grad + s->L.g, 0, (s->L.total - s->L.g) * sizeof(float), s->st));
   if ((rc = forward(s, a, true, nullptr))) return rc;
   const float scale = 2.0f / ((float)B * (float)beams);
@@ -964,13 +1015,13 @@ int gradient(racer_surrogate* s, long first) {
   SURR_CHECK(gemm_launch<256>(a->tg3s, s->tw3t, B, H, H / 64, 1,
                               EpiDTanh{a->h2s, H, a->g2s, H, a->g2f, B, s->grad + s->L.b2, B, H}, s->err, s->st));
   SURR_CHECK(gemm_launch<256>(a->tg2s, s->tw2t, B, H, H / 64, 1,
-                              EpiDTanh{a->h1s, H, s->L.world ? a->g1s : nullptr, H, a->g1f, B, nullptr, B, H}, s->err,
+                              EpiDTanh{a->h1s, H, s->L.grid ? a->g1s : nullptr, H, a->g1f, B, nullptr, B, H}, s->err,
                               s->st));
   if ((rc = wgrad<256>(s, a->tg4f, a->th3f, NP, nout, H, s->L.w4))) return rc;
   if ((rc = wgrad<256>(s, a->tg3f, a->th2f, H, H, H, s->L.w3))) return rc;
   if ((rc = wgrad<256>(s, a->tg2f, a->th1f, H, H, H, s->L.w2))) return rc;
   if ((rc = wgrad<64>(s, a->tg1f, a->txf, H, H, NIN, s->L.w1))) return rc;
-  if (s->L.world) {  // dL/df = g1 W1, then onto the grids
+  if (s->L.grid) {  // dL/df = g1 W1, then onto the grids
     SURR_CHECK(gemm_launch<64>(a->tg1s, s->tw1t, B, NIN, H / 64, 1, EpiRowF32{s->dx, NIN, B, NIN}, s->err, s->st));
     k_grid_grad<<<B / 128, 128, 0, s->st>>>(s->ray, B, s->gg, s->dx, s->grad + s->L.g);
     SURR_CHECK(cudaGetLastError());
@@ -999,8 +1050,8 @@ int racer_surrogate_create_frame(racer_sim* sim, int hidden, int batch, uint64_t
     set_error("racer_surrogate_create: hidden must be 128, 256 or 512 and batch a positive multiple of 128");
     return 1;
   }
-  if (frame != 0 && frame != 1) {
-    set_error("racer_surrogate_create_frame: frame must be 0 (car) or 1 (world)");
+  if (frame < 0 || frame > 2) {
+    set_error("racer_surrogate_create_frame: frame must be 0 (car), 1 (world) or 2 (car, feature grids)");
     return 1;
   }
   if (frame == 1 && ((sim->beams - 1) % 12 != 0 || sim->beams < 13)) {
@@ -1023,8 +1074,9 @@ int racer_surrogate_create_frame(racer_sim* sim, int hidden, int batch, uint64_t
   Layout& L = s->L;
   L.H = hidden;
   L.beams = sim->beams;
-  L.world = frame;
-  L.nout = frame ? 4 * (sim->beams - 1) / 3 : sim->beams;
+  L.world = frame == 1;
+  L.grid = frame != 0;
+  L.nout = L.world ? 4 * (sim->beams - 1) / 3 : sim->beams;
   L.npad = (L.nout + 63) / 64 * 64;
   L.w1 = 0;
   L.w2 = L.w1 + (long)hidden * NIN;
@@ -1033,10 +1085,10 @@ int racer_surrogate_create_frame(racer_sim* sim, int hidden, int batch, uint64_t
   L.b3 = L.w3 + (long)hidden * hidden;
   L.w4 = L.b3 + hidden;
   L.b4 = L.w4 + (long)L.nout * hidden;
-  L.g = frame ? (L.b4 + L.nout + 7) / 8 * 8 : L.b4 + L.nout;  // grids 32-byte aligned
+  L.g = L.grid ? (L.b4 + L.nout + 7) / 8 * 8 : L.b4 + L.nout;  // grids 32-byte aligned
   L.total = L.g;
   const TrackDev& t = sim->t;
-  if (frame) {  // feature grids over the map, per layer
+  if (L.grid) {  // feature grids over the map, per layer
     GridGeom& g = s->gg;
     g.x0 = t.x0, g.y0 = t.y0;
     long off = 0;
@@ -1054,9 +1106,9 @@ int racer_surrogate_create_frame(racer_sim* sim, int hidden, int batch, uint64_t
   s->nm = Norm{t.x0 + hx, 1.0f / hx, t.y0 + hy, 1.0f / hy};
   const int H = hidden, NP = L.npad;
   int rc = 0;
-  if (frame && ((rc = salloc(&s->w1t, (size_t)NIN * H)) || (rc = salloc(&s->wy, (size_t)batch * NP)) ||
-                (rc = salloc(&s->dx, (size_t)batch * NIN)) || (rc = salloc(&s->wbatch, (size_t)batch * NP)) ||
-                (rc = make_tmap_bf16(&s->tw1t, s->w1t, NIN, H, H, 64)))) {
+  if ((L.grid && ((rc = salloc(&s->w1t, (size_t)NIN * H)) || (rc = salloc(&s->dx, (size_t)batch * NIN)) ||
+                   (rc = make_tmap_bf16(&s->tw1t, s->w1t, NIN, H, H, 64)))) ||
+      (L.world && ((rc = salloc(&s->wy, (size_t)batch * NP)) || (rc = salloc(&s->wbatch, (size_t)batch * NP))))) {
     racer_surrogate_destroy(s);
     return rc;
   }
@@ -1141,8 +1193,8 @@ int racer_surrogate_params(racer_surrogate* s, float** theta, float** grad, long
 }
 
 int racer_surrogate_grid(racer_surrogate* s, int* gx, int* gy, float* spacing_m, long* offset) {
-  if (!s || !s->L.world) {
-    racer_host::set_error("racer_surrogate_grid: not a world-frame surrogate");
+  if (!s || !s->L.grid) {
+    racer_host::set_error("racer_surrogate_grid: the surrogate has no feature grids");
     return 1;
   }
   for (int l = 0; l < GRID_LEVELS; ++l) {
@@ -1352,7 +1404,7 @@ int racer_surrogate_train(racer_surrogate* s, int steps, float lr, float* last_m
     const float rate = lr * (0.01f + 0.99f * 0.5f * (1.0f + cosf(3.14159265f * frac)));
     const float c1 = 1.0f - powf(0.9f, (float)s->step), c2 = 1.0f - powf(0.999f, (float)s->step);
     k_adam_s<<<592, 256, 0, s->st>>>(s->L.g, rate, 0.999f, 1e-8f, c1, c2, s->theta, s->grad, s->m1, s->m2);
-    if (s->L.world) {  // the feature grids: a higher rate, beta2 0.99, a tiny epsilon
+    if (s->L.grid) {  // the feature grids: a higher rate, beta2 0.99, a tiny epsilon
       const long g = s->L.g;
       k_adam_s<<<592, 256, 0, s->st>>>(s->L.total - g, rate * GRID_LR_SCALE, 0.99f, 1e-15f, c1,
                                        1.0f - powf(0.99f, (float)s->step), s->theta + g, s->grad + g, s->m1 + g,

@@ -343,17 +343,18 @@ class Surrogate:
 
     frame="car": one output per beam from fixed Fourier features of the frame. frame="world": the
     range profile at fixed world angles (the beam spacing), read at each car's heading offset, from
-    trainable feature grids of the origin (beams - 1 must be a multiple of 12)."""
+    trainable feature grids of the origin (beams - 1 must be a multiple of 12). frame="car_grid": one
+    output per beam from the feature grids beside the frame and heading harmonics."""
 
     GRID_LEVELS, GRID_F = 5, 8
+    FRAMES = {"car": 0, "world": 1, "car_grid": 2}
 
     def __init__(self, sim, hidden=512, batch=8192, seed=0, frame="car"):
-        if frame not in ("car", "world"):
-            raise ValueError("frame must be 'car' or 'world'")
+        if frame not in self.FRAMES:
+            raise ValueError("frame must be 'car', 'world' or 'car_grid'")
         self.sim = sim
         h = ctypes.c_void_p()
-        call("racer_surrogate_create_frame", sim.handle, hidden, batch, seed, int(frame == "world"),
-             ctypes.byref(h))
+        call("racer_surrogate_create_frame", sim.handle, hidden, batch, seed, self.FRAMES[frame], ctypes.byref(h))
         self.handle = h
         self.batch, self.hidden, self.frame = batch, hidden, frame
         self.nout = 4 * (sim.beams - 1) // 3 if frame == "world" else sim.beams
@@ -377,7 +378,7 @@ class Surrogate:
         for name, shape in sizes:
             out[name] = (off, shape)
             off += int(np.prod(shape))
-        if self.frame == "world":
+        if self.frame != "car":
             gx, gy, sp, offs = self.grid()
             layers = (offs[1] - offs[0]) // (gx[0] * gy[0] * self.GRID_F)
             for l in range(self.GRID_LEVELS):

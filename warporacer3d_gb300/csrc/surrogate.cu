@@ -592,12 +592,15 @@ __global__ void __launch_bounds__(WR_THREADS) k_world_rotate(const __half* __res
     pred[(long)b * ldp + m] = __half2float(mine[b]);
 }
 
-// The gather kernel's shared-memory limit (windows of up to 1537 beams), once per device.
+// The world frame's largest beam count (the gather's shared memory: 16 windows of it, 131 KB).
+constexpr int WORLD_MAX_BEAMS = 4093;
+
+// The gather kernel's shared-memory limit, once per device.
 cudaError_t world_rotate_configure() {
   static unsigned long long configured = 0;
   return once_per_device(&configured, [] {
     return cudaFuncSetAttribute(k_world_rotate, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                WR_CARS * world_rotate_words(1537) * 4);
+                                WR_CARS * world_rotate_words(WORLD_MAX_BEAMS) * 4);
   });
 }
 
@@ -914,8 +917,8 @@ int world_profiles(racer_surrogate* s, SurrogateActs* a, const float4* ray, __ha
 // Beam rows pred [beams, ldp] of M cars from their world profiles (k_world_rotate).
 int world_rotate(racer_surrogate* s, const __half* wout, const float4* ray, int M, float* pred, long ldp,
                  cudaStream_t st) {
-  if (s->L.beams > 1537) {
-    racer_host::set_error("surrogate: the world frame serves at most 1537 beams");
+  if (s->L.beams > WORLD_MAX_BEAMS) {
+    racer_host::set_error("surrogate: the world frame serves at most 4093 beams");
     return 1;
   }
   SURR_CHECK(world_rotate_configure());
@@ -1054,9 +1057,9 @@ int racer_surrogate_create_frame(racer_sim* sim, int hidden, int batch, uint64_t
     set_error("racer_surrogate_create_frame: frame must be 0 (car), 1 (world) or 2 (car, feature grids)");
     return 1;
   }
-  if (frame == 1 && ((sim->beams - 1) % 12 != 0 || sim->beams < 13)) {
+  if (frame == 1 && ((sim->beams - 1) % 12 != 0 || sim->beams < 13 || sim->beams > WORLD_MAX_BEAMS)) {
     set_error("racer_surrogate_create_frame: the world frame needs beams - 1 a multiple of 12 (the beam spacing "
-              "then divides the circle into a multiple of 16 world samples)");
+              "then divides the circle into a multiple of 16 world samples) and at most 4093 beams");
     return 1;
   }
   if (sim->seg.count != 1) {

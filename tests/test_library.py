@@ -91,3 +91,17 @@ def test_gather_peak_arguments_checked_on_host(lib):
         assert lib.racer_gather_peak(size, 3, ctypes.byref(gbs)) == 1
         assert b"power of two" in lib.racer_last_error()
     assert lib.racer_gather_peak(1 << 20, 0, ctypes.byref(gbs)) == 1
+
+
+def test_surrogate_arguments_checked_on_host(lib):
+    """The learned lidar's constructor rejects a null sim, a bad width or batch and an unknown
+    output frame before touching the device; the Python mirror rejects unknown frame names."""
+    out = ctypes.c_void_p()
+    assert lib.racer_surrogate_create_frame(None, 512, 8192, 1, 1, ctypes.byref(out)) == 1
+    assert b"hidden must be" in lib.racer_last_error()
+    assert lib.racer_surrogate_create(None, 512, 8192, 1, ctypes.byref(out)) == 1
+    assert lib.racer_surrogate_grid(None, None, None, None, None) == 1
+    assert b"feature grids" in lib.racer_last_error()
+    assert lib.racer_surrogate_batch_inputs(None, None, None) == 1
+    with pytest.raises(ValueError, match="frame"):
+        W.Surrogate(None, frame="polar")
